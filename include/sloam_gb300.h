@@ -1,0 +1,288 @@
+/*
+ * sloam_gb300.h — C ABI of the GB300 (sm_103a) SLOAM keyframe hot path.
+ *
+ * Every entry point is plain C: POD structs, raw pointers and sizes, an int
+ * status (0 = OK).  No C++ exceptions and no torch types cross this boundary.
+ * The caller owns every host buffer; a context owns its device buffers and one
+ * CUDA stream.  A context is thread-compatible: use one context per thread.
+ *
+ * Which reference interface each entry point replaces is stated beside it
+ * (paths are relative to the KumarRobotics/sloam repository).
+ */
+#ifndef SLOAM_GB300_H
+#define SLOAM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define SLOAM_OK                 0
+#define SLOAM_ERR_ARG            1  /* bad argument / size                          */
+#define SLOAM_ERR_CUDA           2  /* a CUDA runtime call failed                   */
+#define SLOAM_ERR_TIMEOUT        3  /* a bounded device-side wait gave up           */
+#define SLOAM_ERR_EMPTY_MAP      4  /* sloam.cpp:476-480  not first scan, empty map */
+#define SLOAM_ERR_NO_MODELS      5  /* sloam.cpp:482-486  no ground or landmarks    */
+#define SLOAM_ERR_NOT_CONVERGED  6  /* sloam.cpp:241     pose solve failed          */
+#define SLOAM_ERR_CAPACITY       7  /* an output or scratch capacity was exceeded   */
+#define SLOAM_ERR_NO_DEVICE      8  /* no CUDA device / kernels not loadable        */
+
+/* ------------------------------------------------------------ parameters */
+/* One POD mirroring FeatureModelParams (include/helpers/definitions.h:76-104),
+ * Instance::Params (include/segmentation/trellis.h:31-40), the Segmentation
+ * constructor arguments (inference.h:57-58) and every constant the reference
+ * hard-codes on the path, made explicit.  sloam_params_default() fills the
+ * values of params/sloam.yaml and sloamNode.cpp:57-128. */
+typedef struct sloam_params {
+  /* FeatureModelParams */
+  int32_t scans_per_sweep;
+  double  min_tree_models;          /* min_tree_models            (5)     */
+  double  min_ground_models;        /* min_ground_models          (36)    */
+  double  max_lidar_dist;           /* max_lidar_dist             (20)    */
+  double  max_ground_lidar_dist;    /* max_ground_dist            (25)    */
+  double  min_ground_lidar_dist;    /* min_ground_dist            (5)     */
+  int32_t two_step_optim;           /* two_step_optim             (1)     */
+  int32_t ground_radii_bins;        /* ground_radii_bins          (2)     */
+  int32_t ground_theta_bins;        /* ground_theta_bins          (18)    */
+  double  ground_retain_thresh;     /* ground_retain_thresh       (0.05)  */
+  double  ground_match_thresh;      /* ground_match_thresh        (1.0)   */
+  double  rough_tree_match_thresh;  /* rough_tree_match_thresh    (2.5)   */
+  double  tree_match_thresh;        /* tree_match_thresh          (0.5)   */
+  double  max_tree_radius;          /* sloamNode.cpp:104          (0.3)   */
+  double  max_axis_theta;           /* sloamNode.cpp:105          (10 deg)*/
+  double  max_focus_outlier_distance;/* sloamNode.cpp:106         (0.5)   */
+  double  add_new_tree_thresh_dist; /* add_new_tree_thresh_dist   (1.5)   */
+  int32_t features_per_tree;        /* features_per_tree          (20)    */
+  int32_t num_ground_features;      /* num_ground_features        (5)     */
+  double  default_tree_radius;      /* default_tree_radius        (0.2)   */
+  /* minPlanes_ of sloam.cpp:11.  The reference reads it from an
+   * uninitialised struct; here it is explicit (default 0.1 * bins). */
+  double  min_planes;
+
+  /* Instance::Params */
+  float   beam_cluster_threshold;   /* (0.5, unused on the path)          */
+  float   max_dist_to_centroid;     /* (0.2) trellis.cpp:90               */
+  int32_t min_vertex_size;          /* (4,   unused on the path)          */
+  int32_t min_landmark_size;        /* (5,   unused on the path)          */
+  float   min_landmark_height;      /* (1.0, unused on the path)          */
+
+  /* Segmentation (range-image projection) */
+  float   fov_up_deg;               /* seg_lidar_fov  (+22.5)             */
+  float   fov_down_deg;             /* -seg_lidar_fov (-22.5)             */
+  int32_t img_w;                    /* seg_lidar_w    (2048)              */
+  int32_t img_h;                    /* seg_lidar_h    (64)                */
+  int32_t do_destagger;             /* do_destagger   (1)                 */
+
+  /* constants hard-coded in the reference, explicit here */
+  float   cc_dist_threshold;        /* trellis.cpp:23         1.0 m       */
+  int32_t trellis_min_cluster;      /* trellis.cpp:109        > 80 pts    */
+  int32_t trellis_min_beam_points;  /* trellis.cpp:119        > 3 pts     */
+  int32_t trellis_min_vertices;     /* trellis.cpp:124        > 16        */
+  int32_t trellis_max_vertices;     /* trellis.cpp:125-126    56          */
+  double  line_ransac_thresh;       /* cylinder.cpp:122       0.25 m      */
+  int32_t line_ransac_max_iter;     /* PCL SACSegmentation default 50     */
+  double  line_ransac_probability;  /* PCL SACSegmentation default 0.99   */
+  double  min_tree_height_sq;       /* cylinder.cpp:109       1.5 m^2     */
+  double  root_plane_max_dist;      /* cylinder.cpp:48        2.0 m       */
+  double  plane_match_thresh;       /* sloam.cpp:490          1.0 m       */
+  double  huber_delta;              /* sloam.cpp:69,130,181   0.1         */
+
+  /* extensions of this implementation (no reference counterpart) */
+  uint64_t seed;                    /* RANSAC counter-based RNG key       */
+  int32_t cyl_mode;                 /* 0 = vertex-line RANSAC (reference) ;
+                                       1 = + point-level cylinder RANSAC  */
+  int32_t cyl_hypotheses;           /* K hypotheses per tree (mode 1)     */
+  float   cyl_inlier_thresh;        /* tau, metres (mode 1)               */
+  int32_t cyl_ls_iters;             /* LS refinement iterations (mode 1)  */
+  float   cyl_max_hyp_radius;       /* reject circle hypotheses above     */
+  int32_t gn_iters;                 /* Gauss-Newton iterations (pose)     */
+  int32_t max_landmarks;            /* context capacity: trees per scan   */
+  int32_t max_map;                  /* context capacity: submap cylinders */
+  int32_t max_ground;               /* context capacity: ground points    */
+} sloam_params;
+
+void sloam_params_default(sloam_params* p);
+
+/* --------------------------------------------------------- common types */
+/* SE(3) as a unit quaternion (x, y, z, w) and a translation. */
+typedef struct sloam_se3 {
+  double q[4];
+  double t[3];
+} sloam_se3;
+
+/* Landmarks in Trellis form: the output of Instance::computeGraph
+ * (trellis.cpp:134-139), std::vector<std::vector<TreeVertex>> flattened to
+ * SoA.  Vertex v of landmark l is v in [vertex_begin[l], vertex_begin[l+1]),
+ * bottom beam first; its kept points are [point_begin[v], point_begin[v+1])
+ * in z order (x, y, z, intensity).  The caller sets the cap_* fields and the
+ * pointers; the callee sets n_*.  vertex_row is the range-image row of the
+ * vertex (the reference stores beam = 0). */
+typedef struct sloam_landmarks {
+  int32_t  cap_landmarks, cap_vertices, cap_points;
+  int32_t  n_landmarks, n_vertices, n_points;
+  int32_t* tree_id;        /* [cap_landmarks]    CC label of the tree     */
+  int32_t* vertex_begin;   /* [cap_landmarks+1]                           */
+  float*   vertex_xyz;     /* [cap_vertices*3]   per-axis median          */
+  double*  vertex_radius;  /* [cap_vertices]                              */
+  int32_t* vertex_row;     /* [cap_vertices]                              */
+  int32_t* point_begin;    /* [cap_vertices+1]                            */
+  float*   point_xyzi;     /* [cap_points*4]                              */
+} sloam_landmarks;
+
+/* Cylinder model (CylinderParameters, cylinder.h:8-17) */
+typedef struct sloam_cylinder {
+  double  root[3];
+  double  ray[3];
+  double  radius;
+  int32_t id;              /* tree id (vertex[2].treeId)                  */
+  int32_t valid;
+} sloam_cylinder;
+
+/* Plane model (PlaneParameters, plane.h:13-18) */
+typedef struct sloam_plane {
+  double  plane[4];        /* n (unit), d                                 */
+  double  centroid[3];
+  int32_t bin;             /* r_bin * theta_bins + t_bin                  */
+  int32_t valid;
+} sloam_plane;
+
+/* ------------------------------------------------------------- context */
+typedef struct sloam_ctx sloam_ctx;
+
+/* Creates a context on `device`.  Replaces the construction of
+ * seg::Segmentation (inference.cpp:5-19), Instance (trellis.cpp:13) and
+ * sloam::sloam (sloam.cpp:6-12) state owned by SLOAMNode (sloamNode.cpp:57-118).
+ * Returns NULL and sets *status on failure. */
+sloam_ctx* sloam_create(const sloam_params* params, int device, int* status);
+void       sloam_destroy(sloam_ctx* ctx);
+/* Copies the last error message (NUL-terminated) into buf. */
+int        sloam_last_error(const sloam_ctx* ctx, char* buf, size_t n);
+/* Resets the per-sequence state (firstScan_, prevGPlanes_; sloam.cpp:9-10). */
+int        sloam_reset(sloam_ctx* ctx);
+/* Replaces the parameters (sloam::sloam::setFmParams, sloam.h:77). */
+int        sloam_set_params(sloam_ctx* ctx, const sloam_params* params);
+
+/* ------------------------------------------ a1/a2: projection + masking */
+/* Segmentation::_doProjection (inference.cpp:80-165) followed by
+ * Segmentation::maskCloud (inference.cpp:230-273) for val = 1 (ground list)
+ * and val = 255, dense (organised tree cloud, destaggered per
+ * inference.cpp:200-228).  Input is n = H*W points, packed x,y,z,intensity.
+ * Labels come either as a per-pixel mask image (the network output, codes
+ * 0/1/255, `mask_image` non-NULL) or as per-point labels (`point_labels`
+ * non-NULL): the mask of a pixel is then the label of the point that wins the
+ * pixel (the nearest).  Any output pointer may be NULL.
+ *   px, py       [n]     pixel of each point (proj_xs/proj_ys)
+ *   range_image  [H*W]   range of the winning point, 0 where empty
+ *   mask_out     [H*W]   mask used
+ *   ground_idx   [n]     indices of ground points, point order; *n_ground
+ *   tree_cloud   [H*W*4] organised tree cloud, NaN xyz where not tree   */
+typedef struct sloam_scan_out {
+  int32_t* px;
+  int32_t* py;
+  float*   range_image;
+  uint8_t* mask_out;
+  int32_t* ground_idx;
+  int32_t  n_ground;
+  float*   tree_cloud;
+} sloam_scan_out;
+
+int sloam_project_mask(sloam_ctx* ctx, const float* xyzi, int32_t n,
+                       const uint8_t* point_labels, const uint8_t* mask_image,
+                       sloam_scan_out* out);
+
+/* ------------------------------------------------ a3-a5: Trellis       */
+/* Instance::computeGraph (trellis.cpp:134-139): organised connected
+ * components (trellis.cpp:15-43) + per-beam vertices (trellis.cpp:45-132).
+ * tree_cloud is the organised H*W cloud (x,y,z,i; NaN = no tree).
+ * cc_labels [H*W] (may be NULL) receives the component label of each pixel
+ * (0xFFFFFFFF where not finite); *n_components the number of components. */
+int sloam_trellis(sloam_ctx* ctx, const float* tree_cloud, int32_t H, int32_t W,
+                  uint32_t* cc_labels, int32_t* n_components,
+                  sloam_landmarks* out);
+
+/* --------------------------------------- a6-a8: ground planes, cylinders */
+/* sloam::computeModels (sloam.cpp:388-436): ground binning
+ * (sloam.cpp:330-386), Plane (plane.cpp:3-17,96-128) with the angle/height
+ * gates, then per landmark the nearest plane and Cylinder
+ * (cylinder.cpp:3-173).  Outputs the valid planes and valid cylinders in
+ * reference order; cyl_features [cap_cyl*features_per_tree*4] receives the
+ * F features of each valid cylinder (may be NULL). */
+typedef struct sloam_models_out {
+  int32_t         cap_planes, cap_cylinders;
+  int32_t         n_planes, n_cylinders;
+  sloam_plane*    planes;
+  sloam_cylinder* cylinders;
+  float*          cyl_features;
+  int32_t*        cyl_inliers;    /* [cap_cyl] best RANSAC inlier count (mode 1:
+                                     point cylinder, else vertex line) */
+} sloam_models_out;
+
+int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose_estimate,
+                         const float* ground_xyzi, int32_t n_ground,
+                         const sloam_landmarks* landmarks,
+                         sloam_models_out* out);
+
+/* --------------------------------------------- a9-a11: RunSloam        */
+/* sloam::sloam::RunSloam (sloam.cpp:453-532): computeModels, first-scan
+ * logic, matchFeatures (sloam.cpp:257-296), OptimizePose /
+ * TwoStepOptimizePose (sloam.cpp:33-255), projectModels (sloam.cpp:438-451)
+ * and matchModels (sloam.cpp:298-328).  Keeps firstScan_ / prevGPlanes_ in
+ * the context like the reference object.
+ *   map       [n_map]  submap cylinders (SloamInput::mapModels, map frame)
+ *   out->matches [cap_cylinders]  index into map or -1 (SloamOutput::matches)
+ *   out->models.cylinders          SloamOutput::tm (map frame)
+ * Returns SLOAM_OK on success; SLOAM_ERR_EMPTY_MAP / SLOAM_ERR_NO_MODELS /
+ * SLOAM_ERR_NOT_CONVERGED where the reference returns false. */
+typedef struct sloam_run_out {
+  sloam_models_out models;       /* tm (projected) + current planes        */
+  int32_t*  matches;             /* [models.cap_cylinders]                 */
+  sloam_se3 T_Map_Curr;
+  sloam_se3 T_Delta;
+  int32_t   success;
+  int32_t   first_scan;
+  int32_t   n_tree_matches;      /* feature matches (residuals), trees     */
+  int32_t   n_plane_matches;     /* feature matches (residuals), planes    */
+  int32_t   tree_check, ground_check;
+} sloam_run_out;
+
+int sloam_run(sloam_ctx* ctx, const sloam_se3* pose_estimate,
+              const float* ground_xyzi, int32_t n_ground,
+              const sloam_landmarks* landmarks,
+              const sloam_cylinder* map, int32_t n_map,
+              sloam_run_out* out);
+
+/* ---------------------------------------------- whole keyframe          */
+/* SLOAMNode::run (sloamNode.cpp:186-282) minus the ROS publishing, the
+ * segmentation network and the map manager: projection + masking, Trellis,
+ * RunSloam on one scan, all on the device in one CUDA graph.  pose_estimate
+ * is prevKeyPose * initialGuess; map is the submap the map manager supplies. */
+int sloam_keyframe(sloam_ctx* ctx, const float* xyzi, int32_t n,
+                   const uint8_t* point_labels, const uint8_t* mask_image,
+                   const sloam_se3* pose_estimate,
+                   const sloam_cylinder* map, int32_t n_map,
+                   sloam_run_out* out);
+
+/* Device-resident variant for batch throughput: every pointer is a device
+ * pointer; nkf scans of n points each are processed back to back on the
+ * context stream with the same pose estimate and submap; per-keyframe pose
+ * (7 doubles: q xyzw, t), success and cylinder count land in device arrays. */
+int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32_t n,
+                           int32_t nkf, const uint8_t* d_point_labels,
+                           const sloam_se3* pose_estimate,
+                           const sloam_cylinder* d_map, int32_t n_map,
+                           double* d_pose_out, int32_t* d_success_out,
+                           int32_t* d_ncyl_out);
+
+/* Returns the number of kernels launched by the last call (for accounting). */
+int64_t sloam_last_launch_count(const sloam_ctx* ctx);
+
+/* The CUDA stream the context runs on (as void*). */
+void* sloam_stream(sloam_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLOAM_GB300_H */
