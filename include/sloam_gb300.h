@@ -130,6 +130,12 @@ typedef struct sloam_landmarks {
   int32_t* vertex_row;     /* [cap_vertices]                              */
   int32_t* point_begin;    /* [cap_vertices+1]                            */
   float*   point_xyzi;     /* [cap_points*4]                              */
+  /* optional: every point of each landmark's connected component in raster
+   * order (cluster_begin[cap_landmarks+1]), used by the point-level
+   * cylinder fit; NULL pointers = not requested / not provided */
+  int32_t  cap_cluster, n_cluster;
+  int32_t* cluster_begin;
+  float*   cluster_xyzi;   /* [cap_cluster*4]                             */
 } sloam_landmarks;
 
 /* Cylinder model (CylinderParameters, cylinder.h:8-17) */
@@ -265,13 +271,16 @@ int sloam_keyframe(sloam_ctx* ctx, const float* xyzi, int32_t n,
                    const sloam_cylinder* map, int32_t n_map,
                    sloam_run_out* out);
 
-/* Device-resident variant for batch throughput: every pointer is a device
- * pointer; nkf scans of n points each are processed back to back on the
- * context stream with the same pose estimate and submap; per-keyframe pose
- * (7 doubles: q xyzw, t), success and cylinder count land in device arrays. */
+/* Device-resident batch for throughput.  d_xyzi / d_point_labels / d_map
+ * and the three outputs are device pointers; pose_estimates is a host array
+ * of nkf poses.  The nkf scans (n points each, back to back) are processed
+ * as independent non-first keyframes against the same submap and the
+ * context's previous-scan planes; the context state is not advanced (the
+ * context must have seen a first scan).  Per keyframe: T_Map_Curr (7
+ * doubles: q xyzw, t), the success flag and the number of valid cylinders. */
 int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32_t n,
                            int32_t nkf, const uint8_t* d_point_labels,
-                           const sloam_se3* pose_estimate,
+                           const sloam_se3* pose_estimates,
                            const sloam_cylinder* d_map, int32_t n_map,
                            double* d_pose_out, int32_t* d_success_out,
                            int32_t* d_ncyl_out);

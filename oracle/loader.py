@@ -44,19 +44,17 @@ def lib():
                                       C.POINTER(A.ScanOut)]
     L.oracle_trellis.argtypes = [C.POINTER(A.Params), C.POINTER(C.c_float), C.c_int32, C.c_int32,
                                  C.c_int, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
-                                 C.POINTER(A.Landmarks), C.POINTER(C.c_int32),
-                                 C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_int32)]
+                                 C.POINTER(A.Landmarks)]
     L.oracle_create.restype = vp
     L.oracle_create.argtypes = [C.POINTER(A.Params)]
     L.oracle_destroy.argtypes = [vp]
     L.oracle_set_params.argtypes = [vp, C.POINTER(A.Params)]
     L.oracle_reset.argtypes = [vp]
     L.oracle_compute_models.argtypes = [vp, C.POINTER(A.SE3), C.POINTER(C.c_float), C.c_int32,
-                                        C.POINTER(A.Landmarks), C.POINTER(C.c_int32),
-                                        C.POINTER(C.c_float), C.POINTER(A.ModelsOut)]
+                                        C.POINTER(A.Landmarks), C.POINTER(A.ModelsOut)]
     L.oracle_run.argtypes = [vp, C.POINTER(A.SE3), C.POINTER(C.c_float), C.c_int32,
-                             C.POINTER(A.Landmarks), C.POINTER(C.c_int32), C.POINTER(C.c_float),
-                             C.POINTER(A.Cylinder), C.c_int32, C.POINTER(A.RunOut)]
+                             C.POINTER(A.Landmarks), C.POINTER(A.Cylinder), C.c_int32,
+                             C.POINTER(A.RunOut)]
     L.oracle_keyframe.argtypes = [vp, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_uint8),
                                   C.POINTER(C.c_uint8), C.POINTER(A.SE3), C.POINTER(A.Cylinder),
                                   C.c_int32, C.POINTER(A.RunOut)]

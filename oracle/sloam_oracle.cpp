@@ -1433,9 +1433,10 @@ CylObj cyl_from(const sloam_cylinder& c) {
   return o;
 }
 
-std::vector<std::vector<Pt>> read_clusters(const sloam_landmarks* lm, const int32_t* cb,
-                                           const float* cx) {
+std::vector<std::vector<Pt>> read_clusters(const sloam_landmarks* lm) {
   std::vector<std::vector<Pt>> cl;
+  const int32_t* cb = lm->cluster_begin;
+  const float* cx = lm->cluster_xyzi;
   if (!cb || !cx) return cl;
   cl.resize(lm->n_landmarks);
   for (int l = 0; l < lm->n_landmarks; ++l)
@@ -1524,8 +1525,7 @@ int oracle_project_mask(const sloam_params* p, const float* xyzi, int32_t n,
 
 int oracle_trellis(const sloam_params* p, const float* tree_cloud, int32_t H, int32_t W,
                    int sort_variant, int radius_half, uint32_t* cc_labels,
-                   int32_t* n_components, sloam_landmarks* out, int32_t* cluster_begin,
-                   float* cluster_xyzi, int32_t cap_cluster, int32_t* n_cluster) {
+                   int32_t* n_components, sloam_landmarks* out) {
   std::vector<uint32_t> labels;
   std::vector<std::vector<int>> li;
   organized_cc(tree_cloud, H, W, p->cc_dist_threshold, labels, li);
@@ -1535,19 +1535,20 @@ int oracle_trellis(const sloam_params* p, const float* tree_cloud, int32_t H, in
   std::vector<int> tl;
   find_trees(*p, tree_cloud, H, W, labels, li, sort_variant, radius_half != 0, trees, tl);
   int st = write_landmarks(trees, out);
-  if (cluster_begin) {
+  out->n_cluster = 0;
+  if (out->cluster_begin && st == SLOAM_OK) {
     int k = 0;
     for (size_t l = 0; l < tl.size(); ++l) {
-      cluster_begin[l] = k;
+      out->cluster_begin[l] = k;
       for (int idx : li[tl[l]]) {
-        if (k < cap_cluster && cluster_xyzi)
-          std::memcpy(cluster_xyzi + 4 * (size_t)k, tree_cloud + 4 * (size_t)idx, 16);
+        if (k < out->cap_cluster && out->cluster_xyzi)
+          std::memcpy(out->cluster_xyzi + 4 * (size_t)k, tree_cloud + 4 * (size_t)idx, 16);
         ++k;
       }
     }
-    cluster_begin[tl.size()] = k;
-    if (n_cluster) *n_cluster = k;
-    if (k > cap_cluster) st = SLOAM_ERR_CAPACITY;
+    out->cluster_begin[tl.size()] = k;
+    out->n_cluster = k;
+    if (k > out->cap_cluster) st = SLOAM_ERR_CAPACITY;
   }
   return st;
 }
@@ -1565,28 +1566,27 @@ void oracle_reset(oracle_state* s) {
 }
 
 int oracle_compute_models(oracle_state* s, const sloam_se3* pose, const float* g,
-                          int32_t ng, const sloam_landmarks* lm, const int32_t* cb,
-                          const float* cx, sloam_models_out* out) {
+                          int32_t ng, const sloam_landmarks* lm, sloam_models_out* out) {
   std::vector<Tree> trees = read_landmarks(lm);
-  auto cl = read_clusters(lm, cb, cx);
+  auto cl = read_clusters(lm);
   std::vector<PlaneObj> planes;
   std::vector<CylObj> cyls;
-  compute_models(s->P, se3_from(*pose), g, ng, trees, cb ? &cl : nullptr, planes, cyls);
+  compute_models(s->P, se3_from(*pose), g, ng, trees, cl.empty() ? nullptr : &cl, planes, cyls);
   int st = SLOAM_OK;
   write_models(s->P, planes, cyls, out, st);
   return st;
 }
 
 int oracle_run(oracle_state* s, const sloam_se3* pose_in, const float* g, int32_t ng,
-               const sloam_landmarks* lm, const int32_t* cb, const float* cx,
-               const sloam_cylinder* map_in, int32_t n_map, sloam_run_out* out) {
+               const sloam_landmarks* lm, const sloam_cylinder* map_in, int32_t n_map,
+               sloam_run_out* out) {
   const sloam_params& P = s->P;
   std::vector<Tree> trees = read_landmarks(lm);
-  auto cl = read_clusters(lm, cb, cx);
+  auto cl = read_clusters(lm);
   std::vector<PlaneObj> planes;
   std::vector<CylObj> cyls;
   SE3 pose = se3_from(*pose_in);
-  compute_models(P, pose, g, ng, trees, cb ? &cl : nullptr, planes, cyls);
+  compute_models(P, pose, g, ng, trees, cl.empty() ? nullptr : &cl, planes, cyls);
   out->first_scan = s->firstScan ? 1 : 0;
   out->T_Delta = se3_identity();
   out->n_tree_matches = out->n_plane_matches = 0;
@@ -1718,8 +1718,10 @@ int oracle_keyframe(oracle_state* s, const float* xyzi, int32_t n, const uint8_t
     }
   }
   cb[tl.size()] = k;
-  return oracle_run(s, pose, ground.data(), so.n_ground, &lm, cb.data(), cx.data(), map, n_map,
-                    out);
+  lm.cap_cluster = lm.n_cluster = k;
+  lm.cluster_begin = cb.data();
+  lm.cluster_xyzi = cx.data();
+  return oracle_run(s, pose, ground.data(), so.n_ground, &lm, map, n_map, out);
 }
 
 int oracle_plane(const sloam_params* p, const float* xyzi, int32_t n, sloam_plane* out,

@@ -40,14 +40,12 @@ int oracle_project_mask(const sloam_params* p, const float* xyzi, int32_t n,
  * (z, y, x, column); ORACLE_LIBM runs std::sort x, y, z like trellis.cpp.
  * radius_half: 1 stores 0.5*|first-last| (the convention of the reference's
  * stored fixtures), 0 the current formula |first-last| (trellis.cpp:96-99).
- * cluster_* (may be NULL): every point of each landmark's CC cluster in
- * raster order, for the point-level cylinder fit. */
+ * out->cluster_* (may be NULL): every point of each landmark's CC cluster
+ * in raster order, for the point-level cylinder fit. */
 int oracle_trellis(const sloam_params* p, const float* tree_cloud, int32_t H,
                    int32_t W, int sort_variant, int radius_half,
                    uint32_t* cc_labels, int32_t* n_components,
-                   sloam_landmarks* out, int32_t* cluster_begin,
-                   float* cluster_xyzi, int32_t cap_cluster,
-                   int32_t* n_cluster);
+                   sloam_landmarks* out);
 
 typedef struct oracle_state oracle_state;
 oracle_state* oracle_create(const sloam_params* p);
@@ -55,18 +53,15 @@ void          oracle_destroy(oracle_state* s);
 void          oracle_set_params(oracle_state* s, const sloam_params* p);
 void          oracle_reset(oracle_state* s);
 
-/* computeModels (sloam.cpp:388-436).  cluster_* may be NULL (mode 1 then
- * fits the landmark's vertex points). */
+/* computeModels (sloam.cpp:388-436).  Without lm->cluster_* the point-level
+ * cylinder fit uses the landmark's vertex points. */
 int oracle_compute_models(oracle_state* s, const sloam_se3* pose,
                           const float* ground_xyzi, int32_t n_ground,
-                          const sloam_landmarks* lm,
-                          const int32_t* cluster_begin,
-                          const float* cluster_xyzi, sloam_models_out* out);
+                          const sloam_landmarks* lm, sloam_models_out* out);
 
 /* RunSloam (sloam.cpp:453-532). */
 int oracle_run(oracle_state* s, const sloam_se3* pose, const float* ground_xyzi,
                int32_t n_ground, const sloam_landmarks* lm,
-               const int32_t* cluster_begin, const float* cluster_xyzi,
                const sloam_cylinder* map, int32_t n_map, sloam_run_out* out);
 
 /* Whole keyframe: projection + mask, Trellis, RunSloam. */

@@ -185,6 +185,9 @@ class Landmarks(C.Structure):
         ("vertex_row", C.POINTER(C.c_int32)),
         ("point_begin", C.POINTER(C.c_int32)),
         ("point_xyzi", C.POINTER(C.c_float)),
+        ("cap_cluster", C.c_int32), ("n_cluster", C.c_int32),
+        ("cluster_begin", C.POINTER(C.c_int32)),
+        ("cluster_xyzi", C.POINTER(C.c_float)),
     ]
 
 
@@ -238,7 +241,7 @@ def ptr(a, ctype):
 class LandmarkBuffers:
     """numpy storage behind a Landmarks struct (cap_* sized)."""
 
-    def __init__(self, cap_lm=1024, cap_v=1024 * 56, cap_p=1 << 20):
+    def __init__(self, cap_lm=1024, cap_v=1024 * 56, cap_p=1 << 20, cap_cluster=0):
         self.tree_id = np.zeros(cap_lm, np.int32)
         self.vertex_begin = np.zeros(cap_lm + 1, np.int32)
         self.vertex_xyz = np.zeros(cap_v * 3, np.float32)
@@ -255,7 +258,20 @@ class LandmarkBuffers:
         s.vertex_row = ptr(self.vertex_row, C.c_int32)
         s.point_begin = ptr(self.point_begin, C.c_int32)
         s.point_xyzi = ptr(self.point_xyzi, C.c_float)
+        if cap_cluster > 0:
+            self.cluster_begin = np.zeros(cap_lm + 1, np.int32)
+            self.cluster_xyzi = np.zeros(cap_cluster * 4, np.float32)
+            s.cap_cluster = cap_cluster
+            s.cluster_begin = ptr(self.cluster_begin, C.c_int32)
+            s.cluster_xyzi = ptr(self.cluster_xyzi, C.c_float)
         self.s = s
+
+    def clusters(self):
+        s = self.s
+        if not s.cluster_begin:
+            return None
+        return [self.cluster_xyzi[4 * self.cluster_begin[l]:4 * self.cluster_begin[l + 1]].reshape(-1, 4)
+                for l in range(s.n_landmarks)]
 
     @staticmethod
     def from_trees(trees):

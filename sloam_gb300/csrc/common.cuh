@@ -1,0 +1,271 @@
+// common.cuh — device helpers shared by the SLOAM kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/sloam_gb300.h"
+
+#define SLOAM_HD __host__ __device__ __forceinline__
+#define SLOAM_D __device__ __forceinline__
+
+namespace sg {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr double kPIDEF = 3.14159265;  // definitions.h:28
+
+// ---------------------------------------------------------- exact float ops
+// Bit-exact paths use these so nvcc never contracts them into FMA: they are
+// IEEE single operations with round-to-nearest, like the host's SSE/NEON code
+// built with -ffp-contract=off.
+SLOAM_D float fadd(float a, float b) { return __fadd_rn(a, b); }
+SLOAM_D float fsub(float a, float b) { return __fsub_rn(a, b); }
+SLOAM_D float fmul(float a, float b) { return __fmul_rn(a, b); }
+SLOAM_D float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+SLOAM_D float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// pcl::euclideanDistance: sqrt((dx*dx + dy*dy) + dz*dz), float.
+SLOAM_D float pcl_euclid(float ax, float ay, float az, float bx, float by, float bz) {
+  float dx = fsub(bx, ax), dy = fsub(by, ay), dz = fsub(bz, az);
+  return fsqrt(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+}
+// Eigen Vector3f (a-b).squaredNorm(): dx*dx + (dy*dy + dz*dz).
+SLOAM_D float eigen_sqnorm3(float ax, float ay, float az, float bx, float by, float bz) {
+  float dx = fsub(ax, bx), dy = fsub(ay, by), dz = fsub(az, bz);
+  return fadd(fmul(dx, dx), fadd(fmul(dy, dy), fmul(dz, dz)));
+}
+
+// Orderable key of a float range (range >= 0 or NaN): NaN sorts last.
+SLOAM_D uint32_t range_key(float r) {
+  return isnan(r) ? 0x7fc00000u : __float_as_uint(r);
+}
+
+// ------------------------------------------------------------------- RNG
+// Philox4x32-10 (Salmon et al., SC'11).  key = seed, counter = 4 words.
+SLOAM_HD void philox(uint64_t key64, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                     uint32_t out[4]) {
+  uint32_t k0 = (uint32_t)key64, k1 = (uint32_t)(key64 >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    uint32_t n1 = (uint32_t)p1;
+    uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    uint32_t n3 = (uint32_t)p0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+SLOAM_HD uint32_t mulhi_idx(uint32_t u, uint32_t n) {
+  return (uint32_t)(((uint64_t)u * n) >> 32);
+}
+// k (<= 3) distinct indices in [0, n) from one Philox block.
+SLOAM_HD void draw_distinct(const uint32_t u[4], uint32_t n, int k, uint32_t* idx) {
+  uint32_t a = mulhi_idx(u[0], n);
+  idx[0] = a;
+  if (k < 2) return;
+  uint32_t b = mulhi_idx(u[1], n - 1);
+  if (b >= a) ++b;
+  idx[1] = b;
+  if (k < 3) return;
+  uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+  uint32_t c = mulhi_idx(u[2], n - 2);
+  if (c >= lo) ++c;
+  if (c >= hi) ++c;
+  idx[2] = c;
+}
+
+// --------------------------------------------------------- warp helpers
+SLOAM_D float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+SLOAM_D double warp_sumd(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+SLOAM_D int warp_sumi(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// argmin over (value, index): smallest value, then smallest index.
+SLOAM_D void warp_argmin(double& v, int& i) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    int oi = __shfl_xor_sync(0xffffffffu, i, o);
+    if (ov < v || (ov == v && oi < i) || (isnan(v) && !isnan(ov))) {
+      v = ov;
+      i = oi;
+    }
+  }
+}
+
+// ------------------------------------------------------------ FP64 algebra
+struct d3 {
+  double x, y, z;
+};
+SLOAM_HD d3 mk3(double x, double y, double z) { return d3{x, y, z}; }
+SLOAM_HD d3 add3(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+SLOAM_HD d3 sub3(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+SLOAM_HD d3 scl3(double s, d3 a) { return {s * a.x, s * a.y, s * a.z}; }
+SLOAM_HD double dot3(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SLOAM_HD d3 cross3(d3 a, d3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+SLOAM_HD double norm3(d3 a) { return sqrt(dot3(a, a)); }
+
+struct Pose {  // rotation (row-major) + translation, FP64
+  double R[9];
+  d3 t;
+};
+SLOAM_HD Pose pose_from(const sloam_se3& p) {
+  double x = p.q[0], y = p.q[1], z = p.q[2], w = p.q[3];
+  double n = sqrt(x * x + y * y + z * z + w * w);
+  x /= n; y /= n; z /= n; w /= n;
+  Pose T;
+  T.R[0] = 1 - 2 * (y * y + z * z); T.R[1] = 2 * (x * y - w * z); T.R[2] = 2 * (x * z + w * y);
+  T.R[3] = 2 * (x * y + w * z); T.R[4] = 1 - 2 * (x * x + z * z); T.R[5] = 2 * (y * z - w * x);
+  T.R[6] = 2 * (x * z - w * y); T.R[7] = 2 * (y * z + w * x); T.R[8] = 1 - 2 * (x * x + y * y);
+  T.t = {p.t[0], p.t[1], p.t[2]};
+  return T;
+}
+SLOAM_HD d3 rot3(const double* R, d3 p) {
+  return {R[0] * p.x + R[1] * p.y + R[2] * p.z, R[3] * p.x + R[4] * p.y + R[5] * p.z,
+          R[6] * p.x + R[7] * p.y + R[8] * p.z};
+}
+SLOAM_HD d3 xform(const Pose& T, d3 p) { return add3(rot3(T.R, p), T.t); }
+SLOAM_HD void quat_from_R(const double* R, double* q) {
+  double tr = R[0] + R[4] + R[8];
+  double x, y, z, w;
+  if (tr > 0) {
+    double s = sqrt(tr + 1.0) * 2;
+    w = 0.25 * s; x = (R[7] - R[5]) / s; y = (R[2] - R[6]) / s; z = (R[3] - R[1]) / s;
+  } else if (R[0] > R[4] && R[0] > R[8]) {
+    double s = sqrt(1.0 + R[0] - R[4] - R[8]) * 2;
+    w = (R[7] - R[5]) / s; x = 0.25 * s; y = (R[1] + R[3]) / s; z = (R[2] + R[6]) / s;
+  } else if (R[4] > R[8]) {
+    double s = sqrt(1.0 + R[4] - R[0] - R[8]) * 2;
+    w = (R[2] - R[6]) / s; x = (R[1] + R[3]) / s; y = 0.25 * s; z = (R[5] + R[7]) / s;
+  } else {
+    double s = sqrt(1.0 + R[8] - R[0] - R[4]) * 2;
+    w = (R[3] - R[1]) / s; x = (R[2] + R[6]) / s; y = (R[5] + R[7]) / s; z = 0.25 * s;
+  }
+  double n = sqrt(x * x + y * y + z * z + w * w);
+  q[0] = x / n; q[1] = y / n; q[2] = z / n; q[3] = w / n;
+}
+SLOAM_HD sloam_se3 pose_to(const Pose& T) {
+  sloam_se3 o;
+  quat_from_R(T.R, o.q);
+  o.t[0] = T.t.x; o.t[1] = T.t.y; o.t[2] = T.t.z;
+  return o;
+}
+SLOAM_HD void matmul3(const double* A, const double* B, double* C) {
+  double T[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      T[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] + A[3 * i + 2] * B[6 + j];
+  for (int k = 0; k < 9; ++k) C[k] = T[k];
+}
+SLOAM_HD void so3_exp(d3 w, double* R) {
+  double th2 = dot3(w, w), th = sqrt(th2);
+  double A, B;
+  if (th2 < 1e-24) {
+    A = 1.0; B = 0.5;
+  } else {
+    A = sin(th) / th;
+    B = (1.0 - cos(th)) / th2;
+  }
+  double K[9] = {0, -w.z, w.y, w.z, 0, -w.x, -w.y, w.x, 0}, K2[9];
+  matmul3(K, K, K2);
+  for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0 ? 1.0 : 0.0) + A * K[i] + B * K2[i];
+}
+
+// Symmetric 3x3 eigen-decomposition, cyclic Jacobi (FP64); eigenvalues
+// ascending, eigenvectors as columns of V.
+SLOAM_HD void jacobi3(const double* A_in, double* evals, double* V) {
+  double A[9];
+  for (int i = 0; i < 9; ++i) A[i] = A_in[i];
+  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 32; ++sweep) {
+    double off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+    double diag = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
+    if (off <= 1e-300 || off <= diag * 1e-32) break;
+    for (int p = 0; p < 2; ++p) {
+      for (int q = p + 1; q < 3; ++q) {
+        double apq = A[3 * p + q];
+        if (apq == 0.0) continue;
+        double app = A[3 * p + p], aqq = A[3 * q + q];
+        double theta = (aqq - app) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; ++k) {
+          double akp = A[3 * k + p], akq = A[3 * k + q];
+          A[3 * k + p] = c * akp - s * akq;
+          A[3 * k + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double apk = A[3 * p + k], aqk = A[3 * q + k];
+          A[3 * p + k] = c * apk - s * aqk;
+          A[3 * q + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          double vkp = V[3 * k + p], vkq = V[3 * k + q];
+          V[3 * k + p] = c * vkp - s * vkq;
+          V[3 * k + q] = s * vkp + c * vkq;
+        }
+      }
+    }
+  }
+  double d[3] = {A[0], A[4], A[8]};
+  int o0 = 0, o1 = 1, o2 = 2, tmp;
+  if (d[o1] < d[o0]) { tmp = o0; o0 = o1; o1 = tmp; }
+  if (d[o2] < d[o1]) { tmp = o1; o1 = o2; o2 = tmp; }
+  if (d[o1] < d[o0]) { tmp = o0; o0 = o1; o1 = tmp; }
+  int ord[3] = {o0, o1, o2};
+  double Vs[9];
+  for (int c = 0; c < 3; ++c) {
+    evals[c] = d[ord[c]];
+    for (int r = 0; r < 3; ++r) Vs[3 * r + c] = V[3 * r + ord[c]];
+  }
+  for (int i = 0; i < 9; ++i) V[i] = Vs[i];
+}
+
+// Cholesky solve of an n x n SPD system (n <= 6, row-major).
+SLOAM_HD bool chol_solve(int n, const double* H, const double* b, double* x) {
+  double L[36];
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j <= i; ++j) {
+      double s = H[i * n + j];
+      for (int k = 0; k < j; ++k) s -= L[i * n + k] * L[j * n + k];
+      if (i == j) {
+        if (!(s > 0.0)) return false;
+        L[i * n + i] = sqrt(s);
+      } else {
+        L[i * n + j] = s / L[j * n + j];
+      }
+    }
+  }
+  double y[6];
+  for (int i = 0; i < n; ++i) {
+    double s = b[i];
+    for (int k = 0; k < i; ++k) s -= L[i * n + k] * y[k];
+    y[i] = s / L[i * n + i];
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = y[i];
+    for (int k = i + 1; k < n; ++k) s -= L[k * n + i] * x[k];
+    x[i] = s / L[i * n + i];
+  }
+  for (int i = 0; i < n; ++i)
+    if (!isfinite(x[i])) return false;
+  return true;
+}
+
+}  // namespace sg

@@ -1,0 +1,878 @@
+// context.cu — the C ABI (include/sloam_gb300.h): context life cycle, the
+// device arena, host<->device staging, the exact boundary tables, CUDA-graph
+// capture of the keyframe pipeline, and the stage entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+using namespace sg;
+
+// ------------------------------------------------------------- parameters
+extern "C" void sloam_params_default(sloam_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->scans_per_sweep = 1;
+  p->min_tree_models = 5;
+  p->min_ground_models = 36;
+  p->max_lidar_dist = 20.0;
+  p->max_ground_lidar_dist = 25.0;
+  p->min_ground_lidar_dist = 5.0;
+  p->two_step_optim = 1;
+  p->ground_radii_bins = 2;
+  p->ground_theta_bins = 18;
+  p->ground_retain_thresh = 0.05;
+  p->ground_match_thresh = 1.0;
+  p->rough_tree_match_thresh = 2.5;
+  p->tree_match_thresh = 0.5;
+  p->max_tree_radius = 0.3;
+  p->max_axis_theta = 10.0;
+  p->max_focus_outlier_distance = 0.5;
+  p->add_new_tree_thresh_dist = 1.5;
+  p->features_per_tree = 20;
+  p->num_ground_features = 5;
+  p->default_tree_radius = 0.2;
+  p->min_planes = 0.1 * 2 * 18;
+  p->beam_cluster_threshold = 0.5f;
+  p->max_dist_to_centroid = 0.2f;
+  p->min_vertex_size = 4;
+  p->min_landmark_size = 5;
+  p->min_landmark_height = 1.0f;
+  p->fov_up_deg = 22.5f;
+  p->fov_down_deg = -22.5f;
+  p->img_w = 2048;
+  p->img_h = 64;
+  p->do_destagger = 1;
+  p->cc_dist_threshold = 1.0f;
+  p->trellis_min_cluster = 80;
+  p->trellis_min_beam_points = 3;
+  p->trellis_min_vertices = 16;
+  p->trellis_max_vertices = 56;
+  p->line_ransac_thresh = 0.25;
+  p->line_ransac_max_iter = 50;
+  p->line_ransac_probability = 0.99;
+  p->min_tree_height_sq = 1.5;
+  p->root_plane_max_dist = 2.0;
+  p->plane_match_thresh = 1.0;
+  p->huber_delta = 0.1;
+  p->seed = 0;
+  p->cyl_mode = 0;
+  p->cyl_hypotheses = 256;
+  p->cyl_inlier_thresh = 0.03f;
+  p->cyl_ls_iters = 3;
+  p->cyl_max_hyp_radius = 1.0f;
+  p->gn_iters = 10;
+  p->max_landmarks = 1024;
+  p->max_map = 4096;
+  p->max_ground = 0;
+}
+
+// sizeof() of every ABI struct, for binding checks.
+extern "C" int sloam_abi_sizes(int32_t* out, int n) {
+  const int32_t s[] = {(int32_t)sizeof(sloam_params), (int32_t)sizeof(sloam_se3),
+                       (int32_t)sizeof(sloam_landmarks), (int32_t)sizeof(sloam_cylinder),
+                       (int32_t)sizeof(sloam_plane), (int32_t)sizeof(sloam_scan_out),
+                       (int32_t)sizeof(sloam_models_out), (int32_t)sizeof(sloam_run_out)};
+  const int k = (int)(sizeof(s) / sizeof(s[0]));
+  for (int i = 0; i < k && i < n; ++i) out[i] = s[i];
+  return k;
+}
+
+namespace sg {
+
+// ------------------------------------------------------ boundary tables
+namespace {
+int32_t f2o(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (u & 0x80000000u) ? -(int32_t)(u & 0x7fffffffu) : (int32_t)u;
+}
+float o2f(int32_t o) {
+  uint32_t u = o < 0 ? (0x80000000u | (uint32_t)(-o)) : (uint32_t)o;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+// smallest float v in [lo, hi] with g(v) >= k (g non-decreasing); hi if none
+template <typename G>
+float first_at_least(G g, int k, float lo, float hi) {
+  int32_t a = f2o(lo), b = f2o(hi);
+  if (g(o2f(a)) >= k) return o2f(a);
+  if (g(o2f(b)) < k) return o2f(b);
+  while (b - a > 1) {
+    const int32_t m = a + (b - a) / 2;
+    if (g(o2f(m)) >= k) b = m;
+    else a = m;
+  }
+  return o2f(b);
+}
+inline float ref_min(float a, float b) { return (b < a) ? b : a; }
+inline float ref_max(float a, float b) { return (a < b) ? b : a; }
+}  // namespace
+
+// Column of a float yaw exactly as inference.cpp:111-121 computes it.
+void build_px_table(const sloam_params& p, float* tab) {
+  const int W = p.img_w;
+  auto col = [W](float yaw) {
+    float proj_x = 0.5 * (yaw / M_PI + 1.0);
+    proj_x *= W;
+    proj_x = std::floor(proj_x);
+    proj_x = ref_min(W - 1.0f, proj_x);
+    proj_x = ref_max(0.0f, proj_x);
+    return (int)proj_x;
+  };
+  tab[0] = -INFINITY;
+  for (int k = 1; k < W; ++k) tab[k] = first_at_least(col, k, -4.0f, 4.0f);
+  tab[W] = INFINITY;
+}
+
+// Theta and radius bins of sloam.cpp:346-357 as float boundary tables, and
+// the float window equivalent to r < maxG && r > minG in double.
+void build_ground_tables(const sloam_params& p, float* tb, float* rb, float* r_lo, float* r_hi) {
+  const int Rb = p.ground_radii_bins, Tb = p.ground_theta_bins;
+  const double maxG = p.max_ground_lidar_dist, minG = p.min_ground_lidar_dist;
+  auto tbin = [Tb](float th) {
+    int t = (int)std::floor((kPIDEF + (double)th) / (2 * kPIDEF / (double)Tb));
+    return std::max(0, std::min(t, Tb - 1));
+  };
+  auto rbin = [Rb, maxG](float r) {
+    int t = (int)std::floor((double)r / (maxG / (double)Rb));
+    return std::max(0, std::min(t, Rb - 1));
+  };
+  tb[0] = -INFINITY;
+  for (int k = 1; k < Tb; ++k) tb[k] = first_at_least(tbin, k, -4.0f, 4.0f);
+  tb[Tb] = INFINITY;
+  rb[0] = -INFINITY;
+  const float rmax = (float)maxG * 2.0f + 1.0f;
+  for (int k = 1; k < Rb; ++k) rb[k] = first_at_least(rbin, k, 0.0f, rmax);
+  rb[Rb] = INFINITY;
+  // r < maxG (double) <=> r <= hi ; r > minG <=> r >= lo
+  float hi = (float)maxG;
+  while ((double)hi >= maxG) hi = std::nextafter(hi, -INFINITY);
+  while ((double)std::nextafter(hi, INFINITY) < maxG) hi = std::nextafter(hi, INFINITY);
+  float lo = (float)minG;
+  while ((double)lo <= minG) lo = std::nextafter(lo, INFINITY);
+  while ((double)std::nextafter(lo, -INFINITY) > minG) lo = std::nextafter(lo, -INFINITY);
+  *r_lo = lo;
+  *r_hi = hi;
+}
+
+}  // namespace sg
+
+// ================================================================ context
+struct sloam_ctx {
+  sloam_params P;
+  KParams kp;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  Dev d{};
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  // pinned staging
+  Counters* h_cnt = nullptr;
+  double* h_pose = nullptr;     // 21 doubles
+  InPtrs* h_in = nullptr;       // per-keyframe input pointer blocks (batch)
+  double* h_poses = nullptr;    // per-keyframe estimates (batch)
+  int h_batch_cap = 0;
+  bool first_scan = true;
+  std::string err;
+  int64_t launches = 0;
+  int64_t last_launches = 0;
+  // graphs: [first][label mode][state update]
+  cudaGraphExec_t gx[2][2][2] = {};
+  int gx_launches[2][2][2] = {};
+};
+
+namespace {
+
+int fail(sloam_ctx* c, int code, const char* what, cudaError_t e = cudaSuccess) {
+  if (c) {
+    char buf[512];
+    if (e != cudaSuccess)
+      std::snprintf(buf, sizeof(buf), "%s: %s (%s)", what, cudaGetErrorName(e),
+                    cudaGetErrorString(e));
+    else
+      std::snprintf(buf, sizeof(buf), "%s", what);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                  \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return fail(ctx, SLOAM_ERR_CUDA, #call, e_); \
+  } while (0)
+
+struct Carver {
+  char* base;
+  size_t off = 0;
+  bool dry;
+  template <typename T>
+  T* take(size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = dry ? nullptr : reinterpret_cast<T*>(base + off);
+    off += sizeof(T) * std::max<size_t>(n, 1);
+    return p;
+  }
+};
+
+void carve(Dev& d, Carver& c, int n_blk) {
+  const int N = d.N;
+  d.in = c.take<InPtrs>(1);
+  d.buf_xyzi = c.take<float4>(N);
+  d.buf_plabel = c.take<uint8_t>(N);
+  d.buf_mask_in = c.take<uint8_t>(N);
+  d.pix = c.take<int32_t>(N);
+  d.pkey = c.take<unsigned long long>(N);
+  d.range_img = c.take<float>(N);
+  d.mask = c.take<uint8_t>(N);
+  d.tree = c.take<float4>(N);
+  d.gbits = c.take<uint32_t>((size_t)((N + 1023) / 1024) * 32 + 32);
+  d.blk = c.take<int32_t>(n_blk);
+  d.ground_idx = c.take<int32_t>(N);
+  d.ground = c.take<float4>(d.cap_ground);
+  d.px_tab = c.take<float>(d.W + 1);
+  d.tb_tab = c.take<float>(4096);
+  d.rb_tab = c.take<float>(4096);
+  d.parent = c.take<uint32_t>(N);
+  d.label = c.take<uint32_t>(N);
+  d.rank = c.take<uint32_t>(std::max(N, 4 * d.cap_cand));
+  d.comp_size = c.take<int32_t>(N);
+  d.comp_cmin = c.take<int32_t>(N);
+  d.comp_cmax = c.take<int32_t>(N);
+  d.comp_cand = c.take<int32_t>(N);
+  d.cand_comp = c.take<int32_t>(d.cap_cand);
+  d.rc = c.take<int32_t>((size_t)d.cap_cand * d.H);
+  d.roff = c.take<int32_t>((size_t)d.cap_cand * d.H + 1);
+  d.bucket = c.take<int32_t>(N);
+  d.kept = c.take<float4>(N);
+  d.vmed = c.take<float4>((size_t)d.cap_cand * d.H);
+  d.vrad = c.take<double>((size_t)d.cap_cand * d.H);
+  d.vkept = c.take<int32_t>((size_t)d.cap_cand * d.H);
+  d.cand_nv = c.take<int32_t>(d.cap_cand);
+  d.cand_lm = c.take<int32_t>(d.cap_cand);
+  d.lm_tree = c.take<int32_t>(d.cap_lm);
+  d.lm_vbeg = c.take<int32_t>(d.cap_lm + 1);
+  d.lm_vxyz = c.take<float>((size_t)d.cap_v * 3);
+  d.lm_vrad = c.take<double>(d.cap_v);
+  d.lm_vrow = c.take<int32_t>(d.cap_v);
+  d.lm_pbeg = c.take<int32_t>(d.cap_v + 1);
+  d.lm_pts = c.take<float4>(d.cap_p);
+  d.lm_cbeg = c.take<int32_t>(d.cap_lm + 1);
+  d.lm_cpts = c.take<float4>(d.cap_cluster);
+  d.bin_of = c.take<int32_t>(d.cap_ground);
+  d.bin_cnt = c.take<int32_t>(d.n_bins);
+  d.bin_off = c.take<int32_t>(d.n_bins + 1);
+  d.bin_keys = c.take<unsigned long long>(d.cap_ground);
+  d.plane_all = c.take<PlaneD>(d.n_bins);
+  d.plane_feat_all = c.take<float4>((size_t)d.n_bins * d.G);
+  d.planes = c.take<PlaneD>(d.n_bins);
+  d.plane_feat = c.take<float4>((size_t)d.n_bins * d.G);
+  d.prev_planes = c.take<PlaneD>(d.n_bins);
+  d.prev_feat = c.take<float4>((size_t)d.n_bins * d.G);
+  d.cyl_all = c.take<CylD>(d.cap_lm);
+  d.cyl_feat_all = c.take<float4>((size_t)d.cap_lm * d.F);
+  d.cyl_best = c.take<unsigned long long>(d.cap_lm);
+  d.cyls = c.take<CylD>(d.cap_lm);
+  d.cyl_feat = c.take<float4>((size_t)d.cap_lm * d.F);
+  d.buf_map = c.take<sloam_cylinder>(d.cap_map);
+  d.cyl_match = c.take<int32_t>(d.cap_lm);
+  d.plane_match = c.take<int32_t>(d.n_bins);
+  d.match_out = c.take<int32_t>(d.cap_lm);
+  d.pose_io = c.take<double>(32);
+  d.cnt = c.take<Counters>(1);
+}
+
+int check_params(const sloam_params& p) {
+  if (p.img_w < 32 || p.img_h < 1 || (int64_t)p.img_w * p.img_h > (1 << 26)) return 1;
+  if (p.ground_radii_bins < 1 || p.ground_theta_bins < 1 ||
+      p.ground_radii_bins * p.ground_theta_bins > 4096)
+    return 1;
+  if (p.features_per_tree < 0 || p.num_ground_features < 0) return 1;
+  if (p.trellis_max_vertices < 1 || p.trellis_max_vertices > 4096) return 1;
+  if (p.cyl_hypotheses < 0 || p.cyl_hypotheses > 4096 || p.line_ransac_max_iter > 256) return 1;
+  if (!(p.ground_retain_thresh > 0)) return 1;
+  return 0;
+}
+
+int setup(sloam_ctx* ctx, const sloam_params& P) {
+  ctx->P = P;
+  ctx->kp = make_kparams(P);
+  Dev& d = ctx->d;
+  d.H = P.img_h;
+  d.W = P.img_w;
+  d.N = P.img_h * P.img_w;
+  d.cap_ground = P.max_ground > 0 ? std::min(P.max_ground, d.N) : d.N;
+  d.cap_cand = d.N / (std::max(P.trellis_min_cluster, 0) + 1) + 1;
+  d.cap_lm = std::max(1, std::min(P.max_landmarks, d.cap_cand));
+  d.cap_v = d.cap_lm * P.trellis_max_vertices;
+  d.cap_p = d.N;
+  d.cap_cluster = d.N;
+  d.cap_map = std::max(1, P.max_map);
+  d.n_bins = P.ground_radii_bins * P.ground_theta_bins;
+  d.F = P.features_per_tree;
+  d.G = P.num_ground_features;
+  d.K = P.cyl_hypotheses;
+  const int n_blk = d.N / 256 + 64;
+  Carver dry{nullptr, 0, true};
+  carve(d, dry, n_blk);
+  const size_t bytes = dry.off + 256;
+  if (ctx->arena && bytes > ctx->arena_bytes) {
+    cudaFree(ctx->arena);
+    ctx->arena = nullptr;
+  }
+  if (!ctx->arena) {
+    CK(cudaMalloc(&ctx->arena, bytes));
+    ctx->arena_bytes = bytes;
+  }
+  Carver real{reinterpret_cast<char*>(ctx->arena), 0, false};
+  carve(d, real, n_blk);
+  // tables
+  std::vector<float> tab(d.W + 1), tb(4096), rb(4096);
+  build_px_table(P, tab.data());
+  build_ground_tables(P, tb.data(), rb.data(), &d.r_lo, &d.r_hi);
+  CK(cudaMemcpyAsync(d.px_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice,
+                     ctx->st));
+  CK(cudaMemcpyAsync(d.tb_tab, tb.data(), sizeof(float) * (P.ground_theta_bins + 1),
+                     cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(d.rb_tab, rb.data(), sizeof(float) * (P.ground_radii_bins + 1),
+                     cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemsetAsync(d.pkey, 0xFF, sizeof(unsigned long long) * d.N, ctx->st));
+  CK(cudaMemsetAsync(d.cnt, 0, sizeof(Counters), ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  for (auto& a : ctx->gx)
+    for (auto& b : a)
+      for (auto& g : b)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+  ctx->first_scan = true;
+  return SLOAM_OK;
+}
+
+// Reads back counters and pose; maps overflow / device errors to a status.
+int sync_counters(sloam_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_cnt, ctx->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->h_pose, ctx->d.pose_io, sizeof(double) * 21, cudaMemcpyDeviceToHost,
+                     ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  CK(cudaGetLastError());
+  if (ctx->h_cnt->overflow)
+    return fail(ctx, SLOAM_ERR_CAPACITY, "a context capacity was exceeded (overflow flags set)");
+  if (ctx->h_cnt->cc_iter_exceeded)
+    return fail(ctx, SLOAM_ERR_TIMEOUT, "connected-components union loop hit its iteration limit");
+  return SLOAM_OK;
+}
+
+int set_inputs(sloam_ctx* ctx, const float4* xyzi, const uint8_t* pl, const uint8_t* mi,
+               const sloam_cylinder* map, int n_map) {
+  InPtrs& h = ctx->h_in[0];
+  h.xyzi = xyzi;
+  h.plabel = pl;
+  h.mask_in = mi;
+  h.map = map;
+  h.n_map = n_map;
+  CK(cudaMemcpyAsync(ctx->d.in, &h, sizeof(InPtrs), cudaMemcpyHostToDevice, ctx->st));
+  // the pinned block must stay unchanged until the copy ran
+  CK(cudaStreamSynchronize(ctx->st));
+  return SLOAM_OK;
+}
+
+int upload_pose(sloam_ctx* ctx, const sloam_se3* pose) {
+  for (int j = 0; j < 4; ++j) ctx->h_pose[j] = pose->q[j];
+  for (int j = 0; j < 3; ++j) ctx->h_pose[4 + j] = pose->t[j];
+  CK(cudaMemcpyAsync(ctx->d.pose_io, ctx->h_pose, sizeof(double) * 7, cudaMemcpyHostToDevice,
+                     ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SLOAM_OK;
+}
+
+int upload_landmarks(sloam_ctx* ctx, const sloam_landmarks* lm, int* nl, int* nv, int* np,
+                     int* ncl) {
+  Dev& d = ctx->d;
+  *nl = lm ? lm->n_landmarks : 0;
+  *nv = *nl ? lm->vertex_begin[*nl] : 0;
+  *np = *nv ? lm->point_begin[*nv] : 0;
+  *ncl = 0;
+  if (*nl > d.cap_lm || *nv > d.cap_v || *np > d.cap_p)
+    return fail(ctx, SLOAM_ERR_CAPACITY, "landmarks exceed the context capacity");
+  if (*nl == 0) {
+    const int zero = 0;
+    CK(cudaMemcpyAsync(d.lm_vbeg, &zero, 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d.lm_cbeg, &zero, 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return SLOAM_OK;
+  }
+  CK(cudaMemcpyAsync(d.lm_tree, lm->tree_id, 4 * *nl, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(d.lm_vbeg, lm->vertex_begin, 4 * (*nl + 1), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(d.lm_vxyz, lm->vertex_xyz, 12 * (size_t)*nv, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(d.lm_vrad, lm->vertex_radius, 8 * (size_t)*nv, cudaMemcpyHostToDevice,
+                     ctx->st));
+  if (lm->vertex_row)
+    CK(cudaMemcpyAsync(d.lm_vrow, lm->vertex_row, 4 * (size_t)*nv, cudaMemcpyHostToDevice,
+                       ctx->st));
+  CK(cudaMemcpyAsync(d.lm_pbeg, lm->point_begin, 4 * (size_t)(*nv + 1), cudaMemcpyHostToDevice,
+                     ctx->st));
+  if (*np)
+    CK(cudaMemcpyAsync(d.lm_pts, lm->point_xyzi, 16 * (size_t)*np, cudaMemcpyHostToDevice,
+                       ctx->st));
+  std::vector<int32_t> zeros;
+  if (lm->cluster_begin && lm->cluster_xyzi) {
+    *ncl = lm->cluster_begin[*nl];
+    if (*ncl > d.cap_cluster) return fail(ctx, SLOAM_ERR_CAPACITY, "cluster points exceed capacity");
+    CK(cudaMemcpyAsync(d.lm_cbeg, lm->cluster_begin, 4 * (*nl + 1), cudaMemcpyHostToDevice,
+                       ctx->st));
+    if (*ncl)
+      CK(cudaMemcpyAsync(d.lm_cpts, lm->cluster_xyzi, 16 * (size_t)*ncl, cudaMemcpyHostToDevice,
+                         ctx->st));
+  } else {
+    zeros.assign(*nl + 1, 0);
+    CK(cudaMemcpyAsync(d.lm_cbeg, zeros.data(), 4 * (*nl + 1), cudaMemcpyHostToDevice, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  return SLOAM_OK;
+}
+
+int upload_ground(sloam_ctx* ctx, const float* g, int n) {
+  if (n > ctx->d.cap_ground) return fail(ctx, SLOAM_ERR_CAPACITY, "ground points exceed capacity");
+  if (n > 0)
+    CK(cudaMemcpyAsync(ctx->d.ground, g, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+  return SLOAM_OK;
+}
+
+// planes + cylinders (+ features, inliers) into a sloam_models_out
+int download_models(sloam_ctx* ctx, sloam_models_out* out) {
+  Dev& d = ctx->d;
+  const Counters& c = *ctx->h_cnt;
+  out->n_planes = c.n_planes;
+  out->n_cylinders = c.n_cyl;
+  std::vector<PlaneD> pl(std::max(1, c.n_planes));
+  std::vector<CylD> cy(std::max(1, c.n_cyl));
+  if (c.n_planes)
+    CK(cudaMemcpyAsync(pl.data(), d.planes, sizeof(PlaneD) * c.n_planes, cudaMemcpyDeviceToHost,
+                       ctx->st));
+  if (c.n_cyl)
+    CK(cudaMemcpyAsync(cy.data(), d.cyls, sizeof(CylD) * c.n_cyl, cudaMemcpyDeviceToHost, ctx->st));
+  std::vector<float4> feat((size_t)std::max(1, c.n_cyl) * std::max(1, d.F));
+  if (c.n_cyl && out->cyl_features && d.F)
+    CK(cudaMemcpyAsync(feat.data(), d.cyl_feat, sizeof(float4) * (size_t)c.n_cyl * d.F,
+                       cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  const int np = std::min(c.n_planes, out->cap_planes);
+  for (int k = 0; k < np && out->planes; ++k) {
+    sloam_plane& o = out->planes[k];
+    for (int j = 0; j < 4; ++j) o.plane[j] = pl[k].plane[j];
+    for (int j = 0; j < 3; ++j) o.centroid[j] = pl[k].centroid[j];
+    o.bin = pl[k].bin;
+    o.valid = 1;
+  }
+  const int nc = std::min(c.n_cyl, out->cap_cylinders);
+  for (int k = 0; k < nc && out->cylinders; ++k) {
+    sloam_cylinder& o = out->cylinders[k];
+    for (int j = 0; j < 3; ++j) {
+      o.root[j] = cy[k].root[j];
+      o.ray[j] = cy[k].ray[j];
+    }
+    o.radius = cy[k].radius;
+    o.id = cy[k].id;
+    o.valid = 1;
+    if (out->cyl_inliers) out->cyl_inliers[k] = cy[k].inliers;
+  }
+  if (out->cyl_features && nc)
+    std::memcpy(out->cyl_features, feat.data(), sizeof(float4) * (size_t)nc * d.F);
+  if (c.n_planes > out->cap_planes || c.n_cyl > out->cap_cylinders)
+    return fail(ctx, SLOAM_ERR_CAPACITY, "output capacity too small for the models");
+  return SLOAM_OK;
+}
+
+void to_se3(const double* p, sloam_se3* s) {
+  for (int j = 0; j < 4; ++j) s->q[j] = p[j];
+  for (int j = 0; j < 3; ++j) s->t[j] = p[4 + j];
+}
+
+int download_run(sloam_ctx* ctx, sloam_run_out* out, bool first) {
+  const Counters& c = *ctx->h_cnt;
+  out->first_scan = first ? 1 : 0;
+  out->success = c.success;
+  out->n_tree_matches = c.n_tm;
+  out->n_plane_matches = c.n_pm;
+  out->tree_check = c.tree_check;
+  out->ground_check = c.ground_check;
+  to_se3(ctx->h_pose + 7, &out->T_Map_Curr);
+  to_se3(ctx->h_pose + 14, &out->T_Delta);
+  int st = download_models(ctx, &out->models);
+  if (st) return st;
+  const int nc = std::min(c.n_cyl, out->models.cap_cylinders);
+  if (nc && out->matches)
+    CK(cudaMemcpy(out->matches, ctx->d.match_out, 4 * (size_t)nc, cudaMemcpyDeviceToHost));
+  return SLOAM_OK;
+}
+
+}  // namespace
+
+// ================================================================== ABI
+extern "C" sloam_ctx* sloam_create(const sloam_params* params, int device, int* status) {
+  int dummy;
+  if (!status) status = &dummy;
+  if (!params || check_params(*params)) {
+    *status = SLOAM_ERR_ARG;
+    return nullptr;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    *status = SLOAM_ERR_NO_DEVICE;
+    return nullptr;
+  }
+  sloam_ctx* ctx = new sloam_ctx;
+  ctx->device = device;
+  auto bail = [&](int code) {
+    *status = code;
+    sloam_destroy(ctx);
+    return (sloam_ctx*)nullptr;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(SLOAM_ERR_NO_DEVICE);
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(SLOAM_ERR_CUDA);
+  if (cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
+      cudaMallocHost((void**)&ctx->h_pose, sizeof(double) * 32) != cudaSuccess ||
+      cudaMallocHost((void**)&ctx->h_in, sizeof(InPtrs) * 64) != cudaSuccess ||
+      cudaMallocHost((void**)&ctx->h_poses, sizeof(double) * 8 * 64) != cudaSuccess)
+    return bail(SLOAM_ERR_CUDA);
+  ctx->h_batch_cap = 64;
+  init_kernel_attributes();
+  const int st = setup(ctx, *params);
+  if (st != SLOAM_OK) return bail(st);
+  *status = SLOAM_OK;
+  return ctx;
+}
+
+extern "C" void sloam_destroy(sloam_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  for (auto& a : ctx->gx)
+    for (auto& b : a)
+      for (auto& g : b)
+        if (g) cudaGraphExecDestroy(g);
+  if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
+  if (ctx->h_pose) cudaFreeHost(ctx->h_pose);
+  if (ctx->h_in) cudaFreeHost(ctx->h_in);
+  if (ctx->h_poses) cudaFreeHost(ctx->h_poses);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+}
+
+extern "C" int sloam_last_error(const sloam_ctx* ctx, char* buf, size_t n) {
+  if (!ctx || !buf || n == 0) return SLOAM_ERR_ARG;
+  std::snprintf(buf, n, "%s", ctx->err.c_str());
+  return SLOAM_OK;
+}
+
+extern "C" int sloam_reset(sloam_ctx* ctx) {
+  if (!ctx) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  ctx->first_scan = true;
+  CK(cudaMemsetAsync(ctx->d.cnt, 0, sizeof(Counters), ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return SLOAM_OK;
+}
+
+extern "C" int sloam_set_params(sloam_ctx* ctx, const sloam_params* params) {
+  if (!ctx || !params || check_params(*params)) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->st));
+  return setup(ctx, *params);
+}
+
+extern "C" int64_t sloam_last_launch_count(const sloam_ctx* ctx) {
+  return ctx ? ctx->last_launches : 0;
+}
+extern "C" void* sloam_stream(sloam_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
+
+// ----------------------------------------------------------- a1/a2
+extern "C" int sloam_project_mask(sloam_ctx* ctx, const float* xyzi, int32_t n,
+                                  const uint8_t* point_labels, const uint8_t* mask_image,
+                                  sloam_scan_out* out) {
+  if (!ctx || !xyzi || !out || (!point_labels && !mask_image)) return SLOAM_ERR_ARG;
+  Dev& d = ctx->d;
+  if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
+  cudaSetDevice(ctx->device);
+  CK(cudaMemcpyAsync(d.buf_xyzi, xyzi, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+  if (point_labels)
+    CK(cudaMemcpyAsync(d.buf_plabel, point_labels, n, cudaMemcpyHostToDevice, ctx->st));
+  else
+    CK(cudaMemcpyAsync(d.buf_mask_in, mask_image, n, cudaMemcpyHostToDevice, ctx->st));
+  int st = set_inputs(ctx, d.buf_xyzi, d.buf_plabel, d.buf_mask_in, d.buf_map, 0);
+  if (st) return st;
+  int nl = launch_begin(d, -1, 0, 0, 0, 0, ctx->st);
+  nl += launch_project(d, ctx->kp, point_labels != nullptr, ctx->st);
+  ctx->last_launches = nl;
+  st = sync_counters(ctx);
+  if (st) return st;
+  const int ng = ctx->h_cnt->n_ground;
+  out->n_ground = ng;
+  if (out->px || out->py) {
+    std::vector<int32_t> pix(n);
+    CK(cudaMemcpy(pix.data(), d.pix, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) {
+      if (out->px) out->px[i] = pix[i] % d.W;
+      if (out->py) out->py[i] = pix[i] / d.W;
+    }
+  }
+  if (out->range_image)
+    CK(cudaMemcpy(out->range_image, d.range_img, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+  if (out->mask_out) CK(cudaMemcpy(out->mask_out, d.mask, n, cudaMemcpyDeviceToHost));
+  if (out->ground_idx && ng)
+    CK(cudaMemcpy(out->ground_idx, d.ground_idx, 4 * (size_t)ng, cudaMemcpyDeviceToHost));
+  if (out->tree_cloud)
+    CK(cudaMemcpy(out->tree_cloud, d.tree, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+  return SLOAM_OK;
+}
+
+// --------------------------------------------------------------- a3-a5
+extern "C" int sloam_trellis(sloam_ctx* ctx, const float* tree_cloud, int32_t H, int32_t W,
+                             uint32_t* cc_labels, int32_t* n_components, sloam_landmarks* out) {
+  if (!ctx || !tree_cloud || !out) return SLOAM_ERR_ARG;
+  Dev& d = ctx->d;
+  if (H != d.H || W != d.W) return fail(ctx, SLOAM_ERR_ARG, "H, W must match the context");
+  cudaSetDevice(ctx->device);
+  CK(cudaMemcpyAsync(d.tree, tree_cloud, 16 * (size_t)d.N, cudaMemcpyHostToDevice, ctx->st));
+  int nl = launch_begin(d, 0, -1, -1, -1, -1, ctx->st);
+  nl += launch_trellis(d, ctx->kp, ctx->st);
+  ctx->last_launches = nl;
+  int st = sync_counters(ctx);
+  if (st) return st;
+  const Counters& c = *ctx->h_cnt;
+  if (n_components) *n_components = c.n_comp;
+  if (cc_labels) CK(cudaMemcpy(cc_labels, d.label, 4 * (size_t)d.N, cudaMemcpyDeviceToHost));
+  out->n_landmarks = c.n_lm;
+  out->n_vertices = c.n_v;
+  out->n_points = c.n_p;
+  out->n_cluster = c.n_cluster;
+  if (c.n_lm > out->cap_landmarks || c.n_v > out->cap_vertices || c.n_p > out->cap_points)
+    return fail(ctx, SLOAM_ERR_CAPACITY, "landmark output capacity too small");
+  if (c.n_lm) {
+    CK(cudaMemcpy(out->tree_id, d.lm_tree, 4 * (size_t)c.n_lm, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out->vertex_begin, d.lm_vbeg, 4 * (size_t)(c.n_lm + 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out->vertex_xyz, d.lm_vxyz, 12 * (size_t)c.n_v, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out->vertex_radius, d.lm_vrad, 8 * (size_t)c.n_v, cudaMemcpyDeviceToHost));
+    if (out->vertex_row)
+      CK(cudaMemcpy(out->vertex_row, d.lm_vrow, 4 * (size_t)c.n_v, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out->point_begin, d.lm_pbeg, 4 * (size_t)(c.n_v + 1), cudaMemcpyDeviceToHost));
+    if (c.n_p)
+      CK(cudaMemcpy(out->point_xyzi, d.lm_pts, 16 * (size_t)c.n_p, cudaMemcpyDeviceToHost));
+    if (out->cluster_begin) {
+      if (c.n_cluster > out->cap_cluster)
+        return fail(ctx, SLOAM_ERR_CAPACITY, "cluster output capacity too small");
+      CK(cudaMemcpy(out->cluster_begin, d.lm_cbeg, 4 * (size_t)(c.n_lm + 1),
+                    cudaMemcpyDeviceToHost));
+      if (out->cluster_xyzi && c.n_cluster)
+        CK(cudaMemcpy(out->cluster_xyzi, d.lm_cpts, 16 * (size_t)c.n_cluster,
+                      cudaMemcpyDeviceToHost));
+    }
+  } else {
+    out->vertex_begin[0] = 0;
+    if (out->cluster_begin) out->cluster_begin[0] = 0;
+  }
+  return SLOAM_OK;
+}
+
+// --------------------------------------------------------------- a6-a8
+extern "C" int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose,
+                                    const float* ground_xyzi, int32_t n_ground,
+                                    const sloam_landmarks* lm, sloam_models_out* out) {
+  if (!ctx || !pose || !out || (n_ground > 0 && !ground_xyzi) || n_ground < 0)
+    return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  int nl, nv, np, ncl;
+  int st = upload_landmarks(ctx, lm, &nl, &nv, &np, &ncl);
+  if (st) return st;
+  if ((st = upload_ground(ctx, ground_xyzi, n_ground))) return st;
+  if ((st = upload_pose(ctx, pose))) return st;
+  int k = launch_begin(d, n_ground, nl, nv, np, ncl, ctx->st);
+  k += launch_models(d, ctx->kp, false, ctx->st);
+  ctx->last_launches = k;
+  if ((st = sync_counters(ctx))) return st;
+  return download_models(ctx, out);
+}
+
+// ---------------------------------------------------------------- a9-a11
+extern "C" int sloam_run(sloam_ctx* ctx, const sloam_se3* pose, const float* ground_xyzi,
+                         int32_t n_ground, const sloam_landmarks* lm, const sloam_cylinder* map,
+                         int32_t n_map, sloam_run_out* out) {
+  if (!ctx || !pose || !out || n_ground < 0 || n_map < 0 || (n_map > 0 && !map))
+    return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  const bool first = ctx->first_scan;
+  if (!first && n_map == 0) {
+    out->success = 0;
+    return fail(ctx, SLOAM_ERR_EMPTY_MAP, "not the first scan but the map is empty");
+  }
+  if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
+  int nl, nv, np, ncl;
+  int st = upload_landmarks(ctx, lm, &nl, &nv, &np, &ncl);
+  if (st) return st;
+  if ((st = upload_ground(ctx, ground_xyzi, n_ground))) return st;
+  if (n_map)
+    CK(cudaMemcpyAsync(d.buf_map, map, sizeof(sloam_cylinder) * n_map, cudaMemcpyHostToDevice,
+                       ctx->st));
+  if ((st = set_inputs(ctx, d.buf_xyzi, d.buf_plabel, d.buf_mask_in, d.buf_map, n_map))) return st;
+  if ((st = upload_pose(ctx, pose))) return st;
+  int k = launch_begin(d, n_ground, nl, nv, np, ncl, ctx->st);
+  k += launch_models(d, ctx->kp, false, ctx->st);
+  k += launch_run(d, ctx->kp, first, true, ctx->st);
+  ctx->last_launches = k;
+  if ((st = sync_counters(ctx))) return st;
+  ctx->first_scan = false;
+  const int status = first ? SLOAM_OK : ctx->h_cnt->status;
+  if (status == SLOAM_ERR_NO_MODELS) {
+    out->success = 0;
+    return fail(ctx, SLOAM_ERR_NO_MODELS, "no ground or landmark models found");
+  }
+  if ((st = download_run(ctx, out, first))) return st;
+  return status;
+}
+
+// ----------------------------------------------------------- keyframe
+namespace {
+int enqueue_keyframe(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
+  Dev& d = ctx->d;
+  int k = launch_begin(d, -1, -1, -1, -1, -1, ctx->st);
+  k += launch_project(d, ctx->kp, point_labels, ctx->st);
+  k += launch_trellis(d, ctx->kp, ctx->st);
+  k += launch_models(d, ctx->kp, true, ctx->st);
+  k += launch_run(d, ctx->kp, first, update, ctx->st);
+  return k;
+}
+
+// The whole keyframe (a1-a11) as one CUDA graph, captured on first use.
+int run_keyframe_graph(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
+  const int a = first ? 1 : 0, b = point_labels ? 1 : 0, u = update ? 1 : 0;
+  if (!ctx->gx[a][b][u]) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    const int k = enqueue_keyframe(ctx, first, point_labels, update);
+    CK(cudaStreamEndCapture(ctx->st, &g));
+    cudaError_t e = cudaGraphInstantiate(&ctx->gx[a][b][u], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ctx, SLOAM_ERR_CUDA, "cudaGraphInstantiate", e);
+    ctx->gx_launches[a][b][u] = k;
+  }
+  CK(cudaGraphLaunch(ctx->gx[a][b][u], ctx->st));
+  ctx->last_launches = ctx->gx_launches[a][b][u];
+  return SLOAM_OK;
+}
+}  // namespace
+
+extern "C" int sloam_keyframe(sloam_ctx* ctx, const float* xyzi, int32_t n,
+                              const uint8_t* point_labels, const uint8_t* mask_image,
+                              const sloam_se3* pose, const sloam_cylinder* map, int32_t n_map,
+                              sloam_run_out* out) {
+  if (!ctx || !xyzi || !pose || !out || (!point_labels && !mask_image) || n_map < 0 ||
+      (n_map > 0 && !map))
+    return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
+  const bool first = ctx->first_scan;
+  if (!first && n_map == 0) {
+    out->success = 0;
+    return fail(ctx, SLOAM_ERR_EMPTY_MAP, "not the first scan but the map is empty");
+  }
+  if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
+  CK(cudaMemcpyAsync(d.buf_xyzi, xyzi, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+  if (point_labels)
+    CK(cudaMemcpyAsync(d.buf_plabel, point_labels, n, cudaMemcpyHostToDevice, ctx->st));
+  else
+    CK(cudaMemcpyAsync(d.buf_mask_in, mask_image, n, cudaMemcpyHostToDevice, ctx->st));
+  if (n_map)
+    CK(cudaMemcpyAsync(d.buf_map, map, sizeof(sloam_cylinder) * n_map, cudaMemcpyHostToDevice,
+                       ctx->st));
+  int st = set_inputs(ctx, d.buf_xyzi, d.buf_plabel, d.buf_mask_in, d.buf_map, n_map);
+  if (st) return st;
+  if ((st = upload_pose(ctx, pose))) return st;
+  if ((st = run_keyframe_graph(ctx, first, point_labels != nullptr, true))) return st;
+  if ((st = sync_counters(ctx))) return st;
+  ctx->first_scan = false;
+  const int status = first ? SLOAM_OK : ctx->h_cnt->status;
+  if (status == SLOAM_ERR_NO_MODELS) {
+    out->success = 0;
+    return fail(ctx, SLOAM_ERR_NO_MODELS, "no ground or landmark models found");
+  }
+  if ((st = download_run(ctx, out, first))) return st;
+  return status;
+}
+
+namespace sg {
+// per-keyframe outputs of a device batch
+__global__ void k_batch_out(Counters* c, const double* pose_io, double* pose_out,
+                            int32_t* success_out, int32_t* ncyl_out, int k) {
+  if (threadIdx.x < 7) pose_out[7 * k + threadIdx.x] = pose_io[7 + threadIdx.x];
+  if (threadIdx.x == 0) {
+    success_out[k] = c->status == SLOAM_OK ? c->success : 0;
+    ncyl_out[k] = c->n_cyl;
+  }
+}
+}  // namespace sg
+
+extern "C" int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32_t n,
+                                      int32_t nkf, const uint8_t* d_point_labels,
+                                      const sloam_se3* poses, const sloam_cylinder* d_map,
+                                      int32_t n_map, double* d_pose_out, int32_t* d_success_out,
+                                      int32_t* d_ncyl_out) {
+  if (!ctx || !d_xyzi || !d_point_labels || !poses || nkf < 0 || !d_pose_out ||
+      !d_success_out || !d_ncyl_out || n_map <= 0 || !d_map)
+    return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
+  if (ctx->first_scan) return fail(ctx, SLOAM_ERR_ARG, "the context has not seen a first scan");
+  if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
+  CK(cudaStreamSynchronize(ctx->st));
+  if (nkf > ctx->h_batch_cap) {
+    cudaFreeHost(ctx->h_in);
+    cudaFreeHost(ctx->h_poses);
+    ctx->h_in = nullptr;
+    ctx->h_poses = nullptr;
+    CK(cudaMallocHost((void**)&ctx->h_in, sizeof(InPtrs) * nkf));
+    CK(cudaMallocHost((void**)&ctx->h_poses, sizeof(double) * 8 * nkf));
+    ctx->h_batch_cap = nkf;
+  }
+  for (int k = 0; k < nkf; ++k) {
+    InPtrs& h = ctx->h_in[k];
+    h.xyzi = reinterpret_cast<const float4*>(d_xyzi) + (size_t)k * n;
+    h.plabel = d_point_labels + (size_t)k * n;
+    h.mask_in = nullptr;
+    h.map = d_map;
+    h.n_map = n_map;
+    for (int j = 0; j < 4; ++j) ctx->h_poses[8 * k + j] = poses[k].q[j];
+    for (int j = 0; j < 3; ++j) ctx->h_poses[8 * k + 4 + j] = poses[k].t[j];
+  }
+  int64_t launches = 0;
+  for (int k = 0; k < nkf; ++k) {
+    CK(cudaMemcpyAsync(d.in, ctx->h_in + k, sizeof(InPtrs), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d.pose_io, ctx->h_poses + 8 * k, sizeof(double) * 7,
+                       cudaMemcpyHostToDevice, ctx->st));
+    // the previous-scan planes are not advanced inside a batch
+    int st = run_keyframe_graph(ctx, false, true, false);
+    if (st) return st;
+    launches += ctx->last_launches;
+    k_batch_out<<<1, 32, 0, ctx->st>>>(d.cnt, d.pose_io, d_pose_out, d_success_out, d_ncyl_out, k);
+    ++launches;
+  }
+  ctx->last_launches = launches;
+  CK(cudaGetLastError());
+  return SLOAM_OK;
+}

@@ -1,0 +1,192 @@
+// internal.h — device state of a context and the kernel launchers of each
+// stage.  Everything lives in one device arena sized at context creation
+// (nothing is allocated per keyframe).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/sloam_gb300.h"
+
+namespace sg {
+
+// Device-side counters and flags of one keyframe.
+struct Counters {
+  int32_t n_ground;      // ground points (a2)
+  int32_t n_comp;        // connected components (a3)
+  int32_t n_cand;        // components with > trellis_min_cluster points
+  int32_t n_lm;          // landmarks (a4)
+  int32_t n_v;           // landmark vertices
+  int32_t n_p;           // landmark points
+  int32_t n_cluster;     // landmark cluster points
+  int32_t n_planes;      // valid ground planes (a7)
+  int32_t n_cyl;         // valid cylinders (a6)
+  int32_t n_prev;        // planes of the previous scan (state)
+  int32_t n_tm;          // tree feature matches
+  int32_t n_pm;          // plane feature matches
+  int32_t tree_check, ground_check;
+  int32_t status;        // SLOAM_* of the pose stage
+  int32_t success;
+  int32_t overflow;      // bit mask of capacity overflows
+  int32_t ransac_fail;
+  int32_t n_slow_px;     // projection points that took the FP64 path
+  int32_t n_slow_theta;
+  int32_t cc_iter_exceeded;
+  int32_t pad[11];
+};
+
+// Plane and cylinder records used on the device (FP64 models).
+struct PlaneD {
+  double plane[4];
+  double centroid[3];
+  int32_t bin;
+  int32_t valid;
+};
+struct CylD {
+  double root[3];
+  double ray[3];
+  double radius;
+  int32_t id;
+  int32_t valid;
+  int32_t inliers;
+  int32_t landmark;  // index of the landmark it came from
+  int32_t plane;     // nearest plane
+  int32_t stage;     // 0 none, 1 vertex line ok (mode 0 model), 2 point fit applied
+};
+
+// Per-call inputs, read by the kernels through a device pointer so that a
+// captured CUDA graph can be replayed over different input buffers.
+struct InPtrs {
+  const float4* xyzi;
+  const uint8_t* plabel;
+  const uint8_t* mask_in;
+  const sloam_cylinder* map;
+  int32_t n_map;
+  int32_t pad;
+};
+
+struct Dev {
+  InPtrs* in;          // device copy of the current inputs
+  int H, W, N;
+  int cap_cand, cap_lm, cap_v, cap_p, cap_ground, cap_map, cap_cluster;
+  int n_bins, F, G, K;
+  // -- scan (buf_* are the context's own upload buffers)
+  float4* buf_xyzi;
+  uint8_t* buf_plabel;
+  uint8_t* buf_mask_in;
+  int32_t* pix;
+  unsigned long long* pkey;
+  float* range_img;
+  uint8_t* mask;
+  float4* tree;
+  uint32_t* gbits;
+  int32_t* blk;        // per-block scratch counts
+  int32_t* ground_idx;
+  float4* ground;
+  float* px_tab;       // [W+1]
+  float* tb_tab;       // [Tb+1]
+  float* rb_tab;       // [Rb+1]
+  float r_lo, r_hi;    // float ground radius window
+  // -- connected components
+  uint32_t* parent;
+  uint32_t* label;
+  uint32_t* rank;
+  int32_t* comp_size;
+  int32_t* comp_cmin;
+  int32_t* comp_cmax;
+  int32_t* comp_cand;
+  // -- Trellis buckets
+  int32_t* cand_comp;
+  int32_t* rc;         // [cap_cand*H]
+  int32_t* roff;       // [cap_cand*H+1]
+  int32_t* bucket;     // [N] pixel index per (cand,row) slot, column order
+  float4* kept;        // [N] kept vertex points (z order), same offsets
+  float4* vmed;        // [cap_cand*H] median (w unused)
+  double* vrad;        // [cap_cand*H]
+  int32_t* vkept;      // [cap_cand*H] kept count, 0 if not a valid vertex
+  int32_t* cand_nv;    // [cap_cand] landmark vertex count (0 = not a landmark)
+  int32_t* cand_lm;    // [cap_cand] landmark index or -1
+  // -- landmarks (SoA, also filled by uploads)
+  int32_t* lm_tree;
+  int32_t* lm_vbeg;    // [cap_lm+1]
+  float* lm_vxyz;      // [cap_v*3]
+  double* lm_vrad;
+  int32_t* lm_vrow;
+  int32_t* lm_pbeg;    // [cap_v+1]
+  float4* lm_pts;      // [cap_p]
+  int32_t* lm_cbeg;    // [cap_lm+1]
+  float4* lm_cpts;     // [cap_cluster]
+  // -- ground bins / planes
+  int32_t* bin_of;     // [cap_ground]
+  int32_t* bin_cnt;    // [n_bins]
+  int32_t* bin_off;    // [n_bins+1]
+  unsigned long long* bin_keys;  // [cap_ground]
+  PlaneD* plane_all;   // [n_bins]
+  float4* plane_feat_all;  // [n_bins*G]
+  PlaneD* planes;      // compact [n_bins]
+  float4* plane_feat;  // [n_bins*G]
+  PlaneD* prev_planes; // [n_bins]
+  float4* prev_feat;   // [n_bins*G]
+  // -- cylinders
+  CylD* cyl_all;       // [cap_lm]
+  float4* cyl_feat_all;  // [cap_lm*F]
+  unsigned long long* cyl_best;  // [cap_lm] point-fit best (count<<32 | ~h)
+  CylD* cyls;          // compact [cap_lm]
+  float4* cyl_feat;    // [cap_lm*F]
+  // -- map / association / pose
+  sloam_cylinder* buf_map;  // [cap_map]
+  int32_t* cyl_match;   // [cap_lm] map object matched for the pose (-1)
+  int32_t* plane_match; // [n_bins]
+  int32_t* match_out;   // [cap_lm] matchModels result
+  double* pose_io;      // [16] in: estimate (q xyzw, t); out: T_Map_Curr, T_Delta
+  Counters* cnt;
+};
+
+// scalar parameters the kernels need (copied by value into launches)
+struct KParams {
+  float fov_down_abs, fov;
+  int img_w, img_h, do_destagger;
+  float cc_thr;
+  int min_cluster, min_beam, min_vertices, max_vertices;
+  float max_d_centroid;
+  int Rb, Tb;
+  double retain_num;
+  int G, F;
+  double max_lidar_dist, min_tree_height_sq, root_plane_max_dist;
+  double max_tree_radius, max_axis_theta, default_tree_radius;
+  double line_thr;
+  int line_max_iter;
+  double line_prob;
+  uint64_t seed;
+  int cyl_mode, K, ls_iters;
+  float tau, max_hyp_r;
+  double tree_match_thresh, plane_match_thresh, add_new_tree_thresh;
+  double min_tree_models, min_ground_models, min_planes;
+  int two_step;
+  int gn_iters;
+  double huber;
+};
+
+KParams make_kparams(const sloam_params& p);
+
+// ---------------------------------------------------------------- stages
+// Every launcher enqueues on `st` and returns the number of kernels launched.
+int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st);
+int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st);
+int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
+int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_state,
+               cudaStream_t st);
+int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trellis,
+                               cudaStream_t st);
+
+// per-call counter reset: counts >= 0 are set, -1 left to the pipeline
+int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster,
+                 cudaStream_t st);
+void init_kernel_attributes();
+
+// host-built tables (context.cu)
+void build_px_table(const sloam_params& p, float* tab);
+void build_ground_tables(const sloam_params& p, float* tb, float* rb, float* r_lo,
+                         float* r_hi);
+
+}  // namespace sg

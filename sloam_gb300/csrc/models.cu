@@ -1,0 +1,986 @@
+// models.cu — a6-a8: sloam::computeModels (sloam.cpp:388-436).
+//
+// a7 binGroundPoints (sloam.cpp:330-386) + Plane (plane.cpp:3-17, 96-128) +
+//    the angle/height gates (sloam.cpp:394-412): per-point bins from exact
+//    float boundary tables (theta is the correctly rounded float atan2, same
+//    fast/slow scheme as the projection), one block per bin selects the
+//    lowest int(n / retainNum) points by (z, index) with a shared-memory
+//    bitonic sort (radix select first when a bin exceeds the staging size),
+//    float centroid in that order, FP64 scatter + Jacobi normal (n_z > 0).
+// a8 landmark -> nearest plane (sloam.cpp:418-431), and
+// a6 Cylinder (cylinder.cpp:3-173): one warp per landmark runs the
+//    vertex-line RANSAC (Philox hypotheses, PCL's sequential stopping rule),
+//    the PCL-style PCA refit, the radius median and the gates; the optional
+//    point-level cylinder RANSAC spreads each tree's hypotheses over blocks
+//    that stage the tree's projected points in shared memory, then one block
+//    per tree runs the least-squares refinement (FP32 sums, FP64 5x5 solve).
+#include <cfloat>
+#include <climits>
+
+#include "internal.h"
+#include "scan_util.cuh"
+
+namespace sg {
+
+KParams make_kparams(const sloam_params& p) {
+  KParams k{};
+  const float fov_up = (float)(p.fov_up_deg / 180.0 * 3.14159265358979323846);
+  const float fov_down = (float)(p.fov_down_deg / 180.0 * 3.14159265358979323846);
+  k.fov_down_abs = fov_down < 0 ? -fov_down : fov_down;
+  k.fov = k.fov_down_abs + (fov_up < 0 ? -fov_up : fov_up);
+  k.img_w = p.img_w;
+  k.img_h = p.img_h;
+  k.do_destagger = p.do_destagger;
+  k.cc_thr = p.cc_dist_threshold;
+  k.min_cluster = p.trellis_min_cluster;
+  k.min_beam = p.trellis_min_beam_points;
+  k.min_vertices = p.trellis_min_vertices;
+  k.max_vertices = p.trellis_max_vertices;
+  k.max_d_centroid = p.max_dist_to_centroid;
+  k.Rb = p.ground_radii_bins;
+  k.Tb = p.ground_theta_bins;
+  k.retain_num = 1 / p.ground_retain_thresh;
+  k.G = p.num_ground_features;
+  k.F = p.features_per_tree;
+  k.max_lidar_dist = p.max_lidar_dist;
+  k.min_tree_height_sq = p.min_tree_height_sq;
+  k.root_plane_max_dist = p.root_plane_max_dist;
+  k.max_tree_radius = p.max_tree_radius;
+  k.max_axis_theta = p.max_axis_theta;
+  k.default_tree_radius = p.default_tree_radius;
+  k.line_thr = p.line_ransac_thresh;
+  k.line_max_iter = p.line_ransac_max_iter;
+  k.line_prob = p.line_ransac_probability;
+  k.seed = p.seed;
+  k.cyl_mode = p.cyl_mode;
+  k.K = p.cyl_hypotheses;
+  k.ls_iters = p.cyl_ls_iters;
+  k.tau = p.cyl_inlier_thresh;
+  k.max_hyp_r = p.cyl_max_hyp_radius;
+  k.tree_match_thresh = p.tree_match_thresh;
+  k.plane_match_thresh = p.plane_match_thresh;
+  k.add_new_tree_thresh = p.add_new_tree_thresh_dist;
+  k.min_tree_models = p.min_tree_models;
+  k.min_ground_models = p.min_ground_models;
+  k.min_planes = p.min_planes;
+  k.two_step = p.two_step_optim;
+  k.gn_iters = p.gn_iters;
+  k.huber = p.huber_delta;
+  return k;
+}
+
+namespace {
+
+// ============================================================ ground bins
+__device__ __forceinline__ int bin_from_table(const float* __restrict__ tab, float v, int nb) {
+  int k = 0;
+  while (k < nb - 1 && v >= tab[k + 1]) ++k;
+  return k;
+}
+
+__device__ __forceinline__ uint32_t zkey(float z) {
+  if (z == 0.0f) z = 0.0f;  // -0 == +0
+  const uint32_t u = __float_as_uint(z);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void __launch_bounds__(256) k_gbin(Dev d, KParams kp) {
+  const int n = d.cnt->n_ground;
+  int slow = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 p = d.ground[i];
+    const float dx = fsub(0.0f, p.x), dy = fsub(0.0f, p.y);
+    const float r = fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
+    int bin = -1;
+    if (r >= d.r_lo && r <= d.r_hi) {
+      const float y = fsub(p.y, 0.0f), x = fsub(p.x, 0.0f);
+      float th = atan2f(y, x);
+      int tb;
+      bool need = !(isfinite(x) && isfinite(y)) || x == 0.0f || y == 0.0f;
+      if (!need) {
+        const float m = fmaxf(fabsf(th) * 1.2e-6f, 1e-30f);
+        tb = bin_from_table(d.tb_tab, th - m, kp.Tb);
+        need = tb != bin_from_table(d.tb_tab, th + m, kp.Tb);
+      }
+      if (need) {
+        th = (float)atan2((double)y, (double)x);
+        tb = bin_from_table(d.tb_tab, th, kp.Tb);
+        ++slow;
+      }
+      const int rb = bin_from_table(d.rb_tab, r, kp.Rb);
+      bin = rb * kp.Tb + tb;
+      atomicAdd(d.bin_cnt + bin, 1);
+    }
+    d.bin_of[i] = bin;
+  }
+  slow = warp_sumi(slow);
+  if ((threadIdx.x & 31) == 0 && slow) atomicAdd(&d.cnt->n_slow_theta, slow);
+}
+
+__global__ void __launch_bounds__(1024) k_gbin_scan(Dev d) {
+  __shared__ int sm[33];
+  int base = 0;
+  for (int b0 = 0; b0 < d.n_bins; b0 += blockDim.x) {
+    const int b = b0 + threadIdx.x;
+    const int v = b < d.n_bins ? d.bin_cnt[b] : 0;
+    int total;
+    const int ex = block_excl_scan(v, sm, &total);
+    if (b < d.n_bins) {
+      d.bin_off[b] = base + ex;
+      d.bin_cnt[b] = base + ex;  // becomes the scatter cursor
+    }
+    base += total;
+  }
+  if (threadIdx.x == 0) d.bin_off[d.n_bins] = base;
+}
+
+__global__ void __launch_bounds__(256) k_gbin_scatter(Dev d) {
+  const int n = d.cnt->n_ground;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int b = d.bin_of[i];
+    if (b < 0) continue;
+    const int pos = atomicAdd(d.bin_cnt + b, 1);
+    d.bin_keys[pos] = ((unsigned long long)zkey(d.ground[i].z) << 32) | (uint32_t)i;
+  }
+}
+
+// ------------------------------------------------ Eigen euler gate (FP64)
+// Quaternion::setFromTwoVectors + toRotationMatrix + eulerAngles(0,1,2),
+// restated (Eigen 3.3); returns the three angles.
+__device__ void euler_two_vectors(d3 a, d3 b, double* ang) {
+  d3 v0 = scl3(1.0 / norm3(a), a), v1 = scl3(1.0 / norm3(b), b);
+  double c = dot3(v1, v0);
+  double qx, qy, qz, qw;
+  if (c < -1.0 + 1e-12) {
+    c = fmax(c, -1.0);
+    d3 axis = fabs(v0.x) < 0.9 ? cross3(v0, mk3(1, 0, 0)) : cross3(v0, mk3(0, 1, 0));
+    axis = scl3(1.0 / norm3(axis), axis);
+    const double w2 = (1.0 + c) * 0.5;
+    qw = sqrt(w2);
+    const double s = sqrt(1.0 - w2);
+    qx = axis.x * s; qy = axis.y * s; qz = axis.z * s;
+  } else {
+    const d3 axis = cross3(v0, v1);
+    const double s = sqrt((1.0 + c) * 2.0), invs = 1.0 / s;
+    qx = axis.x * invs; qy = axis.y * invs; qz = axis.z * invs;
+    qw = s * 0.5;
+  }
+  const double tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
+  const double twx = tx * qw, twy = ty * qw, twz = tz * qw;
+  const double txx = tx * qx, txy = ty * qx, txz = tz * qx;
+  const double tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+  const double M00 = 1 - (tyy + tzz), M01 = txy - twz, M02 = txz + twy;
+  const double M10 = txy + twz, M11 = 1 - (txx + tzz), M12 = tyz - twx;
+  const double M20 = txz - twy, M21 = tyz + twx, M22 = 1 - (txx + tyy);
+  double r0 = atan2(M12, M22);
+  const double c2 = hypot(M00, M01);
+  double r1;
+  if (r0 > 0) {
+    r0 -= 3.14159265358979323846;
+    r1 = atan2(-M02, -c2);
+  } else {
+    r1 = atan2(-M02, c2);
+  }
+  const double s1 = sin(r0), c1 = cos(r0);
+  const double r2 = atan2(s1 * M20 - c1 * M10, c1 * M11 - s1 * M21);
+  ang[0] = -r0; ang[1] = -r1; ang[2] = -r2;
+}
+
+constexpr int kBinCap = 4096;   // keys of one bin staged in shared memory
+constexpr int kPlaneThreads = 512;
+
+__device__ void bitonic_sort(unsigned long long* a, int n2) {
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const bool up = (i & k) == 0;
+          const unsigned long long x = a[i], y = a[l];
+          if ((x > y) == up) { a[i] = y; a[l] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// One block per bin: retained points, plane model, gates, features.
+__global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
+  __shared__ unsigned long long keys[kBinCap];
+  __shared__ unsigned int hist[256];
+  __shared__ double red[6 * 32];
+  __shared__ float cen[3];
+  __shared__ unsigned long long sel_prefix;
+  __shared__ int sel_k, s_cnt;
+  const int b = blockIdx.x;
+  if (b >= d.n_bins) return;
+  const int off = d.bin_off[b], n = d.bin_off[b + 1] - off;
+  const unsigned long long* src = d.bin_keys + off;
+  PlaneD out{};
+  out.bin = b;
+  out.valid = 0;
+  const bool retain = n > 0 && kp.retain_num < (double)n;
+  const int k = n == 0 ? 0 : (retain ? (int)((double)n / kp.retain_num) : n);
+  // the retained set sorted by (z, index); without retention, by index
+  int kk = k;
+  if (n > 0 && k > 0) {
+    if (n <= kBinCap) {
+      int n2 = 1;
+      while (n2 < n) n2 <<= 1;
+      for (int i = threadIdx.x; i < n2; i += blockDim.x)
+        keys[i] = i < n ? (retain ? src[i] : (src[i] & 0xffffffffull)) : ~0ull;
+      __syncthreads();
+      bitonic_sort(keys, n2);
+    } else if (k > kBinCap) {
+      if (threadIdx.x == 0) atomicOr(&d.cnt->overflow, 8);
+      kk = 0;
+    } else {
+      // radix select of the k-th smallest 64-bit key, 8 bits at a time
+      if (threadIdx.x == 0) { sel_prefix = 0; sel_k = k; }
+      __syncthreads();
+      for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        const unsigned long long pre = sel_prefix;
+        const unsigned long long hmask = shift == 56 ? 0ull : (~0ull << (shift + 8));
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+          const unsigned long long v = src[i];
+          if ((v & hmask) == pre) atomicAdd(hist + ((v >> shift) & 255u), 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          int rem = sel_k, dg = 0;
+          for (; dg < 256; ++dg) {
+            if (rem <= (int)hist[dg]) break;
+            rem -= hist[dg];
+          }
+          sel_prefix = pre | ((unsigned long long)dg << shift);
+          sel_k = rem;
+        }
+        __syncthreads();
+      }
+      const unsigned long long T = sel_prefix;  // k-th smallest (keys unique)
+      if (threadIdx.x == 0) s_cnt = 0;
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long v = src[i];
+        if (v <= T) keys[atomicAdd(&s_cnt, 1)] = v;
+      }
+      __syncthreads();
+      int n2 = 1;
+      while (n2 < k) n2 <<= 1;
+      for (int i = k + threadIdx.x; i < n2; i += blockDim.x) keys[i] = ~0ull;
+      __syncthreads();
+      bitonic_sort(keys, n2);
+    }
+  }
+  __syncthreads();
+  const bool enough = kk > 0 && kk >= kp.G && kk >= 3;
+  if (enough) {
+    // float centroid, sequential in feature order (utils.h:14-28)
+    if (threadIdx.x == 0) {
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      for (int i = 0; i < kk; ++i) {
+        const float4 p = d.ground[(uint32_t)keys[i]];
+        sx = fadd(sx, p.x);
+        sy = fadd(sy, p.y);
+        sz = fadd(sz, p.z);
+      }
+      cen[0] = (float)((double)sx / (double)kk);
+      cen[1] = (float)((double)sy / (double)kk);
+      cen[2] = (float)((double)sz / (double)kk);
+    }
+    __syncthreads();
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < kk; i += blockDim.x) {
+      const float4 p = d.ground[(uint32_t)keys[i]];
+      const double a0 = (double)fsub(p.x, cen[0]), a1 = (double)fsub(p.y, cen[1]),
+                   a2 = (double)fsub(p.z, cen[2]);
+      s[0] += a0 * a0; s[1] += a0 * a1; s[2] += a0 * a2;
+      s[3] += a1 * a1; s[4] += a1 * a2; s[5] += a2 * a2;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int j = 0; j < 6; ++j) {
+      const double v = warp_sumd(s[j]);
+      if (lane == 0) red[j * 32 + w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double S6[6];
+      for (int j = 0; j < 6; ++j) {
+        double t = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[j * 32 + q];
+        S6[j] = t;
+      }
+      const double S[9] = {S6[0], S6[1], S6[2], S6[1], S6[3], S6[4], S6[2], S6[4], S6[5]};
+      double ev[3], V[9];
+      jacobi3(S, ev, V);
+      d3 nrm = mk3(V[0], V[3], V[6]);
+      const bool flip = nrm.z < 0 || (nrm.z == 0 && (nrm.y < 0 || (nrm.y == 0 && nrm.x < 0)));
+      if (flip) nrm = scl3(-1.0, nrm);
+      const double dd = -(nrm.x * cen[0] + nrm.y * cen[1] + nrm.z * cen[2]);
+      out.plane[0] = nrm.x; out.plane[1] = nrm.y; out.plane[2] = nrm.z; out.plane[3] = dd;
+      out.centroid[0] = cen[0]; out.centroid[1] = cen[1]; out.centroid[2] = cen[2];
+      // gates (sloam.cpp:394-408): normal in the map frame = R n
+      sloam_se3 pe;
+      for (int j = 0; j < 4; ++j) pe.q[j] = d.pose_io[j];
+      for (int j = 0; j < 3; ++j) pe.t[j] = d.pose_io[4 + j];
+      const Pose T = pose_from(pe);
+      const d3 nw = rot3(T.R, nrm);
+      double ang[3];
+      euler_two_vectors(mk3(0, 0, 1), nw, ang);
+      const double PI = 3.14159265358979323846;
+      const bool angle_ok = (ang[0] < 0.1 && ang[1] < 0.1 && ang[2] < 0.1) ||
+                            (PI - fabs(ang[0]) < 0.1 && PI - fabs(ang[1]) < 0.1 &&
+                             PI - fabs(ang[2]) < 0.1);
+      const bool height_ok =
+          xform(T, mk3(out.centroid[0], out.centroid[1], out.centroid[2])).z < T.t.z;
+      out.valid = angle_ok && height_ok;
+      d.plane_all[b] = out;
+    }
+    for (int i = threadIdx.x; i < kp.G; i += blockDim.x)
+      d.plane_feat_all[(size_t)b * kp.G + i] = d.ground[(uint32_t)keys[i]];
+  } else if (threadIdx.x == 0) {
+    d.plane_all[b] = out;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_plane_compact(Dev d, KParams kp) {
+  __shared__ int sm[33];
+  int base = 0;
+  for (int b0 = 0; b0 < d.n_bins; b0 += blockDim.x) {
+    const int b = b0 + threadIdx.x;
+    const bool v = b < d.n_bins && d.plane_all[b].valid;
+    int total;
+    const int ex = block_excl_scan(v ? 1 : 0, sm, &total);
+    if (v) {
+      d.planes[base + ex] = d.plane_all[b];
+      for (int j = 0; j < kp.G; ++j)
+        d.plane_feat[(size_t)(base + ex) * kp.G + j] = d.plane_feat_all[(size_t)b * kp.G + j];
+    }
+    base += total;
+  }
+  if (threadIdx.x == 0) d.cnt->n_planes = base;
+}
+
+// ============================================================ cylinders
+__device__ __forceinline__ float euclid2d_f(float ax, float ay, float bx, float by) {
+  const float dx = fsub(ax, bx), dy = fsub(ay, by);
+  return fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
+}
+
+// PCL line refit direction with pcl::computeCorrespondingEigenVector's sign.
+__device__ d3 pcl_line_direction(const double* S) {
+  double ev[3], V[9];
+  jacobi3(S, ev, V);
+  const double lam = ev[2];
+  double scale = 0;
+  for (int k = 0; k < 9; ++k) scale = fmax(scale, fabs(S[k]));
+  if (scale <= DBL_MIN) scale = 1.0;
+  double M[9];
+  for (int k = 0; k < 9; ++k) M[k] = S[k] / scale;
+  M[0] -= lam / scale; M[4] -= lam / scale; M[8] -= lam / scale;
+  const d3 r0 = mk3(M[0], M[1], M[2]), r1 = mk3(M[3], M[4], M[5]), r2 = mk3(M[6], M[7], M[8]);
+  const d3 c1 = cross3(r0, r1), c2 = cross3(r0, r2), c3 = cross3(r1, r2);
+  const double l1 = dot3(c1, c1), l2 = dot3(c2, c2), l3 = dot3(c3, c3);
+  d3 v;
+  if (l1 >= l2 && l1 >= l3) v = scl3(1.0 / sqrt(l1), c1);
+  else if (l2 >= l1 && l2 >= l3) v = scl3(1.0 / sqrt(l2), c2);
+  else v = scl3(1.0 / sqrt(l3), c3);
+  if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z))) v = mk3(V[2], V[5], V[8]);
+  return v;
+}
+
+__device__ __forceinline__ int line_count(const float* vx, int V, float ax, float ay, float az,
+                                          float dx, float dy, float dz, float thr2, int j0,
+                                          int step) {
+  int cnt = 0;
+  for (int j = j0; j < V; j += step) {
+    const float vxj = fsub(ax, vx[3 * j]), vyj = fsub(ay, vx[3 * j + 1]),
+                vzj = fsub(az, vx[3 * j + 2]);
+    const float cx = fsub(fmul(vyj, dz), fmul(vzj, dy));
+    const float cy = fsub(fmul(vzj, dx), fmul(vxj, dz));
+    const float cz = fsub(fmul(vxj, dy), fmul(vyj, dx));
+    const float sq = fadd(fadd(fmul(cx, cx), fmul(cy, cy)), fmul(cz, cz));
+    cnt += sq < thr2;
+  }
+  return cnt;
+}
+
+// One warp per landmark: nearest plane, vertex-line RANSAC model, radius,
+// features.  Writes cyl_all[l] with stage 1 when a model exists.
+constexpr int kCylWarps = 4;
+constexpr int kMaxLineHyp = 256;
+
+__global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
+  __shared__ int scnt[kCylWarps][kMaxLineHyp];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int nl = d.cnt->n_lm, np = d.cnt->n_planes;
+  for (int l = wg; l < nl; l += nw) {
+    CylD c{};
+    c.landmark = l;
+    c.plane = -1;
+    c.stage = 0;
+    c.valid = 0;
+    c.radius = -1;
+    if (lane == 0) d.cyl_best[l] = 0ull;
+    const int vb = d.lm_vbeg[l], V = d.lm_vbeg[l + 1] - vb;
+    const float* vx = d.lm_vxyz + 3 * (size_t)vb;
+    c.id = d.lm_tree[l];
+    // features (cylinder.cpp:82-91, 172): the first F vertex points
+    {
+      const int p0 = d.lm_pbeg[vb], p1 = d.lm_pbeg[vb + V];
+      for (int f = lane; f < kp.F; f += 32) {
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p0 + f < p1) {
+          q = d.lm_pts[p0 + f];
+          q.w = (float)c.id;
+        }
+        d.cyl_feat_all[(size_t)l * kp.F + f] = q;
+      }
+    }
+    if (V < 3 || np == 0) {
+      if (lane == 0) d.cyl_all[l] = c;
+      continue;
+    }
+    // ---- nearest plane to vertex[1] (sloam.cpp:420-431)
+    const d3 v1 = mk3(vx[3], vx[4], vx[5]);
+    double bd = 100000.0;
+    int bi = 0;
+    for (int k = lane; k < np; k += 32) {
+      const PlaneD& P = d.planes[k];
+      const double dist = fabs(P.plane[0] * v1.x + P.plane[1] * v1.y + P.plane[2] * v1.z + P.plane[3]) /
+                          norm3(mk3(P.plane[0], P.plane[1], P.plane[2]));
+      if (dist < bd) { bd = dist; bi = k; }
+    }
+    warp_argmin(bd, bi);
+    if (!(bd < 100000.0)) bi = 0;
+    c.plane = bi;
+    const PlaneD P = d.planes[bi];
+    // ---- within maxLidarDist (cylinder.cpp:11-13)
+    const float cxf = (float)P.centroid[0], cyf = (float)P.centroid[1];
+    const bool within = (double)euclid2d_f(vx[3], vx[4], cxf, cyf) < kp.max_lidar_dist;
+    if (!within) {
+      if (lane == 0) d.cyl_all[l] = c;
+      continue;
+    }
+    c.root[0] = vx[3]; c.root[1] = vx[4]; c.root[2] = vx[5];
+    // ---- validRadii median (cylinder.cpp:141-163)
+    int nvalid = 0, nle0 = 0;
+    for (int j = lane; j < V; j += 32) {
+      const int npj = d.lm_pbeg[vb + j + 1] - d.lm_pbeg[vb + j];
+      if (npj > 3) {
+        ++nvalid;
+        if (!((float)d.lm_vrad[vb + j] > 0.0f)) ++nle0;
+      }
+    }
+    nvalid = warp_sumi(nvalid);
+    nle0 = warp_sumi(nle0);
+    float rad_med = -1.0f;
+    if (nvalid > 0) {
+      const int dd = nle0;
+      const int middle = min(nvalid - 1, (dd + 1) + (nvalid - dd) / 2);
+      float found = -FLT_MAX;
+      for (int j = lane; j < V; j += 32) {
+        const int npj = d.lm_pbeg[vb + j + 1] - d.lm_pbeg[vb + j];
+        if (npj <= 3) continue;
+        const float rj = (float)d.lm_vrad[vb + j];
+        int rank = 0;
+        for (int k = 0; k < V; ++k) {
+          const int npk = d.lm_pbeg[vb + k + 1] - d.lm_pbeg[vb + k];
+          if (npk <= 3) continue;
+          const float rk = (float)d.lm_vrad[vb + k];
+          rank += (rk < rj) || (rk == rj && k < j);
+        }
+        if (rank == middle) found = rj;
+      }
+      for (int o = 16; o > 0; o >>= 1) found = fmaxf(found, __shfl_xor_sync(0xffffffffu, found, o));
+      rad_med = found;
+    }
+    // ---- tree height (cylinder.cpp:101-113)
+    const float* top = vx + 3 * (V - 2);
+    if (eigen_sqnorm3(vx[3], vx[4], vx[5], top[0], top[1], top[2]) < kp.min_tree_height_sq) {
+      if (lane == 0) d.cyl_all[l] = c;  // radius -1: invalid
+      continue;
+    }
+    // ---- vertex-line RANSAC (PCL SACMODEL_LINE semantics)
+    const float thr2 = (float)(kp.line_thr * kp.line_thr);
+    const int K = min(kp.line_max_iter, kMaxLineHyp);
+    for (int h = lane; h < K; h += 32) {
+      uint32_t u[4], id[2];
+      philox(kp.seed, (uint32_t)h, (uint32_t)c.id, 0u, 0u, u);
+      draw_distinct(u, (uint32_t)V, 2, id);
+      const float ax = vx[3 * id[0]], ay = vx[3 * id[0] + 1], az = vx[3 * id[0] + 2];
+      float dx = fsub(vx[3 * id[1]], ax), dy = fsub(vx[3 * id[1] + 1], ay),
+            dz = fsub(vx[3 * id[1] + 2], az);
+      const float nn = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+      int cnt = -1;
+      if (nn != 0.0f) {
+        const float nr = fsqrt(nn);
+        dx = fdiv(dx, nr); dy = fdiv(dy, nr); dz = fdiv(dz, nr);
+        cnt = line_count(vx, V, ax, ay, az, dx, dy, dz, thr2, 0, 1);
+      }
+      scnt[w][h] = cnt;
+    }
+    __syncwarp();
+    int best = -1, best_count = 0;
+    if (lane == 0) {
+      double k = 1.0;
+      int itn = 0;
+      const double log_p = log(1.0 - kp.line_prob);
+      const double eps = DBL_EPSILON;
+      for (int h = 0; h < K; ++h) {
+        if (!(itn < k)) break;
+        const int cnt = scnt[w][h];
+        if (cnt < 0) continue;
+        if (cnt > best_count) {
+          best_count = cnt;
+          best = h;
+          const double wgt = (double)best_count / V;
+          double p_no = 1.0 - wgt * wgt;
+          p_no = fmax(eps, fmin(1.0 - eps, p_no));
+          k = log_p / log(p_no);
+        }
+        ++itn;
+      }
+    }
+    best = __shfl_sync(0xffffffffu, best, 0);
+    best_count = __shfl_sync(0xffffffffu, best_count, 0);
+    c.inliers = best_count;
+    if (best < 0) {
+      if (lane == 0) d.cyl_all[l] = c;
+      continue;
+    }
+    uint32_t u[4], id[2];
+    philox(kp.seed, (uint32_t)best, (uint32_t)c.id, 0u, 0u, u);
+    draw_distinct(u, (uint32_t)V, 2, id);
+    const float ax = vx[3 * id[0]], ay = vx[3 * id[0] + 1], az = vx[3 * id[0] + 2];
+    float dx = fsub(vx[3 * id[1]], ax), dy = fsub(vx[3 * id[1] + 1], ay),
+          dz = fsub(vx[3 * id[1] + 2], az);
+    {
+      const float nr = fsqrt(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+      dx = fdiv(dx, nr); dy = fdiv(dy, nr); dz = fdiv(dz, nr);
+    }
+    // inliers of the best model -> PCA refit (FP64)
+    int ni = 0;
+    double sx = 0, sy = 0, sz = 0;
+    unsigned inl_lo = 0, inl_hi = 0;  // V <= 64 inlier bit mask
+    for (int j = lane; j < V; j += 32) {
+      const float vxj = fsub(ax, vx[3 * j]), vyj = fsub(ay, vx[3 * j + 1]),
+                  vzj = fsub(az, vx[3 * j + 2]);
+      const float cx = fsub(fmul(vyj, dz), fmul(vzj, dy));
+      const float cy = fsub(fmul(vzj, dx), fmul(vxj, dz));
+      const float cz = fsub(fmul(vxj, dy), fmul(vyj, dx));
+      const float sq = fadd(fadd(fmul(cx, cx), fmul(cy, cy)), fmul(cz, cz));
+      if (sq < thr2) {
+        ++ni;
+        sx += vx[3 * j]; sy += vx[3 * j + 1]; sz += vx[3 * j + 2];
+        if (j < 32) inl_lo |= 1u << j;
+        else inl_hi |= 1u << (j - 32);
+      }
+    }
+    ni = warp_sumi(ni);
+    sx = warp_sumd(sx); sy = warp_sumd(sy); sz = warp_sumd(sz);
+    for (int o = 16; o > 0; o >>= 1) {
+      inl_lo |= __shfl_xor_sync(0xffffffffu, inl_lo, o);
+      inl_hi |= __shfl_xor_sync(0xffffffffu, inl_hi, o);
+    }
+    d3 cpt = mk3(ax, ay, az), dir = mk3(dx, dy, dz);
+    if (ni > 2) {
+      const d3 m = mk3(sx / ni, sy / ni, sz / ni);
+      double s6[6] = {0, 0, 0, 0, 0, 0};
+      for (int j = lane; j < V; j += 32) {
+        const bool in = j < 32 ? ((inl_lo >> j) & 1u) : ((inl_hi >> (j - 32)) & 1u);
+        if (!in) continue;
+        const double q0 = vx[3 * j] - m.x, q1 = vx[3 * j + 1] - m.y, q2 = vx[3 * j + 2] - m.z;
+        s6[0] += q0 * q0; s6[1] += q0 * q1; s6[2] += q0 * q2;
+        s6[3] += q1 * q1; s6[4] += q1 * q2; s6[5] += q2 * q2;
+      }
+      for (int j = 0; j < 6; ++j) s6[j] = warp_sumd(s6[j]);
+      const double S[9] = {s6[0], s6[1], s6[2], s6[1], s6[3], s6[4], s6[2], s6[4], s6[5]};
+      cpt = m;
+      dir = pcl_line_direction(S);
+    }
+    int reinl = 0;
+    for (int j = lane; j < V; j += 32) {
+      const d3 q = sub3(mk3(vx[3 * j], vx[3 * j + 1], vx[3 * j + 2]), cpt);
+      const d3 x = cross3(q, dir);
+      reinl += dot3(x, x) < kp.line_thr * kp.line_thr;
+    }
+    reinl = warp_sumi(reinl);
+    if (reinl == 0) {
+      if (lane == 0) d.cyl_all[l] = c;
+      continue;
+    }
+    c.ray[0] = (double)(float)dir.x;
+    c.ray[1] = (double)(float)dir.y;
+    c.ray[2] = (double)(float)dir.z;
+    double radius = -1.0;
+    if (nvalid > 0) {
+      radius = rad_med;
+      if (radius == 0) radius = -1;
+      else if (radius < kp.default_tree_radius) radius = kp.default_tree_radius;
+    }
+    c.radius = radius;
+    c.stage = 1;
+    if (lane == 0) d.cyl_all[l] = c;
+  }
+}
+
+// ---------------------------------------------- point-level cylinder fit
+constexpr int kHypThreads = 128;
+constexpr int kPtCap = 12288;  // projected points staged in shared memory
+
+struct CylFrame {
+  float ox, oy, oz;
+  float ax, ay, az;
+  float e1x, e1y, e1z, e2x, e2y, e2z;
+};
+
+__device__ __forceinline__ CylFrame make_frame(const Dev& d, const CylD& c) {
+  CylFrame f;
+  const float* vx = d.lm_vxyz + 3 * (size_t)d.lm_vbeg[c.landmark];
+  f.ox = vx[3]; f.oy = vx[4]; f.oz = vx[5];
+  float ax = (float)c.ray[0], ay = (float)c.ray[1], az = (float)c.ray[2];
+  if (az < 0) { ax = -ax; ay = -ay; az = -az; }
+  float tx = 1.0f, ty = 0.0f, tz = 0.0f;
+  if (!(fabsf(ax) < 0.9f)) { tx = 0.0f; ty = 1.0f; }
+  float e1x = fsub(fmul(ay, tz), fmul(az, ty)), e1y = fsub(fmul(az, tx), fmul(ax, tz)),
+        e1z = fsub(fmul(ax, ty), fmul(ay, tx));
+  const float e1n = fsqrt(fadd(fadd(fmul(e1x, e1x), fmul(e1y, e1y)), fmul(e1z, e1z)));
+  e1x = fdiv(e1x, e1n); e1y = fdiv(e1y, e1n); e1z = fdiv(e1z, e1n);
+  f.e2x = fsub(fmul(ay, e1z), fmul(az, e1y));
+  f.e2y = fsub(fmul(az, e1x), fmul(ax, e1z));
+  f.e2z = fsub(fmul(ax, e1y), fmul(ay, e1x));
+  f.ax = ax; f.ay = ay; f.az = az;
+  f.e1x = e1x; f.e1y = e1y; f.e1z = e1z;
+  return f;
+}
+
+__device__ __forceinline__ float2 project_uv(const CylFrame& f, float4 q) {
+  const float dx = fsub(q.x, f.ox), dy = fsub(q.y, f.oy), dz = fsub(q.z, f.oz);
+  const float u = fadd(fadd(fmul(dx, f.e1x), fmul(dy, f.e1y)), fmul(dz, f.e1z));
+  const float v = fadd(fadd(fmul(dx, f.e2x), fmul(dy, f.e2y)), fmul(dz, f.e2z));
+  return make_float2(u, v);
+}
+
+// The tree's points: its CC cluster, or its vertex points when no cluster.
+__device__ __forceinline__ void tree_points(const Dev& d, int l, const float4** pts, int* n) {
+  const int c0 = d.lm_cbeg[l], c1 = d.lm_cbeg[l + 1];
+  if (c1 > c0) {
+    *pts = d.lm_cpts + c0;
+    *n = c1 - c0;
+  } else {
+    const int vb = d.lm_vbeg[l], ve = d.lm_vbeg[l + 1];
+    *pts = d.lm_pts + d.lm_pbeg[vb];
+    *n = d.lm_pbeg[ve] - d.lm_pbeg[vb];
+  }
+}
+
+struct Hyp {
+  float cu, cv, r, lo2, hi2;
+  bool ok;
+};
+
+template <typename UV>
+__device__ __forceinline__ Hyp make_hyp(const KParams& kp, int h, int tree_id, int n, UV uv) {
+  Hyp H{};
+  H.ok = false;
+  uint32_t u[4], id[3];
+  philox(kp.seed, (uint32_t)h, (uint32_t)tree_id, 1u, 0u, u);
+  draw_distinct(u, (uint32_t)n, 3, id);
+  const float2 p0 = uv(id[0]), p1 = uv(id[1]), p2 = uv(id[2]);
+  const float bx = fsub(p1.x, p0.x), by = fsub(p1.y, p0.y);
+  const float cx = fsub(p2.x, p0.x), cy = fsub(p2.y, p0.y);
+  const float t1 = fmul(bx, cy), t2 = fmul(by, cx);
+  const float den = fmul(2.0f, fsub(t1, t2));
+  if (den == 0.0f) return H;
+  const float b2 = fadd(fmul(bx, bx), fmul(by, by)), c2 = fadd(fmul(cx, cx), fmul(cy, cy));
+  const float ox = fdiv(fsub(fmul(cy, b2), fmul(by, c2)), den);
+  const float oy = fdiv(fsub(fmul(bx, c2), fmul(cx, b2)), den);
+  const float r = fsqrt(fadd(fmul(ox, ox), fmul(oy, oy)));
+  if (!(r <= kp.max_hyp_r)) return H;
+  H.cu = fadd(p0.x, ox);
+  H.cv = fadd(p0.y, oy);
+  H.r = r;
+  const float lo = fsub(r, kp.tau), hi = fadd(r, kp.tau);
+  H.lo2 = lo > 0.0f ? fmul(lo, lo) : -1.0f;
+  H.hi2 = fmul(hi, hi);
+  H.ok = true;
+  return H;
+}
+
+// Blocks of kHypThreads: one hypothesis per thread, the tree's projected
+// points in shared memory, every thread sweeps all points (broadcast reads).
+__global__ void __launch_bounds__(kHypThreads) k_cyl_hyp(Dev d, KParams kp) {
+  extern __shared__ float2 suv[];
+  const int nl = d.cnt->n_lm;
+  const int chunks = (kp.K + kHypThreads - 1) / kHypThreads;
+  for (int item = blockIdx.x; item < nl * chunks; item += gridDim.x) {
+    const int l = item / chunks, ch = item - l * chunks;
+    const CylD c = d.cyl_all[l];
+    if (c.stage != 1 || c.radius == -1.0) continue;
+    const float4* pts;
+    int n;
+    tree_points(d, l, &pts, &n);
+    if (n < 3) continue;
+    const CylFrame f = make_frame(d, c);
+    const bool inshm = n <= kPtCap;
+    if (inshm) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) suv[i] = project_uv(f, pts[i]);
+      __syncthreads();
+    }
+    const int h = ch * kHypThreads + threadIdx.x;
+    if (h < kp.K) {
+      Hyp H;
+      if (inshm) H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return suv[i]; });
+      else H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return project_uv(f, pts[i]); });
+      if (H.ok) {
+        int cnt = 0;
+        if (inshm) {
+#pragma unroll 4
+          for (int i = 0; i < n; ++i) {
+            const float2 q = suv[i];
+            const float du = fsub(q.x, H.cu), dv = fsub(q.y, H.cv);
+            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+            cnt += (d2 > H.lo2) & (d2 < H.hi2);
+          }
+        } else {
+          for (int i = 0; i < n; ++i) {
+            const float2 q = project_uv(f, pts[i]);
+            const float du = fsub(q.x, H.cu), dv = fsub(q.y, H.cv);
+            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+            cnt += (d2 > H.lo2) & (d2 < H.hi2);
+          }
+        }
+        if (cnt > 0) {
+          const unsigned long long key =
+              ((unsigned long long)cnt << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
+          atomicMax(d.cyl_best + l, key);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One block per tree: inliers of the best hypothesis, LS refinement.
+constexpr int kLsThreads = 256;
+__global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
+  __shared__ float red[20][kLsThreads / 32];
+  __shared__ double st[8];  // c(3), dir(3), r, ok
+  const int nl = d.cnt->n_lm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int l = blockIdx.x; l < nl; l += gridDim.x) {
+    CylD c = d.cyl_all[l];
+    const unsigned long long key = d.cyl_best[l];
+    if (c.stage != 1 || c.radius == -1.0 || key == 0ull) continue;
+    const int h = (int)(0xFFFFFFFFu - (uint32_t)(key & 0xffffffffull));
+    const int best_cnt = (int)(key >> 32);
+    const float4* pts;
+    int n;
+    tree_points(d, l, &pts, &n);
+    const CylFrame f = make_frame(d, c);
+    const Hyp H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return project_uv(f, pts[i]); });
+    if (threadIdx.x == 0) {
+      st[0] = f.ox + (double)H.cu * f.e1x + (double)H.cv * f.e2x;
+      st[1] = f.oy + (double)H.cu * f.e1y + (double)H.cv * f.e2y;
+      st[2] = f.oz + (double)H.cu * f.e1z + (double)H.cv * f.e2z;
+      const double an = sqrt((double)f.ax * f.ax + (double)f.ay * f.ay + (double)f.az * f.az);
+      st[3] = f.ax / an; st[4] = f.ay / an; st[5] = f.az / an;
+      st[6] = H.r;
+      st[7] = 1.0;
+    }
+    __syncthreads();
+    for (int itn = 0; itn < kp.ls_iters; ++itn) {
+      if (st[7] == 0.0) break;
+      const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
+      const double r = st[6];
+      const d3 t = fabs(dd.x) < 0.9 ? mk3(1, 0, 0) : mk3(0, 1, 0);
+      d3 b1 = cross3(dd, t);
+      b1 = scl3(1.0 / norm3(b1), b1);
+      const d3 b2 = cross3(dd, b1);
+      const float cx = (float)cc.x, cy = (float)cc.y, cz = (float)cc.z;
+      const float dx = (float)dd.x, dy = (float)dd.y, dz = (float)dd.z;
+      const float b1x = (float)b1.x, b1y = (float)b1.y, b1z = (float)b1.z;
+      const float b2x = (float)b2.x, b2y = (float)b2.y, b2z = (float)b2.z;
+      const float rf = (float)r;
+      float acc[20];
+#pragma unroll
+      for (int j = 0; j < 20; ++j) acc[j] = 0.f;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float4 q = pts[i];
+        const float2 uv = project_uv(f, q);
+        const float du = fsub(uv.x, H.cu), dv = fsub(uv.y, H.cv);
+        const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+        if (!((d2 > H.lo2) & (d2 < H.hi2))) continue;
+        const float wx = q.x - cx, wy = q.y - cy, wz = q.z - cz;
+        const float wd = wx * dx + wy * dy + wz * dz;
+        const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
+        const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
+        if (!(rho > 0.f)) continue;
+        const float res = rho - rf;
+        const float a1 = (px_ * b1x + py_ * b1y + pz_ * b1z) / rho;
+        const float a2 = (px_ * b2x + py_ * b2y + pz_ * b2z) / rho;
+        const float J[5] = {-a1, -a2, -wd * a1, -wd * a2, -1.0f};
+        int k = 0;
+#pragma unroll
+        for (int p = 0; p < 5; ++p)
+#pragma unroll
+          for (int q2 = p; q2 < 5; ++q2) acc[k++] += J[p] * J[q2];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) acc[15 + p] += J[p] * res;
+      }
+#pragma unroll
+      for (int j = 0; j < 20; ++j) {
+        const float v = warp_sum(acc[j]);
+        if (lane == 0) red[j][w] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double s[20];
+        for (int j = 0; j < 20; ++j) {
+          double t2 = 0;
+          for (int q2 = 0; q2 < kLsThreads / 32; ++q2) t2 += red[j][q2];
+          s[j] = t2;
+        }
+        double Hm[25], g[5], x[5];
+        int k = 0;
+        for (int p = 0; p < 5; ++p)
+          for (int q2 = p; q2 < 5; ++q2) {
+            Hm[5 * p + q2] = s[k];
+            Hm[5 * q2 + p] = s[k];
+            ++k;
+          }
+        for (int p = 0; p < 5; ++p) g[p] = -s[15 + p];
+        if (chol_solve(5, Hm, g, x)) {
+          d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
+          d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
+          d2 = scl3(1.0 / norm3(d2), d2);
+          st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
+          st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
+          st[6] = r + x[4];
+        } else {
+          st[7] = 0.0;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
+      if (dd.z < 0) dd = scl3(-1.0, dd);
+      const float* vx = d.lm_vxyz + 3 * (size_t)d.lm_vbeg[l];
+      const d3 b = mk3(vx[3], vx[4], vx[5]);
+      const d3 root = add3(cc, scl3(dot3(sub3(b, cc), dd), dd));
+      c.root[0] = root.x; c.root[1] = root.y; c.root[2] = root.z;
+      c.ray[0] = dd.x; c.ray[1] = dd.y; c.ray[2] = dd.z;
+      c.radius = st[6] > 0 ? st[6] : -1.0;
+      c.inliers = best_cnt;
+      c.stage = 2;
+      d.cyl_all[l] = c;
+    }
+    __syncthreads();
+  }
+}
+
+// groundBasedRoot (cylinder.cpp:41-55), validNorm, filter (cylinder.cpp:57-73).
+__global__ void __launch_bounds__(256) k_cyl_finalize(Dev d, KParams kp) {
+  const int nl = d.cnt->n_lm;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
+    CylD c = d.cyl_all[l];
+    if (c.stage == 0) {
+      c.valid = 0;
+      d.cyl_all[l] = c;
+      continue;
+    }
+    const PlaneD P = d.planes[c.plane];
+    const d3 n = mk3(P.plane[0], P.plane[1], P.plane[2]);
+    d3 root = mk3(c.root[0], c.root[1], c.root[2]);
+    const d3 ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
+    const float dist = (float)(fabs(P.plane[0] * root.x + P.plane[1] * root.y +
+                                    P.plane[2] * root.z + P.plane[3]) / norm3(n));
+    bool validZ = false;
+    if (dist < kp.root_plane_max_dist) {
+      // rayPlaneIntersection, utils.h:41-51
+      const float denom = (float)dot3(n, ray);
+      if (fabsf(denom) > 0.001f) {
+        const float t = (float)(dot3(sub3(mk3(P.centroid[0], P.centroid[1], P.centroid[2]), root), n) /
+                                (double)denom);
+        if (t >= 0.001f) root = add3(root, scl3((double)t, ray));
+      }
+      validZ = true;
+    }
+    c.root[0] = root.x; c.root[1] = root.y; c.root[2] = root.z;
+    const bool validNorm = norm3(root) > 0.01;
+    const bool validRadius = c.radius > 0.0;
+    bool validTree = false;
+    if (c.radius != -1.0) {
+      const double theta = (180.0 / kPIDEF) * acos(dot3(ray, n) / (norm3(ray) * norm3(n)));
+      validTree = (c.radius < kp.max_tree_radius) &&
+                  ((theta <= kp.max_axis_theta) || (theta >= 180.0 - kp.max_axis_theta));
+    }
+    c.valid = validZ && validRadius && validTree && validNorm;
+    d.cyl_all[l] = c;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_cyl_compact(Dev d, KParams kp) {
+  __shared__ int sm[33];
+  const int nl = d.cnt->n_lm;
+  int base = 0;
+  for (int l0 = 0; l0 < nl; l0 += blockDim.x) {
+    const int l = l0 + threadIdx.x;
+    const bool v = l < nl && d.cyl_all[l].valid;
+    int total;
+    const int ex = block_excl_scan(v ? 1 : 0, sm, &total);
+    if (v) {
+      d.cyls[base + ex] = d.cyl_all[l];
+      for (int f = 0; f < kp.F; ++f)
+        d.cyl_feat[(size_t)(base + ex) * kp.F + f] = d.cyl_feat_all[(size_t)l * kp.F + f];
+    }
+    base += total;
+  }
+  if (threadIdx.x == 0) d.cnt->n_cyl = base;
+}
+
+__global__ void k_zero_bins(Dev d) {
+  for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x) d.bin_cnt[b] = 0;
+}
+
+}  // namespace
+
+int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream_t st) {
+  const size_t smem = (size_t)kPtCap * sizeof(float2);
+  k_cyl_hyp<<<152 * 6, kHypThreads, smem, st>>>(d, kp);
+  k_cyl_ls<<<152 * 2, kLsThreads, 0, st>>>(d, kp);
+  return 2;
+}
+
+int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
+  int n = 0;
+  k_zero_bins<<<1, 256, 0, st>>>(d);
+  const int gg = (d.cap_ground + 255) / 256;
+  k_gbin<<<gg < 1 ? 1 : gg, 256, 0, st>>>(d, kp);
+  k_gbin_scan<<<1, 1024, 0, st>>>(d);
+  k_gbin_scatter<<<gg < 1 ? 1 : gg, 256, 0, st>>>(d);
+  k_plane<<<d.n_bins, kPlaneThreads, 0, st>>>(d, kp);
+  k_plane_compact<<<1, 1024, 0, st>>>(d, kp);
+  n += 6;
+  const int gl = (d.cap_lm + kCylWarps - 1) / kCylWarps;
+  k_cyl_fit<<<gl < 1 ? 1 : gl, kCylWarps * 32, 0, st>>>(d, kp);
+  ++n;
+  if (kp.cyl_mode == 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
+  k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
+  k_cyl_compact<<<1, 1024, 0, st>>>(d, kp);
+  return n + 2;
+}
+
+void init_kernel_attributes() {
+  cudaFuncSetAttribute(k_cyl_hyp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(kPtCap * sizeof(float2)));
+}
+
+}  // namespace sg

@@ -1,0 +1,511 @@
+// pose.cu — a9-a11: association, pose update, re-projection and map
+// association of sloam::sloam::RunSloam (sloam.cpp:453-532).
+//
+// a9  matchFeatures (sloam.cpp:257-296): one warp per current object, lanes
+//     over the map, FP64 model distances, argmin with first-index ties.
+// a10 pose (replacing Ceres LM, sloam.cpp:33-255): fixed gn_iters
+//     Gauss-Newton iterations with IRLS Huber weights in one 1024-thread
+//     block; residuals and Jacobians in FP32 in a frame anchored at the pose
+//     estimate's translation, J^T J / J^T r reduced with warp shuffles, the
+//     normal equations solved and the SE(3) update applied in FP64.  Joint
+//     mode: left SO(3) perturbation + translation (6x6).  Two-step mode:
+//     the reference's angle-axis 6-vector with {x, y, yaw} then
+//     {z, roll, pitch} free (3x3 each) and its angle-axis recombination.
+// a11 projectModels + matchModels (sloam.cpp:298-328, 438-451) and the
+//     prevGPlanes_ update.
+#include <cfloat>
+
+#include "internal.h"
+#include "scan_util.cuh"
+
+namespace sg {
+
+namespace {
+
+__device__ __forceinline__ Pose pose_at(const double* p) {
+  sloam_se3 s;
+  for (int j = 0; j < 4; ++j) s.q[j] = p[j];
+  for (int j = 0; j < 3; ++j) s.t[j] = p[4 + j];
+  return pose_from(s);
+}
+__device__ __forceinline__ void pose_store(double* p, const Pose& T) {
+  const sloam_se3 s = pose_to(T);
+  for (int j = 0; j < 4; ++j) p[j] = s.q[j];
+  for (int j = 0; j < 3; ++j) p[4 + j] = s.t[j];
+}
+
+// Cylinder::distance(model), cylinder.cpp:175-194 (self = map object).
+__device__ __forceinline__ double cyl_dist(d3 sr, d3 sd, d3 tr, d3 td) {
+  double acc = 0.0;
+  const double hs[3] = {0.0, 3.0, 6.0};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double st = (hs[k] - sr.z) / sd.z;
+    const d3 mp = add3(sr, scl3(st, sd));
+    const double tt = (hs[k] - tr.z) / td.z;
+    const d3 tp = add3(tr, scl3(tt, td));
+    acc += norm3(sub3(mp, tp));
+  }
+  return acc / 3.0;
+}
+
+// Cylinder::project, cylinder.cpp:205-211
+__device__ __forceinline__ void cyl_project(const Pose& T, d3& root, d3& ray) {
+  const d3 other = xform(T, add3(root, ray));
+  root = xform(T, root);
+  ray = sub3(other, root);
+}
+
+__global__ void __launch_bounds__(256) k_assoc(Dev d, KParams kp) {
+  const int lane = threadIdx.x & 31;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int nc = d.cnt->n_cyl, np = d.cnt->n_planes, nprev = d.cnt->n_prev;
+  const Pose T = pose_at(d.pose_io);
+  for (int it = wg; it < nc + np; it += nw) {
+    if (it < nc) {
+      const CylD c = d.cyls[it];
+      d3 root = mk3(c.root[0], c.root[1], c.root[2]), ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
+      cyl_project(T, root, ray);
+      double bd = kp.tree_match_thresh + 100;
+      int bi = 0;
+      const int n_map = d.in->n_map;
+      const sloam_cylinder* map = d.in->map;
+      for (int k = lane; k < n_map; k += 32) {
+        const sloam_cylinder& m = map[k];
+        const double dist = cyl_dist(mk3(m.root[0], m.root[1], m.root[2]),
+                                     mk3(m.ray[0], m.ray[1], m.ray[2]), root, ray);
+        if (dist < bd) { bd = dist; bi = k; }
+      }
+      warp_argmin(bd, bi);
+      if (lane == 0) d.cyl_match[it] = (n_map > 0 && bd < kp.tree_match_thresh) ? bi : -1;
+    } else {
+      const int p = it - nc;
+      const PlaneD P = d.planes[p];
+      const d3 c = xform(T, mk3(P.centroid[0], P.centroid[1], P.centroid[2]));
+      double bd = kp.plane_match_thresh + 100;
+      int bi = 0;
+      for (int k = lane; k < nprev; k += 32) {
+        const PlaneD& Q = d.prev_planes[k];
+        const double dist = norm3(sub3(mk3(Q.centroid[0], Q.centroid[1], Q.centroid[2]), c));
+        if (dist < bd) { bd = dist; bi = k; }
+      }
+      warp_argmin(bd, bi);
+      if (lane == 0) d.plane_match[p] = (nprev > 0 && bd < kp.plane_match_thresh) ? bi : -1;
+    }
+  }
+}
+
+constexpr int kGN = 1024;
+
+// block reduction of NV floats: result valid in thread 0's `out`
+template <int NV>
+__device__ __forceinline__ void block_reduce(float* acc, float (*red)[kGN / 32], double* out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    const float v = warp_sum(acc[j]);
+    if (lane == 0) red[j][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < NV; ++j) {
+      double s = 0;
+      for (int q = 0; q < kGN / 32; ++q) s += red[j][q];
+      out[j] = s;
+    }
+  }
+}
+
+struct ResRef {
+  int kind;  // 0 none, 1 cylinder, 2 plane
+  float px, py, pz;
+  int obj;
+};
+
+__device__ __forceinline__ ResRef residual_at(const Dev& d, const KParams& kp, int i, int nc,
+                                              int np) {
+  ResRef r{0, 0, 0, 0, -1};
+  if (i < nc * kp.F) {
+    const int c = i / kp.F;
+    const int m = d.cyl_match[c];
+    if (m < 0) return r;
+    const float4 f = d.cyl_feat[(size_t)c * kp.F + (i - c * kp.F)];
+    return ResRef{1, f.x, f.y, f.z, m};
+  }
+  i -= nc * kp.F;
+  if (i < np * kp.G) {
+    const int p = i / kp.G;
+    const int m = d.plane_match[p];
+    if (m < 0) return r;
+    const float4 f = d.plane_feat[(size_t)p * kp.G + (i - p * kp.G)];
+    return ResRef{2, f.x, f.y, f.z, m};
+  }
+  return r;
+}
+
+// residual and gradient w.r.t. the transformed point lp (float)
+__device__ __forceinline__ float residual_eval(const Dev& d, const ResRef& rr, float lx, float ly,
+                                               float lz, const double* anchor, float* J) {
+  if (rr.kind == 1) {
+    const sloam_cylinder& m = d.in->map[rr.obj];
+    const float rx = (float)(m.root[0] - anchor[0]), ry = (float)(m.root[1] - anchor[1]),
+                rz = (float)(m.root[2] - anchor[2]);
+    const float ax = (float)m.ray[0], ay = (float)m.ray[1], az = (float)m.ray[2];
+    const float vx = lx - rx, vy = ly - ry, vz = lz - rz;
+    const float s = (vx * ax + vy * ay + vz * az) / (ax * ax + ay * ay + az * az);
+    const float wx = vx - s * ax, wy = vy - s * ay, wz = vz - s * az;
+    const float nw = sqrtf(wx * wx + wy * wy + wz * wz);
+    if (nw > 0.f) {
+      J[0] = wx / nw; J[1] = wy / nw; J[2] = wz / nw;
+    } else {
+      J[0] = J[1] = J[2] = 0.f;
+    }
+    return nw - (float)m.radius;
+  }
+  const PlaneD& Q = d.prev_planes[rr.obj];
+  const float nx = (float)Q.plane[0], ny = (float)Q.plane[1], nz = (float)Q.plane[2];
+  const float dd = (float)(Q.plane[3] + Q.plane[0] * anchor[0] + Q.plane[1] * anchor[1] +
+                           Q.plane[2] * anchor[2]);
+  const float num = nx * lx + ny * ly + nz * lz + dd;
+  const float nn = sqrtf(nx * nx + ny * ny + nz * nz);
+  const float sg = num > 0.f ? 1.f : (num < 0.f ? -1.f : 0.f);
+  J[0] = sg * nx / nn; J[1] = sg * ny / nn; J[2] = sg * nz / nn;
+  return fabsf(num) / nn;
+}
+
+__device__ __forceinline__ float huber_w(float r, float delta) {
+  const float a = fabsf(r);
+  return a <= delta ? 1.0f : delta / a;
+}
+
+// Ceres QuaternionToAngleAxis / AngleAxisToQuaternion (rotation.h), restated.
+__device__ void quat_to_aa(const double* qwxyz, double* aa) {
+  const double q1 = qwxyz[1], q2 = qwxyz[2], q3 = qwxyz[3];
+  const double s2 = q1 * q1 + q2 * q2 + q3 * q3;
+  if (s2 > 0.0) {
+    const double s = sqrt(s2), c = qwxyz[0];
+    const double two_theta = 2.0 * ((c < 0.0) ? atan2(-s, -c) : atan2(s, c));
+    const double k = two_theta / s;
+    aa[0] = q1 * k; aa[1] = q2 * k; aa[2] = q3 * k;
+  } else {
+    aa[0] = q1 * 2.0; aa[1] = q2 * 2.0; aa[2] = q3 * 2.0;
+  }
+}
+__device__ void aa_to_quat(const double* aa, double* qwxyz) {
+  const double t2 = aa[0] * aa[0] + aa[1] * aa[1] + aa[2] * aa[2];
+  if (t2 > 0.0) {
+    const double th = sqrt(t2), h = th * 0.5, k = sin(h) / th;
+    qwxyz[0] = cos(h); qwxyz[1] = aa[0] * k; qwxyz[2] = aa[1] * k; qwxyz[3] = aa[2] * k;
+  } else {
+    qwxyz[0] = 1.0; qwxyz[1] = aa[0] * 0.5; qwxyz[2] = aa[1] * 0.5; qwxyz[3] = aa[2] * 0.5;
+  }
+}
+
+// Rotation (Rm: the point map) and the pieces of d(R(r)p)/dr = -Rj [p]x Jr for
+// an angle-axis vector r (Ceres AngleAxisRotatePoint semantics, including its
+// first-order branch for theta^2 <= DBL_EPSILON).
+__device__ void aa_mats(const double* r, double* Rm, double* Rj, double* Jr) {
+  const double th2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  if (th2 > DBL_EPSILON) {
+    const double th = sqrt(th2);
+    so3_exp(mk3(r[0], r[1], r[2]), Rm);
+    for (int k = 0; k < 9; ++k) Rj[k] = Rm[k];
+    const double A = (1.0 - cos(th)) / th2, B = (th - sin(th)) / (th2 * th);
+    const double K[9] = {0, -r[2], r[1], r[2], 0, -r[0], -r[1], r[0], 0};
+    double K2[9];
+    matmul3(K, K, K2);
+    for (int i = 0; i < 9; ++i) Jr[i] = (i % 4 == 0 ? 1.0 : 0.0) - A * K[i] + B * K2[i];
+  } else {
+    const double K[9] = {0, -r[2], r[1], r[2], 0, -r[0], -r[1], r[0], 0};
+    for (int i = 0; i < 9; ++i) {
+      Rm[i] = (i % 4 == 0 ? 1.0 : 0.0) + K[i];
+      Rj[i] = (i % 4 == 0 ? 1.0 : 0.0);
+      Jr[i] = (i % 4 == 0 ? 1.0 : 0.0);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
+  __shared__ float red[27][kGN / 32];
+  __shared__ double s_out[27];
+  __shared__ float sR[9], sT[3], sRj[9], sJr[9];
+  __shared__ double s_R[9], s_t[3], s_x[6], s_anchor[3];
+  __shared__ int s_ok, s_checks[4];
+  const int nc = d.cnt->n_cyl, np = d.cnt->n_planes;
+  const int nitems = nc * kp.F + np * kp.G;
+  // ---- counts and gates (sloam.cpp:499-500)
+  {
+    __shared__ int sm[33];
+    int mc = 0, mp = 0;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) mc += d.cyl_match[c] >= 0;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) mp += d.plane_match[p] >= 0;
+    int tc, tp;
+    block_excl_scan(mc, sm, &tc);
+    block_excl_scan(mp, sm, &tp);
+    if (threadIdx.x == 0) {
+      const int ntm = tc * kp.F, npm = tp * kp.G;
+      d.cnt->n_tm = ntm;
+      d.cnt->n_pm = npm;
+      const int tchk = nc > kp.min_tree_models && ntm > 5.0 * kp.F;
+      const int gchk = npm > kp.min_ground_models && np > kp.min_planes;
+      d.cnt->tree_check = tchk;
+      d.cnt->ground_check = gchk;
+      s_checks[0] = tchk;
+      s_checks[1] = gchk;
+      const Pose E = pose_at(d.pose_io);
+      for (int k = 0; k < 9; ++k) s_R[k] = E.R[k];
+      s_anchor[0] = E.t.x; s_anchor[1] = E.t.y; s_anchor[2] = E.t.z;
+      s_t[0] = s_t[1] = s_t[2] = 0.0;
+      s_ok = 1;
+      d.cnt->status = (np == 0 || nc == 0) ? SLOAM_ERR_NO_MODELS : SLOAM_OK;
+      // defaults: T_Map_Curr = estimate, T_Delta = identity
+      for (int j = 0; j < 7; ++j) d.pose_io[7 + j] = d.pose_io[j];
+      for (int j = 0; j < 7; ++j) d.pose_io[14 + j] = (j == 3) ? 1.0 : 0.0;
+      d.cnt->success = 1;
+    }
+    __syncthreads();
+  }
+  if (np == 0 || nc == 0) return;
+  const int tchk = s_checks[0], gchk = s_checks[1];
+  const float delta = (float)kp.huber;
+  if (!kp.two_step) {
+    if (!(tchk && gchk)) return;
+    // ---------------------------------------------------------- joint
+    for (int itn = 0; itn < kp.gn_iters; ++itn) {
+      if (threadIdx.x == 0) {
+        for (int k = 0; k < 9; ++k) sR[k] = (float)s_R[k];
+        for (int k = 0; k < 3; ++k) sT[k] = (float)s_t[k];
+      }
+      __syncthreads();
+      float acc[27];
+#pragma unroll
+      for (int j = 0; j < 27; ++j) acc[j] = 0.f;
+      for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
+        const ResRef rr = residual_at(d, kp, i, nc, np);
+        if (rr.kind == 0) continue;
+        const float qx = sR[0] * rr.px + sR[1] * rr.py + sR[2] * rr.pz;
+        const float qy = sR[3] * rr.px + sR[4] * rr.py + sR[5] * rr.pz;
+        const float qz = sR[6] * rr.px + sR[7] * rr.py + sR[8] * rr.pz;
+        float Jl[3];
+        const float res = residual_eval(d, rr, qx + sT[0], qy + sT[1], qz + sT[2], s_anchor, Jl);
+        const float J[6] = {qy * Jl[2] - qz * Jl[1], qz * Jl[0] - qx * Jl[2],
+                            qx * Jl[1] - qy * Jl[0], Jl[0], Jl[1], Jl[2]};
+        const float wgt = huber_w(res, delta);
+        int k = 0;
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+          for (int b = a; b < 6; ++b) acc[k++] += wgt * J[a] * J[b];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) acc[21 + a] += wgt * J[a] * res;
+      }
+      block_reduce<27>(acc, red, s_out);
+      if (threadIdx.x == 0) {
+        double Hm[36], g[6], x[6];
+        int k = 0;
+        for (int a = 0; a < 6; ++a)
+          for (int b = a; b < 6; ++b) {
+            Hm[6 * a + b] = s_out[k];
+            Hm[6 * b + a] = s_out[k];
+            ++k;
+          }
+        for (int a = 0; a < 6; ++a) g[a] = -s_out[21 + a];
+        if (s_ok && chol_solve(6, Hm, g, x)) {
+          double dR[9];
+          so3_exp(mk3(x[0], x[1], x[2]), dR);
+          matmul3(dR, s_R, s_R);
+          s_t[0] += x[3]; s_t[1] += x[4]; s_t[2] += x[5];
+        } else {
+          s_ok = 0;
+        }
+      }
+      __syncthreads();
+      if (!s_ok) break;
+    }
+    if (threadIdx.x == 0) {
+      d.cnt->success = s_ok;
+      if (s_ok) {
+        Pose T;
+        for (int k = 0; k < 9; ++k) T.R[k] = s_R[k];
+        T.t = mk3(s_t[0] + s_anchor[0], s_t[1] + s_anchor[1], s_t[2] + s_anchor[2]);
+        pose_store(d.pose_io + 7, T);
+        pose_store(d.pose_io + 14, T);
+      } else {
+        d.cnt->status = SLOAM_ERR_NOT_CONVERGED;
+      }
+    }
+    return;
+  }
+  // -------------------------------------------------------- two-step
+  double rpy[3];
+  double out_tree[3], out_ground[3];
+  {
+    const sloam_se3 e = pose_to(pose_at(d.pose_io));
+    const double qwxyz[4] = {e.q[3], e.q[0], e.q[1], e.q[2]};
+    quat_to_aa(qwxyz, rpy);
+  }
+  for (int step = 0; step < 2; ++step) {
+    const bool opt = step == 0 ? tchk : gchk;
+    const int f0 = step == 0 ? 0 : 2, f1 = step == 0 ? 1 : 3, f2 = step == 0 ? 5 : 4;
+    if (threadIdx.x == 0) {
+      s_x[0] = s_anchor[0]; s_x[1] = s_anchor[1]; s_x[2] = s_anchor[2];
+      s_x[3] = rpy[0]; s_x[4] = rpy[1]; s_x[5] = rpy[2];
+      s_ok = opt ? 1 : 0;
+    }
+    __syncthreads();
+    const int lo = step == 0 ? 0 : nc * kp.F;
+    const int hi = step == 0 ? nc * kp.F : nitems;
+    for (int itn = 0; itn < kp.gn_iters && s_ok; ++itn) {
+      if (threadIdx.x == 0) {
+        double Rm[9], Rj[9], Jr[9];
+        aa_mats(s_x + 3, Rm, Rj, Jr);
+        for (int k = 0; k < 9; ++k) {
+          sR[k] = (float)Rm[k];
+          sRj[k] = (float)Rj[k];
+          sJr[k] = (float)Jr[k];
+        }
+        for (int k = 0; k < 3; ++k) sT[k] = (float)(s_x[k] - s_anchor[k]);
+      }
+      __syncthreads();
+      float acc[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) acc[j] = 0.f;
+      for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const ResRef rr = residual_at(d, kp, i, nc, np);
+        if (rr.kind == 0) continue;
+        const float qx = sR[0] * rr.px + sR[1] * rr.py + sR[2] * rr.pz;
+        const float qy = sR[3] * rr.px + sR[4] * rr.py + sR[5] * rr.pz;
+        const float qz = sR[6] * rr.px + sR[7] * rr.py + sR[8] * rr.pz;
+        float Jl[3];
+        const float res = residual_eval(d, rr, qx + sT[0], qy + sT[1], qz + sT[2], s_anchor, Jl);
+        // d lp / d r_k = -Rj (p x Jr[:,k])
+        float Jfull[6] = {Jl[0], Jl[1], Jl[2], 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float vx = sJr[k], vy = sJr[3 + k], vz = sJr[6 + k];
+          const float cx = rr.py * vz - rr.pz * vy, cy = rr.pz * vx - rr.px * vz,
+                      cz = rr.px * vy - rr.py * vx;
+          const float mx = -(sRj[0] * cx + sRj[1] * cy + sRj[2] * cz);
+          const float my = -(sRj[3] * cx + sRj[4] * cy + sRj[5] * cz);
+          const float mz = -(sRj[6] * cx + sRj[7] * cy + sRj[8] * cz);
+          Jfull[3 + k] = Jl[0] * mx + Jl[1] * my + Jl[2] * mz;
+        }
+        const float J[3] = {Jfull[f0], Jfull[f1], Jfull[f2]};
+        const float wgt = huber_w(res, delta);
+        acc[0] += wgt * J[0] * J[0]; acc[1] += wgt * J[0] * J[1]; acc[2] += wgt * J[0] * J[2];
+        acc[3] += wgt * J[1] * J[1]; acc[4] += wgt * J[1] * J[2]; acc[5] += wgt * J[2] * J[2];
+        acc[6] += wgt * J[0] * res; acc[7] += wgt * J[1] * res; acc[8] += wgt * J[2] * res;
+      }
+      block_reduce<9>(acc, red, s_out);
+      if (threadIdx.x == 0) {
+        const double Hm[9] = {s_out[0], s_out[1], s_out[2], s_out[1], s_out[3],
+                              s_out[4], s_out[2], s_out[4], s_out[5]};
+        const double g[3] = {-s_out[6], -s_out[7], -s_out[8]};
+        double x[3];
+        if (chol_solve(3, Hm, g, x)) {
+          s_x[f0] += x[0]; s_x[f1] += x[1]; s_x[f2] += x[2];
+        } else {
+          s_ok = 0;
+        }
+      }
+      __syncthreads();
+    }
+    if (step == 0) {
+      if (s_ok) { out_tree[0] = s_x[0]; out_tree[1] = s_x[1]; out_tree[2] = s_x[5]; }
+      else { out_tree[0] = s_anchor[0]; out_tree[1] = s_anchor[1]; out_tree[2] = rpy[2]; }
+    } else {
+      if (s_ok) { out_ground[0] = s_x[2]; out_ground[1] = s_x[3]; out_ground[2] = s_x[4]; }
+      else { out_ground[0] = s_anchor[2]; out_ground[1] = rpy[0]; out_ground[2] = rpy[1]; }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double aa[3] = {out_ground[1], out_ground[2], out_tree[2]};
+    double q[4];
+    aa_to_quat(aa, q);
+    sloam_se3 o;
+    o.q[0] = q[1]; o.q[1] = q[2]; o.q[2] = q[3]; o.q[3] = q[0];
+    o.t[0] = out_tree[0]; o.t[1] = out_tree[1]; o.t[2] = out_ground[0];
+    const Pose T = pose_from(o);
+    pose_store(d.pose_io + 7, T);
+    d.cnt->success = 1;
+  }
+}
+
+// projectModels + matchModels + prevGPlanes_ (first scan: projection by the
+// estimate, no matching).
+__global__ void __launch_bounds__(256) k_finalize(Dev d, KParams kp, int first, int update) {
+  const int nc = d.cnt->n_cyl, np = d.cnt->n_planes;
+  if (first) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      for (int j = 0; j < 7; ++j) d.pose_io[7 + j] = d.pose_io[j];
+      for (int j = 0; j < 7; ++j) d.pose_io[14 + j] = (j == 3) ? 1.0 : 0.0;
+      d.cnt->status = SLOAM_OK;
+      d.cnt->success = 1;
+      d.cnt->n_tm = d.cnt->n_pm = 0;
+      d.cnt->tree_check = d.cnt->ground_check = 0;
+    }
+  } else if (d.cnt->status == SLOAM_ERR_NO_MODELS) {
+    return;
+  }
+  const Pose T = pose_at(d.pose_io + (first ? 0 : 7));
+  const int lane = threadIdx.x & 31;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  // planes: project and become the next scan's prevGPlanes_ (block 0)
+  if (blockIdx.x == 0) {
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+      PlaneD P = d.planes[p];
+      const d3 n2 = rot3(T.R, mk3(P.plane[0], P.plane[1], P.plane[2]));
+      const double d2 = P.plane[3] - dot3(T.t, n2);
+      const d3 c2 = xform(T, mk3(P.centroid[0], P.centroid[1], P.centroid[2]));
+      P.plane[0] = n2.x; P.plane[1] = n2.y; P.plane[2] = n2.z; P.plane[3] = d2;
+      P.centroid[0] = c2.x; P.centroid[1] = c2.y; P.centroid[2] = c2.z;
+      d.planes[p] = P;
+      if (update) d.prev_planes[p] = P;
+    }
+    if (threadIdx.x == 0 && update) d.cnt->n_prev = np;
+  }
+  for (int c = wg; c < nc; c += nw) {
+    CylD C = d.cyls[c];
+    d3 root = mk3(C.root[0], C.root[1], C.root[2]), ray = mk3(C.ray[0], C.ray[1], C.ray[2]);
+    cyl_project(T, root, ray);
+    int out = -1;
+    if (!first) {
+      double bd = kp.tree_match_thresh + 100;
+      int bi = 0;
+      const int n_map = d.in->n_map;
+      const sloam_cylinder* map = d.in->map;
+      for (int k = lane; k < n_map; k += 32) {
+        const sloam_cylinder& m = map[k];
+        const double dist = cyl_dist(mk3(m.root[0], m.root[1], m.root[2]),
+                                     mk3(m.ray[0], m.ray[1], m.ray[2]), root, ray);
+        if (dist < bd) { bd = dist; bi = k; }
+      }
+      warp_argmin(bd, bi);
+      out = (n_map > 0 && bd < kp.add_new_tree_thresh) ? bi : -1;
+    }
+    if (lane == 0) {
+      C.root[0] = root.x; C.root[1] = root.y; C.root[2] = root.z;
+      C.ray[0] = ray.x; C.ray[1] = ray.y; C.ray[2] = ray.z;
+      d.cyls[c] = C;
+      d.match_out[c] = out;
+    }
+  }
+}
+
+}  // namespace
+
+int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update, cudaStream_t st) {
+  if (first_scan) {
+    k_finalize<<<64, 256, 0, st>>>(d, kp, 1, update ? 1 : 0);
+    return 1;
+  }
+  k_assoc<<<152, 256, 0, st>>>(d, kp);
+  k_gn<<<1, kGN, 0, st>>>(d, kp);
+  k_finalize<<<64, 256, 0, st>>>(d, kp, 0, update ? 1 : 0);
+  return 3;
+}
+
+}  // namespace sg

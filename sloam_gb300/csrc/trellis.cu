@@ -1,0 +1,514 @@
+// trellis.cu — a3-a5: Instance::computeGraph (trellis.cpp:134-139).
+//
+// a3 organised connected components (PCL OrganizedConnectedComponentSegmentation
+//    + EuclideanClusterComparator(1.0), trellis.cpp:15-43): a pixel is valid
+//    iff x is finite; 4-neighbours join when |p - q| < thr (float,
+//    sqrt(dx^2 + (dy^2 + dz^2))).  Lock-free union-find whose roots are the
+//    minimum pixel index of each component, so ranking the roots in raster
+//    order reproduces PCL's label numbering.
+// a4 Instance::findTrees (trellis.cpp:104-132): the pixels of every component
+//    with > min_cluster points are bucketed per (component, row) in column
+//    order in one pass over each component's column span (instead of a scan
+//    of the whole image per component).
+// a5 computeTreeVertex / computeVertexProperties (trellis.cpp:45-102): one
+//    warp per (component, row) bucket; medians and the (z, y, x, column)
+//    order by rank counting in shared memory.
+#include <climits>
+
+#include "internal.h"
+#include "scan_util.cuh"
+
+namespace sg {
+
+namespace {
+
+constexpr int kCCIterLimit = 1 << 20;
+
+__device__ __forceinline__ bool cc_close(const float4& a, const float4& b, float thr) {
+  const float dx = fsub(a.x, b.x), dy = fsub(a.y, b.y), dz = fsub(a.z, b.z);
+  const float dd = fadd(fmul(dx, dx), fadd(fmul(dy, dy), fmul(dz, dz)));
+  return fsqrt(dd) < thr;
+}
+
+__device__ __forceinline__ uint32_t cc_find(volatile uint32_t* P, uint32_t x) {
+  uint32_t p = P[x];
+  while (p != x) {
+    const uint32_t gp = P[p];
+    if (gp != p) P[x] = gp;  // path halving: parents only ever decrease
+    x = p;
+    p = P[x];
+  }
+  return x;
+}
+
+__global__ void __launch_bounds__(256) k_cc_init(Dev d) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.N; p += gridDim.x * blockDim.x)
+    d.parent[p] = isfinite(d.tree[p].x) ? (uint32_t)p : kInvalid;
+}
+
+__global__ void __launch_bounds__(256) k_cc_union(Dev d, float thr) {
+  volatile uint32_t* P = d.parent;
+  const int W = d.W;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.N; p += gridDim.x * blockDim.x) {
+    if (d.parent[p] == kInvalid) continue;
+    const float4 a = d.tree[p];
+    const int col = p % W;
+    for (int e = 0; e < 2; ++e) {
+      int q;
+      if (e == 0) {
+        if (col == 0) continue;
+        q = p - 1;
+      } else {
+        if (p < W) continue;
+        q = p - W;
+      }
+      const float4 b = d.tree[q];
+      if (!isfinite(b.x) || !cc_close(a, b, thr)) continue;
+      uint32_t u = (uint32_t)p, v = (uint32_t)q;
+      int it = 0;
+      for (; it < kCCIterLimit; ++it) {
+        uint32_t ru = cc_find(P, u), rv = cc_find(P, v);
+        if (ru == rv) break;
+        if (ru > rv) { uint32_t t = ru; ru = rv; rv = t; }
+        const uint32_t old = atomicCAS(d.parent + rv, rv, ru);
+        if (old == rv) break;
+        u = ru;
+        v = old;
+      }
+      if (it == kCCIterLimit) atomicOr(&d.cnt->cc_iter_exceeded, 1);
+    }
+  }
+}
+
+// Roots -> per-block counts; every valid pixel stores its root in label[].
+__global__ void __launch_bounds__(1024) k_cc_flatten(Dev d) {
+  __shared__ int sm[33];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  bool root = false;
+  if (p < d.N) {
+    const uint32_t par = d.parent[p];
+    if (par != kInvalid) {
+      const uint32_t r = cc_find(d.parent, (uint32_t)p);
+      d.label[p] = r;
+      root = (r == (uint32_t)p);
+    } else {
+      d.label[p] = kInvalid;
+    }
+  }
+  int total;
+  block_excl_scan(root ? 1 : 0, sm, &total);
+  if (threadIdx.x == 0) d.blk[blockIdx.x] = total;
+}
+
+// Rank of each root in raster order = the component label.
+__global__ void __launch_bounds__(1024) k_cc_rank(Dev d) {
+  __shared__ int sm[33];
+  const int base = block_sum_prefix(d.blk, blockIdx.x, sm);
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool root = p < d.N && d.label[p] == (uint32_t)p;
+  int total;
+  const int ex = block_excl_scan(root ? 1 : 0, sm, &total);
+  if (root) {
+    const int r = base + ex;
+    d.rank[p] = (uint32_t)r;
+    d.comp_size[r] = 0;
+    d.comp_cmin[r] = INT_MAX;
+    d.comp_cmax[r] = -1;
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) d.cnt->n_comp = base + total;
+}
+
+// Final labels + component size and column span (warp-aggregated atomics).
+__global__ void __launch_bounds__(256) k_cc_label(Dev d) {
+  const int W = d.W;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t l = kInvalid;
+  if (p < d.N) {
+    const uint32_t r = d.label[p];
+    if (r != kInvalid) {
+      l = d.rank[r];
+      d.label[p] = l;
+    }
+  }
+  const bool valid = l != kInvalid;
+  const unsigned act = __ballot_sync(0xffffffffu, valid);
+  if (!valid) return;
+  const unsigned peers = __match_any_sync(act, l);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  if (lane == leader) {
+    const int last = 31 - __clz(peers);
+    const int p0 = p, p1 = p + (last - lane);
+    int c0 = p0 % W, c1 = p1 % W;
+    // a warp may straddle two rows (W % 32 != 0): fall back to per-lane span
+    if (p0 / W != p1 / W) { c0 = 0; c1 = W - 1; }
+    atomicAdd(d.comp_size + l, __popc(peers));
+    atomicMin(d.comp_cmin + l, c0);
+    atomicMax(d.comp_cmax + l, c1);
+  }
+}
+
+// Ordered selection of the candidate components (size > min_cluster).
+__global__ void __launch_bounds__(1024) k_cands(Dev d, int min_cluster) {
+  __shared__ int sm[33];
+  const int nc = d.cnt->n_comp;
+  int base = 0;
+  for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
+    const int c = c0 + threadIdx.x;
+    const bool cand = c < nc && d.comp_size[c] > min_cluster;
+    int total;
+    const int ex = block_excl_scan(cand ? 1 : 0, sm, &total);
+    if (c < nc) {
+      const int k = base + ex;
+      if (cand && k < d.cap_cand) {
+        d.cand_comp[k] = c;
+        d.comp_cand[c] = k;
+      } else {
+        d.comp_cand[c] = -1;
+      }
+    }
+    base += total;
+  }
+  if (threadIdx.x == 0) {
+    d.cnt->n_cand = base < d.cap_cand ? base : d.cap_cand;
+    if (base > d.cap_cand) atomicOr(&d.cnt->overflow, 2);
+  }
+}
+
+// One warp per (candidate, row): count (pass 0) or scatter (pass 1) the
+// component's pixels of that row in column order.
+template <int PASS>
+__global__ void __launch_bounds__(256) k_rows(Dev d) {
+  const int H = d.H, W = d.W;
+  const int lane = threadIdx.x & 31;
+  const int nitems = d.cnt->n_cand * H;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int it = wg; it < nitems; it += nw) {
+    const int cand = it / H, row = it - cand * H;
+    const int comp = d.cand_comp[cand];
+    const int c0 = d.comp_cmin[comp], c1 = d.comp_cmax[comp];
+    const uint32_t* lab = d.label + (size_t)row * W;
+    int run = 0;
+    int out = PASS ? d.roff[it] : 0;
+    for (int c = c0; c <= c1; c += 32) {
+      const int col = c + lane;
+      const bool hit = col <= c1 && lab[col] == (uint32_t)comp;
+      const unsigned b = __ballot_sync(0xffffffffu, hit);
+      if (PASS && hit) d.bucket[out + run + __popc(b & ((1u << lane) - 1u))] = row * W + col;
+      run += __popc(b);
+    }
+    if (!PASS && lane == 0) d.rc[it] = run;
+  }
+}
+
+// Exclusive scan of the (candidate, row) counts; single block.
+__global__ void __launch_bounds__(1024) k_rowscan(Dev d) {
+  __shared__ int sm[33];
+  const int n = d.cnt->n_cand * d.H;
+  int base = 0;
+  for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    const int v = i < n ? d.rc[i] : 0;
+    int total;
+    const int ex = block_excl_scan(v, sm, &total);
+    if (i < n) d.roff[i] = base + ex;
+    base += total;
+  }
+  if (threadIdx.x == 0) d.roff[n] = base;
+}
+
+constexpr int kVtxCap = 256;   // points per vertex staged in shared memory
+constexpr int kVtxWarps = 4;
+
+__device__ __forceinline__ bool zless(float4 a, int ia, float4 b, int ib) {
+  if (a.z < b.z) return true;
+  if (b.z < a.z) return false;
+  if (a.y < b.y) return true;
+  if (b.y < a.y) return false;
+  if (a.x < b.x) return true;
+  if (b.x < a.x) return false;
+  return ia < ib;
+}
+
+// One warp per (candidate, row) bucket with > min_beam points.
+__global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
+  __shared__ float4 spts[kVtxWarps][kVtxCap];
+  __shared__ int srank[kVtxWarps][kVtxCap];
+  const int H = d.H;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nitems = d.cnt->n_cand * H;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int it = wg; it < nitems; it += nw) {
+    const int n = d.rc[it];
+    const int off = d.roff[it];
+    if (n <= kp.min_beam) {
+      if (lane == 0) d.vkept[it] = 0;
+      continue;
+    }
+    // stage: shared memory when it fits, else the global scratch `kept`
+    // region is read directly (rank pass) - bucket points from the cloud
+    const bool inshm = n <= kVtxCap;
+    float4* P = spts[w];
+    if (inshm)
+      for (int j = lane; j < n; j += 32) P[j] = d.tree[d.bucket[off + j]];
+    __syncwarp();
+    auto pt = [&](int j) -> float4 { return inshm ? P[j] : d.tree[d.bucket[off + j]]; };
+    const int mid = n / 2;  // (int)(n / 2.0)
+    // per-axis medians by rank
+    float mx = __int_as_float(0x7fc00000), my = mx, mz = mx;
+    for (int j = lane; j < n; j += 32) {
+      const float4 a = pt(j);
+      int rx = 0, ry = 0, rz = 0;
+      for (int k = 0; k < n; ++k) {
+        const float4 b = pt(k);
+        rx += (b.x < a.x) || (b.x == a.x && k < j);
+        ry += (b.y < a.y) || (b.y == a.y && k < j);
+        rz += (b.z < a.z) || (b.z == a.z && k < j);
+      }
+      if (rx == mid) mx = a.x;
+      if (ry == mid) my = a.y;
+      if (rz == mid) mz = a.z;
+    }
+    // gather the medians (exactly one lane holds each)
+    for (int o = 16; o > 0; o >>= 1) {
+      float ox = __shfl_xor_sync(0xffffffffu, mx, o);
+      float oy = __shfl_xor_sync(0xffffffffu, my, o);
+      float oz = __shfl_xor_sync(0xffffffffu, mz, o);
+      if (isnan(mx)) mx = ox;
+      if (isnan(my)) my = oy;
+      if (isnan(mz)) mz = oz;
+    }
+    // keep test and (z, y, x, column) rank
+    int nkept = 0;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+      const int j = j0 + lane;
+      bool keep = false;
+      if (j < n) {
+        const float4 a = pt(j);
+        keep = pcl_euclid(a.x, a.y, a.z, mx, my, mz) < kp.max_d_centroid;
+        if (inshm) {
+          int r = 0;
+          for (int k = 0; k < n; ++k) r += zless(P[k], k, a, j);
+          srank[w][j] = keep ? r : -1;
+        }
+      }
+      nkept += __popc(__ballot_sync(0xffffffffu, keep));
+    }
+    __syncwarp();
+    const bool valid = nkept > 1;
+    if (!inshm) {
+      // very wide bucket: serial fallback by lane 0 (rare: > kVtxCap points)
+      if (lane == 0) {
+        int first = -1, last = -1, wr = 0;
+        // emit kept points in (z,y,x,col) order by repeated minimum search
+        int prev = -1;
+        for (int c = 0; c < nkept; ++c) {
+          int best = -1;
+          for (int j = 0; j < n; ++j) {
+            const float4 a = pt(j);
+            if (!(pcl_euclid(a.x, a.y, a.z, mx, my, mz) < kp.max_d_centroid)) continue;
+            if (prev >= 0 && !zless(pt(prev), prev, a, j)) continue;
+            if (best < 0 || zless(a, j, pt(best), best)) best = j;
+          }
+          if (c == 0) first = best;
+          last = best;
+          d.kept[off + wr++] = pt(best);
+          prev = best;
+        }
+        double rad = 0.0;
+        if (valid) {
+          const float4 a = pt(first), b = pt(last);
+          rad = (double)pcl_euclid(a.x, a.y, a.z, b.x, b.y, b.z);
+        }
+        d.vmed[it] = make_float4(mx, my, mz, 0.0f);
+        d.vrad[it] = rad;
+        d.vkept[it] = valid ? nkept : 0;
+      }
+      __syncwarp();
+      continue;
+    }
+    // kept rank among kept points -> output slot
+    int ifirst = -1, ilast = -1;
+    for (int j = lane; j < n; j += 32) {
+      const int rj = srank[w][j];
+      if (rj < 0) continue;
+      int kr = 0;
+      for (int k = 0; k < n; ++k) {
+        const int rk = srank[w][k];
+        kr += (rk >= 0 && rk < rj);
+      }
+      d.kept[off + kr] = P[j];
+      if (kr == 0) ifirst = j;
+      if (kr == nkept - 1) ilast = j;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const int a = __shfl_xor_sync(0xffffffffu, ifirst, o);
+      const int b = __shfl_xor_sync(0xffffffffu, ilast, o);
+      ifirst = max(ifirst, a);
+      ilast = max(ilast, b);
+    }
+    if (lane == 0) {
+      double rad = 0.0;
+      if (valid) {
+        const float4 a = P[ifirst], b = P[ilast];
+        rad = (double)pcl_euclid(a.x, a.y, a.z, b.x, b.y, b.z);
+      }
+      d.vmed[it] = make_float4(mx, my, mz, 0.0f);
+      d.vrad[it] = rad;
+      d.vkept[it] = valid ? nkept : 0;
+    }
+    __syncwarp();
+  }
+}
+
+// Per candidate: vertex count of the landmark (0 = rejected), its kept-point
+// count and its cluster size.  Rows are walked bottom (H-1) to top.
+__global__ void __launch_bounds__(256) k_lm_count(Dev d, KParams kp, int32_t* cand_np,
+                                                  int32_t* cand_ncl) {
+  const int H = d.H;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d.cnt->n_cand;
+       c += gridDim.x * blockDim.x) {
+    int nv = 0, np = 0, ncl = 0;
+    for (int row = H - 1; row >= 0; --row) {
+      const int it = c * H + row;
+      ncl += d.rc[it];
+      const int k = d.vkept[it];
+      if (k > 0) {
+        if (nv < kp.max_vertices) np += k;
+        ++nv;
+      }
+    }
+    if (nv <= kp.min_vertices) { nv = 0; np = 0; }
+    if (nv > kp.max_vertices) nv = kp.max_vertices;
+    d.cand_nv[c] = nv;
+    cand_np[c] = np;
+    cand_ncl[c] = nv > 0 ? ncl : 0;
+  }
+}
+
+// Landmark numbering and offsets, single block, candidate (= label) order.
+__global__ void __launch_bounds__(1024) k_lm_scan(Dev d, const int32_t* cand_np,
+                                                  const int32_t* cand_ncl, int32_t* cand_vb,
+                                                  int32_t* cand_pb) {
+  __shared__ int sm[33];
+  const int nc = d.cnt->n_cand;
+  int bl = 0, bv = 0, bp = 0, bc = 0;
+  for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
+    const int c = c0 + threadIdx.x;
+    const int nv = c < nc ? d.cand_nv[c] : 0;
+    const int np = c < nc ? cand_np[c] : 0;
+    const int ncl = c < nc ? cand_ncl[c] : 0;
+    int tl, tv, tp, tc;
+    const int el = block_excl_scan(nv > 0 ? 1 : 0, sm, &tl);
+    const int ev = block_excl_scan(nv, sm, &tv);
+    const int ep = block_excl_scan(np, sm, &tp);
+    const int ec = block_excl_scan(ncl, sm, &tc);
+    if (c < nc) {
+      const bool ok = nv > 0 && bl + el < d.cap_lm && bv + ev + nv <= d.cap_v &&
+                      bp + ep + np <= d.cap_p && bc + ec + ncl <= d.cap_cluster;
+      d.cand_lm[c] = ok ? bl + el : -1;
+      cand_vb[c] = bv + ev;
+      cand_pb[c] = bp + ep;
+      if (ok) {
+        const int l = bl + el;
+        d.lm_tree[l] = d.cand_comp[c];
+        d.lm_vbeg[l] = bv + ev;
+        d.lm_cbeg[l] = bc + ec;
+      } else if (nv > 0) {
+        atomicOr(&d.cnt->overflow, 4);
+      }
+    }
+    bl += tl; bv += tv; bp += tp; bc += tc;
+  }
+  if (threadIdx.x == 0) {
+    const int nl = bl < d.cap_lm ? bl : d.cap_lm;
+    d.cnt->n_lm = nl;
+    d.cnt->n_v = bv < d.cap_v ? bv : d.cap_v;
+    d.cnt->n_p = bp < d.cap_p ? bp : d.cap_p;
+    d.cnt->n_cluster = bc < d.cap_cluster ? bc : d.cap_cluster;
+    d.lm_vbeg[nl] = d.cnt->n_v;
+    d.lm_pbeg[d.cnt->n_v] = d.cnt->n_p;
+    d.lm_cbeg[nl] = d.cnt->n_cluster;
+  }
+}
+
+// One warp per landmark candidate: vertex records, kept points and the
+// cluster points (raster order) into the compact landmark arrays.
+__global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
+                                                  const int32_t* cand_pb) {
+  const int H = d.H;
+  const int lane = threadIdx.x & 31;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int c = wg; c < d.cnt->n_cand; c += nw) {
+    const int l = d.cand_lm[c];
+    if (l < 0) continue;
+    const int nv = d.cand_nv[c];
+    int vbase = cand_vb[c], pbase = cand_pb[c];
+    int vi = 0;
+    for (int r0 = H - 1; r0 >= 0 && vi < nv; r0 -= 32) {
+      const int row = r0 - lane;
+      const int it = c * H + row;
+      const int k = row >= 0 ? d.vkept[it] : 0;
+      const bool v = k > 0;
+      const unsigned b = __ballot_sync(0xffffffffu, v);
+      const int my = vi + __popc(b & ((1u << lane) - 1u));
+      // kept-point prefix inside this chunk
+      int kp = v && my < nv ? k : 0, incl = kp;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int pstart = pbase + incl - kp;
+      if (v && my < nv) {
+        const int vv = vbase + my;
+        const float4 m = d.vmed[it];
+        d.lm_vxyz[3 * vv] = m.x;
+        d.lm_vxyz[3 * vv + 1] = m.y;
+        d.lm_vxyz[3 * vv + 2] = m.z;
+        d.lm_vrad[vv] = d.vrad[it];
+        d.lm_vrow[vv] = row;
+        d.lm_pbeg[vv] = pstart;
+        const int off = d.roff[it];
+        for (int q = 0; q < k; ++q) d.lm_pts[pstart + q] = d.kept[off + q];
+      }
+      pbase += __shfl_sync(0xffffffffu, incl, 31);
+      vi += __popc(b);
+    }
+    // cluster points: the candidate's buckets are contiguous, raster order
+    const int cb = d.lm_cbeg[l];
+    const int s = d.roff[c * H], e = d.roff[c * H + H];
+    for (int q = s + lane; q < e; q += 32) d.lm_cpts[cb + (q - s)] = d.tree[d.bucket[q]];
+  }
+}
+
+}  // namespace
+
+int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
+  const int N = d.N;
+  const int g256 = (N + 255) / 256, g1k = (N + 1023) / 1024;
+  k_cc_init<<<g256, 256, 0, st>>>(d);
+  k_cc_union<<<g256, 256, 0, st>>>(d, kp.cc_thr);
+  k_cc_flatten<<<g1k, 1024, 0, st>>>(d);
+  k_cc_rank<<<g1k, 1024, 0, st>>>(d);
+  k_cc_label<<<g256, 256, 0, st>>>(d);
+  k_cands<<<1, 1024, 0, st>>>(d, kp.min_cluster);
+  const int gw = 152 * 8;  // warps-per-item kernels: grid-stride over items
+  k_rows<0><<<gw, 256, 0, st>>>(d);
+  k_rowscan<<<1, 1024, 0, st>>>(d);
+  k_rows<1><<<gw, 256, 0, st>>>(d);
+  k_vertex<<<gw, kVtxWarps * 32, 0, st>>>(d, kp);
+  // scratch for the landmark offsets lives in the (now unused) rank array
+  int32_t* cand_np = reinterpret_cast<int32_t*>(d.rank);
+  int32_t* cand_ncl = cand_np + d.cap_cand;
+  int32_t* cand_vb = cand_ncl + d.cap_cand;
+  int32_t* cand_pb = cand_vb + d.cap_cand;
+  k_lm_count<<<(d.cap_cand + 255) / 256, 256, 0, st>>>(d, kp, cand_np, cand_ncl);
+  k_lm_scan<<<1, 1024, 0, st>>>(d, cand_np, cand_ncl, cand_vb, cand_pb);
+  k_lm_write<<<gw, 256, 0, st>>>(d, cand_vb, cand_pb);
+  return 13;
+}
+
+}  // namespace sg

@@ -1,0 +1,104 @@
+"""ctypes binding of libsloam_gb300.so (the CUDA C ABI of include/sloam_gb300.h).
+
+There is no CPU fallback: importing the binding without the built library, or
+creating a context without a CUDA device, raises.
+"""
+import ctypes as C
+import os
+
+from . import capi as A
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsloam_gb300.so")
+
+EXPORTS = [
+    "sloam_params_default", "sloam_abi_sizes", "sloam_create", "sloam_destroy",
+    "sloam_last_error", "sloam_reset", "sloam_set_params", "sloam_project_mask",
+    "sloam_trellis", "sloam_compute_models", "sloam_run", "sloam_keyframe",
+    "sloam_keyframes_device", "sloam_last_launch_count", "sloam_stream",
+]
+
+_lib = None
+
+
+class SloamError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"{A.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def load(path=LIB_PATH):
+    """Loads the library (it must have been built: sloam_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m sloam_gb300.build`")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.sloam_params_default.argtypes = [C.POINTER(A.Params)]
+    L.sloam_abi_sizes.argtypes = [C.POINTER(C.c_int32), C.c_int]
+    L.sloam_abi_sizes.restype = C.c_int
+    L.sloam_create.argtypes = [C.POINTER(A.Params), C.c_int, C.POINTER(C.c_int)]
+    L.sloam_create.restype = vp
+    L.sloam_destroy.argtypes = [vp]
+    L.sloam_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.sloam_reset.argtypes = [vp]
+    L.sloam_set_params.argtypes = [vp, C.POINTER(A.Params)]
+    L.sloam_project_mask.argtypes = [vp, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_uint8),
+                                     C.POINTER(C.c_uint8), C.POINTER(A.ScanOut)]
+    L.sloam_trellis.argtypes = [vp, C.POINTER(C.c_float), C.c_int32, C.c_int32,
+                                C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
+                                C.POINTER(A.Landmarks)]
+    L.sloam_compute_models.argtypes = [vp, C.POINTER(A.SE3), C.POINTER(C.c_float), C.c_int32,
+                                       C.POINTER(A.Landmarks), C.POINTER(A.ModelsOut)]
+    L.sloam_run.argtypes = [vp, C.POINTER(A.SE3), C.POINTER(C.c_float), C.c_int32,
+                            C.POINTER(A.Landmarks), C.POINTER(A.Cylinder), C.c_int32,
+                            C.POINTER(A.RunOut)]
+    L.sloam_keyframe.argtypes = [vp, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_uint8),
+                                 C.POINTER(C.c_uint8), C.POINTER(A.SE3), C.POINTER(A.Cylinder),
+                                 C.c_int32, C.POINTER(A.RunOut)]
+    L.sloam_keyframes_device.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.POINTER(A.SE3),
+                                         vp, C.c_int32, vp, vp, vp]
+    L.sloam_last_launch_count.argtypes = [vp]
+    L.sloam_last_launch_count.restype = C.c_int64
+    L.sloam_stream.argtypes = [vp]
+    L.sloam_stream.restype = vp
+    _lib = L
+    return L
+
+
+class Context:
+    """Owns one sloam_ctx (one device arena + one CUDA stream)."""
+
+    def __init__(self, params=None, device=0):
+        self.L = load()
+        self.params = params if params is not None else A.default_params()
+        st = C.c_int(0)
+        self.h = self.L.sloam_create(C.byref(self.params), device, C.byref(st))
+        if not self.h:
+            raise SloamError(st.value, "sloam_create failed (is a CUDA device visible?)")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sloam_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def error(self):
+        buf = C.create_string_buffer(512)
+        self.L.sloam_last_error(self.h, buf, 512)
+        return buf.value.decode()
+
+    def check(self, st, ok=(A.SLOAM_OK,)):
+        if st not in ok:
+            raise SloamError(st, self.error())
+        return st
+
+    def launches(self):
+        return int(self.L.sloam_last_launch_count(self.h))
+
+    def stream(self):
+        return self.L.sloam_stream(self.h)

@@ -1,0 +1,330 @@
+"""GPU kernels vs the oracle through the C ABI, on the same inputs.
+
+Bit-exact: pixel indices, range image, mask, ground list, tree cloud,
+component labels, landmarks (ids, vertices, medians, radii, point lists),
+plane bins, cylinder ids, RANSAC inlier counts, cylinder features, matches.
+Within tolerance (FP64 oracle): plane / cylinder geometry (axis <= 1e-4 rad,
+offset / radius <= 1e-4 m), pose (translation <= 1e-5 m, rotation <= 1e-6 rad).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from sloam_gb300 import capi as A
+from sloam_gb300 import synth
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from sloam_gb300 import build
+    build.build()
+
+
+def make_ctx(P):
+    from sloam_gb300.lib import Context
+    return Context(P)
+
+
+def assert_scan_equal(a, b):
+    np.testing.assert_array_equal(a["px"], b["px"])
+    np.testing.assert_array_equal(a["py"], b["py"])
+    np.testing.assert_array_equal(a["range_image"].view(np.uint32), b["range_image"].view(np.uint32))
+    np.testing.assert_array_equal(a["mask_out"], b["mask_out"])
+    assert a["n_ground"] == b["n_ground"]
+    n = a["n_ground"]
+    np.testing.assert_array_equal(a["ground_idx"][:n], b["ground_idx"][:n])
+    np.testing.assert_array_equal(a["tree_cloud"].view(np.uint32), b["tree_cloud"].view(np.uint32))
+
+
+# ------------------------------------------------------------------ a1/a2
+@pytest.mark.parametrize("name", ["C1", "C2"])
+@pytest.mark.parametrize("destagger", [0, 1])
+def test_projection_point_labels(name, destagger):
+    cfg, forest, kfs = H.scene(name)
+    P = synth.preset_params(cfg, do_destagger=destagger)
+    ctx = make_ctx(P)
+    kf = kfs[0]
+    o = H.oracle_project(P, kf.xyzi, labels=kf.labels)
+    g = H.gpu_project(ctx, kf.xyzi, labels=kf.labels)
+    assert_scan_equal(o, g)
+
+
+def test_projection_mask_image_and_edge_points():
+    cfg, forest, kfs = H.scene("C2")
+    P = synth.preset_params(cfg)
+    ctx = make_ctx(P)
+    xyzi = kfs[0].xyzi.copy()
+    rng = np.random.default_rng(3)
+    n = len(xyzi)
+    # edge cases: zero points, signed zeros on the axes, tiny and huge coordinates
+    idx = rng.choice(n, 64, replace=False)
+    xyzi[idx[0:8], :3] = 0.0
+    xyzi[idx[8:16], 1] = -0.0
+    xyzi[idx[8:16], 0] = -5.0
+    xyzi[idx[16:24], 1] = 0.0
+    xyzi[idx[16:24], 0] = -5.0
+    xyzi[idx[24:32], :3] = 1e-30
+    xyzi[idx[32:40], :3] = [1e19, -1e19, 3e18]
+    xyzi[idx[40:48], 0] = np.nan
+    xyzi[idx[48:56], 2] = 100.0   # beyond the vertical field of view
+    xyzi[idx[56:64], 2] = -100.0
+    labels = kfs[0].labels
+    o = H.oracle_project(P, xyzi, labels=labels)
+    g = H.gpu_project(ctx, xyzi, labels=labels)
+    assert_scan_equal(o, g)
+    # mask-image mode: the network-style per-pixel mask
+    mask = o["mask_out"].copy()
+    o2 = H.oracle_project(P, xyzi, mask=mask)
+    g2 = H.gpu_project(ctx, xyzi, mask=mask)
+    assert_scan_equal(o2, g2)
+
+
+def test_projection_random_directions_many_scans():
+    """Uniform random directions hit column/row boundaries everywhere."""
+    P = A.default_params(img_w=2048, img_h=64)
+    ctx = make_ctx(P)
+    rng = np.random.default_rng(11)
+    for _ in range(4):
+        n = P.img_w * P.img_h
+        v = rng.normal(size=(n, 3)).astype(np.float32)
+        r = rng.uniform(0.5, 40, n).astype(np.float32)
+        xyzi = np.zeros((n, 4), np.float32)
+        xyzi[:, :3] = v / np.linalg.norm(v, axis=1, keepdims=True) * r[:, None]
+        lab = rng.choice(np.array([0, 1, 255], np.uint8), n)
+        o = H.oracle_project(P, xyzi, labels=lab)
+        g = H.gpu_project(ctx, xyzi, labels=lab)
+        assert_scan_equal(o, g)
+
+
+# ------------------------------------------------------------------ a3-a5
+@pytest.mark.parametrize("seq", ["still", "moving"])
+@pytest.mark.parametrize("t", ["t0", "t1"])
+def test_trellis_reference_clouds(seq, t):
+    cloud, h, w = H.golden_tree_cloud(seq, t)
+    P = A.default_params()
+    ctx = make_ctx(P)
+    lo, labo, nco = H.oracle_trellis(P, cloud, h, w)
+    lg, labg, ncg = H.gpu_trellis(ctx, cloud, h, w)
+    assert nco == ncg
+    np.testing.assert_array_equal(labo, labg)
+    H.landmarks_equal_exact(lo, lg)
+
+
+def test_trellis_known_answer_on_gpu():
+    """The reference's stored Trellis output, reproduced by the GPU."""
+    cloud, h, w = H.golden_tree_cloud("still", "t0")
+    ctx = make_ctx(A.default_params())
+    lg, _, _ = H.gpu_trellis(ctx, cloud, h, w)
+    ref = H.golden_landmarks("still", "t0")
+    trees = lg.to_trees()
+    assert [t[0]["tree_id"] for t in trees] == [t[0]["tree_id"] for t in ref]
+    assert [len(t) for t in trees] == [len(t) for t in ref]
+    for tr, rt in zip(trees, ref):
+        for v, rv in zip(tr, rt):
+            np.testing.assert_allclose(v["xyz"], rv["xyz"], atol=2e-6, rtol=0)
+            assert abs(0.5 * v["radius"] - rv["radius"]) < 2e-6
+            np.testing.assert_allclose(v["points"][:, :3], rv["points"][:, :3], atol=2e-6, rtol=0)
+
+
+@pytest.mark.parametrize("name", ["C1", "C2"])
+def test_trellis_synthetic(name):
+    cfg, forest, kfs = H.scene(name)
+    P = synth.preset_params(cfg)
+    ctx = make_ctx(P)
+    o = H.oracle_project(P, kfs[0].xyzi, labels=kfs[0].labels)
+    cloud = o["tree_cloud"]
+    lo, labo, nco = H.oracle_trellis(P, cloud, P.img_h, P.img_w)
+    lg, labg, ncg = H.gpu_trellis(ctx, cloud, P.img_h, P.img_w)
+    assert lo.s.n_landmarks > 0
+    assert nco == ncg
+    np.testing.assert_array_equal(labo, labg)
+    H.landmarks_equal_exact(lo, lg)
+
+
+def test_trellis_empty_cloud():
+    P = A.default_params()
+    ctx = make_ctx(P)
+    cloud = np.full((P.img_w * P.img_h, 4), np.nan, np.float32)
+    lg, labg, ncg = H.gpu_trellis(ctx, cloud, P.img_h, P.img_w)
+    assert ncg == 0 and lg.s.n_landmarks == 0
+    assert (labg == 0xFFFFFFFF).all()
+
+
+# ------------------------------------------------------------------ a6-a8
+def core_params(two_step, cyl_mode=0):
+    from tests.test_oracle_reference import core_params as cp
+    p = cp(two_step)
+    p.cyl_mode = cyl_mode
+    return p
+
+
+@pytest.mark.parametrize("cyl_mode", [0, 1])
+def test_models_reference_landmarks(cyl_mode):
+    P = core_params(1, cyl_mode)
+    ctx = make_ctx(P)
+    lb = A.LandmarkBuffers.from_trees(H.golden_landmarks("still", "t0", resize_points=5))
+    g0 = H.golden_ground("t0")
+    I = A.SE3.identity()
+    mo = H.oracle_models(P, I, g0, lb)
+    mg = H.gpu_models(ctx, I, g0, lb)
+    assert mo.s.n_planes > 0 and mo.s.n_cylinders > 0
+    H.compare_models(mo, mg)
+
+
+@pytest.mark.parametrize("cyl_mode", [0, 1])
+def test_models_synthetic_c2(cyl_mode):
+    cfg, forest, kfs = H.scene("C2")
+    P = synth.preset_params(cfg, cyl_mode=cyl_mode)
+    ctx = make_ctx(P)
+    kf = kfs[0]
+    o = H.oracle_project(P, kf.xyzi, labels=kf.labels)
+    ground = np.ascontiguousarray(kf.xyzi[o["ground_idx"][:o["n_ground"]]])
+    lo, _, _ = H.oracle_trellis(P, o["tree_cloud"], P.img_h, P.img_w)
+    pose = A.SE3.from_qt(*kf.pose_est_qt())
+    mo = H.oracle_models(P, pose, ground, lo)
+    mg = H.gpu_models(ctx, pose, ground, lo)
+    assert mo.s.n_cylinders > 10
+    H.compare_models(mo, mg)
+
+
+# --------------------------------------------------------------- a9-a11
+def gpu_run_pair(ctx):
+    L = ctx.L
+    lm0 = A.LandmarkBuffers.from_trees(H.golden_landmarks("still", "t0", resize_points=5))
+    lm1 = A.LandmarkBuffers.from_trees(H.golden_landmarks("still", "t1", resize_points=5))
+    g0, g1 = H.golden_ground("t0"), H.golden_ground("t1")
+    I = A.SE3.identity()
+    r0 = A.RunBuffers(ctx.params)
+    st0 = L.sloam_run(ctx.h, C.byref(I), A.ptr(g0, C.c_float), len(g0), C.byref(lm0.s), None, 0,
+                      C.byref(r0.s))
+    r0.refresh()
+    m = A.cylinders_from_array(r0.m.cyl_array())
+    r1 = A.RunBuffers(ctx.params)
+    st1 = L.sloam_run(ctx.h, C.byref(I), A.ptr(g1, C.c_float), len(g1), C.byref(lm1.s), m,
+                      r0.s.models.n_cylinders, C.byref(r1.s))
+    r1.refresh()
+    return st0, r0, st1, r1
+
+
+def compare_runs(ro, rg, pose_tol=1.0):
+    assert ro.s.success == rg.s.success
+    assert ro.s.n_tree_matches == rg.s.n_tree_matches
+    assert ro.s.n_plane_matches == rg.s.n_plane_matches
+    assert ro.s.tree_check == rg.s.tree_check and ro.s.ground_check == rg.s.ground_check
+    H.compare_models(ro.m, rg.m, tol_scale=1.0)
+    n = ro.s.models.n_cylinders
+    np.testing.assert_array_equal(ro.matches[:n], rg.matches[:n])
+    qo, to = ro.s.T_Map_Curr.qt()
+    qg, tg = rg.s.T_Map_Curr.qt()
+    assert np.abs(to - tg).max() < H.TOL_TRANS_M * pose_tol, (to, tg)
+    assert H.rot_angle(qo, qg) < H.TOL_ROT_RAD * pose_tol, (qo, qg)
+
+
+@pytest.mark.parametrize("two_step", [0, 1])
+def test_run_reference_pair(two_step):
+    from tests.test_oracle_reference import oracle_run_pair
+    P = core_params(two_step)
+    ctx = make_ctx(P)
+    st0, r0, st1, r1 = gpu_run_pair(ctx)
+    so0, ro0, so1, ro1 = oracle_run_pair(P)
+    assert (st0, st1) == (so0, so1) == (0, 0)
+    compare_runs(ro0, r0)
+    compare_runs(ro1, r1)
+    # core_test.cpp properties on the GPU result
+    assert r0.s.models.n_cylinders > 0 and r0.s.models.n_planes > 0
+    assert r1.s.success and (r1.matches[:r1.s.models.n_cylinders] != -1).any()
+
+
+def keyframe_pair(P, forest, kf, run):
+    """first scan at the true pose (defines map-frame planes), then the
+    keyframe at the perturbed estimate; returns both outputs."""
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    gt = A.SE3.from_qt(*kf.pose_gt_qt())
+    est = A.SE3.from_qt(*kf.pose_est_qt())
+    r0, r1 = A.RunBuffers(P), A.RunBuffers(P)
+    s0 = run(kf, gt, mapc, len(forest.radius), r0)
+    s1 = run(kf, est, mapc, len(forest.radius), r1)
+    r0.refresh()
+    r1.refresh()
+    return s0, r0, s1, r1
+
+
+@pytest.mark.parametrize("two_step,cyl_mode", [(0, 1), (1, 0), (0, 0)])
+def test_keyframe_synthetic_c2(two_step, cyl_mode):
+    cfg, forest, kfs = H.scene("C2")
+    P = synth.preset_params(cfg, two_step_optim=two_step, cyl_mode=cyl_mode)
+    ctx = make_ctx(P)
+    L = H.oracle()
+    os_ = L.oracle_create(C.byref(P))
+
+    def run_o(kf, pose, m, nm, r):
+        return L.oracle_keyframe(os_, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                 A.ptr(kf.labels, C.c_uint8), None, C.byref(pose), m, nm,
+                                 C.byref(r.s))
+
+    def run_g(kf, pose, m, nm, r):
+        return ctx.L.sloam_keyframe(ctx.h, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                    A.ptr(kf.labels, C.c_uint8), None, C.byref(pose), m, nm,
+                                    C.byref(r.s))
+
+    so0, ro0, so1, ro1 = keyframe_pair(P, forest, kfs[0], run_o)
+    sg0, rg0, sg1, rg1 = keyframe_pair(P, forest, kfs[0], run_g)
+    L.oracle_destroy(os_)
+    assert (so0, so1) == (sg0, sg1)
+    compare_runs(ro0, rg0)
+    compare_runs(ro1, rg1)
+    # the pose moved towards the truth
+    q, t = rg1.s.T_Map_Curr.qt()
+    assert np.linalg.norm(t - kfs[0].t_gt) < 0.1
+
+
+def test_keyframes_device_batch_matches_single():
+    import torch
+    cfg, forest, kfs = H.scene("C2", seed=0, n_kf=3)
+    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1)
+    ctx = make_ctx(P)
+    mapa = forest.map_cylinders()
+    mapc = A.cylinders_from_array(mapa)
+    # first scan (true pose of keyframe 0) defines the previous planes
+    r = A.RunBuffers(P)
+    kf0 = kfs[0]
+    ctx.check(ctx.L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), len(kf0.xyzi),
+                                   A.ptr(kf0.labels, C.c_uint8), None,
+                                   C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, len(mapa),
+                                   C.byref(r.s)))
+    n = len(kf0.xyzi)
+    dx = torch.from_numpy(np.stack([k.xyzi for k in kfs])).cuda()
+    dl = torch.from_numpy(np.stack([k.labels for k in kfs])).cuda()
+    dm = torch.from_numpy(np.frombuffer(bytes(mapc), np.uint8).copy()).cuda()
+    poses = (A.SE3 * len(kfs))(*[A.SE3.from_qt(*k.pose_est_qt()) for k in kfs])
+    pose_out = torch.zeros(len(kfs) * 7, dtype=torch.float64, device="cuda")
+    succ = torch.zeros(len(kfs), dtype=torch.int32, device="cuda")
+    ncyl = torch.zeros(len(kfs), dtype=torch.int32, device="cuda")
+    ctx.check(ctx.L.sloam_keyframes_device(ctx.h, dx.data_ptr(), n, len(kfs), dl.data_ptr(),
+                                           poses, dm.data_ptr(), len(mapa), pose_out.data_ptr(),
+                                           succ.data_ptr(), ncyl.data_ptr()))
+    torch.cuda.synchronize()
+    po = pose_out.cpu().numpy().reshape(-1, 7)
+    # the same keyframes one by one through the host API (state restored)
+    for k, kf in enumerate(kfs):
+        ctx2 = make_ctx(P)
+        r0 = A.RunBuffers(P)
+        ctx2.check(ctx2.L.sloam_keyframe(ctx2.h, A.ptr(kf0.xyzi, C.c_float), n,
+                                         A.ptr(kf0.labels, C.c_uint8), None,
+                                         C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc,
+                                         len(mapa), C.byref(r0.s)))
+        r1 = A.RunBuffers(P)
+        st = ctx2.L.sloam_keyframe(ctx2.h, A.ptr(kf.xyzi, C.c_float), n,
+                                   A.ptr(kf.labels, C.c_uint8), None,
+                                   C.byref(A.SE3.from_qt(*kf.pose_est_qt())), mapc, len(mapa),
+                                   C.byref(r1.s))
+        r1.refresh()
+        q, t = r1.s.T_Map_Curr.qt()
+        np.testing.assert_array_equal(po[k, :4], q)
+        np.testing.assert_array_equal(po[k, 4:], t)
+        assert int(ncyl[k]) == r1.s.models.n_cylinders
+        assert int(succ[k]) == (1 if st == 0 and r1.s.success else 0)
