@@ -102,15 +102,15 @@ float o2f(int32_t o) {
 // smallest float v in [lo, hi] with g(v) >= k (g non-decreasing); hi if none
 template <typename G>
 float first_at_least(G g, int k, float lo, float hi) {
-  int32_t a = f2o(lo), b = f2o(hi);
-  if (g(o2f(a)) >= k) return o2f(a);
-  if (g(o2f(b)) < k) return o2f(b);
+  int64_t a = f2o(lo), b = f2o(hi);  // 64-bit: the span exceeds INT32_MAX
+  if (g(o2f((int32_t)a)) >= k) return o2f((int32_t)a);
+  if (g(o2f((int32_t)b)) < k) return o2f((int32_t)b);
   while (b - a > 1) {
-    const int32_t m = a + (b - a) / 2;
-    if (g(o2f(m)) >= k) b = m;
+    const int64_t m = a + (b - a) / 2;
+    if (g(o2f((int32_t)m)) >= k) b = m;
     else a = m;
   }
-  return o2f(b);
+  return o2f((int32_t)b);
 }
 inline float ref_min(float a, float b) { return (b < a) ? b : a; }
 inline float ref_max(float a, float b) { return (a < b) ? b : a; }
@@ -164,6 +164,17 @@ void build_ground_tables(const sloam_params& p, float* tb, float* rb, float* r_l
 }
 
 }  // namespace sg
+
+// Test hook (not part of the public header): the host-built boundary tables
+// a context would upload.  px_tab [img_w+1], tb [theta_bins+1],
+// rb [radii_bins+1], lohi [2].
+extern "C" int sloam_internal_tables(const sloam_params* p, float* px_tab, float* tb, float* rb,
+                                     float* lohi) {
+  if (!p) return SLOAM_ERR_ARG;
+  sg::build_px_table(*p, px_tab);
+  sg::build_ground_tables(*p, tb, rb, lohi, lohi + 1);
+  return SLOAM_OK;
+}
 
 // ================================================================ context
 struct sloam_ctx {

@@ -15,7 +15,7 @@ EXPORTS = [
     "sloam_params_default", "sloam_abi_sizes", "sloam_create", "sloam_destroy",
     "sloam_last_error", "sloam_reset", "sloam_set_params", "sloam_project_mask",
     "sloam_trellis", "sloam_compute_models", "sloam_run", "sloam_keyframe",
-    "sloam_keyframes_device", "sloam_last_launch_count", "sloam_stream",
+    "sloam_keyframes_device", "sloam_last_launch_count", "sloam_stream", "sloam_internal_tables",
 ]
 
 _lib = None

@@ -63,3 +63,41 @@ def test_bad_params_rejected(L):
     p = A.default_params(img_w=0)
     assert not L.sloam_create(C.byref(p), 0, C.byref(st))
     assert st.value == A.SLOAM_ERR_ARG
+
+
+def test_boundary_tables_reproduce_oracle_pixels_and_bins(L):
+    """The host-built float boundary tables (column of a yaw, theta / radius
+    bins of a ground point) give exactly the oracle's integers."""
+    import numpy as np
+    from tests import helpers as H
+    P = A.default_params(img_w=2048, img_h=64)
+    tab = np.zeros(P.img_w + 1, np.float32)
+    tb = np.zeros(P.ground_theta_bins + 1, np.float32)
+    rb = np.zeros(P.ground_radii_bins + 1, np.float32)
+    lohi = np.zeros(2, np.float32)
+    L.sloam_internal_tables(C.byref(P), A.ptr(tab, C.c_float), A.ptr(tb, C.c_float),
+                            A.ptr(rb, C.c_float), A.ptr(lohi, C.c_float))
+    assert np.all(np.diff(tab[1:-1]) > 0)
+    rng = np.random.default_rng(5)
+    n = P.img_w * P.img_h
+    v = rng.normal(size=(n, 3)).astype(np.float32)
+    xyzi = np.zeros((n, 4), np.float32)
+    xyzi[:, :3] = v * rng.uniform(0.5, 40, (n, 1)).astype(np.float32)
+    o = H.oracle_project(P, xyzi, labels=np.zeros(n, np.uint8))
+    yaw = -np.arctan2(xyzi[:, 1].astype(np.float64), xyzi[:, 0].astype(np.float64)).astype(np.float32)
+    px = np.searchsorted(tab[1:P.img_w], yaw, side="right")
+    np.testing.assert_array_equal(px, o["px"])
+    # ground bins: theta from the float atan2, radius window in double
+    x, y = xyzi[:, 0], xyzi[:, 1]
+    r = np.sqrt(x * x + y * y).astype(np.float32)
+    inwin = (r.astype(np.float64) < P.max_ground_lidar_dist) & (r.astype(np.float64) > P.min_ground_lidar_dist)
+    assert np.array_equal(inwin, (r >= lohi[0]) & (r <= lohi[1]))
+    th = np.arctan2(y.astype(np.float64), x.astype(np.float64)).astype(np.float32)
+    tref = np.clip(np.floor((3.14159265 + th.astype(np.float64)) / (2 * 3.14159265 / P.ground_theta_bins)),
+                   0, P.ground_theta_bins - 1).astype(int)
+    ttab = np.searchsorted(tb[1:P.ground_theta_bins], th, side="right")
+    np.testing.assert_array_equal(ttab, tref)
+    rref = np.clip(np.floor(r.astype(np.float64) / (P.max_ground_lidar_dist / P.ground_radii_bins)),
+                   0, P.ground_radii_bins - 1).astype(int)
+    rtab = np.searchsorted(rb[1:P.ground_radii_bins], r, side="right")
+    np.testing.assert_array_equal(rtab[inwin], rref[inwin])
