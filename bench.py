@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Keyframes/s of the SLOAM keyframe hot path on GB300.
+
+Workload (one step): a batch of B synthetic 64x2048 keyframes (float32 XYZI,
+~131k points each; 150 trunks with radius U(0.08, 0.6) m, shrubs, 10%
+outliers; per-point labels from the generator), each run through projection,
+Trellis, ground planes, the point-level cylinder RANSAC (256 hypotheses per
+tree, 3 cm inlier band, 3 LS iterations), association against a 400-landmark
+submap and 10 Gauss-Newton pose iterations (FP32 residuals, FP64 6x6 solve).
+Inputs are device-resident for `value`; `e2e` runs the same keyframes through
+the host C ABI (sloam_keyframe) with host buffers.  L2 is flushed (256 MB
+write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+std-only restatement in oracle/, the reference itself cannot be built here)
+on all host cores, one keyframe per thread per step.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "keyframes/s at 64x2048 (plain GPU RANSAC path, 150 trees, 400-landmark submap)"
+UNIT = "keyframes/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--distinct", type=int, default=16)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--seed", type=int, default=0)
+    return ap.parse_args()
+
+
+def workload(seed, distinct):
+    from sloam_gb300 import synth
+    cfg = synth.C2
+    forest, kfs = synth.scene(cfg, seed=seed, n_kf=distinct)
+    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1, cyl_hypotheses=256,
+                            cyl_ls_iters=3, gn_iters=10)
+    return cfg, forest, kfs, P
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU legs
+def cpu_run_keyframes(P, forest, kfs, seconds, threads=1, min_kf=2):
+    """The oracle (the reference algorithm's std-only restatement) on host
+    threads, one independent keyframe at a time per thread; returns kf/s."""
+    from oracle import loader
+    from sloam_gb300 import capi as A
+    L = loader.lib()
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    nm = len(forest.radius)
+    counts = [0] * threads
+    stop = [False]
+
+    def worker(t):
+        s = L.oracle_create(C.byref(P))
+        kf0 = kfs[0]
+        r = A.RunBuffers(P)
+        L.oracle_keyframe(s, A.ptr(kf0.xyzi, C.c_float), len(kf0.xyzi),
+                          A.ptr(kf0.labels, C.c_uint8), None,
+                          C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, nm, C.byref(r.s))
+        k = 0
+        while not stop[0] or counts[t] < min_kf:
+            kf = kfs[(t + k) % len(kfs)]
+            r = A.RunBuffers(P)
+            L.oracle_keyframe(s, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                              A.ptr(kf.labels, C.c_uint8), None,
+                              C.byref(A.SE3.from_qt(*kf.pose_est_qt())), mapc, nm, C.byref(r.s))
+            counts[t] += 1
+            k += 1
+        L.oracle_destroy(s)
+
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    time.sleep(seconds)
+    stop[0] = True
+    for th in ths:
+        th.join()
+    dt = time.perf_counter() - t0
+    return sum(counts) / dt, sum(counts), dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg, forest, kfs, P = workload(args.seed, min(args.distinct, 8))
+    threads = os.cpu_count() or 1
+    from oracle import loader
+    from sloam_gb300 import capi as A
+    L = loader.lib()
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    nm = len(forest.radius)
+    states = []
+    for t in range(threads):
+        s = L.oracle_create(C.byref(P))
+        kf0 = kfs[0]
+        r = A.RunBuffers(P)
+        L.oracle_keyframe(s, A.ptr(kf0.xyzi, C.c_float), len(kf0.xyzi),
+                          A.ptr(kf0.labels, C.c_uint8), None,
+                          C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, nm, C.byref(r.s))
+        states.append(s)
+
+    def one(t, step):
+        kf = kfs[(t + step) % len(kfs)]
+        r = A.RunBuffers(P)
+        L.oracle_keyframe(states[t], A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                          A.ptr(kf.labels, C.c_uint8), None,
+                          C.byref(A.SE3.from_qt(*kf.pose_est_qt())), mapc, nm, C.byref(r.s))
+
+    from concurrent.futures import ThreadPoolExecutor
+    ex = ThreadPoolExecutor(threads)
+
+    def step(s):
+        list(ex.map(lambda t: one(t, s), range(threads)))
+
+    for s in range(args.warmup):
+        step(s)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        step(s)
+    dt = time.perf_counter() - t0
+    for s in states:
+        L.oracle_destroy(s)
+    v = threads * args.steps / dt
+    sample = f"{threads} keyframes per step (one per host thread), oracle restatement, 64x2048"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": "C2 64x2048 keyframe, 150 trees, 400-landmark "
+                                        "submap, 256 hyp + 3 LS, 10 GN", "threads": threads},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# -------------------------------------------------------------- GPU leg
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    from sloam_gb300 import build, capi as A
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    if rank == 0:
+        build.build()
+    if dist:
+        tdist.barrier()
+    from sloam_gb300.lib import Context, load
+    L = load()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    cfg, forest, kfs, P = workload(args.seed + rank, args.distinct)
+    ctx = Context(P, device=local)
+    mapa = forest.map_cylinders()
+    mapc = A.cylinders_from_array(mapa)
+    nm = len(mapa)
+    N = P.img_w * P.img_h
+    B = args.batch
+    # first scan at the true pose defines the previous-scan ground planes
+    kf0 = kfs[0]
+    r = A.RunBuffers(P)
+    ctx.check(L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), N, A.ptr(kf0.labels, C.c_uint8),
+                               None, C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, nm,
+                               C.byref(r.s)))
+    order = [i % len(kfs) for i in range(B)]
+    X = torch.from_numpy(np.stack([kfs[i].xyzi for i in order])).to(dev)
+    Lb = torch.from_numpy(np.stack([kfs[i].labels for i in order])).to(dev)
+    Mp = torch.from_numpy(np.frombuffer(bytes(mapc), np.uint8).copy()).to(dev)
+    poses = (A.SE3 * B)(*[A.SE3.from_qt(*kfs[i].pose_est_qt()) for i in order])
+    pose_out = torch.zeros(B * 7, dtype=torch.float64, device=dev)
+    succ = torch.zeros(B, dtype=torch.int32, device=dev)
+    ncyl = torch.zeros(B, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+
+    def step():
+        ctx.check(L.sloam_keyframes_device(ctx.h, X.data_ptr(), N, B, Lb.data_ptr(), poses,
+                                           Mp.data_ptr(), nm, pose_out.data_ptr(),
+                                           succ.data_ptr(), ncyl.data_ptr()))
+        return ctx.launches()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    evs = []
+    launches = 0
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for s in range(args.steps):
+        flush.fill_(float(s))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        launches += step()
+        e1.record(ext)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+    ck = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if dist:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = B * args.steps * world / (total_ms / 1000.0)
+    ok = int(succ.sum().item())
+    n_cyl = ncyl.cpu().numpy()
+
+    # per-stage breakdown of one keyframe, and the dominant kernel in isolation
+    stages = (C.c_float * 4)()
+    L.sloam_profile_stages(ctx.h, stages, 4)
+    hyp_ms = C.c_float()
+    L.sloam_time_kernel(ctx.h, 1, 20, C.byref(hyp_ms))
+    proj_ms = C.c_float()
+    L.sloam_time_kernel(ctx.h, 0, 20, C.byref(proj_ms))
+
+    # ---- e2e: the same keyframes through the host C ABI from pinned host
+    # buffers (sloam_keyframes_host): host->device copies of every scan and
+    # label array and the device->host read of every result are inside the
+    # timed region.
+    hX = X.cpu().pin_memory()
+    hL = Lb.cpu().pin_memory()
+    h_pose = np.zeros(B * 7, np.float64)
+    h_succ = np.zeros(B, np.int32)
+    h_ncyl = np.zeros(B, np.int32)
+
+    def e2e_step():
+        ctx.check(L.sloam_keyframes_host(ctx.h, hX.data_ptr(), N, B, hL.data_ptr(), poses, mapc, nm,
+                                         h_pose.ctypes.data, h_succ.ctypes.data,
+                                         h_ncyl.ctypes.data))
+
+    e2e_step()  # warm-up (graph capture of the slots)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(args.e2e_steps):
+        e2e_step()
+    e2e_dt = time.perf_counter() - t0
+    e2e = B * args.e2e_steps / e2e_dt
+    h2d = B * (N * 16 + N + 7 * 8) + C.sizeof(mapc) * min(B, P.batch_slots)
+    d2h = B * (7 * 8 + 4 + 4)
+    e2e_ok = int(h_succ.sum())
+
+    # ---- roofline of the dominant kernel (point-cylinder hypothesis scoring):
+    # algorithmic bytes per launch = every tree point read once (16 B) + per
+    # hypothesis 4 B (count) ; FLOP = 8 per point-hypothesis test.
+    import ctypes as _c
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+
+    # CPU baseline (rank 0, N=1): the oracle, one host thread, bounded sample
+    cpu = None
+    if rank == 0 and world == 1:
+        v, n_kf, dt = cpu_run_keyframes(P, forest, kfs, args.cpu_seconds, threads=1)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n_kf} keyframes of the same 64x2048 workload in {dt:.1f} s, "
+                         "one host thread (the reference path is single-threaded)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "C2: 64x2048 keyframes, 150 trees, 400-landmark submap, "
+                                   "256 hyp + 3 LS per tree, 10 GN iterations",
+                       "batch_keyframes": B, "distinct_scans": args.distinct,
+                       "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "keyframes_ok": e2e_ok,
+                    "api": "sloam_keyframes_host, pinned host buffers"},
+            "gpu_launches": int(launches),
+            "stages_ms_per_keyframe": {"project_mask": stages[0], "trellis": stages[1],
+                                       "models": stages[2], "assoc_pose": stages[3]},
+            "kernels_ms": {"k_cyl_hyp": hyp_ms.value, "k_project": proj_ms.value},
+            "keyframes_ok": ok, "cylinders_per_keyframe": float(n_cyl.mean()),
+            "clocks": ck,
+            "hbm_peak_gbs": hbm_peak,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

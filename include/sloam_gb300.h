@@ -102,6 +102,9 @@ typedef struct sloam_params {
   int32_t max_landmarks;            /* context capacity: trees per scan   */
   int32_t max_map;                  /* context capacity: submap cylinders */
   int32_t max_ground;               /* context capacity: ground points    */
+  int32_t batch_slots;              /* keyframes of a batch in flight at
+                                       once (each slot owns buffers, a
+                                       stream and a captured graph)       */
 } sloam_params;
 
 void sloam_params_default(sloam_params* p);
@@ -284,6 +287,19 @@ int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32_t n,
                            const sloam_cylinder* d_map, int32_t n_map,
                            double* d_pose_out, int32_t* d_success_out,
                            int32_t* d_ncyl_out);
+
+/* Host-buffer batch: the same as sloam_keyframes_device with every pointer a
+ * host pointer (xyzi [nkf*n*4], point_labels [nkf*n], map [n_map]; pinned
+ * host memory lets the copies overlap the compute).  Keyframes are spread
+ * over the context's batch_slots (buffers + stream + graph each), their
+ * host->device copies interleaved with the work of the other slots;
+ * pose_out [nkf*7], success_out [nkf], ncyl_out [nkf] are host arrays,
+ * complete when the call returns.  Each keyframe is SLOAMNode::run's work
+ * (sloamNode.cpp:186-282) for one scan. */
+int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t nkf,
+                         const uint8_t* point_labels, const sloam_se3* pose_estimates,
+                         const sloam_cylinder* map, int32_t n_map, double* pose_out,
+                         int32_t* success_out, int32_t* ncyl_out);
 
 /* Returns the number of kernels launched by the last call (for accounting). */
 int64_t sloam_last_launch_count(const sloam_ctx* ctx);

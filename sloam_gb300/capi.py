@@ -78,6 +78,7 @@ class Params(C.Structure):
         ("max_landmarks", C.c_int32),
         ("max_map", C.c_int32),
         ("max_ground", C.c_int32),
+        ("batch_slots", C.c_int32),
     ]
 
     def copy(self):
@@ -147,6 +148,7 @@ def default_params(**overrides):
     p.max_landmarks = 1024
     p.max_map = 4096
     p.max_ground = 0
+    p.batch_slots = 8
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)

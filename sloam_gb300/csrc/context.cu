@@ -71,6 +71,7 @@ extern "C" void sloam_params_default(sloam_params* p) {
   p->max_landmarks = 1024;
   p->max_map = 4096;
   p->max_ground = 0;
+  p->batch_slots = 8;
 }
 
 // sizeof() of every ABI struct, for binding checks.
@@ -198,6 +199,22 @@ struct sloam_ctx {
   // graphs: [first][label mode][state update]
   cudaGraphExec_t gx[2][2][2] = {};
   int gx_launches[2][2][2] = {};
+  // further keyframe slots of a batch (slot 0 is the fields above)
+  struct Slot {
+    Dev d{};
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t gx[2][2][2] = {};
+    int gxl[2][2][2] = {};
+    cudaEvent_t ev = nullptr;
+  };
+  std::vector<Slot> extra;
+  cudaEvent_t ev_main = nullptr;
+  // host batch staging
+  int32_t* d_out_i = nullptr;   // [2 * cap] success, ncyl
+  double* d_out_pose = nullptr; // [7 * cap]
+  int out_cap = 0;
 };
 
 namespace {
@@ -278,6 +295,7 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.lm_pts = c.take<float4>(d.cap_p);
   d.lm_cbeg = c.take<int32_t>(d.cap_lm + 1);
   d.lm_cpts = c.take<float4>(d.cap_cluster);
+  d.lm_vsrc = c.take<int32_t>(d.cap_v);
   d.bin_of = c.take<int32_t>(d.cap_ground);
   d.bin_cnt = c.take<int32_t>(d.n_bins);
   d.bin_off = c.take<int32_t>(d.n_bins + 1);
@@ -310,13 +328,23 @@ int check_params(const sloam_params& p) {
   if (p.trellis_max_vertices < 1 || p.trellis_max_vertices > 4096) return 1;
   if (p.cyl_hypotheses < 0 || p.cyl_hypotheses > 4096 || p.line_ransac_max_iter > 256) return 1;
   if (!(p.ground_retain_thresh > 0)) return 1;
+  if (p.batch_slots < 0 || p.batch_slots > 64) return 1;
   return 0;
 }
 
-int setup(sloam_ctx* ctx, const sloam_params& P) {
-  ctx->P = P;
-  ctx->kp = make_kparams(P);
-  Dev& d = ctx->d;
+void destroy_graphs(cudaGraphExec_t (&gx)[2][2][2]) {
+  for (auto& a : gx)
+    for (auto& b : a)
+      for (auto& g : b)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+}
+
+// Sizes, carves and initialises one slot's device state.
+int init_dev(sloam_ctx* ctx, const sloam_params& P, Dev& d, void*& arena, size_t& arena_bytes,
+             cudaStream_t st) {
   d.H = P.img_h;
   d.W = P.img_w;
   d.N = P.img_h * P.img_w;
@@ -335,36 +363,55 @@ int setup(sloam_ctx* ctx, const sloam_params& P) {
   Carver dry{nullptr, 0, true};
   carve(d, dry, n_blk);
   const size_t bytes = dry.off + 256;
-  if (ctx->arena && bytes > ctx->arena_bytes) {
-    cudaFree(ctx->arena);
-    ctx->arena = nullptr;
+  if (arena && bytes > arena_bytes) {
+    cudaFree(arena);
+    arena = nullptr;
   }
-  if (!ctx->arena) {
-    CK(cudaMalloc(&ctx->arena, bytes));
-    ctx->arena_bytes = bytes;
+  if (!arena) {
+    CK(cudaMalloc(&arena, bytes));
+    arena_bytes = bytes;
   }
-  Carver real{reinterpret_cast<char*>(ctx->arena), 0, false};
+  Carver real{reinterpret_cast<char*>(arena), 0, false};
   carve(d, real, n_blk);
   // tables
   std::vector<float> tab(d.W + 1), tb(4096), rb(4096);
   build_px_table(P, tab.data());
   build_ground_tables(P, tb.data(), rb.data(), &d.r_lo, &d.r_hi);
-  CK(cudaMemcpyAsync(d.px_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice,
-                     ctx->st));
+  CK(cudaMemcpyAsync(d.px_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.tb_tab, tb.data(), sizeof(float) * (P.ground_theta_bins + 1),
-                     cudaMemcpyHostToDevice, ctx->st));
+                     cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.rb_tab, rb.data(), sizeof(float) * (P.ground_radii_bins + 1),
-                     cudaMemcpyHostToDevice, ctx->st));
-  CK(cudaMemsetAsync(d.pkey, 0xFF, sizeof(unsigned long long) * d.N, ctx->st));
-  CK(cudaMemsetAsync(d.cnt, 0, sizeof(Counters), ctx->st));
-  CK(cudaStreamSynchronize(ctx->st));
-  for (auto& a : ctx->gx)
-    for (auto& b : a)
-      for (auto& g : b)
-        if (g) {
-          cudaGraphExecDestroy(g);
-          g = nullptr;
-        }
+                     cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(d.pkey, 0xFF, sizeof(unsigned long long) * d.N, st));
+  CK(cudaMemsetAsync(d.cnt, 0, sizeof(Counters), st));
+  CK(cudaStreamSynchronize(st));
+  return SLOAM_OK;
+}
+
+int setup(sloam_ctx* ctx, const sloam_params& P) {
+  ctx->P = P;
+  ctx->kp = make_kparams(P);
+  int st = init_dev(ctx, P, ctx->d, ctx->arena, ctx->arena_bytes, ctx->st);
+  if (st) return st;
+  destroy_graphs(ctx->gx);
+  const int ns = std::max(1, std::min(P.batch_slots, 64)) - 1;
+  while ((int)ctx->extra.size() > ns) {
+    auto& s = ctx->extra.back();
+    cudaStreamSynchronize(s.st);
+    destroy_graphs(s.gx);
+    if (s.arena) cudaFree(s.arena);
+    if (s.ev) cudaEventDestroy(s.ev);
+    if (s.st) cudaStreamDestroy(s.st);
+    ctx->extra.pop_back();
+  }
+  ctx->extra.resize(ns);
+  for (auto& s : ctx->extra) {
+    if (!s.st) CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    if (!s.ev) CK(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
+    destroy_graphs(s.gx);
+    if ((st = init_dev(ctx, P, s.d, s.arena, s.arena_bytes, s.st))) return st;
+  }
+  if (!ctx->ev_main) CK(cudaEventCreateWithFlags(&ctx->ev_main, cudaEventDisableTiming));
   ctx->first_scan = true;
   return SLOAM_OK;
 }
@@ -570,10 +617,17 @@ extern "C" void sloam_destroy(sloam_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
-  for (auto& a : ctx->gx)
-    for (auto& b : a)
-      for (auto& g : b)
-        if (g) cudaGraphExecDestroy(g);
+  destroy_graphs(ctx->gx);
+  for (auto& s : ctx->extra) {
+    if (s.st) cudaStreamSynchronize(s.st);
+    destroy_graphs(s.gx);
+    if (s.arena) cudaFree(s.arena);
+    if (s.ev) cudaEventDestroy(s.ev);
+    if (s.st) cudaStreamDestroy(s.st);
+  }
+  if (ctx->ev_main) cudaEventDestroy(ctx->ev_main);
+  if (ctx->d_out_i) cudaFree(ctx->d_out_i);
+  if (ctx->d_out_pose) cudaFree(ctx->d_out_pose);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->h_cnt) cudaFreeHost(ctx->h_cnt);
   if (ctx->h_pose) cudaFreeHost(ctx->h_pose);
@@ -758,32 +812,42 @@ extern "C" int sloam_run(sloam_ctx* ctx, const sloam_se3* pose, const float* gro
 
 // ----------------------------------------------------------- keyframe
 namespace {
-int enqueue_keyframe(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
-  Dev& d = ctx->d;
-  int k = launch_begin(d, -1, -1, -1, -1, -1, ctx->st);
-  k += launch_project(d, ctx->kp, point_labels, ctx->st);
-  k += launch_trellis(d, ctx->kp, ctx->st);
-  k += launch_models(d, ctx->kp, true, ctx->st);
-  k += launch_run(d, ctx->kp, first, update, ctx->st);
+int enqueue_keyframe(sloam_ctx* ctx, const Dev& d, cudaStream_t st, bool first,
+                     bool point_labels, bool update) {
+  int k = launch_begin(d, -1, -1, -1, -1, -1, st);
+  k += launch_project(d, ctx->kp, point_labels, st);
+  k += launch_trellis(d, ctx->kp, st);
+  k += launch_models(d, ctx->kp, true, st);
+  k += launch_run(d, ctx->kp, first, update, st);
   return k;
 }
 
-// The whole keyframe (a1-a11) as one CUDA graph, captured on first use.
-int run_keyframe_graph(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
+// The whole keyframe (a1-a11) of one slot as one CUDA graph, captured on
+// first use; returns the number of kernels it launches in *nk.
+int run_graph(sloam_ctx* ctx, const Dev& d, cudaStream_t st, cudaGraphExec_t (&gx)[2][2][2],
+              int (&gxl)[2][2][2], bool first, bool point_labels, bool update, int* nk) {
   const int a = first ? 1 : 0, b = point_labels ? 1 : 0, u = update ? 1 : 0;
-  if (!ctx->gx[a][b][u]) {
+  if (!gx[a][b][u]) {
     cudaGraph_t g;
-    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-    const int k = enqueue_keyframe(ctx, first, point_labels, update);
-    CK(cudaStreamEndCapture(ctx->st, &g));
-    cudaError_t e = cudaGraphInstantiate(&ctx->gx[a][b][u], g, 0);
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int k = enqueue_keyframe(ctx, d, st, first, point_labels, update);
+    CK(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&gx[a][b][u], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(ctx, SLOAM_ERR_CUDA, "cudaGraphInstantiate", e);
-    ctx->gx_launches[a][b][u] = k;
+    gxl[a][b][u] = k;
   }
-  CK(cudaGraphLaunch(ctx->gx[a][b][u], ctx->st));
-  ctx->last_launches = ctx->gx_launches[a][b][u];
+  CK(cudaGraphLaunch(gx[a][b][u], st));
+  *nk = gxl[a][b][u];
   return SLOAM_OK;
+}
+
+int run_keyframe_graph(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
+  int nk = 0;
+  const int s = run_graph(ctx, ctx->d, ctx->st, ctx->gx, ctx->gx_launches, first, point_labels,
+                          update, &nk);
+  ctx->last_launches = nk;
+  return s;
 }
 }  // namespace
 
@@ -838,6 +902,79 @@ __global__ void k_batch_out(Counters* c, const double* pose_io, double* pose_out
 }
 }  // namespace sg
 
+namespace {
+// A keyframe slot of a batch: slot 0 is the context's own state.
+struct SlotView {
+  Dev* d;
+  cudaStream_t st;
+  cudaGraphExec_t (*gx)[2][2][2];
+  int (*gxl)[2][2][2];
+  cudaEvent_t ev;
+};
+SlotView slot(sloam_ctx* ctx, int s) {
+  if (s == 0) return {&ctx->d, ctx->st, &ctx->gx, &ctx->gx_launches, nullptr};
+  auto& x = ctx->extra[s - 1];
+  return {&x.d, x.st, &x.gx, &x.gxl, x.ev};
+}
+
+int grow_batch(sloam_ctx* ctx, int nkf) {
+  if (nkf <= ctx->h_batch_cap) return SLOAM_OK;
+  cudaFreeHost(ctx->h_in);
+  cudaFreeHost(ctx->h_poses);
+  ctx->h_in = nullptr;
+  ctx->h_poses = nullptr;
+  CK(cudaMallocHost((void**)&ctx->h_in, sizeof(InPtrs) * nkf));
+  CK(cudaMallocHost((void**)&ctx->h_poses, sizeof(double) * 8 * nkf));
+  ctx->h_batch_cap = nkf;
+  return SLOAM_OK;
+}
+
+// Fork: every extra slot waits for the context stream and takes a copy of
+// the previous-scan planes (the batch does not advance the state).
+int batch_fork(sloam_ctx* ctx) {
+  CK(cudaEventRecord(ctx->ev_main, ctx->st));
+  for (auto& s : ctx->extra) {
+    CK(cudaStreamWaitEvent(s.st, ctx->ev_main, 0));
+    CK(cudaMemcpyAsync(s.d.prev_planes, ctx->d.prev_planes, sizeof(PlaneD) * ctx->d.n_bins,
+                       cudaMemcpyDeviceToDevice, s.st));
+    CK(cudaMemcpyAsync(&s.d.cnt->n_prev, &ctx->d.cnt->n_prev, sizeof(int32_t),
+                       cudaMemcpyDeviceToDevice, s.st));
+  }
+  return SLOAM_OK;
+}
+// Join: the context stream waits for every slot.
+int batch_join(sloam_ctx* ctx) {
+  for (auto& s : ctx->extra) {
+    CK(cudaEventRecord(s.ev, s.st));
+    CK(cudaStreamWaitEvent(ctx->st, s.ev, 0));
+  }
+  return SLOAM_OK;
+}
+
+// Keyframe k of a batch on slot k % slots: inputs pointer block and pose
+// estimate from pinned host memory, the slot's graph (no state update),
+// then its outputs into the batch arrays.
+int batch_one(sloam_ctx* ctx, int k, double* pose_out, int32_t* success_out, int32_t* ncyl_out,
+              int64_t* launches) {
+  const int S = 1 + (int)ctx->extra.size();
+  SlotView v = slot(ctx, k % S);
+  CK(cudaMemcpyAsync(v.d->in, ctx->h_in + k, sizeof(InPtrs), cudaMemcpyHostToDevice, v.st));
+  CK(cudaMemcpyAsync(v.d->pose_io, ctx->h_poses + 8 * k, sizeof(double) * 7,
+                     cudaMemcpyHostToDevice, v.st));
+  int nk = 0;
+  int st = run_graph(ctx, *v.d, v.st, *v.gx, *v.gxl, false, true, false, &nk);
+  if (st) return st;
+  k_batch_out<<<1, 32, 0, v.st>>>(v.d->cnt, v.d->pose_io, pose_out, success_out, ncyl_out, k);
+  *launches += nk + 1;
+  return SLOAM_OK;
+}
+
+void fill_pose(sloam_ctx* ctx, int k, const sloam_se3& p) {
+  for (int j = 0; j < 4; ++j) ctx->h_poses[8 * k + j] = p.q[j];
+  for (int j = 0; j < 3; ++j) ctx->h_poses[8 * k + 4 + j] = p.t[j];
+}
+}  // namespace
+
 extern "C" int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32_t n,
                                       int32_t nkf, const uint8_t* d_point_labels,
                                       const sloam_se3* poses, const sloam_cylinder* d_map,
@@ -851,16 +988,9 @@ extern "C" int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32
   if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
   if (ctx->first_scan) return fail(ctx, SLOAM_ERR_ARG, "the context has not seen a first scan");
   if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
-  CK(cudaStreamSynchronize(ctx->st));
-  if (nkf > ctx->h_batch_cap) {
-    cudaFreeHost(ctx->h_in);
-    cudaFreeHost(ctx->h_poses);
-    ctx->h_in = nullptr;
-    ctx->h_poses = nullptr;
-    CK(cudaMallocHost((void**)&ctx->h_in, sizeof(InPtrs) * nkf));
-    CK(cudaMallocHost((void**)&ctx->h_poses, sizeof(double) * 8 * nkf));
-    ctx->h_batch_cap = nkf;
-  }
+  CK(cudaStreamSynchronize(ctx->st));  // the previous batch released the pinned blocks
+  int st = grow_batch(ctx, nkf);
+  if (st) return st;
   for (int k = 0; k < nkf; ++k) {
     InPtrs& h = ctx->h_in[k];
     h.xyzi = reinterpret_cast<const float4*>(d_xyzi) + (size_t)k * n;
@@ -868,22 +998,132 @@ extern "C" int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32
     h.mask_in = nullptr;
     h.map = d_map;
     h.n_map = n_map;
-    for (int j = 0; j < 4; ++j) ctx->h_poses[8 * k + j] = poses[k].q[j];
-    for (int j = 0; j < 3; ++j) ctx->h_poses[8 * k + 4 + j] = poses[k].t[j];
+    fill_pose(ctx, k, poses[k]);
   }
   int64_t launches = 0;
-  for (int k = 0; k < nkf; ++k) {
-    CK(cudaMemcpyAsync(d.in, ctx->h_in + k, sizeof(InPtrs), cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(d.pose_io, ctx->h_poses + 8 * k, sizeof(double) * 7,
-                       cudaMemcpyHostToDevice, ctx->st));
-    // the previous-scan planes are not advanced inside a batch
-    int st = run_keyframe_graph(ctx, false, true, false);
-    if (st) return st;
-    launches += ctx->last_launches;
-    k_batch_out<<<1, 32, 0, ctx->st>>>(d.cnt, d.pose_io, d_pose_out, d_success_out, d_ncyl_out, k);
-    ++launches;
-  }
+  if ((st = batch_fork(ctx))) return st;
+  for (int k = 0; k < nkf; ++k)
+    if ((st = batch_one(ctx, k, d_pose_out, d_success_out, d_ncyl_out, &launches))) return st;
+  if ((st = batch_join(ctx))) return st;
   ctx->last_launches = launches;
   CK(cudaGetLastError());
+  return SLOAM_OK;
+}
+
+extern "C" int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t nkf,
+                                    const uint8_t* point_labels, const sloam_se3* poses,
+                                    const sloam_cylinder* map, int32_t n_map, double* pose_out,
+                                    int32_t* success_out, int32_t* ncyl_out) {
+  if (!ctx || !xyzi || !point_labels || !poses || nkf < 0 || !pose_out || !success_out ||
+      !ncyl_out || n_map <= 0 || !map)
+    return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
+  if (ctx->first_scan) return fail(ctx, SLOAM_ERR_ARG, "the context has not seen a first scan");
+  if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
+  CK(cudaStreamSynchronize(ctx->st));
+  int st = grow_batch(ctx, nkf);
+  if (st) return st;
+  if (nkf > ctx->out_cap) {
+    if (ctx->d_out_i) cudaFree(ctx->d_out_i);
+    if (ctx->d_out_pose) cudaFree(ctx->d_out_pose);
+    ctx->d_out_i = nullptr;
+    ctx->d_out_pose = nullptr;
+    CK(cudaMalloc(&ctx->d_out_i, sizeof(int32_t) * 2 * nkf));
+    CK(cudaMalloc(&ctx->d_out_pose, sizeof(double) * 7 * nkf));
+    ctx->out_cap = nkf;
+  }
+  const int S = 1 + (int)ctx->extra.size();
+  for (int k = 0; k < nkf; ++k) {
+    const SlotView v = slot(ctx, k % S);
+    InPtrs& h = ctx->h_in[k];
+    h.xyzi = v.d->buf_xyzi;
+    h.plabel = v.d->buf_plabel;
+    h.mask_in = nullptr;
+    h.map = v.d->buf_map;
+    h.n_map = n_map;
+    fill_pose(ctx, k, poses[k]);
+  }
+  int64_t launches = 0;
+  if ((st = batch_fork(ctx))) return st;
+  for (int s = 0; s < S && s < nkf; ++s) {
+    const SlotView v = slot(ctx, s);
+    CK(cudaMemcpyAsync(v.d->buf_map, map, sizeof(sloam_cylinder) * n_map, cudaMemcpyHostToDevice,
+                       v.st));
+  }
+  for (int k = 0; k < nkf; ++k) {
+    const SlotView v = slot(ctx, k % S);
+    CK(cudaMemcpyAsync(v.d->buf_xyzi, xyzi + (size_t)k * n * 4, 16 * (size_t)n,
+                       cudaMemcpyHostToDevice, v.st));
+    CK(cudaMemcpyAsync(v.d->buf_plabel, point_labels + (size_t)k * n, (size_t)n,
+                       cudaMemcpyHostToDevice, v.st));
+    if ((st = batch_one(ctx, k, ctx->d_out_pose, ctx->d_out_i, ctx->d_out_i + nkf, &launches)))
+      return st;
+  }
+  if ((st = batch_join(ctx))) return st;
+  CK(cudaMemcpyAsync(pose_out, ctx->d_out_pose, sizeof(double) * 7 * nkf, cudaMemcpyDeviceToHost,
+                     ctx->st));
+  CK(cudaMemcpyAsync(success_out, ctx->d_out_i, sizeof(int32_t) * nkf, cudaMemcpyDeviceToHost,
+                     ctx->st));
+  CK(cudaMemcpyAsync(ncyl_out, ctx->d_out_i + nkf, sizeof(int32_t) * nkf, cudaMemcpyDeviceToHost,
+                     ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  ctx->last_launches = launches;
+  return SLOAM_OK;
+}
+
+// ------------------------------------------------------ profiling hooks
+// Not part of the public header: used by bench.py for per-stage timing and
+// the isolated timing of one kernel.  Both replay work on the inputs and
+// state left by the previous keyframe call and record CUDA events on the
+// context stream.
+extern "C" int sloam_profile_stages(sloam_ctx* ctx, float* ms, int n) {
+  if (!ctx || !ms || n < 4) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  cudaEvent_t ev[5];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CK(cudaEventRecord(ev[0], ctx->st));
+  launch_begin(d, -1, -1, -1, -1, -1, ctx->st);
+  launch_project(d, ctx->kp, true, ctx->st);
+  CK(cudaEventRecord(ev[1], ctx->st));
+  launch_trellis(d, ctx->kp, ctx->st);
+  CK(cudaEventRecord(ev[2], ctx->st));
+  launch_models(d, ctx->kp, true, ctx->st);
+  CK(cudaEventRecord(ev[3], ctx->st));
+  launch_run(d, ctx->kp, false, false, ctx->st);
+  CK(cudaEventRecord(ev[4], ctx->st));
+  CK(cudaEventSynchronize(ev[4]));
+  for (int i = 0; i < 4; ++i) CK(cudaEventElapsedTime(ms + i, ev[i], ev[i + 1]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  return SLOAM_OK;
+}
+
+// which: 0 = projection kernel (k_project), 1 = point-cylinder hypothesis
+// kernel (k_cyl_hyp).  Average milliseconds per launch over `reps`.
+extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg_ms) {
+  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 1) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  // the hypothesis kernel scores trees still at the vertex-line stage
+  if (which == 1) launch_cyl_fit_kernel(d, ctx->kp, ctx->st);
+  CK(cudaEventRecord(a, ctx->st));
+  for (int r = 0; r < reps; ++r) {
+    if (which == 0) launch_project_kernel(d, ctx->kp, ctx->st);
+    else launch_cyl_hyp_kernel(d, ctx->kp, ctx->st);
+  }
+  CK(cudaEventRecord(b, ctx->st));
+  CK(cudaEventSynchronize(b));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  *avg_ms = ms / reps;
+  if (which == 0) launch_resolve_kernel(d, true, ctx->st);  // re-arm the pixel keys
+  CK(cudaStreamSynchronize(ctx->st));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
   return SLOAM_OK;
 }

@@ -116,6 +116,7 @@ struct Dev {
   float4* lm_pts;      // [cap_p]
   int32_t* lm_cbeg;    // [cap_lm+1]
   float4* lm_cpts;     // [cap_cluster]
+  int32_t* lm_vsrc;    // [cap_v] offset of each vertex's kept points in `kept`
   // -- ground bins / planes
   int32_t* bin_of;     // [cap_ground]
   int32_t* bin_cnt;    // [n_bins]
@@ -178,6 +179,12 @@ int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_sta
                cudaStream_t st);
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trellis,
                                cudaStream_t st);
+
+// single kernels, for isolated timing (profiling hooks)
+int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
+int launch_resolve_kernel(const Dev& d, bool point_labels, cudaStream_t st);
+int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
+int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 
 // per-call counter reset: counts >= 0 are set, -1 left to the pipeline
 int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster,

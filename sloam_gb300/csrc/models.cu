@@ -952,6 +952,17 @@ __global__ void k_zero_bins(Dev d) {
 
 }  // namespace
 
+int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
+  const int gl = (d.cap_lm + kCylWarps - 1) / kCylWarps;
+  k_cyl_fit<<<gl < 1 ? 1 : gl, kCylWarps * 32, 0, st>>>(d, kp);
+  return 1;
+}
+
+int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
+  k_cyl_hyp<<<152 * 6, kHypThreads, (size_t)kPtCap * sizeof(float2), st>>>(d, kp);
+  return 1;
+}
+
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream_t st) {
   const size_t smem = (size_t)kPtCap * sizeof(float2);
   k_cyl_hyp<<<152 * 6, kHypThreads, smem, st>>>(d, kp);

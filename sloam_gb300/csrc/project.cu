@@ -185,6 +185,15 @@ int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_c
   return 1;
 }
 
+int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
+  k_project<<<(d.N + 255) / 256, 256, 0, st>>>(d, kp);
+  return 1;
+}
+int launch_resolve_kernel(const Dev& d, bool point_labels, cudaStream_t st) {
+  k_resolve<<<(d.N + 255) / 256, 256, 0, st>>>(d, point_labels ? 1 : 0);
+  return 1;
+}
+
 int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st) {
   const int N = d.N;
   const int g256 = (N + 255) / 256;

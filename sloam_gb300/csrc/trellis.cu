@@ -471,16 +471,39 @@ __global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
         d.lm_vrad[vv] = d.vrad[it];
         d.lm_vrow[vv] = row;
         d.lm_pbeg[vv] = pstart;
-        const int off = d.roff[it];
-        for (int q = 0; q < k; ++q) d.lm_pts[pstart + q] = d.kept[off + q];
+        d.lm_vsrc[vv] = d.roff[it];
       }
       pbase += __shfl_sync(0xffffffffu, incl, 31);
       vi += __popc(b);
     }
-    // cluster points: the candidate's buckets are contiguous, raster order
-    const int cb = d.lm_cbeg[l];
-    const int s = d.roff[c * H], e = d.roff[c * H + H];
-    for (int q = s + lane; q < e; q += 32) d.lm_cpts[cb + (q - s)] = d.tree[d.bucket[q]];
+  }
+}
+
+// Point copies of the landmarks, spread over the whole grid: one warp per
+// vertex for the kept points, one thread per bucket slot for the cluster
+// points (raster order; the candidate of a slot found by binary search).
+__global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
+  const int H = d.H;
+  const int lane = threadIdx.x & 31;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  const int nv = d.cnt->n_v;
+  for (int v = gt >> 5; v < nv; v += nt >> 5) {
+    const int src = d.lm_vsrc[v], dst = d.lm_pbeg[v], cnt = d.lm_pbeg[v + 1] - dst;
+    for (int q = lane; q < cnt; q += 32) d.lm_pts[dst + q] = d.kept[src + q];
+  }
+  const int nc = d.cnt->n_cand;
+  const int total = d.roff[nc * H];
+  for (int q = gt; q < total; q += nt) {
+    int lo = 0, hi = nc - 1;  // last candidate whose first slot <= q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (d.roff[mid * H] <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    const int l = d.cand_lm[lo];
+    if (l < 0) continue;
+    d.lm_cpts[d.lm_cbeg[l] + (q - d.roff[lo * H])] = d.tree[d.bucket[q]];
   }
 }
 
@@ -508,7 +531,8 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   k_lm_count<<<(d.cap_cand + 255) / 256, 256, 0, st>>>(d, kp, cand_np, cand_ncl);
   k_lm_scan<<<1, 1024, 0, st>>>(d, cand_np, cand_ncl, cand_vb, cand_pb);
   k_lm_write<<<gw, 256, 0, st>>>(d, cand_vb, cand_pb);
-  return 13;
+  k_lm_copy<<<gw, 256, 0, st>>>(d);
+  return 14;
 }
 
 }  // namespace sg

@@ -15,7 +15,8 @@ EXPORTS = [
     "sloam_params_default", "sloam_abi_sizes", "sloam_create", "sloam_destroy",
     "sloam_last_error", "sloam_reset", "sloam_set_params", "sloam_project_mask",
     "sloam_trellis", "sloam_compute_models", "sloam_run", "sloam_keyframe",
-    "sloam_keyframes_device", "sloam_last_launch_count", "sloam_stream", "sloam_internal_tables",
+    "sloam_keyframes_device", "sloam_keyframes_host", "sloam_last_launch_count", "sloam_stream",
+    "sloam_internal_tables",
 ]
 
 _lib = None
@@ -60,6 +61,8 @@ def load(path=LIB_PATH):
                                  C.c_int32, C.POINTER(A.RunOut)]
     L.sloam_keyframes_device.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.POINTER(A.SE3),
                                          vp, C.c_int32, vp, vp, vp]
+    L.sloam_keyframes_host.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.POINTER(A.SE3),
+                                       C.POINTER(A.Cylinder), C.c_int32, vp, vp, vp]
     L.sloam_last_launch_count.argtypes = [vp]
     L.sloam_last_launch_count.restype = C.c_int64
     L.sloam_stream.argtypes = [vp]
