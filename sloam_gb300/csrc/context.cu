@@ -315,6 +315,9 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.cyl_match = c.take<int32_t>(d.cap_lm);
   d.plane_match = c.take<int32_t>(d.n_bins);
   d.match_out = c.take<int32_t>(d.cap_lm);
+  d.map_pts = c.take<double>((size_t)d.cap_map * 9);
+  d.res_tab = c.take<float>(((size_t)d.cap_lm * d.F + (size_t)d.n_bins * d.G) * 12);
+  d.lm_uv = c.take<float2>((size_t)d.cap_cluster + d.cap_p);  // cluster | vertex points
   d.pose_io = c.take<double>(32);
   d.cnt = c.take<Counters>(1);
 }

@@ -139,6 +139,9 @@ struct Dev {
   int32_t* cyl_match;   // [cap_lm] map object matched for the pose (-1)
   int32_t* plane_match; // [n_bins]
   int32_t* match_out;   // [cap_lm] matchModels result
+  double* map_pts;      // [cap_map*9] map axis points at z = 0, 3, 6
+  float* res_tab;       // [(cap_lm*F + n_bins*G) * 12] residual table of the pose solve
+  float2* lm_uv;        // [cap_cluster] tree points projected on the prior axis frame
   double* pose_io;      // [16] in: estimate (q xyzw, t); out: T_Map_Curr, T_Delta
   Counters* cnt;
 };

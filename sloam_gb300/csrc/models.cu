@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
 
 // ---------------------------------------------- point-level cylinder fit
 constexpr int kHypThreads = 128;
-constexpr int kPtCap = 12288;  // projected points staged in shared memory
+constexpr int kStage = 2048;  // projected points staged in shared memory per block
 
 struct CylFrame {
   float ox, oy, oz;
@@ -667,16 +667,40 @@ __device__ __forceinline__ float2 project_uv(const CylFrame& f, float4 q) {
   return make_float2(u, v);
 }
 
-// The tree's points: its CC cluster, or its vertex points when no cluster.
-__device__ __forceinline__ void tree_points(const Dev& d, int l, const float4** pts, int* n) {
+// The tree's points: its CC cluster, or its vertex points when no cluster;
+// *uv = where their projections live in lm_uv.
+__device__ __forceinline__ void tree_points(const Dev& d, int l, const float4** pts, int* n,
+                                            const float2** uv) {
   const int c0 = d.lm_cbeg[l], c1 = d.lm_cbeg[l + 1];
   if (c1 > c0) {
     *pts = d.lm_cpts + c0;
     *n = c1 - c0;
+    *uv = d.lm_uv + c0;
   } else {
     const int vb = d.lm_vbeg[l], ve = d.lm_vbeg[l + 1];
     *pts = d.lm_pts + d.lm_pbeg[vb];
     *n = d.lm_pbeg[ve] - d.lm_pbeg[vb];
+    *uv = d.lm_uv + d.cap_cluster + d.lm_pbeg[vb];
+  }
+}
+
+__device__ __forceinline__ bool fit_eligible(const CylD& c) {
+  return c.stage == 1 && c.radius != -1.0;
+}
+
+// Projection of each eligible tree's points on its prior-axis frame.
+__global__ void __launch_bounds__(256) k_cyl_uv(Dev d) {
+  const int nl = d.cnt->n_lm;
+  for (int l = blockIdx.x; l < nl; l += gridDim.x) {
+    const CylD c = d.cyl_all[l];
+    if (!fit_eligible(c)) continue;
+    const float4* pts;
+    const float2* uv;
+    int n;
+    tree_points(d, l, &pts, &n, &uv);
+    const CylFrame f = make_frame(d, c);
+    float2* out = const_cast<float2*>(uv);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = project_uv(f, pts[i]);
   }
 }
 
@@ -713,49 +737,44 @@ __device__ __forceinline__ Hyp make_hyp(const KParams& kp, int h, int tree_id, i
   return H;
 }
 
-// Blocks of kHypThreads: one hypothesis per thread, the tree's projected
-// points in shared memory, every thread sweeps all points (broadcast reads).
+__device__ __forceinline__ int band_count(const float2* q, int n, const Hyp& H) {
+  int cnt = 0;
+#pragma unroll 4
+  for (int i = 0; i < n; ++i) {
+    const float2 p = q[i];
+    const float du = fsub(p.x, H.cu), dv = fsub(p.y, H.cv);
+    const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+    cnt += (d2 > H.lo2) & (d2 < H.hi2);
+  }
+  return cnt;
+}
+
+// Blocks of kHypThreads: one hypothesis per thread; the tree's first kStage
+// projected points staged in shared memory (broadcast reads), the rest read
+// through L1.  Best = most inliers, lowest hypothesis on ties (64-bit max).
 __global__ void __launch_bounds__(kHypThreads) k_cyl_hyp(Dev d, KParams kp) {
-  extern __shared__ float2 suv[];
+  __shared__ float2 suv[kStage];
   const int nl = d.cnt->n_lm;
   const int chunks = (kp.K + kHypThreads - 1) / kHypThreads;
   for (int item = blockIdx.x; item < nl * chunks; item += gridDim.x) {
     const int l = item / chunks, ch = item - l * chunks;
     const CylD c = d.cyl_all[l];
-    if (c.stage != 1 || c.radius == -1.0) continue;
+    if (!fit_eligible(c)) continue;
     const float4* pts;
+    const float2* uv;
     int n;
-    tree_points(d, l, &pts, &n);
+    tree_points(d, l, &pts, &n, &uv);
     if (n < 3) continue;
-    const CylFrame f = make_frame(d, c);
-    const bool inshm = n <= kPtCap;
-    if (inshm) {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) suv[i] = project_uv(f, pts[i]);
-      __syncthreads();
-    }
+    const int ns = min(n, kStage);
+    for (int i = threadIdx.x; i < ns; i += blockDim.x) suv[i] = uv[i];
+    __syncthreads();
     const int h = ch * kHypThreads + threadIdx.x;
     if (h < kp.K) {
-      Hyp H;
-      if (inshm) H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return suv[i]; });
-      else H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return project_uv(f, pts[i]); });
+      const Hyp H =
+          make_hyp(kp, h, c.id, n, [&](uint32_t i) { return i < (uint32_t)ns ? suv[i] : uv[i]; });
       if (H.ok) {
-        int cnt = 0;
-        if (inshm) {
-#pragma unroll 4
-          for (int i = 0; i < n; ++i) {
-            const float2 q = suv[i];
-            const float du = fsub(q.x, H.cu), dv = fsub(q.y, H.cv);
-            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-            cnt += (d2 > H.lo2) & (d2 < H.hi2);
-          }
-        } else {
-          for (int i = 0; i < n; ++i) {
-            const float2 q = project_uv(f, pts[i]);
-            const float du = fsub(q.x, H.cu), dv = fsub(q.y, H.cv);
-            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-            cnt += (d2 > H.lo2) & (d2 < H.hi2);
-          }
-        }
+        int cnt = band_count(suv, ns, H);
+        if (n > ns) cnt += band_count(uv + ns, n - ns, H);
         if (cnt > 0) {
           const unsigned long long key =
               ((unsigned long long)cnt << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
@@ -781,10 +800,11 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
     const int h = (int)(0xFFFFFFFFu - (uint32_t)(key & 0xffffffffull));
     const int best_cnt = (int)(key >> 32);
     const float4* pts;
+    const float2* uvs;
     int n;
-    tree_points(d, l, &pts, &n);
+    tree_points(d, l, &pts, &n, &uvs);
     const CylFrame f = make_frame(d, c);
-    const Hyp H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return project_uv(f, pts[i]); });
+    const Hyp H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return uvs[i]; });
     if (threadIdx.x == 0) {
       st[0] = f.ox + (double)H.cu * f.e1x + (double)H.cv * f.e2x;
       st[1] = f.oy + (double)H.cu * f.e1y + (double)H.cv * f.e2y;
@@ -813,7 +833,7 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
       for (int j = 0; j < 20; ++j) acc[j] = 0.f;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 q = pts[i];
-        const float2 uv = project_uv(f, q);
+        const float2 uv = uvs[i];
         const float du = fsub(uv.x, H.cu), dv = fsub(uv.y, H.cv);
         const float d2 = fadd(fmul(du, du), fmul(dv, dv));
         if (!((d2 > H.lo2) & (d2 < H.hi2))) continue;
@@ -952,22 +972,24 @@ __global__ void k_zero_bins(Dev d) {
 
 }  // namespace
 
+// one wave of warps for the per-landmark kernels (grid-stride beyond it)
+constexpr int kCylBlocks = 64;
+
 int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
-  const int gl = (d.cap_lm + kCylWarps - 1) / kCylWarps;
-  k_cyl_fit<<<gl < 1 ? 1 : gl, kCylWarps * 32, 0, st>>>(d, kp);
+  k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
   return 1;
 }
 
 int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
-  k_cyl_hyp<<<152 * 6, kHypThreads, (size_t)kPtCap * sizeof(float2), st>>>(d, kp);
+  k_cyl_hyp<<<304, kHypThreads, 0, st>>>(d, kp);
   return 1;
 }
 
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream_t st) {
-  const size_t smem = (size_t)kPtCap * sizeof(float2);
-  k_cyl_hyp<<<152 * 6, kHypThreads, smem, st>>>(d, kp);
-  k_cyl_ls<<<152 * 2, kLsThreads, 0, st>>>(d, kp);
-  return 2;
+  k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
+  k_cyl_hyp<<<304, kHypThreads, 0, st>>>(d, kp);
+  k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
+  return 3;
 }
 
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
@@ -980,8 +1002,7 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
   k_plane<<<d.n_bins, kPlaneThreads, 0, st>>>(d, kp);
   k_plane_compact<<<1, 1024, 0, st>>>(d, kp);
   n += 6;
-  const int gl = (d.cap_lm + kCylWarps - 1) / kCylWarps;
-  k_cyl_fit<<<gl < 1 ? 1 : gl, kCylWarps * 32, 0, st>>>(d, kp);
+  k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
   ++n;
   if (kp.cyl_mode == 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
   k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
@@ -989,9 +1010,6 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
   return n + 2;
 }
 
-void init_kernel_attributes() {
-  cudaFuncSetAttribute(k_cyl_hyp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(kPtCap * sizeof(float2)));
-}
+void init_kernel_attributes() {}
 
 }  // namespace sg

@@ -1,16 +1,19 @@
 // pose.cu — a9-a11: association, pose update, re-projection and map
 // association of sloam::sloam::RunSloam (sloam.cpp:453-532).
 //
-// a9  matchFeatures (sloam.cpp:257-296): one warp per current object, lanes
-//     over the map, FP64 model distances, argmin with first-index ties.
+// a9  matchFeatures (sloam.cpp:257-296): the map's axis points at the three
+//     sample heights of Cylinder::distance (cylinder.cpp:175-194) are
+//     computed once per keyframe; then one block per current object, its
+//     threads over the map, FP64 distances, argmin with first-index ties.
 // a10 pose (replacing Ceres LM, sloam.cpp:33-255): fixed gn_iters
-//     Gauss-Newton iterations with IRLS Huber weights in one 1024-thread
-//     block; residuals and Jacobians in FP32 in a frame anchored at the pose
-//     estimate's translation, J^T J / J^T r reduced with warp shuffles, the
-//     normal equations solved and the SE(3) update applied in FP64.  Joint
-//     mode: left SO(3) perturbation + translation (6x6).  Two-step mode:
-//     the reference's angle-axis 6-vector with {x, y, yaw} then
-//     {z, roll, pitch} free (3x3 each) and its angle-axis recombination.
+//     Gauss-Newton iterations with IRLS Huber weights in one block; the
+//     residual table (sensor point, anchored model) is built once, residuals
+//     and Jacobians are FP32 in a frame anchored at the pose estimate's
+//     translation, J^T J / J^T r are reduced with warp shuffles, the normal
+//     equations solved and the SE(3) update applied in FP64.  Joint mode:
+//     left SO(3) perturbation + translation (6x6).  Two-step mode: the
+//     reference's angle-axis 6-vector with {x, y, yaw} then {z, roll, pitch}
+//     free (3x3 each) and its angle-axis recombination.
 // a11 projectModels + matchModels (sloam.cpp:298-328, 438-451) and the
 //     prevGPlanes_ update.
 #include <cfloat>
@@ -21,6 +24,10 @@
 namespace sg {
 
 namespace {
+
+constexpr int kAssocThreads = 128;
+constexpr int kGN = 256;
+constexpr int kResStride = 12;
 
 __device__ __forceinline__ Pose pose_at(const double* p) {
   sloam_se3 s;
@@ -34,18 +41,20 @@ __device__ __forceinline__ void pose_store(double* p, const Pose& T) {
   for (int j = 0; j < 3; ++j) p[4 + j] = s.t[j];
 }
 
-// Cylinder::distance(model), cylinder.cpp:175-194 (self = map object).
-__device__ __forceinline__ double cyl_dist(d3 sr, d3 sd, d3 tr, d3 td) {
-  double acc = 0.0;
+// Axis points of a cylinder at z = 0, 3, 6 (Cylinder::distance's samples).
+__device__ __forceinline__ void axis_points(d3 root, d3 ray, d3* pts) {
   const double hs[3] = {0.0, 3.0, 6.0};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double st = (hs[k] - sr.z) / sd.z;
-    const d3 mp = add3(sr, scl3(st, sd));
-    const double tt = (hs[k] - tr.z) / td.z;
-    const d3 tp = add3(tr, scl3(tt, td));
-    acc += norm3(sub3(mp, tp));
+    const double t = (hs[k] - root.z) / ray.z;
+    pts[k] = add3(root, scl3(t, ray));
   }
+}
+__device__ __forceinline__ double axis_dist(const double* mp, const d3* tp) {
+  double acc = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    acc += norm3(mk3(mp[3 * k] - tp[k].x, mp[3 * k + 1] - tp[k].y, mp[3 * k + 2] - tp[k].z));
   return acc / 3.0;
 }
 
@@ -56,122 +65,83 @@ __device__ __forceinline__ void cyl_project(const Pose& T, d3& root, d3& ray) {
   ray = sub3(other, root);
 }
 
-__global__ void __launch_bounds__(256) k_assoc(Dev d, KParams kp) {
-  const int lane = threadIdx.x & 31;
-  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+// block-wide argmin (value, then index)
+__device__ __forceinline__ void block_argmin(double& v, int& i, double* sv, int* si) {
+  warp_argmin(v, i);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sv[w] = v; si[w] = i; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k)
+      if (sv[k] < sv[0] || (sv[k] == sv[0] && si[k] < si[0])) { sv[0] = sv[k]; si[0] = si[k]; }
+  }
+  __syncthreads();
+  v = sv[0];
+  i = si[0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_map_prep(Dev d) {
+  const int n = d.in->n_map;
+  const sloam_cylinder* map = d.in->map;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const sloam_cylinder& m = map[k];
+    d3 pts[3];
+    axis_points(mk3(m.root[0], m.root[1], m.root[2]), mk3(m.ray[0], m.ray[1], m.ray[2]), pts);
+    for (int j = 0; j < 3; ++j) {
+      d.map_pts[9 * k + 3 * j] = pts[j].x;
+      d.map_pts[9 * k + 3 * j + 1] = pts[j].y;
+      d.map_pts[9 * k + 3 * j + 2] = pts[j].z;
+    }
+  }
+}
+
+// argmin over the map of the distance to a (projected) current cylinder
+__device__ __forceinline__ void map_argmin(const Dev& d, d3 root, d3 ray, double init, double& bd,
+                                           int& bi, double* sv, int* si) {
+  d3 tp[3];
+  axis_points(root, ray, tp);
+  bd = init;
+  bi = 0;
+  const int n_map = d.in->n_map;
+  for (int k = threadIdx.x; k < n_map; k += blockDim.x) {
+    const double dist = axis_dist(d.map_pts + 9 * (size_t)k, tp);
+    if (dist < bd) { bd = dist; bi = k; }
+  }
+  block_argmin(bd, bi, sv, si);
+}
+
+__global__ void __launch_bounds__(kAssocThreads) k_assoc(Dev d, KParams kp) {
+  __shared__ double sv[kAssocThreads / 32];
+  __shared__ int si[kAssocThreads / 32];
   const int nc = d.cnt->n_cyl, np = d.cnt->n_planes, nprev = d.cnt->n_prev;
   const Pose T = pose_at(d.pose_io);
-  for (int it = wg; it < nc + np; it += nw) {
+  for (int it = blockIdx.x; it < nc + np; it += gridDim.x) {
+    double bd;
+    int bi;
     if (it < nc) {
       const CylD c = d.cyls[it];
       d3 root = mk3(c.root[0], c.root[1], c.root[2]), ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
       cyl_project(T, root, ray);
-      double bd = kp.tree_match_thresh + 100;
-      int bi = 0;
-      const int n_map = d.in->n_map;
-      const sloam_cylinder* map = d.in->map;
-      for (int k = lane; k < n_map; k += 32) {
-        const sloam_cylinder& m = map[k];
-        const double dist = cyl_dist(mk3(m.root[0], m.root[1], m.root[2]),
-                                     mk3(m.ray[0], m.ray[1], m.ray[2]), root, ray);
-        if (dist < bd) { bd = dist; bi = k; }
-      }
-      warp_argmin(bd, bi);
-      if (lane == 0) d.cyl_match[it] = (n_map > 0 && bd < kp.tree_match_thresh) ? bi : -1;
+      map_argmin(d, root, ray, kp.tree_match_thresh + 100, bd, bi, sv, si);
+      if (threadIdx.x == 0)
+        d.cyl_match[it] = (d.in->n_map > 0 && bd < kp.tree_match_thresh) ? bi : -1;
     } else {
       const int p = it - nc;
       const PlaneD P = d.planes[p];
       const d3 c = xform(T, mk3(P.centroid[0], P.centroid[1], P.centroid[2]));
-      double bd = kp.plane_match_thresh + 100;
-      int bi = 0;
-      for (int k = lane; k < nprev; k += 32) {
+      bd = kp.plane_match_thresh + 100;
+      bi = 0;
+      for (int k = threadIdx.x; k < nprev; k += blockDim.x) {
         const PlaneD& Q = d.prev_planes[k];
         const double dist = norm3(sub3(mk3(Q.centroid[0], Q.centroid[1], Q.centroid[2]), c));
         if (dist < bd) { bd = dist; bi = k; }
       }
-      warp_argmin(bd, bi);
-      if (lane == 0) d.plane_match[p] = (nprev > 0 && bd < kp.plane_match_thresh) ? bi : -1;
+      block_argmin(bd, bi, sv, si);
+      if (threadIdx.x == 0)
+        d.plane_match[p] = (nprev > 0 && bd < kp.plane_match_thresh) ? bi : -1;
     }
   }
-}
-
-constexpr int kGN = 1024;
-
-// block reduction of NV floats: result valid in thread 0's `out`
-template <int NV>
-__device__ __forceinline__ void block_reduce(float* acc, float (*red)[kGN / 32], double* out) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < NV; ++j) {
-    const float v = warp_sum(acc[j]);
-    if (lane == 0) red[j][w] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int j = 0; j < NV; ++j) {
-      double s = 0;
-      for (int q = 0; q < kGN / 32; ++q) s += red[j][q];
-      out[j] = s;
-    }
-  }
-}
-
-struct ResRef {
-  int kind;  // 0 none, 1 cylinder, 2 plane
-  float px, py, pz;
-  int obj;
-};
-
-__device__ __forceinline__ ResRef residual_at(const Dev& d, const KParams& kp, int i, int nc,
-                                              int np) {
-  ResRef r{0, 0, 0, 0, -1};
-  if (i < nc * kp.F) {
-    const int c = i / kp.F;
-    const int m = d.cyl_match[c];
-    if (m < 0) return r;
-    const float4 f = d.cyl_feat[(size_t)c * kp.F + (i - c * kp.F)];
-    return ResRef{1, f.x, f.y, f.z, m};
-  }
-  i -= nc * kp.F;
-  if (i < np * kp.G) {
-    const int p = i / kp.G;
-    const int m = d.plane_match[p];
-    if (m < 0) return r;
-    const float4 f = d.plane_feat[(size_t)p * kp.G + (i - p * kp.G)];
-    return ResRef{2, f.x, f.y, f.z, m};
-  }
-  return r;
-}
-
-// residual and gradient w.r.t. the transformed point lp (float)
-__device__ __forceinline__ float residual_eval(const Dev& d, const ResRef& rr, float lx, float ly,
-                                               float lz, const double* anchor, float* J) {
-  if (rr.kind == 1) {
-    const sloam_cylinder& m = d.in->map[rr.obj];
-    const float rx = (float)(m.root[0] - anchor[0]), ry = (float)(m.root[1] - anchor[1]),
-                rz = (float)(m.root[2] - anchor[2]);
-    const float ax = (float)m.ray[0], ay = (float)m.ray[1], az = (float)m.ray[2];
-    const float vx = lx - rx, vy = ly - ry, vz = lz - rz;
-    const float s = (vx * ax + vy * ay + vz * az) / (ax * ax + ay * ay + az * az);
-    const float wx = vx - s * ax, wy = vy - s * ay, wz = vz - s * az;
-    const float nw = sqrtf(wx * wx + wy * wy + wz * wz);
-    if (nw > 0.f) {
-      J[0] = wx / nw; J[1] = wy / nw; J[2] = wz / nw;
-    } else {
-      J[0] = J[1] = J[2] = 0.f;
-    }
-    return nw - (float)m.radius;
-  }
-  const PlaneD& Q = d.prev_planes[rr.obj];
-  const float nx = (float)Q.plane[0], ny = (float)Q.plane[1], nz = (float)Q.plane[2];
-  const float dd = (float)(Q.plane[3] + Q.plane[0] * anchor[0] + Q.plane[1] * anchor[1] +
-                           Q.plane[2] * anchor[2]);
-  const float num = nx * lx + ny * ly + nz * lz + dd;
-  const float nn = sqrtf(nx * nx + ny * ny + nz * nz);
-  const float sg = num > 0.f ? 1.f : (num < 0.f ? -1.f : 0.f);
-  J[0] = sg * nx / nn; J[1] = sg * ny / nn; J[2] = sg * nz / nn;
-  return fabsf(num) / nn;
 }
 
 __device__ __forceinline__ float huber_w(float r, float delta) {
@@ -226,17 +196,93 @@ __device__ void aa_mats(const double* r, double* Rm, double* Rj, double* Jr) {
   }
 }
 
+// Residual table entry i: [kind, px, py, pz, m0..m7] with kind 0 = none,
+// 1 = cylinder (root - anchor, ray, 1/ray.ray, radius), 2 = plane (n, d + n.anchor, 1/|n|).
+__device__ void build_residual(const Dev& d, const KParams& kp, int i, int nc, const double* a,
+                               float* e) {
+  e[0] = 0.f;
+  if (i < nc * kp.F) {
+    const int c = i / kp.F;
+    const int m = d.cyl_match[c];
+    if (m < 0) return;
+    const float4 f = d.cyl_feat[(size_t)c * kp.F + (i - c * kp.F)];
+    const sloam_cylinder& M = d.in->map[m];
+    e[0] = 1.f;
+    e[1] = f.x; e[2] = f.y; e[3] = f.z;
+    e[4] = (float)(M.root[0] - a[0]); e[5] = (float)(M.root[1] - a[1]);
+    e[6] = (float)(M.root[2] - a[2]);
+    e[7] = (float)M.ray[0]; e[8] = (float)M.ray[1]; e[9] = (float)M.ray[2];
+    e[10] = (float)(1.0 / (M.ray[0] * M.ray[0] + M.ray[1] * M.ray[1] + M.ray[2] * M.ray[2]));
+    e[11] = (float)M.radius;
+    return;
+  }
+  i -= nc * kp.F;
+  const int p = i / kp.G;
+  const int m = d.plane_match[p];
+  if (m < 0) return;
+  const float4 f = d.plane_feat[(size_t)p * kp.G + (i - p * kp.G)];
+  const PlaneD& Q = d.prev_planes[m];
+  e[0] = 2.f;
+  e[1] = f.x; e[2] = f.y; e[3] = f.z;
+  e[4] = (float)Q.plane[0]; e[5] = (float)Q.plane[1]; e[6] = (float)Q.plane[2];
+  e[7] = (float)(Q.plane[3] + Q.plane[0] * a[0] + Q.plane[1] * a[1] + Q.plane[2] * a[2]);
+  e[8] = (float)(1.0 / sqrt(Q.plane[0] * Q.plane[0] + Q.plane[1] * Q.plane[1] +
+                            Q.plane[2] * Q.plane[2]));
+}
+
+// residual and its gradient w.r.t. the transformed point lp (FP32)
+__device__ __forceinline__ float residual_eval(const float* e, float lx, float ly, float lz,
+                                               float* J) {
+  if (e[0] == 1.f) {
+    const float vx = lx - e[4], vy = ly - e[5], vz = lz - e[6];
+    const float s = (vx * e[7] + vy * e[8] + vz * e[9]) * e[10];
+    const float wx = vx - s * e[7], wy = vy - s * e[8], wz = vz - s * e[9];
+    const float nw = sqrtf(wx * wx + wy * wy + wz * wz);
+    if (nw > 0.f) {
+      const float inv = 1.0f / nw;
+      J[0] = wx * inv; J[1] = wy * inv; J[2] = wz * inv;
+    } else {
+      J[0] = J[1] = J[2] = 0.f;
+    }
+    return nw - e[11];
+  }
+  const float num = e[4] * lx + e[5] * ly + e[6] * lz + e[7];
+  const float sg = num > 0.f ? e[8] : (num < 0.f ? -e[8] : 0.f);
+  J[0] = sg * e[4]; J[1] = sg * e[5]; J[2] = sg * e[6];
+  return fabsf(num) * e[8];
+}
+
+// block reduction of NV floats over kGN threads into s_out (FP64)
+template <int NV>
+__device__ __forceinline__ void reduce_normal(const float* acc, float (*red)[kGN / 32],
+                                              double* s_out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    const float v = warp_sum(acc[j]);
+    if (lane == 0) red[j][w] = v;
+  }
+  __syncthreads();
+  if (w == 0 && lane < NV) {
+    double s = 0;
+#pragma unroll
+    for (int q = 0; q < kGN / 32; ++q) s += red[lane][q];
+    s_out[lane] = s;
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
   __shared__ float red[27][kGN / 32];
   __shared__ double s_out[27];
   __shared__ float sR[9], sT[3], sRj[9], sJr[9];
   __shared__ double s_R[9], s_t[3], s_x[6], s_anchor[3];
-  __shared__ int s_ok, s_checks[4];
+  __shared__ int s_ok, s_checks[2];
+  __shared__ int sm[33];
   const int nc = d.cnt->n_cyl, np = d.cnt->n_planes;
   const int nitems = nc * kp.F + np * kp.G;
   // ---- counts and gates (sloam.cpp:499-500)
   {
-    __shared__ int sm[33];
     int mc = 0, mp = 0;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) mc += d.cyl_match[c] >= 0;
     for (int p = threadIdx.x; p < np; p += blockDim.x) mp += d.plane_match[p] >= 0;
@@ -259,7 +305,6 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
       s_t[0] = s_t[1] = s_t[2] = 0.0;
       s_ok = 1;
       d.cnt->status = (np == 0 || nc == 0) ? SLOAM_ERR_NO_MODELS : SLOAM_OK;
-      // defaults: T_Map_Curr = estimate, T_Delta = identity
       for (int j = 0; j < 7; ++j) d.pose_io[7 + j] = d.pose_io[j];
       for (int j = 0; j < 7; ++j) d.pose_io[14 + j] = (j == 3) ? 1.0 : 0.0;
       d.cnt->success = 1;
@@ -267,6 +312,9 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
     __syncthreads();
   }
   if (np == 0 || nc == 0) return;
+  // ---- residual table (each thread builds and later reads its own entries)
+  for (int i = threadIdx.x; i < nitems; i += blockDim.x)
+    build_residual(d, kp, i, nc, s_anchor, d.res_tab + (size_t)kResStride * i);
   const int tchk = s_checks[0], gchk = s_checks[1];
   const float delta = (float)kp.huber;
   if (!kp.two_step) {
@@ -282,25 +330,27 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
 #pragma unroll
       for (int j = 0; j < 27; ++j) acc[j] = 0.f;
       for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
-        const ResRef rr = residual_at(d, kp, i, nc, np);
-        if (rr.kind == 0) continue;
-        const float qx = sR[0] * rr.px + sR[1] * rr.py + sR[2] * rr.pz;
-        const float qy = sR[3] * rr.px + sR[4] * rr.py + sR[5] * rr.pz;
-        const float qz = sR[6] * rr.px + sR[7] * rr.py + sR[8] * rr.pz;
+        const float* e = d.res_tab + (size_t)kResStride * i;
+        if (e[0] == 0.f) continue;
+        const float px = e[1], py = e[2], pz = e[3];
+        const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
+        const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
+        const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
         float Jl[3];
-        const float res = residual_eval(d, rr, qx + sT[0], qy + sT[1], qz + sT[2], s_anchor, Jl);
+        const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
         const float J[6] = {qy * Jl[2] - qz * Jl[1], qz * Jl[0] - qx * Jl[2],
                             qx * Jl[1] - qy * Jl[0], Jl[0], Jl[1], Jl[2]};
         const float wgt = huber_w(res, delta);
         int k = 0;
 #pragma unroll
-        for (int a = 0; a < 6; ++a)
+        for (int a = 0; a < 6; ++a) {
+          const float wa = wgt * J[a];
 #pragma unroll
-          for (int b = a; b < 6; ++b) acc[k++] += wgt * J[a] * J[b];
-#pragma unroll
-        for (int a = 0; a < 6; ++a) acc[21 + a] += wgt * J[a] * res;
+          for (int b = a; b < 6; ++b) acc[k++] += wa * J[b];
+          acc[21 + a] += wa * res;
+        }
       }
-      block_reduce<27>(acc, red, s_out);
+      reduce_normal<27>(acc, red, s_out);
       if (threadIdx.x == 0) {
         double Hm[36], g[6], x[6];
         int k = 0;
@@ -371,21 +421,23 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
       float acc[9];
 #pragma unroll
       for (int j = 0; j < 9; ++j) acc[j] = 0.f;
-      for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const ResRef rr = residual_at(d, kp, i, nc, np);
-        if (rr.kind == 0) continue;
-        const float qx = sR[0] * rr.px + sR[1] * rr.py + sR[2] * rr.pz;
-        const float qy = sR[3] * rr.px + sR[4] * rr.py + sR[5] * rr.pz;
-        const float qz = sR[6] * rr.px + sR[7] * rr.py + sR[8] * rr.pz;
+      // residuals i == threadIdx.x (mod kGN): the entries this thread built
+      for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
+        if (i < lo || i >= hi) continue;
+        const float* e = d.res_tab + (size_t)kResStride * i;
+        if (e[0] == 0.f) continue;
+        const float px = e[1], py = e[2], pz = e[3];
+        const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
+        const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
+        const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
         float Jl[3];
-        const float res = residual_eval(d, rr, qx + sT[0], qy + sT[1], qz + sT[2], s_anchor, Jl);
+        const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
         // d lp / d r_k = -Rj (p x Jr[:,k])
         float Jfull[6] = {Jl[0], Jl[1], Jl[2], 0.f, 0.f, 0.f};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const float vx = sJr[k], vy = sJr[3 + k], vz = sJr[6 + k];
-          const float cx = rr.py * vz - rr.pz * vy, cy = rr.pz * vx - rr.px * vz,
-                      cz = rr.px * vy - rr.py * vx;
+          const float cx = py * vz - pz * vy, cy = pz * vx - px * vz, cz = px * vy - py * vx;
           const float mx = -(sRj[0] * cx + sRj[1] * cy + sRj[2] * cz);
           const float my = -(sRj[3] * cx + sRj[4] * cy + sRj[5] * cz);
           const float mz = -(sRj[6] * cx + sRj[7] * cy + sRj[8] * cz);
@@ -397,7 +449,7 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
         acc[3] += wgt * J[1] * J[1]; acc[4] += wgt * J[1] * J[2]; acc[5] += wgt * J[2] * J[2];
         acc[6] += wgt * J[0] * res; acc[7] += wgt * J[1] * res; acc[8] += wgt * J[2] * res;
       }
-      block_reduce<9>(acc, red, s_out);
+      reduce_normal<9>(acc, red, s_out);
       if (threadIdx.x == 0) {
         const double Hm[9] = {s_out[0], s_out[1], s_out[2], s_out[1], s_out[3],
                               s_out[4], s_out[2], s_out[4], s_out[5]};
@@ -434,8 +486,11 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
 }
 
 // projectModels + matchModels + prevGPlanes_ (first scan: projection by the
-// estimate, no matching).
-__global__ void __launch_bounds__(256) k_finalize(Dev d, KParams kp, int first, int update) {
+// estimate, no matching).  One block per cylinder.
+__global__ void __launch_bounds__(kAssocThreads) k_finalize(Dev d, KParams kp, int first,
+                                                            int update) {
+  __shared__ double sv[kAssocThreads / 32];
+  __shared__ int si[kAssocThreads / 32];
   const int nc = d.cnt->n_cyl, np = d.cnt->n_planes;
   if (first) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -450,10 +505,6 @@ __global__ void __launch_bounds__(256) k_finalize(Dev d, KParams kp, int first, 
     return;
   }
   const Pose T = pose_at(d.pose_io + (first ? 0 : 7));
-  const int lane = threadIdx.x & 31;
-  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  // planes: project and become the next scan's prevGPlanes_ (block 0)
   if (blockIdx.x == 0) {
     for (int p = threadIdx.x; p < np; p += blockDim.x) {
       PlaneD P = d.planes[p];
@@ -467,26 +518,18 @@ __global__ void __launch_bounds__(256) k_finalize(Dev d, KParams kp, int first, 
     }
     if (threadIdx.x == 0 && update) d.cnt->n_prev = np;
   }
-  for (int c = wg; c < nc; c += nw) {
+  for (int c = blockIdx.x; c < nc; c += gridDim.x) {
     CylD C = d.cyls[c];
     d3 root = mk3(C.root[0], C.root[1], C.root[2]), ray = mk3(C.ray[0], C.ray[1], C.ray[2]);
     cyl_project(T, root, ray);
     int out = -1;
     if (!first) {
-      double bd = kp.tree_match_thresh + 100;
-      int bi = 0;
-      const int n_map = d.in->n_map;
-      const sloam_cylinder* map = d.in->map;
-      for (int k = lane; k < n_map; k += 32) {
-        const sloam_cylinder& m = map[k];
-        const double dist = cyl_dist(mk3(m.root[0], m.root[1], m.root[2]),
-                                     mk3(m.ray[0], m.ray[1], m.ray[2]), root, ray);
-        if (dist < bd) { bd = dist; bi = k; }
-      }
-      warp_argmin(bd, bi);
-      out = (n_map > 0 && bd < kp.add_new_tree_thresh) ? bi : -1;
+      double bd;
+      int bi;
+      map_argmin(d, root, ray, kp.tree_match_thresh + 100, bd, bi, sv, si);
+      out = (d.in->n_map > 0 && bd < kp.add_new_tree_thresh) ? bi : -1;
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
       C.root[0] = root.x; C.root[1] = root.y; C.root[2] = root.z;
       C.ray[0] = ray.x; C.ray[1] = ray.y; C.ray[2] = ray.z;
       d.cyls[c] = C;
@@ -499,13 +542,14 @@ __global__ void __launch_bounds__(256) k_finalize(Dev d, KParams kp, int first, 
 
 int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update, cudaStream_t st) {
   if (first_scan) {
-    k_finalize<<<64, 256, 0, st>>>(d, kp, 1, update ? 1 : 0);
+    k_finalize<<<64, kAssocThreads, 0, st>>>(d, kp, 1, update ? 1 : 0);
     return 1;
   }
-  k_assoc<<<152, 256, 0, st>>>(d, kp);
+  k_map_prep<<<16, 256, 0, st>>>(d);
+  k_assoc<<<96, kAssocThreads, 0, st>>>(d, kp);
   k_gn<<<1, kGN, 0, st>>>(d, kp);
-  k_finalize<<<64, 256, 0, st>>>(d, kp, 0, update ? 1 : 0);
-  return 3;
+  k_finalize<<<64, kAssocThreads, 0, st>>>(d, kp, 0, update ? 1 : 0);
+  return 4;
 }
 
 }  // namespace sg

@@ -518,11 +518,13 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   k_cc_rank<<<g1k, 1024, 0, st>>>(d);
   k_cc_label<<<g256, 256, 0, st>>>(d);
   k_cands<<<1, 1024, 0, st>>>(d, kp.min_cluster);
-  const int gw = 152 * 8;  // warps-per-item kernels: grid-stride over items
+  // warp-per-item kernels stride over the (candidate, row) items: one wave
+  // of 1216 warps on the 152 SMs, leaving room for concurrent keyframes
+  const int gw = 152;
   k_rows<0><<<gw, 256, 0, st>>>(d);
   k_rowscan<<<1, 1024, 0, st>>>(d);
   k_rows<1><<<gw, 256, 0, st>>>(d);
-  k_vertex<<<gw, kVtxWarps * 32, 0, st>>>(d, kp);
+  k_vertex<<<2 * gw, kVtxWarps * 32, 0, st>>>(d, kp);
   // scratch for the landmark offsets lives in the (now unused) rank array
   int32_t* cand_np = reinterpret_cast<int32_t*>(d.rank);
   int32_t* cand_ncl = cand_np + d.cap_cand;
@@ -530,7 +532,7 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   int32_t* cand_pb = cand_vb + d.cap_cand;
   k_lm_count<<<(d.cap_cand + 255) / 256, 256, 0, st>>>(d, kp, cand_np, cand_ncl);
   k_lm_scan<<<1, 1024, 0, st>>>(d, cand_np, cand_ncl, cand_vb, cand_pb);
-  k_lm_write<<<gw, 256, 0, st>>>(d, cand_vb, cand_pb);
+  k_lm_write<<<32, 256, 0, st>>>(d, cand_vb, cand_pb);
   k_lm_copy<<<gw, 256, 0, st>>>(d);
   return 14;
 }
