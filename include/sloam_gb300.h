@@ -301,6 +301,28 @@ int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t n
                          const sloam_cylinder* map, int32_t n_map, double* pose_out,
                          int32_t* success_out, int32_t* ncyl_out);
 
+/* Projection + masking that allocates nothing (no reference counterpart: it
+ * exists for callers that cannot call cudaMalloc, such as plugins inside a
+ * process whose allocator owns the GPU or real-time loops that forbid
+ * allocation after start-up).  The same kernels as sloam_project_mask;
+ * every intermediate buffer lives in a file-scope __device__ array of about
+ * 4.2 MB that each GPU loading the library holds until exit, sized for at
+ * most 131072 points (H*W) and width 4096 - larger scans are rejected with
+ * SLOAM_ERR_CAPACITY.  All data pointers are device pointers: d_xyzi [n*4],
+ * d_point_labels [n] or d_mask_image [H*W], and the outputs d_ground_idx
+ * [n], d_n_ground [1], d_tree_cloud [H*W*4] and, optionally (NULL skips),
+ * d_pix [n] (py*W + px), d_range_image [H*W], d_mask_out [H*W].  `stream`
+ * is a cudaStream_t (NULL = legacy default stream); results are ready when
+ * the stream reaches them.  The first call on a device looks up the array's
+ * address (make it before any stream capture).  All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race.
+ * Host code must treat the array only through this entry point. */
+int sloam_project_mask_noalloc(const sloam_params* params, const float* d_xyzi, int32_t n,
+                               const uint8_t* d_point_labels, const uint8_t* d_mask_image,
+                               int32_t* d_pix, float* d_range_image, uint8_t* d_mask_out,
+                               int32_t* d_ground_idx, int32_t* d_n_ground,
+                               float* d_tree_cloud, void* stream);
+
 /* Returns the number of kernels launched by the last call (for accounting). */
 int64_t sloam_last_launch_count(const sloam_ctx* ctx);
 

@@ -63,6 +63,8 @@ def load(path=LIB_PATH):
                                          vp, C.c_int32, vp, vp, vp]
     L.sloam_keyframes_host.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.POINTER(A.SE3),
                                        C.POINTER(A.Cylinder), C.c_int32, vp, vp, vp]
+    L.sloam_project_mask_noalloc.argtypes = [C.POINTER(A.Params), vp, C.c_int32, vp, vp, vp, vp,
+                                             vp, vp, vp, vp, vp]
     L.sloam_last_launch_count.argtypes = [vp]
     L.sloam_last_launch_count.restype = C.c_int64
     L.sloam_stream.argtypes = [vp]
