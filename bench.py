@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--slots", type=int, default=16,
+                    help="keyframes in flight at once (context batch slots)")
     return ap.parse_args()
 
 
@@ -235,6 +237,7 @@ def main():
     torch.cuda.set_device(dev)
 
     cfg, forest, kfs, P = workload(args.seed + rank, args.distinct)
+    P.batch_slots = args.slots
     ctx = Context(P, device=local)
     mapa = forest.map_cylinders()
     mapc = A.cylinders_from_array(mapa)

@@ -174,11 +174,15 @@ SLOAM_HD void matmul3(const double* A, const double* B, double* C) {
   for (int k = 0; k < 9; ++k) C[k] = T[k];
 }
 SLOAM_HD void so3_exp(d3 w, double* R) {
-  double th2 = dot3(w, w), th = sqrt(th2);
+  const double th2 = dot3(w, w);
   double A, B;
-  if (th2 < 1e-24) {
-    A = 1.0; B = 0.5;
+  if (th2 < 1e-2) {
+    // sin(t)/t and (1-cos(t))/t^2 by their Taylor series (truncation
+    // < 3e-14 relative for t < 0.1): no FP64 transcendental on the GN path
+    A = 1.0 - th2 / 6.0 * (1.0 - th2 / 20.0 * (1.0 - th2 / 42.0));
+    B = 0.5 - th2 / 24.0 * (1.0 - th2 / 30.0 * (1.0 - th2 / 56.0));
   } else {
+    const double th = sqrt(th2);
     A = sin(th) / th;
     B = (1.0 - cos(th)) / th2;
   }
@@ -187,85 +191,97 @@ SLOAM_HD void so3_exp(d3 w, double* R) {
   for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0 ? 1.0 : 0.0) + A * K[i] + B * K2[i];
 }
 
-// Symmetric 3x3 eigen-decomposition, cyclic Jacobi (FP64); eigenvalues
-// ascending, eigenvectors as columns of V.
-SLOAM_HD void jacobi3(const double* A_in, double* evals, double* V) {
-  double A[9];
-  for (int i = 0; i < 9; ++i) A[i] = A_in[i];
-  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 32; ++sweep) {
-    double off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
-    double diag = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
-    if (off <= 1e-300 || off <= diag * 1e-32) break;
-    for (int p = 0; p < 2; ++p) {
-      for (int q = p + 1; q < 3; ++q) {
-        double apq = A[3 * p + q];
-        if (apq == 0.0) continue;
-        double app = A[3 * p + p], aqq = A[3 * q + q];
-        double theta = (aqq - app) / (2.0 * apq);
-        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < 3; ++k) {
-          double akp = A[3 * k + p], akq = A[3 * k + q];
-          A[3 * k + p] = c * akp - s * akq;
-          A[3 * k + q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < 3; ++k) {
-          double apk = A[3 * p + k], aqk = A[3 * q + k];
-          A[3 * p + k] = c * apk - s * aqk;
-          A[3 * q + k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < 3; ++k) {
-          double vkp = V[3 * k + p], vkq = V[3 * k + q];
-          V[3 * k + p] = c * vkp - s * vkq;
-          V[3 * k + q] = s * vkp + c * vkq;
-        }
-      }
-    }
-  }
-  double d[3] = {A[0], A[4], A[8]};
-  int o0 = 0, o1 = 1, o2 = 2, tmp;
-  if (d[o1] < d[o0]) { tmp = o0; o0 = o1; o1 = tmp; }
-  if (d[o2] < d[o1]) { tmp = o1; o1 = o2; o2 = tmp; }
-  if (d[o1] < d[o0]) { tmp = o0; o0 = o1; o1 = tmp; }
-  int ord[3] = {o0, o1, o2};
-  double Vs[9];
-  for (int c = 0; c < 3; ++c) {
-    evals[c] = d[ord[c]];
-    for (int r = 0; r < 3; ++r) Vs[3 * r + c] = V[3 * r + ord[c]];
-  }
-  for (int i = 0; i < 9; ++i) V[i] = Vs[i];
-}
-
-// Cholesky solve of an n x n SPD system (n <= 6, row-major).
+// Cholesky solve of an n x n SPD system (n <= 6, row-major), FP64.  One
+// reciprocal square root per pivot; everything else multiplies (the FP64
+// divide and square root are long dependent sequences on this part).
 SLOAM_HD bool chol_solve(int n, const double* H, const double* b, double* x) {
-  double L[36];
-  for (int i = 0; i < n; ++i) {
-    for (int j = 0; j <= i; ++j) {
-      double s = H[i * n + j];
-      for (int k = 0; k < j; ++k) s -= L[i * n + k] * L[j * n + k];
-      if (i == j) {
-        if (!(s > 0.0)) return false;
-        L[i * n + i] = sqrt(s);
-      } else {
-        L[i * n + j] = s / L[j * n + j];
-      }
+  double L[36], inv[6];
+  for (int j = 0; j < n; ++j) {
+    double s = H[j * n + j];
+    for (int k = 0; k < j; ++k) s -= L[j * n + k] * L[j * n + k];
+    if (!(s > 0.0)) return false;
+#ifdef __CUDA_ARCH__
+    inv[j] = rsqrt(s);
+#else
+    inv[j] = 1.0 / sqrt(s);
+#endif
+    L[j * n + j] = s * inv[j];
+    for (int i = j + 1; i < n; ++i) {
+      double t = H[i * n + j];
+      for (int k = 0; k < j; ++k) t -= L[i * n + k] * L[j * n + k];
+      L[i * n + j] = t * inv[j];
     }
   }
   double y[6];
   for (int i = 0; i < n; ++i) {
     double s = b[i];
     for (int k = 0; k < i; ++k) s -= L[i * n + k] * y[k];
-    y[i] = s / L[i * n + i];
+    y[i] = s * inv[i];
   }
   for (int i = n - 1; i >= 0; --i) {
     double s = y[i];
     for (int k = i + 1; k < n; ++k) s -= L[k * n + i] * x[k];
-    x[i] = s / L[i * n + i];
+    x[i] = s * inv[i];
   }
   for (int i = 0; i < n; ++i)
     if (!isfinite(x[i])) return false;
   return true;
+}
+
+// Symmetric 3x3 eigen-decomposition, cyclic Jacobi in FP32 (the plane
+// normals and line directions: well-separated spectra, ~1e-7 rad accurate).
+// Eigenvalues ascending; eigenvectors as columns of V.
+SLOAM_D void jacobi3f(const float* A_in, float* evals, float* V) {
+  float A[9];
+  for (int i = 0; i < 9; ++i) A[i] = A_in[i];
+  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+  for (int sweep = 0; sweep < 16; ++sweep) {
+    const float off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+    const float diag = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
+    if (off <= 1e-36f || off <= diag * 1e-16f) break;
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+#pragma unroll
+      for (int q = p + 1; q < 3; ++q) {
+        const float apq = A[3 * p + q];
+        if (apq == 0.0f) continue;
+        const float app = A[3 * p + p], aqq = A[3 * q + q];
+        const float theta = (aqq - app) / (2.0f * apq);
+        const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+        const float c = rsqrtf(t * t + 1.0f), s = t * c;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float akp = A[3 * k + p], akq = A[3 * k + q];
+          A[3 * k + p] = c * akp - s * akq;
+          A[3 * k + q] = s * akp + c * akq;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float apk = A[3 * p + k], aqk = A[3 * q + k];
+          A[3 * p + k] = c * apk - s * aqk;
+          A[3 * q + k] = s * apk + c * aqk;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float vkp = V[3 * k + p], vkq = V[3 * k + q];
+          V[3 * k + p] = c * vkp - s * vkq;
+          V[3 * k + q] = s * vkp + c * vkq;
+        }
+      }
+    }
+  }
+  float d[3] = {A[0], A[4], A[8]};
+  int o0 = 0, o1 = 1, o2 = 2, tmp;
+  if (d[o1] < d[o0]) { tmp = o0; o0 = o1; o1 = tmp; }
+  if (d[o2] < d[o1]) { tmp = o1; o1 = o2; o2 = tmp; }
+  if (d[o1] < d[o0]) { tmp = o0; o0 = o1; o1 = tmp; }
+  const int ord[3] = {o0, o1, o2};
+  float Vs[9];
+  for (int c = 0; c < 3; ++c) {
+    evals[c] = d[ord[c]];
+    for (int r = 0; r < 3; ++r) Vs[3 * r + c] = V[3 * r + ord[c]];
+  }
+  for (int i = 0; i < 9; ++i) V[i] = Vs[i];
 }
 
 }  // namespace sg

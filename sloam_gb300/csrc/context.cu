@@ -318,6 +318,8 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.map_pts = c.take<double>((size_t)d.cap_map * 9);
   d.res_tab = c.take<float>(((size_t)d.cap_lm * d.F + (size_t)d.n_bins * d.G) * 12);
   d.lm_uv = c.take<float2>((size_t)d.cap_cluster + d.cap_p);  // cluster | vertex points
+  d.hyp = c.take<float4>((size_t)d.cap_lm * std::max(d.K, 1));
+  d.hyp_cnt = c.take<int32_t>((size_t)d.cap_lm * std::max(d.K, 1));
   d.pose_io = c.take<double>(32);
   d.cnt = c.take<Counters>(1);
 }
@@ -1112,8 +1114,8 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  // the hypothesis kernel scores trees still at the vertex-line stage
-  if (which == 1) launch_cyl_fit_kernel(d, ctx->kp, ctx->st);
+  // the inlier-counting kernel scores trees still at the vertex-line stage
+  if (which == 1) launch_cyl_count_prep(d, ctx->kp, ctx->st);
   CK(cudaEventRecord(a, ctx->st));
   for (int r = 0; r < reps; ++r) {
     if (which == 0) launch_project_kernel(d, ctx->kp, ctx->st);

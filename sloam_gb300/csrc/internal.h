@@ -141,7 +141,9 @@ struct Dev {
   int32_t* match_out;   // [cap_lm] matchModels result
   double* map_pts;      // [cap_map*9] map axis points at z = 0, 3, 6
   float* res_tab;       // [(cap_lm*F + n_bins*G) * 12] residual table of the pose solve
-  float2* lm_uv;        // [cap_cluster] tree points projected on the prior axis frame
+  float2* lm_uv;        // [cap_cluster + cap_p] tree points on the prior axis frame
+  float4* hyp;          // [cap_lm * K] circle hypotheses (cu, cv, lo2, hi2)
+  int32_t* hyp_cnt;     // [cap_lm * K] inlier counts
   double* pose_io;      // [16] in: estimate (q xyzw, t); out: T_Map_Curr, T_Delta
   Counters* cnt;
 };
@@ -188,6 +190,7 @@ int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_resolve_kernel(const Dev& d, bool point_labels, cudaStream_t st);
 int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
+int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st);
 
 // per-call counter reset: counts >= 0 are set, -1 left to the pipeline
 int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster,

@@ -313,9 +313,10 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[j * 32 + q];
         S6[j] = t;
       }
-      const double S[9] = {S6[0], S6[1], S6[2], S6[1], S6[3], S6[4], S6[2], S6[4], S6[5]};
-      double ev[3], V[9];
-      jacobi3(S, ev, V);
+      const float S[9] = {(float)S6[0], (float)S6[1], (float)S6[2], (float)S6[1], (float)S6[3],
+                          (float)S6[4], (float)S6[2], (float)S6[4], (float)S6[5]};
+      float ev[3], V[9];
+      jacobi3f(S, ev, V);
       d3 nrm = mk3(V[0], V[3], V[6]);
       const bool flip = nrm.z < 0 || (nrm.z == 0 && (nrm.y < 0 || (nrm.y == 0 && nrm.x < 0)));
       if (flip) nrm = scl3(-1.0, nrm);
@@ -370,25 +371,40 @@ __device__ __forceinline__ float euclid2d_f(float ax, float ay, float bx, float 
   return fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
 }
 
-// PCL line refit direction with pcl::computeCorrespondingEigenVector's sign.
-__device__ d3 pcl_line_direction(const double* S) {
-  double ev[3], V[9];
-  jacobi3(S, ev, V);
-  const double lam = ev[2];
-  double scale = 0;
-  for (int k = 0; k < 9; ++k) scale = fmax(scale, fabs(S[k]));
-  if (scale <= DBL_MIN) scale = 1.0;
-  double M[9];
-  for (int k = 0; k < 9; ++k) M[k] = S[k] / scale;
-  M[0] -= lam / scale; M[4] -= lam / scale; M[8] -= lam / scale;
-  const d3 r0 = mk3(M[0], M[1], M[2]), r1 = mk3(M[3], M[4], M[5]), r2 = mk3(M[6], M[7], M[8]);
-  const d3 c1 = cross3(r0, r1), c2 = cross3(r0, r2), c3 = cross3(r1, r2);
-  const double l1 = dot3(c1, c1), l2 = dot3(c2, c2), l3 = dot3(c3, c3);
-  d3 v;
-  if (l1 >= l2 && l1 >= l3) v = scl3(1.0 / sqrt(l1), c1);
-  else if (l2 >= l1 && l2 >= l3) v = scl3(1.0 / sqrt(l2), c2);
-  else v = scl3(1.0 / sqrt(l3), c3);
-  if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z))) v = mk3(V[2], V[5], V[8]);
+// PCL line refit direction with pcl::computeCorrespondingEigenVector's sign
+// (the largest cross product of the rows of S - lambda_max I), FP32.
+__device__ d3 pcl_line_direction(const double* Sd) {
+  float S[9], ev[3], V[9];
+  for (int k = 0; k < 9; ++k) S[k] = (float)Sd[k];
+  jacobi3f(S, ev, V);
+  const float lam = ev[2];
+  float scale = 0.f;
+  for (int k = 0; k < 9; ++k) scale = fmaxf(scale, fabsf(S[k]));
+  if (scale <= FLT_MIN) scale = 1.0f;
+  const float is = 1.0f / scale;
+  float M[9];
+  for (int k = 0; k < 9; ++k) M[k] = S[k] * is;
+  M[0] -= lam * is; M[4] -= lam * is; M[8] -= lam * is;
+  auto crs = [](const float* a, const float* b, float* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  float c1[3], c2[3], c3[3];
+  crs(M, M + 3, c1);
+  crs(M, M + 6, c2);
+  crs(M + 3, M + 6, c3);
+  const float l1 = c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2];
+  const float l2 = c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2];
+  const float l3 = c3[0] * c3[0] + c3[1] * c3[1] + c3[2] * c3[2];
+  const float* c;
+  float l;
+  if (l1 >= l2 && l1 >= l3) { c = c1; l = l1; }
+  else if (l2 >= l1 && l2 >= l3) { c = c2; l = l2; }
+  else { c = c3; l = l3; }
+  const float r = rsqrtf(l);
+  d3 v = mk3(c[0] * r, c[1] * r, c[2] * r);
+  if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && l > 0.f)) v = mk3(V[2], V[5], V[8]);
   return v;
 }
 
@@ -631,8 +647,6 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
 }
 
 // ---------------------------------------------- point-level cylinder fit
-constexpr int kHypThreads = 128;
-constexpr int kStage = 2048;  // projected points staged in shared memory per block
 
 struct CylFrame {
   float ox, oy, oz;
@@ -737,50 +751,121 @@ __device__ __forceinline__ Hyp make_hyp(const KParams& kp, int h, int tree_id, i
   return H;
 }
 
-__device__ __forceinline__ int band_count(const float2* q, int n, const Hyp& H) {
-  int cnt = 0;
-#pragma unroll 4
-  for (int i = 0; i < n; ++i) {
-    const float2 p = q[i];
-    const float du = fsub(p.x, H.cu), dv = fsub(p.y, H.cv);
-    const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-    cnt += (d2 > H.lo2) & (d2 < H.hi2);
+// Hypothesis table: one thread per (tree, hypothesis); clears the counts.
+// An invalid hypothesis gets hi2 = -1 (no point can be an inlier).
+__global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp) {
+  const int nl = d.cnt->n_lm, K = kp.K;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * K;
+       it += gridDim.x * blockDim.x) {
+    const int l = it / K, h = it - l * K;
+    d.hyp_cnt[it] = 0;
+    float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
+    const CylD c = d.cyl_all[l];
+    if (fit_eligible(c)) {
+      const float4* pts;
+      const float2* uv;
+      int n;
+      tree_points(d, l, &pts, &n, &uv);
+      if (n >= 3) {
+        const Hyp H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return uv[i]; });
+        if (H.ok) e = make_float4(H.cu, H.cv, H.lo2, H.hi2);
+      }
+    }
+    d.hyp[it] = e;
   }
-  return cnt;
 }
 
-// Blocks of kHypThreads: one hypothesis per thread; the tree's first kStage
-// projected points staged in shared memory (broadcast reads), the rest read
-// through L1.  Best = most inliers, lowest hypothesis on ties (64-bit max).
-__global__ void __launch_bounds__(kHypThreads) k_cyl_hyp(Dev d, KParams kp) {
-  __shared__ float2 suv[kStage];
-  const int nl = d.cnt->n_lm;
-  const int chunks = (kp.K + kHypThreads - 1) / kHypThreads;
-  for (int item = blockIdx.x; item < nl * chunks; item += gridDim.x) {
-    const int l = item / chunks, ch = item - l * chunks;
-    const CylD c = d.cyl_all[l];
-    if (!fit_eligible(c)) continue;
-    const float4* pts;
-    const float2* uv;
-    int n;
-    tree_points(d, l, &pts, &n, &uv);
-    if (n < 3) continue;
-    const int ns = min(n, kStage);
-    for (int i = threadIdx.x; i < ns; i += blockDim.x) suv[i] = uv[i];
-    __syncthreads();
-    const int h = ch * kHypThreads + threadIdx.x;
-    if (h < kp.K) {
-      const Hyp H =
-          make_hyp(kp, h, c.id, n, [&](uint32_t i) { return i < (uint32_t)ns ? suv[i] : uv[i]; });
-      if (H.ok) {
-        int cnt = band_count(suv, ns, H);
-        if (n > ns) cnt += band_count(uv + ns, n - ns, H);
-        if (cnt > 0) {
+constexpr int kCountThreads = 256;
+constexpr int kHypTile = 256;  // hypotheses staged per pass (8 per lane)
+
+// Inlier counting.  The trees' projected points form one flat array (the
+// clusters back to back); blocks take 256-point chunks, one point per lane.
+// For every hypothesis of the point's tree the warp votes (ballot) and the
+// popcount lands in the register of the lane that owns the hypothesis
+// (lane = h % 32); per-block totals go to the (tree, hypothesis) counter.
+// A chunk that straddles trees runs once per tree.
+__global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, KParams kp) {
+  __shared__ float4 sh[kHypTile];
+  __shared__ int sred[kCountThreads / 32][kHypTile];
+  const int nl = d.cnt->n_lm, K = kp.K;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool clusters = d.cnt->n_cluster > 0;
+  const int total = clusters ? d.cnt->n_cluster : d.cnt->n_p;
+  const float2* uvbase = clusters ? d.lm_uv : d.lm_uv + d.cap_cluster;
+  auto seg = [&](int l) { return clusters ? d.lm_cbeg[l] : d.lm_pbeg[d.lm_vbeg[l]]; };
+  for (int q0 = blockIdx.x * kCountThreads; q0 < total; q0 += gridDim.x * kCountThreads) {
+    // first tree whose segment holds q0
+    int lo = 0, hi = nl - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (seg(mid) <= q0) lo = mid;
+      else hi = mid - 1;
+    }
+    for (int l = lo; l < nl && seg(l) < q0 + kCountThreads; ++l) {
+      const int s0 = max(q0, seg(l)), s1 = min(q0 + kCountThreads, seg(l + 1));
+      if (s1 <= s0 || !fit_eligible(d.cyl_all[l])) continue;
+      const int q = q0 + threadIdx.x;
+      const bool mine = q >= s0 && q < s1;
+      float2 p = make_float2(0.f, 0.f);
+      if (mine) p = uvbase[q];
+      for (int t0 = 0; t0 < K; t0 += kHypTile) {
+        const int nt = min(kHypTile, K - t0);
+        for (int i = threadIdx.x; i < kHypTile; i += blockDim.x)
+          sh[i] = i < nt ? d.hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
+        __syncthreads();
+        int acc[kHypTile / 32];
+#pragma unroll
+        for (int hb = 0; hb < kHypTile / 32; ++hb) {
+          acc[hb] = 0;
+#pragma unroll 8
+          for (int j = 0; j < 32; ++j) {
+            const float4 e = sh[hb * 32 + j];
+            const float du = fsub(p.x, e.x), dv = fsub(p.y, e.y);
+            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+            const unsigned b = __ballot_sync(0xffffffffu, mine && (d2 > e.z) && (d2 < e.w));
+            if (lane == j) acc[hb] += __popc(b);
+          }
+        }
+#pragma unroll
+        for (int hb = 0; hb < kHypTile / 32; ++hb) sred[w][hb * 32 + lane] = acc[hb];
+        __syncthreads();
+        for (int h = threadIdx.x; h < nt; h += blockDim.x) {
+          int s = 0;
+#pragma unroll
+          for (int k = 0; k < kCountThreads / 32; ++k) s += sred[k][h];
+          if (s) atomicAdd(d.hyp_cnt + (size_t)l * K + t0 + h, s);
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// Best hypothesis per tree: most inliers, lowest hypothesis on ties.
+__global__ void __launch_bounds__(256) k_cyl_best(Dev d, KParams kp) {
+  __shared__ unsigned long long sk[8];
+  const int nl = d.cnt->n_lm, K = kp.K;
+  for (int l = blockIdx.x; l < nl; l += gridDim.x) {
+    unsigned long long best = 0ull;
+    if (fit_eligible(d.cyl_all[l])) {
+      for (int h = threadIdx.x; h < K; h += blockDim.x) {
+        const int c = d.hyp_cnt[(size_t)l * K + h];
+        if (c > 0) {
           const unsigned long long key =
-              ((unsigned long long)cnt << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
-          atomicMax(d.cyl_best + l, key);
+              ((unsigned long long)c << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
+          best = key > best ? key : best;
         }
       }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+      best = x > best ? x : best;
+    }
+    if ((threadIdx.x & 31) == 0) sk[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 1; k < (int)(blockDim.x >> 5); ++k) best = sk[k] > best ? sk[k] : best;
+      d.cyl_best[l] = best;
     }
     __syncthreads();
   }
@@ -980,16 +1065,29 @@ int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
   return 1;
 }
 
+constexpr int kCountBlocks = 304;
+
+// The inlier-counting kernel alone (its inputs prepared by
+// launch_cyl_count_prep); counts accumulate, so a repeated launch is for
+// timing only.
+int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st) {
+  k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
+  k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
+  k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp);
+  return 3;
+}
 int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
-  k_cyl_hyp<<<304, kHypThreads, 0, st>>>(d, kp);
+  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, kp);
   return 1;
 }
 
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream_t st) {
   k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
-  k_cyl_hyp<<<304, kHypThreads, 0, st>>>(d, kp);
+  k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp);
+  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, kp);
+  k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, kp);
   k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
-  return 3;
+  return 5;
 }
 
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
