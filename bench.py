@@ -8,8 +8,14 @@ Trellis, ground planes, the point-level cylinder RANSAC (256 hypotheses per
 tree, 3 cm inlier band, 3 LS iterations), association against a 400-landmark
 submap and 10 Gauss-Newton pose iterations (FP32 residuals, FP64 6x6 solve).
 Inputs are device-resident for `value`; `e2e` runs the same keyframes through
-the host C ABI (sloam_keyframe) with host buffers.  L2 is flushed (256 MB
-write) before every timed step.
+the host C ABI (sloam_keyframes_host) from pinned host buffers.  L2 is flushed
+(256 MB write) before every timed step.
+
+`roofline` is the batch projection stage (k_project, k_resolve, k_mask,
+k_label, k_ground_compact over 8 keyframes per launch), timed with CUDA
+events on its stream inside the timed steps: 26 algorithmic bytes per point
+(16 B XYZI + 1 B label read, 4 B pixel index + 4 B range + 1 B mask
+written).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -30,11 +36,19 @@ import time
 
 import numpy as np
 
+# Up to 32 hardware work queues instead of 8, so that the keyframe slots'
+# streams do not alias onto shared queues (read when CUDA initialises).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "keyframes/s at 64x2048 (plain GPU RANSAC path, 150 trees, 400-landmark submap)"
 UNIT = "keyframes/s"
+# DRAM bytes (read + write) per keyframe of the batch projection stage, summed
+# over its four kernels in one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum); None until captured.
+FRONT_TRAFFIC_PER_KF = None
 
 
 def parse():
@@ -48,7 +62,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--slots", type=int, default=16,
+    ap.add_argument("--slots", type=int, default=32,
                     help="keyframes in flight at once (context batch slots)")
     return ap.parse_args()
 
@@ -277,15 +291,25 @@ def main():
         tdist.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    fe_ms, fe_launches, fe_kf = 0.0, 0, 0
+    host_s = 0.0  # host time to enqueue a step (the call returns before the GPU is done)
     for s in range(args.steps):
         flush.fill_(float(s))
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(ext)
+        h0 = time.perf_counter()
         launches += step()
+        host_s += time.perf_counter() - h0
         e1.record(ext)
         evs.append((e0, e1))
+        # the batch projection launches of this step (events on their stream)
+        ms, nch, nkf = C.c_float(), C.c_int32(), C.c_int32()
+        ctx.check(L.sloam_frontend_time(ctx.h, C.byref(ms), C.byref(nch), C.byref(nkf)))
+        fe_ms += ms.value
+        fe_launches += nch.value
+        fe_kf += nkf.value
     torch.cuda.synchronize()
     if dist:
         tdist.barrier()
@@ -329,20 +353,33 @@ def main():
         e2e_step()
     e2e_dt = time.perf_counter() - t0
     e2e = B * args.e2e_steps / e2e_dt
-    h2d = B * (N * 16 + N + 7 * 8) + C.sizeof(mapc) * min(B, P.batch_slots)
+    h2d = B * (N * 16 + N + 7 * 8) + C.sizeof(mapc)
     d2h = B * (7 * 8 + 4 + 4)
     e2e_ok = int(h_succ.sum())
 
-    # ---- roofline of the dominant kernel (point-cylinder hypothesis scoring):
-    # algorithmic bytes per launch = every tree point read once (16 B) + per
-    # hypothesis 4 B (count) ; FLOP = 8 per point-hypothesis test.
-    import ctypes as _c
-    peaks = {}
+    # ---- roofline: the batch projection stage (HBM-bound), per launch group
+    # of 8 keyframes; algorithmic bytes = 26 B per point.
+    peaks, peak_src = {}, "fallback"
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
+        peak_src = "measured"
+    except (OSError, ValueError):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    fe_bytes = 26.0 * N * fe_kf
+    achieved = fe_bytes / (fe_ms / 1000.0) / 1e9 if fe_ms > 0 else None
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": achieved / hbm_peak if achieved else None,
+        "traffic": (FRONT_TRAFFIC_PER_KF * fe_kf / fe_launches
+                    if fe_launches and FRONT_TRAFFIC_PER_KF else None),
+        "peak_source": peak_src,
+        "kernel": "batch projection stage: k_project + k_label + k_ground_compact, "
+                  f"{fe_kf / max(fe_launches, 1):.0f} keyframes per launch",
+        "algorithmic_bytes_per_launch": fe_bytes / fe_launches if fe_launches else None,
+        "ms_per_launch": fe_ms / fe_launches if fe_launches else None,
+        "launches_timed": fe_launches,
+    }
 
     # CPU baseline (rank 0, N=1): the oracle, one host thread, bounded sample
     cpu = None
@@ -371,8 +408,9 @@ def main():
                                        "models": stages[2], "assoc_pose": stages[3]},
             "kernels_ms": {"k_cyl_hyp": hyp_ms.value, "k_project": proj_ms.value},
             "keyframes_ok": ok, "cylinders_per_keyframe": float(n_cyl.mean()),
+            "host_enqueue_ms_per_step": 1000.0 * host_s / args.steps,
             "clocks": ck,
-            "hbm_peak_gbs": hbm_peak,
+            "roofline": roofline,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -133,6 +133,27 @@ void build_px_table(const sloam_params& p, float* tab) {
   tab[W] = INFINITY;
 }
 
+// Row of a float pitch exactly as inference.cpp:112-126 computes it (float
+// arithmetic, unfused).  The row falls as the pitch grows, so the table holds
+// tab[k] = smallest float pitch whose row is <= H-1-k (k = 1..H-1): the row
+// of p is H-1 minus the number of k with p >= tab[k].
+void build_py_table(const sloam_params& p, float* tab) {
+  const int H = p.img_h;
+  const KParams kp = make_kparams(p);
+  const float fd = kp.fov_down_abs, fov = kp.fov;
+  auto g = [H, fd, fov](float pitch) {
+    float t = (pitch + fd) / fov;
+    float y = (1.0f - t) * (float)H;
+    y = std::floor(y);
+    y = ref_min(H - 1.0f, y);
+    y = ref_max(0.0f, y);
+    return H - 1 - (int)y;
+  };
+  tab[0] = -INFINITY;
+  for (int k = 1; k < H; ++k) tab[k] = first_at_least(g, k, -2.0f, 2.0f);
+  tab[H] = INFINITY;
+}
+
 // Theta and radius bins of sloam.cpp:346-357 as float boundary tables, and
 // the float window equivalent to r < maxG && r > minG in double.
 void build_ground_tables(const sloam_params& p, float* tb, float* rb, float* r_lo, float* r_hi) {
@@ -168,16 +189,27 @@ void build_ground_tables(const sloam_params& p, float* tb, float* rb, float* r_l
 
 // Test hook (not part of the public header): the host-built boundary tables
 // a context would upload.  px_tab [img_w+1], tb [theta_bins+1],
-// rb [radii_bins+1], lohi [2].
+// rb [radii_bins+1], lohi [2], py_tab [img_h+1].
 extern "C" int sloam_internal_tables(const sloam_params* p, float* px_tab, float* tb, float* rb,
-                                     float* lohi) {
+                                     float* lohi, float* py_tab) {
   if (!p) return SLOAM_ERR_ARG;
   sg::build_px_table(*p, px_tab);
+  sg::build_py_table(*p, py_tab);
   sg::build_ground_tables(*p, tb, rb, lohi, lohi + 1);
   return SLOAM_OK;
 }
 
 // ================================================================ context
+// Keyframes per batch projection launch.
+constexpr int kFrontChunk = 8;
+
+// Captured keyframe graphs of one slot, keyed
+// [first scan][point labels][state update][projection done by a batch launch].
+struct GraphSet {
+  cudaGraphExec_t g[2][2][2][2] = {};
+  int launches[2][2][2][2] = {};
+};
+
 struct sloam_ctx {
   sloam_params P;
   KParams kp;
@@ -196,21 +228,32 @@ struct sloam_ctx {
   std::string err;
   int64_t launches = 0;
   int64_t last_launches = 0;
-  // graphs: [first][label mode][state update]
-  cudaGraphExec_t gx[2][2][2] = {};
-  int gx_launches[2][2][2] = {};
+  GraphSet gx;
   // further keyframe slots of a batch (slot 0 is the fields above)
   struct Slot {
     Dev d{};
     void* arena = nullptr;
     size_t arena_bytes = 0;
     cudaStream_t st = nullptr;
-    cudaGraphExec_t gx[2][2][2] = {};
-    int gxl[2][2][2] = {};
+    GraphSet gx;
     cudaEvent_t ev = nullptr;
   };
   std::vector<Slot> extra;
   cudaEvent_t ev_main = nullptr;
+  // batch projection: a1-a2 of a whole batch on its own stream, one launch
+  // per kernel and chunk of keyframes, into per-keyframe buffers
+  cudaStream_t fe_st = nullptr;
+  void* fb = nullptr;            // [fb_cap] per-keyframe projection buffers
+  size_t fb_stride = 0;          // bytes per keyframe
+  int32_t* fb_pix = nullptr;     // [kFrontChunk * N] point pixels of the chunk in flight
+  unsigned long long* fb_pkey = nullptr;  // [kFrontChunk * N] pixel keys, kept all-ones
+  int fb_cap = 0;
+  bool fb_upload = false;        // the buffers include scan upload space
+  FrontRef* d_refs = nullptr;    // [fb_cap]
+  FrontRef* h_refs = nullptr;    // [fb_cap], pinned
+  int32_t* fb_fe = nullptr;      // [fb_cap * 4] projection counters
+  std::vector<cudaEvent_t> ev_fe;  // chunk c: [2c] before, [2c+1] after
+  int fe_chunks = 0, fe_nkf = 0;
   // host batch staging
   int32_t* d_out_i = nullptr;   // [2 * cap] success, ncyl
   double* d_out_pose = nullptr; // [7 * cap]
@@ -267,6 +310,7 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.ground_idx = c.take<int32_t>(N);
   d.ground = c.take<float4>(d.cap_ground);
   d.px_tab = c.take<float>(d.W + 1);
+  d.py_tab = c.take<float>(d.H + 1);
   d.tb_tab = c.take<float>(4096);
   d.rb_tab = c.take<float>(4096);
   d.parent = c.take<uint32_t>(N);
@@ -325,7 +369,8 @@ void carve(Dev& d, Carver& c, int n_blk) {
 }
 
 int check_params(const sloam_params& p) {
-  if (p.img_w < 32 || p.img_h < 1 || (int64_t)p.img_w * p.img_h > (1 << 26)) return 1;
+  // pixel keys carry a 24-bit point index
+  if (p.img_w < 32 || p.img_h < 1 || (int64_t)p.img_w * p.img_h > (1 << 24)) return 1;
   if (p.ground_radii_bins < 1 || p.ground_theta_bins < 1 ||
       p.ground_radii_bins * p.ground_theta_bins > 4096)
     return 1;
@@ -337,14 +382,15 @@ int check_params(const sloam_params& p) {
   return 0;
 }
 
-void destroy_graphs(cudaGraphExec_t (&gx)[2][2][2]) {
-  for (auto& a : gx)
+void destroy_graphs(GraphSet& gs) {
+  for (auto& a : gs.g)
     for (auto& b : a)
-      for (auto& g : b)
-        if (g) {
-          cudaGraphExecDestroy(g);
-          g = nullptr;
-        }
+      for (auto& c : b)
+        for (auto& g : c)
+          if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+          }
 }
 
 // Sizes, carves and initialises one slot's device state.
@@ -379,21 +425,28 @@ int init_dev(sloam_ctx* ctx, const sloam_params& P, Dev& d, void*& arena, size_t
   Carver real{reinterpret_cast<char*>(arena), 0, false};
   carve(d, real, n_blk);
   // tables
-  std::vector<float> tab(d.W + 1), tb(4096), rb(4096);
+  std::vector<float> tab(d.W + 1), ptab(d.H + 1), tb(4096), rb(4096);
   build_px_table(P, tab.data());
+  build_py_table(P, ptab.data());
   build_ground_tables(P, tb.data(), rb.data(), &d.r_lo, &d.r_hi);
   CK(cudaMemcpyAsync(d.px_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.py_tab, ptab.data(), sizeof(float) * ptab.size(), cudaMemcpyHostToDevice,
+                     st));
   CK(cudaMemcpyAsync(d.tb_tab, tb.data(), sizeof(float) * (P.ground_theta_bins + 1),
                      cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.rb_tab, rb.data(), sizeof(float) * (P.ground_radii_bins + 1),
                      cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(d.pkey, 0xFF, sizeof(unsigned long long) * d.N, st));
   CK(cudaMemsetAsync(d.cnt, 0, sizeof(Counters), st));
+  CK(cudaMemsetAsync(d.in, 0, sizeof(InPtrs), st));
   CK(cudaStreamSynchronize(st));
   return SLOAM_OK;
 }
 
+void free_front(sloam_ctx* ctx);
+
 int setup(sloam_ctx* ctx, const sloam_params& P) {
+  free_front(ctx);  // sized by the scan and ground capacities
   ctx->P = P;
   ctx->kp = make_kparams(P);
   int st = init_dev(ctx, P, ctx->d, ctx->arena, ctx->arena_bytes, ctx->st);
@@ -442,6 +495,9 @@ int set_inputs(sloam_ctx* ctx, const float4* xyzi, const uint8_t* pl, const uint
   h.plabel = pl;
   h.mask_in = mi;
   h.map = map;
+  h.tree = ctx->d.tree;
+  h.ground = ctx->d.ground;
+  h.fe = nullptr;
   h.n_map = n_map;
   CK(cudaMemcpyAsync(ctx->d.in, &h, sizeof(InPtrs), cudaMemcpyHostToDevice, ctx->st));
   // the pinned block must stay unchanged until the copy ran
@@ -603,7 +659,8 @@ extern "C" sloam_ctx* sloam_create(const sloam_params* params, int device, int* 
     return (sloam_ctx*)nullptr;
   };
   if (cudaSetDevice(device) != cudaSuccess) return bail(SLOAM_ERR_NO_DEVICE);
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->fe_st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(SLOAM_ERR_CUDA);
   if (cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
       cudaMallocHost((void**)&ctx->h_pose, sizeof(double) * 32) != cudaSuccess ||
@@ -631,6 +688,9 @@ extern "C" void sloam_destroy(sloam_ctx* ctx) {
     if (s.st) cudaStreamDestroy(s.st);
   }
   if (ctx->ev_main) cudaEventDestroy(ctx->ev_main);
+  free_front(ctx);
+  for (auto e : ctx->ev_fe) cudaEventDestroy(e);
+  if (ctx->fe_st) cudaStreamDestroy(ctx->fe_st);
   if (ctx->d_out_i) cudaFree(ctx->d_out_i);
   if (ctx->d_out_pose) cudaFree(ctx->d_out_pose);
   if (ctx->arena) cudaFree(ctx->arena);
@@ -717,11 +777,12 @@ extern "C" int sloam_trellis(sloam_ctx* ctx, const float* tree_cloud, int32_t H,
   if (H != d.H || W != d.W) return fail(ctx, SLOAM_ERR_ARG, "H, W must match the context");
   cudaSetDevice(ctx->device);
   CK(cudaMemcpyAsync(d.tree, tree_cloud, 16 * (size_t)d.N, cudaMemcpyHostToDevice, ctx->st));
+  int st = set_inputs(ctx, nullptr, nullptr, nullptr, nullptr, 0);
+  if (st) return st;
   int nl = launch_begin(d, 0, -1, -1, -1, -1, ctx->st);
   nl += launch_trellis(d, ctx->kp, ctx->st);
   ctx->last_launches = nl;
-  int st = sync_counters(ctx);
-  if (st) return st;
+  if ((st = sync_counters(ctx))) return st;
   const Counters& c = *ctx->h_cnt;
   if (n_components) *n_components = c.n_comp;
   if (cc_labels) CK(cudaMemcpy(cc_labels, d.label, 4 * (size_t)d.N, cudaMemcpyDeviceToHost));
@@ -770,6 +831,7 @@ extern "C" int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose,
   if (st) return st;
   if ((st = upload_ground(ctx, ground_xyzi, n_ground))) return st;
   if ((st = upload_pose(ctx, pose))) return st;
+  if ((st = set_inputs(ctx, nullptr, nullptr, nullptr, nullptr, 0))) return st;
   int k = launch_begin(d, n_ground, nl, nv, np, ncl, ctx->st);
   k += launch_models(d, ctx->kp, false, ctx->st);
   ctx->last_launches = k;
@@ -818,39 +880,40 @@ extern "C" int sloam_run(sloam_ctx* ctx, const sloam_se3* pose, const float* gro
 // ----------------------------------------------------------- keyframe
 namespace {
 int enqueue_keyframe(sloam_ctx* ctx, const Dev& d, cudaStream_t st, bool first,
-                     bool point_labels, bool update) {
+                     bool point_labels, bool update, bool pre) {
   int k = launch_begin(d, -1, -1, -1, -1, -1, st);
-  k += launch_project(d, ctx->kp, point_labels, st);
+  if (!pre) k += launch_project(d, ctx->kp, point_labels, st);
   k += launch_trellis(d, ctx->kp, st);
   k += launch_models(d, ctx->kp, true, st);
   k += launch_run(d, ctx->kp, first, update, st);
   return k;
 }
 
-// The whole keyframe (a1-a11) of one slot as one CUDA graph, captured on
-// first use; returns the number of kernels it launches in *nk.
-int run_graph(sloam_ctx* ctx, const Dev& d, cudaStream_t st, cudaGraphExec_t (&gx)[2][2][2],
-              int (&gxl)[2][2][2], bool first, bool point_labels, bool update, int* nk) {
-  const int a = first ? 1 : 0, b = point_labels ? 1 : 0, u = update ? 1 : 0;
-  if (!gx[a][b][u]) {
+// The whole keyframe (a1-a11, or a3-a11 when a batch launch did the
+// projection) of one slot as one CUDA graph, captured on first use; returns
+// the number of kernels it launches in *nk.
+int run_graph(sloam_ctx* ctx, const Dev& d, cudaStream_t st, GraphSet& gs, bool first,
+              bool point_labels, bool update, bool pre, int* nk) {
+  const int a = first ? 1 : 0, b = point_labels ? 1 : 0, u = update ? 1 : 0, q = pre ? 1 : 0;
+  cudaGraphExec_t& gx = gs.g[a][b][u][q];
+  if (!gx) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const int k = enqueue_keyframe(ctx, d, st, first, point_labels, update);
+    const int k = enqueue_keyframe(ctx, d, st, first, point_labels, update, pre);
     CK(cudaStreamEndCapture(st, &g));
-    cudaError_t e = cudaGraphInstantiate(&gx[a][b][u], g, 0);
+    cudaError_t e = cudaGraphInstantiate(&gx, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(ctx, SLOAM_ERR_CUDA, "cudaGraphInstantiate", e);
-    gxl[a][b][u] = k;
+    gs.launches[a][b][u][q] = k;
   }
-  CK(cudaGraphLaunch(gx[a][b][u], st));
-  *nk = gxl[a][b][u];
+  CK(cudaGraphLaunch(gx, st));
+  *nk = gs.launches[a][b][u][q];
   return SLOAM_OK;
 }
 
 int run_keyframe_graph(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
   int nk = 0;
-  const int s = run_graph(ctx, ctx->d, ctx->st, ctx->gx, ctx->gx_launches, first, point_labels,
-                          update, &nk);
+  const int s = run_graph(ctx, ctx->d, ctx->st, ctx->gx, first, point_labels, update, false, &nk);
   ctx->last_launches = nk;
   return s;
 }
@@ -912,14 +975,13 @@ namespace {
 struct SlotView {
   Dev* d;
   cudaStream_t st;
-  cudaGraphExec_t (*gx)[2][2][2];
-  int (*gxl)[2][2][2];
+  GraphSet* gx;
   cudaEvent_t ev;
 };
 SlotView slot(sloam_ctx* ctx, int s) {
-  if (s == 0) return {&ctx->d, ctx->st, &ctx->gx, &ctx->gx_launches, nullptr};
+  if (s == 0) return {&ctx->d, ctx->st, &ctx->gx, nullptr};
   auto& x = ctx->extra[s - 1];
-  return {&x.d, x.st, &x.gx, &x.gxl, x.ev};
+  return {&x.d, x.st, &x.gx, x.ev};
 }
 
 int grow_batch(sloam_ctx* ctx, int nkf) {
@@ -934,10 +996,82 @@ int grow_batch(sloam_ctx* ctx, int nkf) {
   return SLOAM_OK;
 }
 
-// Fork: every extra slot waits for the context stream and takes a copy of
-// the previous-scan planes (the batch does not advance the state).
+// One keyframe's projection outputs inside the batch buffers (the scan
+// upload space last, when present).  The point pixels and pixel keys are
+// scratch of the chunk in flight (fb_pix, fb_pkey), small enough to stay in
+// L2 between the chunk's kernels.
+struct FrontSlice {
+  FrontRef f{};
+  float4* up_xyzi = nullptr;
+  uint8_t* up_plabel = nullptr;
+};
+FrontSlice front_slice(const Dev& d, char* base, bool upload, size_t* bytes) {
+  Carver c{base, 0, base == nullptr};
+  const int N = d.N;
+  FrontSlice s;
+  s.f.range_img = c.take<float>(N);
+  s.f.mask = c.take<uint8_t>(N);
+  s.f.tree = c.take<float4>(N);
+  s.f.gbits = c.take<uint32_t>(front_gbits_words(N));
+  s.f.blk = c.take<int32_t>(front_blocks(N));
+  s.f.ground_idx = c.take<int32_t>(N);
+  s.f.ground = c.take<float4>(d.cap_ground);
+  if (upload) {
+    s.up_xyzi = c.take<float4>(N);
+    s.up_plabel = c.take<uint8_t>(N);
+  }
+  if (bytes) *bytes = (c.off + 255) & ~(size_t)255;
+  return s;
+}
+
+void free_front(sloam_ctx* ctx) {
+  if (ctx->fe_st) cudaStreamSynchronize(ctx->fe_st);
+  if (ctx->fb) cudaFree(ctx->fb);
+  if (ctx->fb_pix) cudaFree(ctx->fb_pix);
+  if (ctx->fb_pkey) cudaFree(ctx->fb_pkey);
+  if (ctx->d_refs) cudaFree(ctx->d_refs);
+  if (ctx->fb_fe) cudaFree(ctx->fb_fe);
+  if (ctx->h_refs) cudaFreeHost(ctx->h_refs);
+  ctx->fb = nullptr;
+  ctx->fb_pix = nullptr;
+  ctx->fb_pkey = nullptr;
+  ctx->d_refs = nullptr;
+  ctx->fb_fe = nullptr;
+  ctx->h_refs = nullptr;
+  ctx->fb_cap = 0;
+  ctx->fb_upload = false;
+}
+
+// Batch projection buffers for nkf keyframes (kept and reused; the pixel
+// keys start all-ones and every chunk re-arms them).
+int grow_front(sloam_ctx* ctx, int nkf, bool upload) {
+  if (nkf <= ctx->fb_cap && (!upload || ctx->fb_upload)) return SLOAM_OK;
+  const int cap = std::max(nkf, ctx->fb_cap);
+  upload = upload || ctx->fb_upload;
+  free_front(ctx);
+  size_t stride = 0;
+  front_slice(ctx->d, nullptr, upload, &stride);
+  CK(cudaMalloc(&ctx->fb, stride * cap));
+  const size_t sn = (size_t)kFrontChunk * ctx->d.N;
+  CK(cudaMalloc((void**)&ctx->fb_pix, sizeof(int32_t) * sn));
+  CK(cudaMalloc((void**)&ctx->fb_pkey, sizeof(unsigned long long) * sn));
+  CK(cudaMemsetAsync(ctx->fb_pkey, 0xFF, sizeof(unsigned long long) * sn, ctx->fe_st));
+  CK(cudaMalloc((void**)&ctx->d_refs, sizeof(FrontRef) * cap));
+  CK(cudaMalloc((void**)&ctx->fb_fe, sizeof(int32_t) * 4 * cap));
+  CK(cudaMallocHost((void**)&ctx->h_refs, sizeof(FrontRef) * cap));
+  ctx->fb_stride = stride;
+  ctx->fb_cap = cap;
+  ctx->fb_upload = upload;
+  CK(cudaStreamSynchronize(ctx->fe_st));
+  return SLOAM_OK;
+}
+
+// Fork: the projection stream and every extra slot wait for the context
+// stream; the extra slots take a copy of the previous-scan planes (the batch
+// does not advance the state).
 int batch_fork(sloam_ctx* ctx) {
   CK(cudaEventRecord(ctx->ev_main, ctx->st));
+  CK(cudaStreamWaitEvent(ctx->fe_st, ctx->ev_main, 0));
   for (auto& s : ctx->extra) {
     CK(cudaStreamWaitEvent(s.st, ctx->ev_main, 0));
     CK(cudaMemcpyAsync(s.d.prev_planes, ctx->d.prev_planes, sizeof(PlaneD) * ctx->d.n_bins,
@@ -947,18 +1081,20 @@ int batch_fork(sloam_ctx* ctx) {
   }
   return SLOAM_OK;
 }
-// Join: the context stream waits for every slot.
+// Join: the context stream waits for every slot and the projection stream.
 int batch_join(sloam_ctx* ctx) {
   for (auto& s : ctx->extra) {
     CK(cudaEventRecord(s.ev, s.st));
     CK(cudaStreamWaitEvent(ctx->st, s.ev, 0));
   }
+  if (ctx->fe_chunks > 0)
+    CK(cudaStreamWaitEvent(ctx->st, ctx->ev_fe[2 * ctx->fe_chunks - 1], 0));
   return SLOAM_OK;
 }
 
 // Keyframe k of a batch on slot k % slots: inputs pointer block and pose
-// estimate from pinned host memory, the slot's graph (no state update),
-// then its outputs into the batch arrays.
+// estimate from pinned host memory, the slot's graph (projection already
+// done, no state update), then its outputs into the batch arrays.
 int batch_one(sloam_ctx* ctx, int k, double* pose_out, int32_t* success_out, int32_t* ncyl_out,
               int64_t* launches) {
   const int S = 1 + (int)ctx->extra.size();
@@ -967,7 +1103,7 @@ int batch_one(sloam_ctx* ctx, int k, double* pose_out, int32_t* success_out, int
   CK(cudaMemcpyAsync(v.d->pose_io, ctx->h_poses + 8 * k, sizeof(double) * 7,
                      cudaMemcpyHostToDevice, v.st));
   int nk = 0;
-  int st = run_graph(ctx, *v.d, v.st, *v.gx, *v.gxl, false, true, false, &nk);
+  int st = run_graph(ctx, *v.d, v.st, *v.gx, false, true, false, true, &nk);
   if (st) return st;
   k_batch_out<<<1, 32, 0, v.st>>>(v.d->cnt, v.d->pose_io, pose_out, success_out, ncyl_out, k);
   *launches += nk + 1;
@@ -977,6 +1113,89 @@ int batch_one(sloam_ctx* ctx, int k, double* pose_out, int32_t* success_out, int
 void fill_pose(sloam_ctx* ctx, int k, const sloam_se3& p) {
   for (int j = 0; j < 4; ++j) ctx->h_poses[8 * k + j] = p.q[j];
   for (int j = 0; j < 3; ++j) ctx->h_poses[8 * k + 4 + j] = p.t[j];
+}
+
+// Per-keyframe projection views and input blocks of a batch.  Scans come
+// from the caller's device arrays (xyzi, labels) or, when those are null,
+// from the upload space of the batch buffers.
+void fill_batch(sloam_ctx* ctx, int nkf, const float* xyzi, const uint8_t* labels,
+                const sloam_se3* poses, const sloam_cylinder* d_map, int n_map) {
+  const int n = ctx->d.N;
+  for (int k = 0; k < nkf; ++k) {
+    FrontSlice s = front_slice(ctx->d, (char*)ctx->fb + ctx->fb_stride * k, ctx->fb_upload,
+                               nullptr);
+    FrontRef& f = ctx->h_refs[k];
+    f = s.f;
+    f.pix = ctx->fb_pix + (size_t)(k % kFrontChunk) * n;
+    f.pkey = ctx->fb_pkey + (size_t)(k % kFrontChunk) * n;
+    f.xyzi = xyzi ? reinterpret_cast<const float4*>(xyzi) + (size_t)k * n : s.up_xyzi;
+    f.plabel = labels ? labels + (size_t)k * n : s.up_plabel;
+    f.mask_in = nullptr;
+    f.fe = ctx->fb_fe + 4 * k;
+    InPtrs& h = ctx->h_in[k];
+    h.xyzi = f.xyzi;
+    h.plabel = f.plabel;
+    h.mask_in = nullptr;
+    h.map = d_map;
+    h.tree = f.tree;
+    h.ground = f.ground;
+    h.fe = f.fe;
+    h.n_map = n_map;
+    h.pad = 0;
+    fill_pose(ctx, k, poses[k]);
+  }
+}
+
+// The batch: projection of each chunk of keyframes on the projection stream,
+// then the keyframes on their slots.  Host input: each chunk's scans are
+// uploaded before its projection, and a slot waits only for the chunk of its
+// keyframe, so uploads, projection and the slots overlap.  Device input: the
+// slots wait for the last chunk, so the projection runs alone on the GPU.
+int batch_run(sloam_ctx* ctx, int nkf, const float* h_xyzi, const uint8_t* h_labels,
+              double* pose_out, int32_t* success_out, int32_t* ncyl_out, int64_t* launches) {
+  const int n = ctx->d.N;
+  const int S = 1 + (int)ctx->extra.size();
+  const int nch = (nkf + kFrontChunk - 1) / kFrontChunk;
+  while ((int)ctx->ev_fe.size() < 2 * nch) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    ctx->ev_fe.push_back(e);
+  }
+  CK(cudaMemcpyAsync(ctx->d_refs, ctx->h_refs, sizeof(FrontRef) * nkf, cudaMemcpyHostToDevice,
+                     ctx->fe_st));
+  CK(cudaMemsetAsync(ctx->fb_fe, 0, sizeof(int32_t) * 4 * nkf, ctx->fe_st));
+  ctx->fe_chunks = 0;
+  for (int c = 0; c < nch; ++c) {
+    const int kf0 = c * kFrontChunk, nc = std::min(kFrontChunk, nkf - kf0);
+    if (h_xyzi) {
+      for (int k = kf0; k < kf0 + nc; ++k) {
+        FrontRef& f = ctx->h_refs[k];
+        CK(cudaMemcpyAsync(const_cast<float4*>(f.xyzi), h_xyzi + (size_t)k * n * 4,
+                           16 * (size_t)n, cudaMemcpyHostToDevice, ctx->fe_st));
+        CK(cudaMemcpyAsync(const_cast<uint8_t*>(f.plabel), h_labels + (size_t)k * n, (size_t)n,
+                           cudaMemcpyHostToDevice, ctx->fe_st));
+      }
+    }
+    CK(cudaEventRecord(ctx->ev_fe[2 * c], ctx->fe_st));
+    *launches += launch_project_batch(ctx->d, ctx->kp, ctx->d_refs, kf0, nc, true, ctx->fe_st);
+    CK(cudaEventRecord(ctx->ev_fe[2 * c + 1], ctx->fe_st));
+    ctx->fe_chunks = c + 1;
+    if (!h_xyzi) continue;
+    for (int k = kf0; k < kf0 + nc; ++k) {
+      CK(cudaStreamWaitEvent(slot(ctx, k % S).st, ctx->ev_fe[2 * c + 1], 0));
+      int st = batch_one(ctx, k, pose_out, success_out, ncyl_out, launches);
+      if (st) return st;
+    }
+  }
+  ctx->fe_nkf = nkf;
+  if (h_xyzi || nch == 0) return SLOAM_OK;
+  for (int s = 0; s < S && s < nkf; ++s)
+    CK(cudaStreamWaitEvent(slot(ctx, s).st, ctx->ev_fe[2 * nch - 1], 0));
+  for (int k = 0; k < nkf; ++k) {
+    int st = batch_one(ctx, k, pose_out, success_out, ncyl_out, launches);
+    if (st) return st;
+  }
+  return SLOAM_OK;
 }
 }  // namespace
 
@@ -995,20 +1214,13 @@ extern "C" int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32
   if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
   CK(cudaStreamSynchronize(ctx->st));  // the previous batch released the pinned blocks
   int st = grow_batch(ctx, nkf);
-  if (st) return st;
-  for (int k = 0; k < nkf; ++k) {
-    InPtrs& h = ctx->h_in[k];
-    h.xyzi = reinterpret_cast<const float4*>(d_xyzi) + (size_t)k * n;
-    h.plabel = d_point_labels + (size_t)k * n;
-    h.mask_in = nullptr;
-    h.map = d_map;
-    h.n_map = n_map;
-    fill_pose(ctx, k, poses[k]);
-  }
+  if (st || (st = grow_front(ctx, nkf, false))) return st;
+  fill_batch(ctx, nkf, d_xyzi, d_point_labels, poses, d_map, n_map);
   int64_t launches = 0;
   if ((st = batch_fork(ctx))) return st;
-  for (int k = 0; k < nkf; ++k)
-    if ((st = batch_one(ctx, k, d_pose_out, d_success_out, d_ncyl_out, &launches))) return st;
+  if ((st = batch_run(ctx, nkf, nullptr, nullptr, d_pose_out, d_success_out, d_ncyl_out,
+                      &launches)))
+    return st;
   if ((st = batch_join(ctx))) return st;
   ctx->last_launches = launches;
   CK(cudaGetLastError());
@@ -1029,7 +1241,7 @@ extern "C" int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n
   if (n_map > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "map exceeds max_map");
   CK(cudaStreamSynchronize(ctx->st));
   int st = grow_batch(ctx, nkf);
-  if (st) return st;
+  if (st || (st = grow_front(ctx, nkf, true))) return st;
   if (nkf > ctx->out_cap) {
     if (ctx->d_out_i) cudaFree(ctx->d_out_i);
     if (ctx->d_out_pose) cudaFree(ctx->d_out_pose);
@@ -1039,33 +1251,15 @@ extern "C" int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n
     CK(cudaMalloc(&ctx->d_out_pose, sizeof(double) * 7 * nkf));
     ctx->out_cap = nkf;
   }
-  const int S = 1 + (int)ctx->extra.size();
-  for (int k = 0; k < nkf; ++k) {
-    const SlotView v = slot(ctx, k % S);
-    InPtrs& h = ctx->h_in[k];
-    h.xyzi = v.d->buf_xyzi;
-    h.plabel = v.d->buf_plabel;
-    h.mask_in = nullptr;
-    h.map = v.d->buf_map;
-    h.n_map = n_map;
-    fill_pose(ctx, k, poses[k]);
-  }
+  // one map upload shared by every slot (read-only during the batch)
+  fill_batch(ctx, nkf, nullptr, nullptr, poses, d.buf_map, n_map);
   int64_t launches = 0;
   if ((st = batch_fork(ctx))) return st;
-  for (int s = 0; s < S && s < nkf; ++s) {
-    const SlotView v = slot(ctx, s);
-    CK(cudaMemcpyAsync(v.d->buf_map, map, sizeof(sloam_cylinder) * n_map, cudaMemcpyHostToDevice,
-                       v.st));
-  }
-  for (int k = 0; k < nkf; ++k) {
-    const SlotView v = slot(ctx, k % S);
-    CK(cudaMemcpyAsync(v.d->buf_xyzi, xyzi + (size_t)k * n * 4, 16 * (size_t)n,
-                       cudaMemcpyHostToDevice, v.st));
-    CK(cudaMemcpyAsync(v.d->buf_plabel, point_labels + (size_t)k * n, (size_t)n,
-                       cudaMemcpyHostToDevice, v.st));
-    if ((st = batch_one(ctx, k, ctx->d_out_pose, ctx->d_out_i, ctx->d_out_i + nkf, &launches)))
-      return st;
-  }
+  CK(cudaMemcpyAsync(d.buf_map, map, sizeof(sloam_cylinder) * n_map, cudaMemcpyHostToDevice,
+                     ctx->fe_st));
+  if ((st = batch_run(ctx, nkf, xyzi, point_labels, ctx->d_out_pose, ctx->d_out_i,
+                      ctx->d_out_i + nkf, &launches)))
+    return st;
   if ((st = batch_join(ctx))) return st;
   CK(cudaMemcpyAsync(pose_out, ctx->d_out_pose, sizeof(double) * 7 * nkf, cudaMemcpyDeviceToHost,
                      ctx->st));
@@ -1083,10 +1277,26 @@ extern "C" int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n
 // the isolated timing of one kernel.  Both replay work on the inputs and
 // state left by the previous keyframe call and record CUDA events on the
 // context stream.
+namespace {
+// The profiling hooks replay single-keyframe stages: point the input block's
+// cloud and ground views back at the context's own buffers.
+int own_views(sloam_ctx* ctx) {
+  InPtrs h;
+  CK(cudaStreamSynchronize(ctx->st));
+  CK(cudaMemcpy(&h, ctx->d.in, sizeof(h), cudaMemcpyDeviceToHost));
+  h.tree = ctx->d.tree;
+  h.ground = ctx->d.ground;
+  h.fe = nullptr;
+  CK(cudaMemcpy(ctx->d.in, &h, sizeof(h), cudaMemcpyHostToDevice));
+  return SLOAM_OK;
+}
+}  // namespace
+
 extern "C" int sloam_profile_stages(sloam_ctx* ctx, float* ms, int n) {
   if (!ctx || !ms || n < 4) return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
   Dev& d = ctx->d;
+  if (int st = own_views(ctx)) return st;
   cudaEvent_t ev[5];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], ctx->st));
@@ -1111,6 +1321,7 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
   if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 1) return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
   Dev& d = ctx->d;
+  if (int st = own_views(ctx)) return st;
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
@@ -1126,9 +1337,29 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, a, b));
   *avg_ms = ms / reps;
-  if (which == 0) launch_resolve_kernel(d, true, ctx->st);  // re-arm the pixel keys
+  if (which == 0) launch_project_rest(d, ctx->kp, true, ctx->st);  // re-arm the pixel keys
   CK(cudaStreamSynchronize(ctx->st));
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  return SLOAM_OK;
+}
+
+// Device time of the batch projection launches of the last batch call: the
+// sum over its chunks of the CUDA-event time between the first and the last
+// kernel of the chunk on the projection stream.
+extern "C" int sloam_frontend_time(sloam_ctx* ctx, float* ms, int32_t* n_chunks,
+                                   int32_t* n_keyframes) {
+  if (!ctx || !ms) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  float total = 0.0f;
+  for (int c = 0; c < ctx->fe_chunks; ++c) {
+    CK(cudaEventSynchronize(ctx->ev_fe[2 * c + 1]));
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, ctx->ev_fe[2 * c], ctx->ev_fe[2 * c + 1]));
+    total += t;
+  }
+  *ms = total;
+  if (n_chunks) *n_chunks = ctx->fe_chunks;
+  if (n_keyframes) *n_keyframes = ctx->fe_nkf;
   return SLOAM_OK;
 }

@@ -56,13 +56,39 @@ struct CylD {
 
 // Per-call inputs, read by the kernels through a device pointer so that a
 // captured CUDA graph can be replayed over different input buffers.
+// `tree` and `ground` are the organised tree cloud and ground list the later
+// stages read: the context's own buffers, or one keyframe's slice of the
+// batch projection buffers.  `fe` (batch only) holds that keyframe's
+// projection counters {n_ground, overflow, n_slow_px}, copied into the
+// counters by the first kernel of the keyframe.
 struct InPtrs {
   const float4* xyzi;
   const uint8_t* plabel;
   const uint8_t* mask_in;
   const sloam_cylinder* map;
+  const float4* tree;
+  const float4* ground;
+  const int32_t* fe;
   int32_t n_map;
   int32_t pad;
+};
+
+// One keyframe's projection buffers (a1-a2).  A batch launch reads an array
+// of these, one per keyframe, indexed by blockIdx.y.
+struct FrontRef {
+  const float4* xyzi;
+  const uint8_t* plabel;
+  const uint8_t* mask_in;
+  int32_t* pix;
+  unsigned long long* pkey;
+  float* range_img;
+  uint8_t* mask;
+  float4* tree;
+  uint32_t* gbits;
+  int32_t* blk;
+  int32_t* ground_idx;
+  float4* ground;
+  int32_t* fe;  // {n_ground, overflow, n_slow_px, pad}
 };
 
 struct Dev {
@@ -84,6 +110,7 @@ struct Dev {
   int32_t* ground_idx;
   float4* ground;
   float* px_tab;       // [W+1]
+  float* py_tab;       // [H+1]
   float* tb_tab;       // [Tb+1]
   float* rb_tab;       // [Rb+1]
   float r_lo, r_hi;    // float ground radius window
@@ -178,6 +205,11 @@ KParams make_kparams(const sloam_params& p);
 // ---------------------------------------------------------------- stages
 // Every launcher enqueues on `st` and returns the number of kernels launched.
 int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st);
+// a1-a2 for keyframes [kf0, kf0 + nkf) of refs (device array), one launch per kernel
+int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, int kf0,
+                         int nkf, bool point_labels, cudaStream_t st);
+size_t front_gbits_words(int N);
+int front_blocks(int N);
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
 int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_state,
@@ -187,7 +219,8 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trelli
 
 // single kernels, for isolated timing (profiling hooks)
 int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
-int launch_resolve_kernel(const Dev& d, bool point_labels, cudaStream_t st);
+// the projection stage after k_project (labels, tree cloud, ground list, key re-arm)
+int launch_project_rest(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st);
 int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st);
@@ -199,6 +232,7 @@ void init_kernel_attributes();
 
 // host-built tables (context.cu)
 void build_px_table(const sloam_params& p, float* tab);
+void build_py_table(const sloam_params& p, float* tab);
 void build_ground_tables(const sloam_params& p, float* tb, float* rb, float* r_lo,
                          float* r_hi);
 

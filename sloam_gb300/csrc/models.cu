@@ -84,37 +84,63 @@ __device__ __forceinline__ uint32_t zkey(float z) {
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+// Bin counts are combined per warp (match on the bin) and per block (shared
+// histogram) before one global atomicAdd per bin and block: the ground list
+// falls into a few dozen bins, so plain global atomics serialise.
+constexpr int kMaxBins = 4096;
+
+__device__ __forceinline__ int warp_bin_add(int* hist, int bin, int lane) {
+  const unsigned peers = __match_any_sync(0xffffffffu, bin);
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (bin >= 0 && lane == leader) base = atomicAdd(hist + bin, __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 __global__ void __launch_bounds__(256) k_gbin(Dev d, KParams kp) {
+  __shared__ int hist[kMaxBins];
+  const float4* __restrict__ ground = d.in->ground;
   const int n = d.cnt->n_ground;
+  if (blockIdx.x * blockDim.x >= n) return;
+  const int lane = threadIdx.x & 31;
+  for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
   int slow = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 p = d.ground[i];
-    const float dx = fsub(0.0f, p.x), dy = fsub(0.0f, p.y);
-    const float r = fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
     int bin = -1;
-    if (r >= d.r_lo && r <= d.r_hi) {
-      const float y = fsub(p.y, 0.0f), x = fsub(p.x, 0.0f);
-      float th = atan2f(y, x);
-      int tb;
-      bool need = !(isfinite(x) && isfinite(y)) || x == 0.0f || y == 0.0f;
-      if (!need) {
-        const float m = fmaxf(fabsf(th) * 1.2e-6f, 1e-30f);
-        tb = bin_from_table(d.tb_tab, th - m, kp.Tb);
-        need = tb != bin_from_table(d.tb_tab, th + m, kp.Tb);
+    if (i < n) {
+      const float4 p = ground[i];
+      const float dx = fsub(0.0f, p.x), dy = fsub(0.0f, p.y);
+      const float r = fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
+      if (r >= d.r_lo && r <= d.r_hi) {
+        const float y = fsub(p.y, 0.0f), x = fsub(p.x, 0.0f);
+        float th = atan2f(y, x);
+        int tb;
+        bool need = !(isfinite(x) && isfinite(y)) || x == 0.0f || y == 0.0f;
+        if (!need) {
+          const float m = fmaxf(fabsf(th) * 1.2e-6f, 1e-30f);
+          tb = bin_from_table(d.tb_tab, th - m, kp.Tb);
+          need = tb != bin_from_table(d.tb_tab, th + m, kp.Tb);
+        }
+        if (need) {
+          th = (float)atan2((double)y, (double)x);
+          tb = bin_from_table(d.tb_tab, th, kp.Tb);
+          ++slow;
+        }
+        const int rb = bin_from_table(d.rb_tab, r, kp.Rb);
+        bin = rb * kp.Tb + tb;
       }
-      if (need) {
-        th = (float)atan2((double)y, (double)x);
-        tb = bin_from_table(d.tb_tab, th, kp.Tb);
-        ++slow;
-      }
-      const int rb = bin_from_table(d.rb_tab, r, kp.Rb);
-      bin = rb * kp.Tb + tb;
-      atomicAdd(d.bin_cnt + bin, 1);
+      d.bin_of[i] = bin;
     }
-    d.bin_of[i] = bin;
+    warp_bin_add(hist, bin, lane);
   }
+  __syncthreads();
+  for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x)
+    if (hist[b]) atomicAdd(d.bin_cnt + b, hist[b]);
   slow = warp_sumi(slow);
-  if ((threadIdx.x & 31) == 0 && slow) atomicAdd(&d.cnt->n_slow_theta, slow);
+  if (lane == 0 && slow) atomicAdd(&d.cnt->n_slow_theta, slow);
 }
 
 __global__ void __launch_bounds__(1024) k_gbin_scan(Dev d) {
@@ -134,13 +160,27 @@ __global__ void __launch_bounds__(1024) k_gbin_scan(Dev d) {
   if (threadIdx.x == 0) d.bin_off[d.n_bins] = base;
 }
 
+// Scatter of (z key, index) into the bins; the order inside a bin is free
+// (k_plane orders every bin by key).
 __global__ void __launch_bounds__(256) k_gbin_scatter(Dev d) {
+  __shared__ int hist[kMaxBins];
+  const float4* __restrict__ ground = d.in->ground;
   const int n = d.cnt->n_ground;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int b = d.bin_of[i];
-    if (b < 0) continue;
-    const int pos = atomicAdd(d.bin_cnt + b, 1);
-    d.bin_keys[pos] = ((unsigned long long)zkey(d.ground[i].z) << 32) | (uint32_t)i;
+  if (blockIdx.x * blockDim.x >= n) return;
+  const int lane = threadIdx.x & 31;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const int bin = i < n ? d.bin_of[i] : -1;
+    const int local = warp_bin_add(hist, bin, lane);
+    __syncthreads();
+    for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x)
+      if (hist[b]) hist[b] = atomicAdd(d.bin_cnt + b, hist[b]);
+    __syncthreads();
+    if (bin >= 0)
+      d.bin_keys[hist[bin] + local] = ((unsigned long long)zkey(ground[i].z) << 32) | (uint32_t)i;
+    __syncthreads();
   }
 }
 
@@ -213,6 +253,7 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
   __shared__ float cen[3];
   __shared__ unsigned long long sel_prefix;
   __shared__ int sel_k, s_cnt;
+  const float4* __restrict__ ground = d.in->ground;
   const int b = blockIdx.x;
   if (b >= d.n_bins) return;
   const int off = d.bin_off[b], n = d.bin_off[b + 1] - off;
@@ -282,7 +323,7 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
     if (threadIdx.x == 0) {
       float sx = 0.f, sy = 0.f, sz = 0.f;
       for (int i = 0; i < kk; ++i) {
-        const float4 p = d.ground[(uint32_t)keys[i]];
+        const float4 p = ground[(uint32_t)keys[i]];
         sx = fadd(sx, p.x);
         sy = fadd(sy, p.y);
         sz = fadd(sz, p.z);
@@ -294,7 +335,7 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
     __syncthreads();
     double s[6] = {0, 0, 0, 0, 0, 0};
     for (int i = threadIdx.x; i < kk; i += blockDim.x) {
-      const float4 p = d.ground[(uint32_t)keys[i]];
+      const float4 p = ground[(uint32_t)keys[i]];
       const double a0 = (double)fsub(p.x, cen[0]), a1 = (double)fsub(p.y, cen[1]),
                    a2 = (double)fsub(p.z, cen[2]);
       s[0] += a0 * a0; s[1] += a0 * a1; s[2] += a0 * a2;
@@ -341,7 +382,7 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
       d.plane_all[b] = out;
     }
     for (int i = threadIdx.x; i < kp.G; i += blockDim.x)
-      d.plane_feat_all[(size_t)b * kp.G + i] = d.ground[(uint32_t)keys[i]];
+      d.plane_feat_all[(size_t)b * kp.G + i] = ground[(uint32_t)keys[i]];
   } else if (threadIdx.x == 0) {
     d.plane_all[b] = out;
   }

@@ -32,7 +32,9 @@ constexpr size_t kOffGround = al(kOffMask + 1ull * kNoAllocMaxPoints);
 constexpr size_t kOffBits = al(kOffGround + 16ull * kNoAllocMaxPoints);
 constexpr size_t kOffBlk = al(kOffBits + 4ull * ((kNoAllocMaxPoints + 1023) / 1024 * 32 + 32));
 constexpr size_t kOffTab = al(kOffBlk + 4ull * (kNoAllocMaxPoints / 256 + 64));
-constexpr size_t kOffIn = al(kOffTab + 4ull * (kNoAllocMaxW + 1));
+constexpr int kNoAllocMaxH = kNoAllocMaxPoints / 32;  // W >= 32
+constexpr size_t kOffRowTab = al(kOffTab + 4ull * (kNoAllocMaxW + 1));
+constexpr size_t kOffIn = al(kOffRowTab + 4ull * (kNoAllocMaxH + 1));
 constexpr size_t kOffCnt = al(kOffIn + sizeof(sg::InPtrs));
 constexpr size_t kNoAllocBytes = al(kOffCnt + sizeof(sg::Counters));
 
@@ -49,6 +51,7 @@ namespace {
 std::mutex g_mu;
 unsigned char* g_base[kMaxDevices] = {};  // device address of the scratch, per device
 float g_tab[kNoAllocMaxW + 1];            // host staging of the column table
+float g_row_tab[kNoAllocMaxH + 1];        // host staging of the row table
 
 }  // namespace
 
@@ -100,19 +103,24 @@ extern "C" int sloam_project_mask_noalloc(const sloam_params* p, const float* d_
   d.gbits = reinterpret_cast<uint32_t*>(b + kOffBits);
   d.blk = reinterpret_cast<int32_t*>(b + kOffBlk);
   d.px_tab = reinterpret_cast<float*>(b + kOffTab);
+  d.py_tab = reinterpret_cast<float*>(b + kOffRowTab);
   d.cnt = reinterpret_cast<sg::Counters*>(b + kOffCnt);
   d.tree = reinterpret_cast<float4*>(d_tree_cloud);
   d.ground_idx = d_ground_idx;
   const sg::KParams kp = sg::make_kparams(*p);
-  // The previous call's contents remain: re-upload the table and the input
+  // The previous call's contents remain: re-upload the tables and the input
   // pointers, and re-arm the pixel keys (they must start empty).
   sg::build_px_table(*p, g_tab);
+  sg::build_py_table(*p, g_row_tab);
   sg::InPtrs in{};
   in.xyzi = reinterpret_cast<const float4*>(d_xyzi);
   in.plabel = d_point_labels;
   in.mask_in = d_mask_image;
   cudaError_t e = cudaMemcpyAsync(d.px_tab, g_tab, sizeof(float) * (p->img_w + 1),
                                   cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d.py_tab, g_row_tab, sizeof(float) * (p->img_h + 1),
+                        cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d.in, &in, sizeof(in), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.pkey, 0xFF, sizeof(unsigned long long) * n, st);
   if (e != cudaSuccess) {

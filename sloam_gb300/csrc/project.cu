@@ -11,8 +11,15 @@
 // evaluates atan2f/asinf in FP32 and accepts the result when a +-1.2e-6
 // relative margin (about 10 ulp, above the documented error of the CUDA
 // functions) cannot change the pixel; otherwise the point takes the FP64
-// path.  The nearest point wins its pixel (64-bit atomicMin on
-// range-bits:index), ties to the lowest index.
+// path.  The row likewise comes from an exact boundary table of the pitch.
+// The nearest point wins its pixel: 64-bit atomicMin on
+// range bits (32) : point index (24) : point label (8), ties to the lowest
+// index; the label rides in the key so the winner's label needs no gather.
+//
+// Every kernel runs in two forms: one keyframe on the context's own buffers
+// (inputs read through the context's input block, so a captured graph can be
+// replayed on new inputs), or a batch of keyframes, blockIdx.y selecting the
+// keyframe's FrontRef.
 #include "internal.h"
 #include "scan_util.cuh"
 
@@ -20,147 +27,235 @@ namespace sg {
 
 namespace {
 
-__device__ __forceinline__ int px_from_yaw(const float* __restrict__ tab, float yaw, int W) {
-  if (isnan(yaw)) return W - 1;  // std::min/max with NaN keep the bound
-  float e = (yaw * 0.318309886f + 1.0f) * 0.5f * (float)W;
-  int k = (int)floorf(fminf(fmaxf(e, -1.0f), (float)W));
-  k = max(0, min(W - 1, k));
-  while (k < W - 1 && yaw >= __ldg(tab + k + 1)) ++k;
-  while (k > 0 && yaw < __ldg(tab + k)) --k;
+// Index k in [0, n-1] with tab[k] <= v < tab[k+1] (tab[0] = -inf, tab[n] =
+// +inf, non-decreasing), searched from the estimate e.
+__device__ __forceinline__ int table_index(const float* __restrict__ tab, float v, float e,
+                                           int n) {
+  int k = (int)floorf(fminf(fmaxf(e, -1.0f), (float)n));
+  k = max(0, min(n - 1, k));
+  while (k < n - 1 && v >= __ldg(tab + k + 1)) ++k;
+  while (k > 0 && v < __ldg(tab + k)) --k;
   return k;
 }
-
-__device__ __forceinline__ int py_from_pitch(float pitch, float fd_abs, float fov, int H) {
-  float t = fdiv(fadd(pitch, fd_abs), fov);
-  float y = fmul(fsub(1.0f, t), (float)H);  // (float)(1.0 - (double)t) == 1.0f - t
-  y = floorf(y);
-  y = (y < H - 1.0f) ? y : (H - 1.0f);       // std::min(H - 1.0f, y)
-  y = (0.0f < y) ? y : 0.0f;                 // std::max(0.0f, y)
-  return (int)y;
+// The index of v when the whole interval [v - m, v + m] has it, else -1.
+__device__ __forceinline__ int table_index_margin(const float* __restrict__ tab, float v,
+                                                  float m, float e, int n) {
+  const int k = table_index(tab, v - m, e, n);
+  return (k == n - 1 || v + m < __ldg(tab + k + 1)) ? k : -1;
+}
+// Column of a yaw: px_tab[k] = smallest yaw of column k (inference.cpp:111-121;
+// NaN: std::min/max keep the bound, W - 1).
+__device__ __forceinline__ float col_estimate(float yaw, int W) {
+  return (yaw * 0.318309886f + 1.0f) * 0.5f * (float)W;
+}
+// Row of a pitch: py_tab[k] = smallest pitch of row H-1-k (inference.cpp:
+// 112-126; NaN: row H - 1).
+__device__ __forceinline__ float row_estimate(float pitch, const KParams& kp) {
+  return (pitch + kp.fov_down_abs) * (1.0f / kp.fov) * (float)kp.img_h;
 }
 
-__global__ void __launch_bounds__(256) k_project(Dev d, KParams kp) {
+// The buffers of the keyframe this block works on.
+template <bool kBatch>
+__device__ __forceinline__ FrontRef front(const Dev& d, const FrontRef* refs, int kf0) {
+  if (kBatch) return refs[kf0 + blockIdx.y];
+  const InPtrs* in = d.in;
+  FrontRef f;
+  f.xyzi = in->xyzi;
+  f.plabel = in->plabel;
+  f.mask_in = in->mask_in;
+  f.pix = d.pix;
+  f.pkey = d.pkey;
+  f.range_img = d.range_img;
+  f.mask = d.mask;
+  f.tree = d.tree;
+  f.gbits = d.gbits;
+  f.blk = d.blk;
+  f.ground_idx = d.ground_idx;
+  f.ground = d.ground;
+  f.fe = nullptr;
+  return f;
+}
+// projection counters: the context's counters, or the keyframe's fe block
+template <bool kBatch>
+__device__ __forceinline__ int32_t* fe_slot(const Dev& d, const FrontRef& f, int which) {
+  if (kBatch) return f.fe + which;
+  return which == 0 ? &d.cnt->n_ground : which == 1 ? &d.cnt->overflow : &d.cnt->n_slow_px;
+}
+
+// Pixel keys are combined before the atomics: one atomicMin per distinct
+// pixel per warp, and for pixel (0, W-1) -- where every no-return (NaN)
+// point lands -- one per block through shared memory.  The minimum is the
+// same, so the winner is unchanged.
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontRef* refs,
+                                                 int kf0, int point_labels) {
+  __shared__ unsigned long long hot_min;
+  const FrontRef f = front<kBatch>(d, refs, kf0);
   const int N = d.N, W = kp.img_w, H = kp.img_h;
+  const int hot = N - 1;  // the pixel of NaN points: row H - 1, column W - 1
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) hot_min = ~0ull;
+  __syncthreads();
   int slow = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-    const float4 p = __ldcs(d.in->xyzi + i);
-    const float x = p.x, y = p.y, z = p.z;
-    const float range = fsqrt(fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z)));
-    // ---- column
-    int px;
-    {
-      float yaw = -atan2f(y, x);
-      bool need = !(isfinite(x) && isfinite(y)) || x == 0.0f || y == 0.0f;
-      if (!need) {
-        float m = fmaxf(fabsf(yaw) * 1.2e-6f, 1e-30f);
-        px = px_from_yaw(d.px_tab, yaw - m, W);
-        need = px != px_from_yaw(d.px_tab, yaw + m, W);
+  for (int i0 = blockIdx.x * blockDim.x; i0 < N; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    const bool valid = i < N;
+    int pix = -1;
+    unsigned long long key = ~0ull;
+    if (valid) {
+      const float4 p = f.xyzi[i];  // kept in L2 for k_label
+      const uint32_t lab = point_labels ? f.plabel[i] : 0u;
+      const float x = p.x, y = p.y, z = p.z;
+      const float range = fsqrt(fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z)));
+      // ---- column
+      int px;
+      {
+        float yaw = -atan2f(y, x);
+        // NaN in, NaN out on both paths: no-return points stay on the fast path.
+        const bool nan_in = isnan(x) || isnan(y);
+        if (nan_in) {
+          px = W - 1;
+        } else {
+          px = -1;
+          if (!(isinf(x) || isinf(y) || x == 0.0f || y == 0.0f))
+            px = table_index_margin(d.px_tab, yaw, fmaxf(fabsf(yaw) * 1.2e-6f, 1e-30f),
+                                    col_estimate(yaw, W), W);
+          if (px < 0) {
+            yaw = -(float)atan2((double)y, (double)x);
+            px = table_index(d.px_tab, yaw, col_estimate(yaw, W), W);
+            ++slow;
+          }
+        }
       }
-      if (need) {
-        yaw = -(float)atan2((double)y, (double)x);
-        px = px_from_yaw(d.px_tab, yaw, W);
-        ++slow;
+      // ---- row
+      int py;
+      {
+        const float q = fdiv(z, range);
+        float pitch = asinf(q);
+        if (isnan(q)) {
+          py = H - 1;
+        } else {
+          int g = -1;
+          if (fabsf(q) < 1.0f)
+            g = table_index_margin(d.py_tab, pitch, fmaxf(fabsf(pitch) * 1.2e-6f, 1e-30f),
+                                   row_estimate(pitch, kp), H);
+          if (g < 0) {
+            pitch = (float)asin((double)q);
+            g = table_index(d.py_tab, pitch, row_estimate(pitch, kp), H);
+            ++slow;
+          }
+          py = H - 1 - g;
+        }
       }
+      pix = py * W + px;
+      f.pix[i] = pix;
+      key = ((unsigned long long)range_key(range) << 32) | ((uint32_t)i << 8) | lab;
     }
-    // ---- row
-    int py;
-    {
-      const float q = fdiv(z, range);
-      float pitch = asinf(q);
-      bool need = !(fabsf(q) < 1.0f);
-      if (!need) {
-        float m = fmaxf(fabsf(pitch) * 1.2e-6f, 1e-30f);
-        py = py_from_pitch(pitch - m, kp.fov_down_abs, kp.fov, H);
-        need = py != py_from_pitch(pitch + m, kp.fov_down_abs, kp.fov, H);
-      }
-      if (need) {
-        pitch = (float)asin((double)q);
-        py = py_from_pitch(pitch, kp.fov_down_abs, kp.fov, H);
-        ++slow;
-      }
+    const unsigned peers = __match_any_sync(0xffffffffu, pix);
+    const uint32_t hi = (uint32_t)(key >> 32);
+    const uint32_t hmin = __reduce_min_sync(peers, hi);
+    const uint32_t lmin = __reduce_min_sync(peers, hi == hmin ? (uint32_t)key : 0xffffffffu);
+    if (valid && lane == __ffs(peers) - 1) {
+      const unsigned long long kmin = ((unsigned long long)hmin << 32) | lmin;
+      if (pix == hot)
+        atomicMin(&hot_min, kmin);
+      else
+        atomicMin(f.pkey + pix, kmin);
     }
-    const int pix = py * W + px;
-    d.pix[i] = pix;
-    const unsigned long long key = ((unsigned long long)range_key(range) << 32) | (uint32_t)i;
-    atomicMin(d.pkey + pix, key);
   }
+  __syncthreads();
+  if (threadIdx.x == 0 && hot_min != ~0ull) atomicMin(f.pkey + hot, hot_min);
   slow = warp_sumi(slow);
-  if ((threadIdx.x & 31) == 0 && slow) atomicAdd(&d.cnt->n_slow_px, slow);
+  if (lane == 0 && slow) atomicAdd(fe_slot<kBatch>(d, f, 2), slow);
 }
 
-// Per pixel: range image and mask from the winner; re-arms the winner key.
-__global__ void __launch_bounds__(256) k_resolve(Dev d, int point_labels) {
-  const int N = d.N;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
-    const unsigned long long key = d.pkey[p];
-    d.pkey[p] = ~0ull;
-    float r = 0.0f;
-    uint8_t m = 0;
-    if (key != ~0ull) {
-      r = __uint_as_float((uint32_t)(key >> 32));
-      if (point_labels) m = d.in->plabel[(uint32_t)key];
-    }
-    if (!point_labels) m = d.in->mask_in[p];
-    d.range_img[p] = r;
-    d.mask[p] = m;
-  }
+// Label of pixel `pix`'s winner: the point label carried in the key of the
+// nearest point (the pixel holds at least the caller's point), or the given
+// mask image.
+__device__ __forceinline__ uint8_t pixel_label(const FrontRef& f, int pix, int point_labels) {
+  if (!point_labels) return f.mask_in[pix];
+  return (uint8_t)f.pkey[pix];
 }
 
-// maskCloud: organised tree cloud (with the Ouster destagger as a gather:
-// even rows take x,y,z from column c-32 for c >= 32 and keep their own
-// intensity; inference.cpp:200-228) and the ground membership bits.
-__global__ void __launch_bounds__(1024) k_mask(Dev d, KParams kp) {
+// Thread o is pixel o and point o.  Pixel: range image and mask from the
+// winner.  Point: maskCloud -- the organised tree cloud (with the Ouster
+// destagger as a gather: even rows take x,y,z from column c-32 for c >= 32
+// and keep their own intensity; inference.cpp:200-228) and the ground bit,
+// both from the label of the point's pixel.
+template <bool kBatch>
+__global__ void __launch_bounds__(1024) k_label(Dev d, KParams kp, const FrontRef* refs, int kf0,
+                                                int point_labels) {
   __shared__ int sm[33];
+  const FrontRef f = front<kBatch>(d, refs, kf0);
   const int N = d.N, W = kp.img_w;
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   bool ground = false;
   if (o < N) {
-    const uint8_t mo = d.mask[d.pix[o]];
+    const unsigned long long key = f.pkey[o];
+    float r = 0.0f;
+    uint8_t m = 0;
+    if (key != ~0ull) {
+      r = __uint_as_float((uint32_t)(key >> 32));
+      if (point_labels) m = (uint8_t)key;
+    }
+    if (!point_labels) m = f.mask_in[o];
+    f.range_img[o] = r;
+    f.mask[o] = m;
+
+    const uint8_t mo = pixel_label(f, f.pix[o], point_labels);
     ground = (mo == 1);
     const float nan = __int_as_float(0x7fc00000);
-    const float4* X = d.in->xyzi;
+    const float4* X = f.xyzi;
     float4 src = X[o];
     float4 t = (mo == 255) ? src : make_float4(nan, nan, nan, 0.0f);
     const int row = o / W, c = o - row * W;
     if (kp.do_destagger && (row & 1) == 0 && c >= 32) {
       const int s = o - 32;
-      const uint8_t ms = d.mask[d.pix[s]];
+      const uint8_t ms = pixel_label(f, f.pix[s], point_labels);
       float4 q = X[s];
       t.x = (ms == 255) ? q.x : nan;
       t.y = (ms == 255) ? q.y : nan;
       t.z = (ms == 255) ? q.z : nan;
     }
-    d.tree[o] = t;
+    f.tree[o] = t;
   }
   const unsigned b = __ballot_sync(0xffffffffu, ground);
-  if ((threadIdx.x & 31) == 0 && o < N + 31) d.gbits[o >> 5] = b;
+  if ((threadIdx.x & 31) == 0 && o < N + 31) f.gbits[o >> 5] = b;
   int total;
   block_excl_scan(ground ? 1 : 0, sm, &total);
-  if (threadIdx.x == 0) d.blk[blockIdx.x] = total;
+  if (threadIdx.x == 0) f.blk[blockIdx.x] = total;
 }
 
-// Ordered compaction of the ground points (point order).
-__global__ void __launch_bounds__(1024) k_ground_compact(Dev d) {
+// Ordered compaction of the ground points (point order); re-arms the pixel
+// keys for the next scan.
+template <bool kBatch>
+__global__ void __launch_bounds__(1024) k_ground_compact(Dev d, const FrontRef* refs, int kf0) {
   __shared__ int sm[33];
+  const FrontRef f = front<kBatch>(d, refs, kf0);
   const int N = d.N;
-  const int base = block_sum_prefix(d.blk, blockIdx.x, sm);
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned b = (o < N + 31) ? d.gbits[o >> 5] : 0u;
+  const unsigned b = (o < N + 31) ? f.gbits[o >> 5] : 0u;
   const bool g = o < N && ((b >> (threadIdx.x & 31)) & 1u);
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (g) v = f.xyzi[o];  // issued before the prefix sums
+  if (o < N) f.pkey[o] = ~0ull;
+  const int base = block_sum_prefix(f.blk, blockIdx.x, sm);
   int total;
   const int ex = block_excl_scan(g ? 1 : 0, sm, &total);
   const int pos = base + ex;
   if (g) {
-    d.ground_idx[pos] = o;
-    if (pos < d.cap_ground) d.ground[pos] = d.in->xyzi[o];
+    f.ground_idx[pos] = o;
+    if (pos < d.cap_ground) f.ground[pos] = v;
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
     const int n = base + total;
-    d.cnt->n_ground = n < d.cap_ground ? n : d.cap_ground;
-    if (n > d.cap_ground) atomicOr(&d.cnt->overflow, 1);
+    *fe_slot<kBatch>(d, f, 0) = n < d.cap_ground ? n : d.cap_ground;
+    if (n > d.cap_ground) atomicOr(fe_slot<kBatch>(d, f, 1), 1);
   }
 }
 
+// Per-keyframe counter reset.  A keyframe whose projection ran in a batch
+// launch takes the counts of that launch from its fe block.
 __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster) {
   Counters* c = d.cnt;
   const int n_prev = c->n_prev;
@@ -169,6 +264,12 @@ __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_c
   __syncthreads();
   if (threadIdx.x == 0) {
     c->n_prev = n_prev;
+    const int32_t* fe = d.in->fe;
+    if (fe) {
+      c->n_ground = fe[0];
+      c->overflow = fe[1];
+      c->n_slow_px = fe[2];
+    }
     if (n_ground >= 0) c->n_ground = n_ground;
     if (n_lm >= 0) c->n_lm = n_lm;
     if (n_v >= 0) c->n_v = n_v;
@@ -179,6 +280,9 @@ __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_c
 
 }  // namespace
 
+size_t front_gbits_words(int N) { return (size_t)((N + 1023) / 1024) * 32 + 32; }
+int front_blocks(int N) { return (N + 1023) / 1024; }
+
 int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster,
                  cudaStream_t st) {
   k_begin<<<1, 64, 0, st>>>(d, n_ground, n_lm, n_v, n_p, n_cluster);
@@ -186,23 +290,29 @@ int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_c
 }
 
 int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
-  k_project<<<(d.N + 255) / 256, 256, 0, st>>>(d, kp);
+  k_project<false><<<(d.N + 255) / 256, 256, 0, st>>>(d, kp, nullptr, 0, 1);
   return 1;
 }
-int launch_resolve_kernel(const Dev& d, bool point_labels, cudaStream_t st) {
-  k_resolve<<<(d.N + 255) / 256, 256, 0, st>>>(d, point_labels ? 1 : 0);
-  return 1;
+int launch_project_rest(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st) {
+  const int g1k = front_blocks(d.N);
+  k_label<false><<<g1k, 1024, 0, st>>>(d, kp, nullptr, 0, point_labels ? 1 : 0);
+  k_ground_compact<false><<<g1k, 1024, 0, st>>>(d, nullptr, 0);
+  return 2;
 }
 
 int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st) {
-  const int N = d.N;
-  const int g256 = (N + 255) / 256;
-  k_project<<<g256, 256, 0, st>>>(d, kp);
-  k_resolve<<<g256, 256, 0, st>>>(d, point_labels ? 1 : 0);
-  const int g1k = (N + 1023) / 1024;
-  k_mask<<<g1k, 1024, 0, st>>>(d, kp);
-  k_ground_compact<<<g1k, 1024, 0, st>>>(d);
-  return 4;
+  k_project<false><<<(d.N + 255) / 256, 256, 0, st>>>(d, kp, nullptr, 0, point_labels ? 1 : 0);
+  return 1 + launch_project_rest(d, kp, point_labels, st);
+}
+
+int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, int kf0,
+                         int nkf, bool point_labels, cudaStream_t st) {
+  if (nkf <= 0) return 0;
+  const dim3 g256((d.N + 255) / 256, nkf), g1k(front_blocks(d.N), nkf);
+  k_project<true><<<g256, 256, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
+  k_label<true><<<g1k, 1024, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
+  k_ground_compact<true><<<g1k, 1024, 0, st>>>(d, refs, kf0);
+  return 3;
 }
 
 }  // namespace sg

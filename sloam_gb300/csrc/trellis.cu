@@ -42,16 +42,18 @@ __device__ __forceinline__ uint32_t cc_find(volatile uint32_t* P, uint32_t x) {
 }
 
 __global__ void __launch_bounds__(256) k_cc_init(Dev d) {
+  const float4* __restrict__ tree = d.in->tree;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.N; p += gridDim.x * blockDim.x)
-    d.parent[p] = isfinite(d.tree[p].x) ? (uint32_t)p : kInvalid;
+    d.parent[p] = isfinite(tree[p].x) ? (uint32_t)p : kInvalid;
 }
 
 __global__ void __launch_bounds__(256) k_cc_union(Dev d, float thr) {
   volatile uint32_t* P = d.parent;
+  const float4* __restrict__ tree = d.in->tree;
   const int W = d.W;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.N; p += gridDim.x * blockDim.x) {
     if (d.parent[p] == kInvalid) continue;
-    const float4 a = d.tree[p];
+    const float4 a = tree[p];
     const int col = p % W;
     for (int e = 0; e < 2; ++e) {
       int q;
@@ -62,7 +64,7 @@ __global__ void __launch_bounds__(256) k_cc_union(Dev d, float thr) {
         if (p < W) continue;
         q = p - W;
       }
-      const float4 b = d.tree[q];
+      const float4 b = tree[q];
       if (!isfinite(b.x) || !cc_close(a, b, thr)) continue;
       uint32_t u = (uint32_t)p, v = (uint32_t)q;
       int it = 0;
@@ -235,6 +237,7 @@ __device__ __forceinline__ bool zless(float4 a, int ia, float4 b, int ib) {
 __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
   __shared__ float4 spts[kVtxWarps][kVtxCap];
   __shared__ int srank[kVtxWarps][kVtxCap];
+  const float4* __restrict__ tree = d.in->tree;
   const int H = d.H;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nitems = d.cnt->n_cand * H;
@@ -252,9 +255,9 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
     const bool inshm = n <= kVtxCap;
     float4* P = spts[w];
     if (inshm)
-      for (int j = lane; j < n; j += 32) P[j] = d.tree[d.bucket[off + j]];
+      for (int j = lane; j < n; j += 32) P[j] = tree[d.bucket[off + j]];
     __syncwarp();
-    auto pt = [&](int j) -> float4 { return inshm ? P[j] : d.tree[d.bucket[off + j]]; };
+    auto pt = [&](int j) -> float4 { return inshm ? P[j] : tree[d.bucket[off + j]]; };
     const int mid = n / 2;  // (int)(n / 2.0)
     // per-axis medians by rank
     float mx = __int_as_float(0x7fc00000), my = mx, mz = mx;
@@ -483,6 +486,7 @@ __global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
 // vertex for the kept points, one thread per bucket slot for the cluster
 // points (raster order; the candidate of a slot found by binary search).
 __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
+  const float4* __restrict__ tree = d.in->tree;
   const int H = d.H;
   const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
     }
     const int l = d.cand_lm[lo];
     if (l < 0) continue;
-    d.lm_cpts[d.lm_cbeg[l] + (q - d.roff[lo * H])] = d.tree[d.bucket[q]];
+    d.lm_cpts[d.lm_cbeg[l] + (q - d.roff[lo * H])] = tree[d.bucket[q]];
   }
 }
 

@@ -69,6 +69,11 @@ def load(path=LIB_PATH):
     L.sloam_last_launch_count.restype = C.c_int64
     L.sloam_stream.argtypes = [vp]
     L.sloam_stream.restype = vp
+    # profiling hooks (not in the public header)
+    L.sloam_profile_stages.argtypes = [vp, C.POINTER(C.c_float), C.c_int]
+    L.sloam_time_kernel.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
+    L.sloam_frontend_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32)]
     _lib = L
     return L
 

@@ -75,8 +75,9 @@ def test_boundary_tables_reproduce_oracle_pixels_and_bins(L):
     tb = np.zeros(P.ground_theta_bins + 1, np.float32)
     rb = np.zeros(P.ground_radii_bins + 1, np.float32)
     lohi = np.zeros(2, np.float32)
+    ptab = np.zeros(P.img_h + 1, np.float32)
     L.sloam_internal_tables(C.byref(P), A.ptr(tab, C.c_float), A.ptr(tb, C.c_float),
-                            A.ptr(rb, C.c_float), A.ptr(lohi, C.c_float))
+                            A.ptr(rb, C.c_float), A.ptr(lohi, C.c_float), A.ptr(ptab, C.c_float))
     assert np.all(np.diff(tab[1:-1]) > 0)
     rng = np.random.default_rng(5)
     n = P.img_w * P.img_h
@@ -87,6 +88,13 @@ def test_boundary_tables_reproduce_oracle_pixels_and_bins(L):
     yaw = -np.arctan2(xyzi[:, 1].astype(np.float64), xyzi[:, 0].astype(np.float64)).astype(np.float32)
     px = np.searchsorted(tab[1:P.img_w], yaw, side="right")
     np.testing.assert_array_equal(px, o["px"])
+    # rows: pitch = float asin of the float z / range, row from the table
+    x, y, z = xyzi[:, 0], xyzi[:, 1], xyzi[:, 2]
+    rng3 = np.sqrt((x * x + y * y) + z * z)
+    pitch = np.arcsin((z / rng3).astype(np.float64)).astype(np.float32)
+    assert np.all(np.diff(ptab[1:-1]) >= 0)
+    py = P.img_h - 1 - np.searchsorted(ptab[1:P.img_h], pitch, side="right")
+    np.testing.assert_array_equal(py, o["py"])
     # ground bins: theta from the float atan2, radius window in double
     x, y = xyzi[:, 0], xyzi[:, 1]
     r = np.sqrt(x * x + y * y).astype(np.float32)

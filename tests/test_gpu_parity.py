@@ -282,49 +282,84 @@ def test_keyframe_synthetic_c2(two_step, cyl_mode):
     assert np.linalg.norm(t - kfs[0].t_gt) < 0.1
 
 
-def test_keyframes_device_batch_matches_single():
+def _first_scan(ctx, P, kf0, mapc, n_map):
+    r = A.RunBuffers(P)
+    ctx.check(ctx.L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), len(kf0.xyzi),
+                                   A.ptr(kf0.labels, C.c_uint8), None,
+                                   C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, n_map,
+                                   C.byref(r.s)))
+
+
+def _single_results(P, kfs, mapc, n_map):
+    """Each keyframe alone through sloam_keyframe on a fresh context whose
+    first scan is keyframe 0 at its true pose: (q, t, n_cylinders, success)."""
+    out = []
+    for kf in kfs:
+        ctx = make_ctx(P)
+        _first_scan(ctx, P, kfs[0], mapc, n_map)
+        r1 = A.RunBuffers(P)
+        st = ctx.L.sloam_keyframe(ctx.h, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                  A.ptr(kf.labels, C.c_uint8), None,
+                                  C.byref(A.SE3.from_qt(*kf.pose_est_qt())), mapc, n_map,
+                                  C.byref(r1.s))
+        r1.refresh()
+        q, t = r1.s.T_Map_Curr.qt()
+        out.append((q, t, r1.s.models.n_cylinders, 1 if st == 0 and r1.s.success else 0))
+        ctx.close()
+    return out
+
+
+def _check_batch(po, succ, ncyl, order, ref):
+    for k, j in enumerate(order):
+        q, t, nc, ok = ref[j]
+        np.testing.assert_array_equal(po[k, :4], q)
+        np.testing.assert_array_equal(po[k, 4:], t)
+        assert int(ncyl[k]) == nc
+        assert int(succ[k]) == ok
+
+
+def test_keyframes_batches_match_single():
+    """Batches through the device and the host entry points: 37 keyframes
+    (several batch projection launches, the last one partial) over five
+    slots, each result bit-identical to the keyframe run alone."""
     import torch
     cfg, forest, kfs = H.scene("C2", seed=0, n_kf=3)
     P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1)
-    ctx = make_ctx(P)
+    P.batch_slots = 5
     mapa = forest.map_cylinders()
     mapc = A.cylinders_from_array(mapa)
-    # first scan (true pose of keyframe 0) defines the previous planes
-    r = A.RunBuffers(P)
-    kf0 = kfs[0]
-    ctx.check(ctx.L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), len(kf0.xyzi),
-                                   A.ptr(kf0.labels, C.c_uint8), None,
-                                   C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, len(mapa),
-                                   C.byref(r.s)))
-    n = len(kf0.xyzi)
-    dx = torch.from_numpy(np.stack([k.xyzi for k in kfs])).cuda()
-    dl = torch.from_numpy(np.stack([k.labels for k in kfs])).cuda()
+    nm = len(mapa)
+    ref = _single_results(P, kfs, mapc, nm)
+    ctx = make_ctx(P)
+    _first_scan(ctx, P, kfs[0], mapc, nm)
+    B = 37
+    order = [k % len(kfs) for k in range(B)]
+    n = len(kfs[0].xyzi)
+    xs = np.stack([kfs[j].xyzi for j in order])
+    ls = np.stack([kfs[j].labels for j in order])
+    poses = (A.SE3 * B)(*[A.SE3.from_qt(*kfs[j].pose_est_qt()) for j in order])
+    dx = torch.from_numpy(xs).cuda()
+    dl = torch.from_numpy(ls).cuda()
     dm = torch.from_numpy(np.frombuffer(bytes(mapc), np.uint8).copy()).cuda()
-    poses = (A.SE3 * len(kfs))(*[A.SE3.from_qt(*k.pose_est_qt()) for k in kfs])
-    pose_out = torch.zeros(len(kfs) * 7, dtype=torch.float64, device="cuda")
-    succ = torch.zeros(len(kfs), dtype=torch.int32, device="cuda")
-    ncyl = torch.zeros(len(kfs), dtype=torch.int32, device="cuda")
-    ctx.check(ctx.L.sloam_keyframes_device(ctx.h, dx.data_ptr(), n, len(kfs), dl.data_ptr(),
-                                           poses, dm.data_ptr(), len(mapa), pose_out.data_ptr(),
-                                           succ.data_ptr(), ncyl.data_ptr()))
-    torch.cuda.synchronize()
-    po = pose_out.cpu().numpy().reshape(-1, 7)
-    # the same keyframes one by one through the host API (state restored)
-    for k, kf in enumerate(kfs):
-        ctx2 = make_ctx(P)
-        r0 = A.RunBuffers(P)
-        ctx2.check(ctx2.L.sloam_keyframe(ctx2.h, A.ptr(kf0.xyzi, C.c_float), n,
-                                         A.ptr(kf0.labels, C.c_uint8), None,
-                                         C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc,
-                                         len(mapa), C.byref(r0.s)))
-        r1 = A.RunBuffers(P)
-        st = ctx2.L.sloam_keyframe(ctx2.h, A.ptr(kf.xyzi, C.c_float), n,
-                                   A.ptr(kf.labels, C.c_uint8), None,
-                                   C.byref(A.SE3.from_qt(*kf.pose_est_qt())), mapc, len(mapa),
-                                   C.byref(r1.s))
-        r1.refresh()
-        q, t = r1.s.T_Map_Curr.qt()
-        np.testing.assert_array_equal(po[k, :4], q)
-        np.testing.assert_array_equal(po[k, 4:], t)
-        assert int(ncyl[k]) == r1.s.models.n_cylinders
-        assert int(succ[k]) == (1 if st == 0 and r1.s.success else 0)
+    pose_out = torch.zeros(B * 7, dtype=torch.float64, device="cuda")
+    succ = torch.zeros(B, dtype=torch.int32, device="cuda")
+    ncyl = torch.zeros(B, dtype=torch.int32, device="cuda")
+    for _ in range(2):  # the second call reuses the batch buffers and graphs
+        pose_out.zero_()
+        ctx.check(ctx.L.sloam_keyframes_device(ctx.h, dx.data_ptr(), n, B, dl.data_ptr(), poses,
+                                               dm.data_ptr(), nm, pose_out.data_ptr(),
+                                               succ.data_ptr(), ncyl.data_ptr()))
+        torch.cuda.synchronize()
+        _check_batch(pose_out.cpu().numpy().reshape(-1, 7), succ.cpu(), ncyl.cpu(), order, ref)
+    h_pose = np.zeros(B * 7, np.float64)
+    h_succ = np.zeros(B, np.int32)
+    h_ncyl = np.zeros(B, np.int32)
+    ctx.check(ctx.L.sloam_keyframes_host(ctx.h, A.ptr(xs, C.c_float), n, B,
+                                         A.ptr(ls, C.c_uint8), poses, mapc, nm,
+                                         h_pose.ctypes.data, h_succ.ctypes.data,
+                                         h_ncyl.ctypes.data))
+    _check_batch(h_pose.reshape(-1, 7), h_succ, h_ncyl, order, ref)
+    ms, nch, nkf = C.c_float(), C.c_int32(), C.c_int32()
+    ctx.check(ctx.L.sloam_frontend_time(ctx.h, C.byref(ms), C.byref(nch), C.byref(nkf)))
+    assert nkf.value == B and nch.value >= 2 and ms.value > 0
+    ctx.close()
