@@ -43,12 +43,31 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "keyframes/s at 64x2048 (plain GPU RANSAC path, 150 trees, 400-landmark submap)"
+METRIC = "keyframes/s at 64\u00d72048: learned-proposal vs plain RANSAC, equal cylinder error"
 UNIT = "keyframes/s"
+WORKLOAD = ("C2: 64x2048 keyframes, 150 trees, 400-landmark submap, 256 hyp + 3 LS per tree, "
+            "10 GN iterations; plain GPU RANSAC path (the learned proposal is not built)")
 # DRAM bytes (read + write) per keyframe of the batch projection stage, summed
 # over its four kernels in one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum); None until captured.
 FRONT_TRAFFIC_PER_KF = None
+
+
+def max_over_ranks(x, device=None):
+    """The maximum of x over the ranks of the job (the slowest rank's time is
+    the job's time); x itself without a process group."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()):
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(batch, steps, world, total_ms):
+    """Whole-job keyframes/s: every rank processed batch * steps keyframes."""
+    return batch * steps * world / (total_ms / 1000.0)
 
 
 def parse():
@@ -217,8 +236,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": "C2 64x2048 keyframe, 150 trees, 400-landmark "
-                                        "submap, 256 hyp + 3 LS, 10 GN", "threads": threads},
+        "data": "synthetic", "config": {"workload": WORKLOAD, "threads": threads},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -314,12 +332,8 @@ def main():
     if dist:
         tdist.barrier()
     ck = clocks.stop()
-    total_ms = sum(a.elapsed_time(b) for a, b in evs)
-    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-    if dist:
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-    total_ms = float(t.item())
-    value = B * args.steps * world / (total_ms / 1000.0)
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), dev)
+    value = job_value(B, args.steps, world, total_ms)
     ok = int(succ.sum().item())
     n_cyl = ncyl.cpu().numpy()
 
@@ -395,8 +409,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "C2: 64x2048 keyframes, 150 trees, 400-landmark submap, "
-                                   "256 hyp + 3 LS per tree, 10 GN iterations",
+            "config": {"workload": WORKLOAD,
                        "batch_keyframes": B, "distinct_scans": args.distinct,
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{world}"},

@@ -234,6 +234,23 @@ int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose_estimate,
                          const sloam_landmarks* landmarks,
                          sloam_models_out* out);
 
+/* Plane::Plane(points, fmParams) (plane.cpp:3-17, computeModel :96-128):
+ * the plane of all n points (float centroid, smallest-eigenvalue normal,
+ * sign canonical n_z > 0), valid iff n >= num_ground_features (no gates;
+ * those belong to computeModels).  features [num_ground_features*4]
+ * receives the first points (may be NULL).  n <= max_ground. */
+int sloam_fit_plane(sloam_ctx* ctx, const float* xyzi, int32_t n, sloam_plane* out,
+                    float* features);
+
+/* Cylinder::Cylinder(vertices, gplane, fmParams) (cylinder.cpp:3-28) for
+ * every landmark, each against the nearest of the given planes
+ * (sloam.cpp:414-435 with the planes supplied instead of binned from a
+ * ground cloud).  out->planes echoes the given planes; out->cylinders holds
+ * the valid cylinders in landmark order.  n_planes <= radii_bins*theta_bins. */
+int sloam_fit_cylinders(sloam_ctx* ctx, const sloam_landmarks* landmarks,
+                        const sloam_plane* planes, int32_t n_planes,
+                        sloam_models_out* out);
+
 /* --------------------------------------------- a9-a11: RunSloam        */
 /* sloam::sloam::RunSloam (sloam.cpp:453-532): computeModels, first-scan
  * logic, matchFeatures (sloam.cpp:257-296), OptimizePose /

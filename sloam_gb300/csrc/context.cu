@@ -839,6 +839,58 @@ extern "C" int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose,
   return download_models(ctx, out);
 }
 
+extern "C" int sloam_fit_plane(sloam_ctx* ctx, const float* xyzi, int32_t n, sloam_plane* out,
+                               float* features) {
+  if (!ctx || !out || n < 0 || (n > 0 && !xyzi)) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  if (n > d.cap_ground) return fail(ctx, SLOAM_ERR_CAPACITY, "more points than max_ground");
+  int st = upload_ground(ctx, xyzi, n);
+  if (st || (st = set_inputs(ctx, nullptr, nullptr, nullptr, nullptr, 0))) return st;
+  int k = launch_begin(d, n, -1, -1, -1, -1, ctx->st);
+  k += launch_plane_points(d, ctx->kp, n, ctx->st);
+  ctx->last_launches = k;
+  if ((st = sync_counters(ctx))) return st;
+  PlaneD pl;
+  CK(cudaMemcpy(&pl, d.plane_all, sizeof(PlaneD), cudaMemcpyDeviceToHost));
+  for (int j = 0; j < 4; ++j) out->plane[j] = pl.plane[j];
+  for (int j = 0; j < 3; ++j) out->centroid[j] = pl.centroid[j];
+  out->bin = pl.bin;
+  out->valid = pl.valid;
+  if (features && pl.valid && d.G > 0)
+    CK(cudaMemcpy(features, d.plane_feat_all, sizeof(float4) * d.G, cudaMemcpyDeviceToHost));
+  return SLOAM_OK;
+}
+
+extern "C" int sloam_fit_cylinders(sloam_ctx* ctx, const sloam_landmarks* lm,
+                                   const sloam_plane* planes, int32_t n_planes,
+                                   sloam_models_out* out) {
+  if (!ctx || !lm || !out || n_planes < 0 || (n_planes > 0 && !planes)) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  Dev& d = ctx->d;
+  if (n_planes > d.n_bins) return fail(ctx, SLOAM_ERR_CAPACITY, "more planes than ground bins");
+  int nl, nv, np, ncl;
+  int st = upload_landmarks(ctx, lm, &nl, &nv, &np, &ncl);
+  if (st || (st = set_inputs(ctx, nullptr, nullptr, nullptr, nullptr, 0))) return st;
+  std::vector<PlaneD> pl(std::max(1, (int)n_planes));
+  for (int k = 0; k < n_planes; ++k) {
+    for (int j = 0; j < 4; ++j) pl[k].plane[j] = planes[k].plane[j];
+    for (int j = 0; j < 3; ++j) pl[k].centroid[j] = planes[k].centroid[j];
+    pl[k].bin = planes[k].bin;
+    pl[k].valid = 1;
+  }
+  int k = launch_begin(d, 0, nl, nv, np, ncl, ctx->st);
+  if (n_planes)
+    CK(cudaMemcpyAsync(d.planes, pl.data(), sizeof(PlaneD) * n_planes, cudaMemcpyHostToDevice,
+                       ctx->st));
+  CK(cudaMemcpyAsync(&d.cnt->n_planes, &n_planes, sizeof(int32_t), cudaMemcpyHostToDevice,
+                     ctx->st));
+  k += launch_cylinders(d, ctx->kp, false, ctx->st);
+  ctx->last_launches = k;
+  if ((st = sync_counters(ctx))) return st;
+  return download_models(ctx, out);
+}
+
 // ---------------------------------------------------------------- a9-a11
 extern "C" int sloam_run(sloam_ctx* ctx, const sloam_se3* pose, const float* ground_xyzi,
                          int32_t n_ground, const sloam_landmarks* lm, const sloam_cylinder* map,

@@ -216,6 +216,10 @@ int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_sta
                cudaStream_t st);
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trellis,
                                cudaStream_t st);
+// a6 alone: cylinders of the landmarks against the planes already in d.planes
+int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
+// Plane(points) of the n points of the ground view into plane_all[0]
+int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st);
 
 // single kernels, for isolated timing (profiling hooks)
 int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st);

@@ -245,6 +245,61 @@ __device__ void bitonic_sort(unsigned long long* a, int n2) {
   }
 }
 
+// Plane::computeModel (plane.cpp:96-128) over points at(0..n-1) by the whole
+// block: float centroid accumulated sequentially in feature order
+// (utils.h:14-28), FP64 scatter about it, normal = eigenvector of the
+// smallest eigenvalue (FP32 Jacobi), sign canonical (n_z > 0, then n_y, n_x),
+// d = -n.c.  `cen` (3 floats) and `red` (6 * 32 doubles) are shared memory;
+// the model lands in `out` of thread 0.
+template <typename At>
+__device__ void fit_plane_block(At at, int n, float* cen, double* red, PlaneD& out) {
+  if (threadIdx.x == 0) {
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int i = 0; i < n; ++i) {
+      const float4 p = at(i);
+      sx = fadd(sx, p.x);
+      sy = fadd(sy, p.y);
+      sz = fadd(sz, p.z);
+    }
+    cen[0] = (float)((double)sx / (double)n);
+    cen[1] = (float)((double)sy / (double)n);
+    cen[2] = (float)((double)sz / (double)n);
+  }
+  __syncthreads();
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float4 p = at(i);
+    const double a0 = (double)fsub(p.x, cen[0]), a1 = (double)fsub(p.y, cen[1]),
+                 a2 = (double)fsub(p.z, cen[2]);
+    s[0] += a0 * a0; s[1] += a0 * a1; s[2] += a0 * a2;
+    s[3] += a1 * a1; s[4] += a1 * a2; s[5] += a2 * a2;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = 0; j < 6; ++j) {
+    const double v = warp_sumd(s[j]);
+    if (lane == 0) red[j * 32 + w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S6[6];
+    for (int j = 0; j < 6; ++j) {
+      double t = 0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[j * 32 + q];
+      S6[j] = t;
+    }
+    const float S[9] = {(float)S6[0], (float)S6[1], (float)S6[2], (float)S6[1], (float)S6[3],
+                        (float)S6[4], (float)S6[2], (float)S6[4], (float)S6[5]};
+    float ev[3], V[9];
+    jacobi3f(S, ev, V);
+    d3 nrm = mk3(V[0], V[3], V[6]);
+    const bool flip = nrm.z < 0 || (nrm.z == 0 && (nrm.y < 0 || (nrm.y == 0 && nrm.x < 0)));
+    if (flip) nrm = scl3(-1.0, nrm);
+    const double dd = -(nrm.x * cen[0] + nrm.y * cen[1] + nrm.z * cen[2]);
+    out.plane[0] = nrm.x; out.plane[1] = nrm.y; out.plane[2] = nrm.z; out.plane[3] = dd;
+    out.centroid[0] = cen[0]; out.centroid[1] = cen[1]; out.centroid[2] = cen[2];
+  }
+}
+
 // One block per bin: retained points, plane model, gates, features.
 __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
   __shared__ unsigned long long keys[kBinCap];
@@ -319,51 +374,9 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
   __syncthreads();
   const bool enough = kk > 0 && kk >= kp.G && kk >= 3;
   if (enough) {
-    // float centroid, sequential in feature order (utils.h:14-28)
+    fit_plane_block([&](int i) { return ground[(uint32_t)keys[i]]; }, kk, cen, red, out);
     if (threadIdx.x == 0) {
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      for (int i = 0; i < kk; ++i) {
-        const float4 p = ground[(uint32_t)keys[i]];
-        sx = fadd(sx, p.x);
-        sy = fadd(sy, p.y);
-        sz = fadd(sz, p.z);
-      }
-      cen[0] = (float)((double)sx / (double)kk);
-      cen[1] = (float)((double)sy / (double)kk);
-      cen[2] = (float)((double)sz / (double)kk);
-    }
-    __syncthreads();
-    double s[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = threadIdx.x; i < kk; i += blockDim.x) {
-      const float4 p = ground[(uint32_t)keys[i]];
-      const double a0 = (double)fsub(p.x, cen[0]), a1 = (double)fsub(p.y, cen[1]),
-                   a2 = (double)fsub(p.z, cen[2]);
-      s[0] += a0 * a0; s[1] += a0 * a1; s[2] += a0 * a2;
-      s[3] += a1 * a1; s[4] += a1 * a2; s[5] += a2 * a2;
-    }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int j = 0; j < 6; ++j) {
-      const double v = warp_sumd(s[j]);
-      if (lane == 0) red[j * 32 + w] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double S6[6];
-      for (int j = 0; j < 6; ++j) {
-        double t = 0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[j * 32 + q];
-        S6[j] = t;
-      }
-      const float S[9] = {(float)S6[0], (float)S6[1], (float)S6[2], (float)S6[1], (float)S6[3],
-                          (float)S6[4], (float)S6[2], (float)S6[4], (float)S6[5]};
-      float ev[3], V[9];
-      jacobi3f(S, ev, V);
-      d3 nrm = mk3(V[0], V[3], V[6]);
-      const bool flip = nrm.z < 0 || (nrm.z == 0 && (nrm.y < 0 || (nrm.y == 0 && nrm.x < 0)));
-      if (flip) nrm = scl3(-1.0, nrm);
-      const double dd = -(nrm.x * cen[0] + nrm.y * cen[1] + nrm.z * cen[2]);
-      out.plane[0] = nrm.x; out.plane[1] = nrm.y; out.plane[2] = nrm.z; out.plane[3] = dd;
-      out.centroid[0] = cen[0]; out.centroid[1] = cen[1]; out.centroid[2] = cen[2];
+      const d3 nrm = mk3(out.plane[0], out.plane[1], out.plane[2]);
       // gates (sloam.cpp:394-408): normal in the map frame = R n
       sloam_se3 pe;
       for (int j = 0; j < 4; ++j) pe.q[j] = d.pose_io[j];
@@ -385,6 +398,29 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
       d.plane_feat_all[(size_t)b * kp.G + i] = ground[(uint32_t)keys[i]];
   } else if (threadIdx.x == 0) {
     d.plane_all[b] = out;
+  }
+}
+
+// Plane(points, params) (plane.cpp:3-17) over the input block's ground
+// view: the model of all n points; valid iff n >= numGroundFeatures; the
+// features are the first numGroundFeatures points.  Result in plane_all[0],
+// plane_feat_all[0 .. G).
+__global__ void __launch_bounds__(kPlaneThreads) k_plane_points(Dev d, KParams kp, int n) {
+  __shared__ double red[6 * 32];
+  __shared__ float cen[3];
+  const float4* __restrict__ pts = d.in->ground;
+  PlaneD out{};
+  out.bin = -1;
+  out.valid = 0;
+  if (n > 0 && n >= kp.G) {
+    fit_plane_block([&](int i) { return pts[i]; }, n, cen, red, out);
+    if (threadIdx.x == 0) {
+      out.valid = 1;
+      d.plane_all[0] = out;
+    }
+    for (int i = threadIdx.x; i < kp.G; i += blockDim.x) d.plane_feat_all[i] = pts[i];
+  } else if (threadIdx.x == 0) {
+    d.plane_all[0] = out;
   }
 }
 
@@ -1131,6 +1167,20 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream
   return 5;
 }
 
+int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st) {
+  k_plane_points<<<1, kPlaneThreads, 0, st>>>(d, kp, n);
+  return 1;
+}
+
+int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
+  int n = 1;
+  k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
+  if (kp.cyl_mode == 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
+  k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
+  k_cyl_compact<<<1, 1024, 0, st>>>(d, kp);
+  return n + 2;
+}
+
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
   int n = 0;
   k_zero_bins<<<1, 256, 0, st>>>(d);
@@ -1141,12 +1191,7 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
   k_plane<<<d.n_bins, kPlaneThreads, 0, st>>>(d, kp);
   k_plane_compact<<<1, 1024, 0, st>>>(d, kp);
   n += 6;
-  k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
-  ++n;
-  if (kp.cyl_mode == 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
-  k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
-  k_cyl_compact<<<1, 1024, 0, st>>>(d, kp);
-  return n + 2;
+  return n + launch_cylinders(d, kp, from_trellis, st);
 }
 
 void init_kernel_attributes() {}

@@ -14,7 +14,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libsloam_gb300.so")
 EXPORTS = [
     "sloam_params_default", "sloam_abi_sizes", "sloam_create", "sloam_destroy",
     "sloam_last_error", "sloam_reset", "sloam_set_params", "sloam_project_mask",
-    "sloam_trellis", "sloam_compute_models", "sloam_run", "sloam_keyframe",
+    "sloam_trellis", "sloam_compute_models", "sloam_fit_plane", "sloam_fit_cylinders",
+    "sloam_run", "sloam_keyframe",
     "sloam_keyframes_device", "sloam_keyframes_host", "sloam_last_launch_count", "sloam_stream",
     "sloam_internal_tables",
 ]
@@ -53,6 +54,10 @@ def load(path=LIB_PATH):
                                 C.POINTER(A.Landmarks)]
     L.sloam_compute_models.argtypes = [vp, C.POINTER(A.SE3), C.POINTER(C.c_float), C.c_int32,
                                        C.POINTER(A.Landmarks), C.POINTER(A.ModelsOut)]
+    L.sloam_fit_plane.argtypes = [vp, C.POINTER(C.c_float), C.c_int32, C.POINTER(A.Plane),
+                                  C.POINTER(C.c_float)]
+    L.sloam_fit_cylinders.argtypes = [vp, C.POINTER(A.Landmarks), C.POINTER(A.Plane), C.c_int32,
+                                      C.POINTER(A.ModelsOut)]
     L.sloam_run.argtypes = [vp, C.POINTER(A.SE3), C.POINTER(C.c_float), C.c_int32,
                             C.POINTER(A.Landmarks), C.POINTER(A.Cylinder), C.c_int32,
                             C.POINTER(A.RunOut)]
