@@ -325,3 +325,75 @@ def preset_params(cfg: SceneConfig, base=None, **kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+# ------------------------------------------------------------ uneven batch
+# 64 keyframes of 64x2048, tree counts log-uniform in 20-400 per keyframe,
+# cluster sizes from tens of points (far, thin trunks) to ~20k (a thick trunk
+# a metre from the sensor).  Each keyframe sits at the centre of its own
+# 80 m cell of one forest (cells are beyond each other's 30 m range); the map
+# holds every tree of every cell.
+C3 = SceneConfig(slope_max_deg=2.0, disc=28.0)
+C3_CELL = 80.0
+
+
+def c3_scene(seed: int = 0, n_kf: int = 64, counts=None):
+    """(forest, keyframes, tree counts).  `counts` overrides the drawn tree
+    count of each keyframe."""
+    cfg = C3
+    rng = np.random.default_rng(seed)
+    if counts is None:
+        counts = np.round(np.exp(rng.uniform(math.log(20), math.log(400), n_kf))).astype(int)
+    counts = [int(c) for c in counts]
+    slope = math.radians(rng.uniform(0, cfg.slope_max_deg))
+    az = rng.uniform(0, 2 * math.pi)
+    n = np.array([-math.sin(slope) * math.cos(az), -math.sin(slope) * math.sin(az),
+                  math.cos(slope)])
+    side = int(math.ceil(math.sqrt(len(counts))))
+    centres = [(C3_CELL * (k % side), C3_CELL * (k // side)) for k in range(len(counts))]
+    xs, ys = [], []
+    for (cx, cy), T in zip(centres, counts):
+        cell = []
+        # one trunk close to the sensor per cell (the large clusters)
+        while len(cell) < T:
+            r = (1.2 + 0.8 * rng.uniform()) if not cell else cfg.disc * math.sqrt(rng.uniform(0.004, 1))
+            t = rng.uniform(0, 2 * math.pi)
+            x, y = r * math.cos(t), r * math.sin(t)
+            if any((x - a) ** 2 + (y - b) ** 2 < 1.5 ** 2 for a, b in cell):
+                continue
+            cell.append((x, y))
+        xs += [cx + a for a, _ in cell]
+        ys += [cy + b for _, b in cell]
+    T = len(xs)
+    xs, ys = np.array(xs), np.array(ys)
+    tilt = np.radians(rng.uniform(0, cfg.tilt_max_deg, T))
+    taz = rng.uniform(0, 2 * math.pi, T)
+    axis = np.stack([np.sin(tilt) * np.cos(taz), np.sin(tilt) * np.sin(taz), np.cos(tilt)], 1)
+    f = Forest(n, 0.0, None, axis, rng.uniform(*cfg.r_range, T), rng.uniform(*cfg.h_range, T))
+    f.base = np.stack([xs, ys, f.ground_z(xs, ys)], 1)
+    near = np.cumsum([0] + counts[:-1])  # the first trunk of each cell
+    f.radius[near] = rng.uniform(0.45, 0.6, len(near))
+    f.height[near] = rng.uniform(5.0, 6.0, len(near))
+    sc, sr = [], []
+    for cx, cy in centres:
+        r = cfg.disc * np.sqrt(rng.uniform(0.02, 1, 40))
+        t = rng.uniform(0, 2 * math.pi, 40)
+        sx, sy = cx + r * np.cos(t), cy + r * np.sin(t)
+        rr = rng.uniform(0.4, 1.4, 40)
+        sc.append(np.stack([sx, sy, f.ground_z(sx, sy) + 0.5 * rr], 1))
+        sr.append(rr)
+    f.shrub_c, f.shrub_r = np.concatenate(sc), np.concatenate(sr)
+    kfs = [make_keyframe(f, cfg, rng, xy=c) for c in centres]
+    return f, kfs, counts
+
+
+def c3_params(forest: Forest, base=None, **kw):
+    """C2's reference presets with capacities for the uneven batch: every
+    tree of the forest in the map, up to 400 trees (plus shrub blobs) per
+    keyframe."""
+    p = preset_params(C3, base, **kw)
+    p.max_map = max(p.max_map, len(forest.radius))
+    p.max_landmarks = max(p.max_landmarks, 1024)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p

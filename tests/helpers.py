@@ -72,6 +72,11 @@ def scene(name, seed=0, n_kf=1):
     return cfg, forest, kfs
 
 
+@functools.lru_cache(None)
+def c3_scene(counts, seed=0):
+    return synth.c3_scene(seed, counts=list(counts))
+
+
 def oracle():
     return oracle_loader.lib()
 
@@ -193,7 +198,11 @@ def compare_models(mo, mg, ints_only=False, tol_scale=1.0):
         if not ints_only:
             for a, b in zip(po, pg):
                 assert angle_between(a[:3], b[:3]) < TOL_AXIS_RAD * tol_scale
-                assert abs(a[3] - b[3]) < TOL_OFFSET_M * tol_scale
+                # offset where the plane is: the oracle centroid's distance to
+                # the GPU plane (d itself grows with the distance of the plane
+                # from the map origin: d = -n.c)
+                nb = b[:3] / np.linalg.norm(b[:3])
+                assert abs(nb @ a[4:7] + b[3] / np.linalg.norm(b[:3])) < TOL_OFFSET_M * tol_scale
                 np.testing.assert_allclose(a[4:7], b[4:7], atol=TOL_OFFSET_M * tol_scale)
     co, cg = mo.cyl_array(), mg.cyl_array()
     n = len(co)
