@@ -48,9 +48,10 @@ UNIT = "keyframes/s"
 WORKLOAD = ("C2: 64x2048 keyframes, 150 trees, 400-landmark submap, 256 hyp + 3 LS per tree, "
             "10 GN iterations; plain GPU RANSAC path (the learned proposal is not built)")
 # DRAM bytes (read + write) per keyframe of the batch projection stage, summed
-# over its four kernels in one ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum); None until captured.
-FRONT_TRAFFIC_PER_KF = None
+# over its three kernels in one ncu capture with the caches left as they are
+# (dram__bytes_read.sum + dram__bytes_write.sum of the 8-keyframe chunk
+# launches: 6.05 and 6.50 MB per keyframe in two chunks).
+FRONT_TRAFFIC_PER_KF = 6.28e6
 
 
 def max_over_ranks(x, device=None):
