@@ -93,7 +93,9 @@ typedef struct sloam_params {
   /* extensions of this implementation (no reference counterpart) */
   uint64_t seed;                    /* RANSAC counter-based RNG key       */
   int32_t cyl_mode;                 /* 0 = vertex-line RANSAC (reference) ;
-                                       1 = + point-level cylinder RANSAC  */
+                                       1 = + point-level cylinder RANSAC ;
+                                       2 = + learned proposals, RANSAC as
+                                           fallback                       */
   int32_t cyl_hypotheses;           /* K hypotheses per tree (mode 1)     */
   float   cyl_inlier_thresh;        /* tau, metres (mode 1)               */
   int32_t cyl_ls_iters;             /* LS refinement iterations (mode 1)  */
@@ -105,6 +107,11 @@ typedef struct sloam_params {
   int32_t batch_slots;              /* keyframes of a batch in flight at
                                        once (each slot owns buffers, a
                                        stream and a captured graph)       */
+  int32_t prop_samples;             /* mode 2: network proposals per tree
+                                       (128-point samples)            (8) */
+  float   prop_min_inlier_ratio;    /* mode 2: best proposal's inliers /
+                                       tree points below this -> RANSAC
+                                       fallback for the tree        (0.6) */
 } sloam_params;
 
 void sloam_params_default(sloam_params* p);
@@ -317,6 +324,14 @@ int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t n
                          const uint8_t* point_labels, const sloam_se3* pose_estimates,
                          const sloam_cylinder* map, int32_t n_map, double* pose_out,
                          int32_t* success_out, int32_t* ncyl_out);
+
+/* Weights of the learned cylinder proposal (cyl_mode 2; no reference
+ * counterpart): n = 75399 FP32 values of the point-set network
+ * (shared MLP 3-64-128-256, max-pool, head 256-128-7, row-major W[in][out]
+ * then bias, layer by layer), trained by sloam_gb300/proposal.py; stored
+ * as bf16 for the tensor cores.  A context in cyl_mode 2 refuses keyframes
+ * until weights are set. */
+int sloam_set_proposal_weights(sloam_ctx* ctx, const float* weights, int32_t n);
 
 /* Projection + masking that allocates nothing (no reference counterpart: it
  * exists for callers that cannot call cudaMalloc, such as plugins inside a

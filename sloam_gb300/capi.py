@@ -79,6 +79,8 @@ class Params(C.Structure):
         ("max_map", C.c_int32),
         ("max_ground", C.c_int32),
         ("batch_slots", C.c_int32),
+        ("prop_samples", C.c_int32),
+        ("prop_min_inlier_ratio", C.c_float),
     ]
 
     def copy(self):
@@ -149,6 +151,8 @@ def default_params(**overrides):
     p.max_map = 4096
     p.max_ground = 0
     p.batch_slots = 8
+    p.prop_samples = 8
+    p.prop_min_inlier_ratio = 0.6
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)

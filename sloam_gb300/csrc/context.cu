@@ -12,6 +12,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "proposal.cuh"
 
 using namespace sg;
 
@@ -72,6 +73,8 @@ extern "C" void sloam_params_default(sloam_params* p) {
   p->max_map = 4096;
   p->max_ground = 0;
   p->batch_slots = 8;
+  p->prop_samples = 8;
+  p->prop_min_inlier_ratio = 0.6f;
 }
 
 // sizeof() of every ABI struct, for binding checks.
@@ -254,6 +257,8 @@ struct sloam_ctx {
   int32_t* fb_fe = nullptr;      // [fb_cap * 4] projection counters
   std::vector<cudaEvent_t> ev_fe;  // chunk c: [2c] before, [2c+1] after
   int fe_chunks = 0, fe_nkf = 0;
+  // learned proposal: bf16 network weights in the tensor-core layout
+  unsigned char* prop_tc = nullptr;
   // host batch staging
   int32_t* d_out_i = nullptr;   // [2 * cap] success, ncyl
   double* d_out_pose = nullptr; // [7 * cap]
@@ -364,8 +369,17 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.lm_uv = c.take<float2>((size_t)d.cap_cluster + d.cap_p);  // cluster | vertex points
   d.hyp = c.take<float4>((size_t)d.cap_lm * std::max(d.K, 1));
   d.hyp_cnt = c.take<int32_t>((size_t)d.cap_lm * std::max(d.K, 1));
+  const size_t ps = (size_t)std::max(d.prop_cap, 1);
+  d.prop_x = c.take<float>(ps * 384);
+  d.prop_f = c.take<float4>(ps);
+  d.prop_out = c.take<float>(ps * 8);
+  d.phyp = c.take<float4>(ps);
+  d.phyp_cnt = c.take<int32_t>(ps);
+  d.pbest = c.take<unsigned long long>(d.cap_lm);
+  d.pflag = c.take<int32_t>(d.cap_lm);
   d.pose_io = c.take<double>(32);
   d.cnt = c.take<Counters>(1);
+  d.prop_err = c.dry ? nullptr : &d.cnt->prop_err;
 }
 
 int check_params(const sloam_params& p) {
@@ -379,6 +393,7 @@ int check_params(const sloam_params& p) {
   if (p.cyl_hypotheses < 0 || p.cyl_hypotheses > 4096 || p.line_ransac_max_iter > 256) return 1;
   if (!(p.ground_retain_thresh > 0)) return 1;
   if (p.batch_slots < 0 || p.batch_slots > 64) return 1;
+  if (p.cyl_mode < 0 || p.cyl_mode > 2 || p.prop_samples < 1 || p.prop_samples > 32) return 1;
   return 0;
 }
 
@@ -410,6 +425,8 @@ int init_dev(sloam_ctx* ctx, const sloam_params& P, Dev& d, void*& arena, size_t
   d.F = P.features_per_tree;
   d.G = P.num_ground_features;
   d.K = P.cyl_hypotheses;
+  d.prop_cap = P.cyl_mode == 2 ? d.cap_lm * P.prop_samples : 0;
+  d.prop_tc = ctx->prop_tc;
   const int n_blk = d.N / 256 + 64;
   Carver dry{nullptr, 0, true};
   carve(d, dry, n_blk);
@@ -485,6 +502,15 @@ int sync_counters(sloam_ctx* ctx) {
     return fail(ctx, SLOAM_ERR_CAPACITY, "a context capacity was exceeded (overflow flags set)");
   if (ctx->h_cnt->cc_iter_exceeded)
     return fail(ctx, SLOAM_ERR_TIMEOUT, "connected-components union loop hit its iteration limit");
+  if (ctx->h_cnt->prop_err)
+    return fail(ctx, SLOAM_ERR_TIMEOUT, "proposal network: a tensor-core wait gave up");
+  return SLOAM_OK;
+}
+
+// cyl_mode 2 runs the proposal network: its weights must be loaded
+int need_weights(sloam_ctx* ctx) {
+  if (ctx->P.cyl_mode == 2 && !ctx->prop_tc)
+    return fail(ctx, SLOAM_ERR_ARG, "cyl_mode 2 needs sloam_set_proposal_weights first");
   return SLOAM_OK;
 }
 
@@ -688,6 +714,7 @@ extern "C" void sloam_destroy(sloam_ctx* ctx) {
     if (s.st) cudaStreamDestroy(s.st);
   }
   if (ctx->ev_main) cudaEventDestroy(ctx->ev_main);
+  if (ctx->prop_tc) cudaFree(ctx->prop_tc);
   free_front(ctx);
   for (auto e : ctx->ev_fe) cudaEventDestroy(e);
   if (ctx->fe_st) cudaStreamDestroy(ctx->fe_st);
@@ -825,6 +852,7 @@ extern "C" int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose,
   if (!ctx || !pose || !out || (n_ground > 0 && !ground_xyzi) || n_ground < 0)
     return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
   Dev& d = ctx->d;
   int nl, nv, np, ncl;
   int st = upload_landmarks(ctx, lm, &nl, &nv, &np, &ncl);
@@ -867,6 +895,7 @@ extern "C" int sloam_fit_cylinders(sloam_ctx* ctx, const sloam_landmarks* lm,
                                    sloam_models_out* out) {
   if (!ctx || !lm || !out || n_planes < 0 || (n_planes > 0 && !planes)) return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
   Dev& d = ctx->d;
   if (n_planes > d.n_bins) return fail(ctx, SLOAM_ERR_CAPACITY, "more planes than ground bins");
   int nl, nv, np, ncl;
@@ -898,6 +927,7 @@ extern "C" int sloam_run(sloam_ctx* ctx, const sloam_se3* pose, const float* gro
   if (!ctx || !pose || !out || n_ground < 0 || n_map < 0 || (n_map > 0 && !map))
     return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
   Dev& d = ctx->d;
   const bool first = ctx->first_scan;
   if (!first && n_map == 0) {
@@ -979,6 +1009,7 @@ extern "C" int sloam_keyframe(sloam_ctx* ctx, const float* xyzi, int32_t n,
       (n_map > 0 && !map))
     return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
   Dev& d = ctx->d;
   if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
   const bool first = ctx->first_scan;
@@ -1260,6 +1291,7 @@ extern "C" int sloam_keyframes_device(sloam_ctx* ctx, const float* d_xyzi, int32
       !d_success_out || !d_ncyl_out || n_map <= 0 || !d_map)
     return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
   Dev& d = ctx->d;
   if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
   if (ctx->first_scan) return fail(ctx, SLOAM_ERR_ARG, "the context has not seen a first scan");
@@ -1287,6 +1319,7 @@ extern "C" int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n
       !ncyl_out || n_map <= 0 || !map)
     return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
   Dev& d = ctx->d;
   if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
   if (ctx->first_scan) return fail(ctx, SLOAM_ERR_ARG, "the context has not seen a first scan");
@@ -1413,5 +1446,32 @@ extern "C" int sloam_frontend_time(sloam_ctx* ctx, float* ms, int32_t* n_chunks,
   *ms = total;
   if (n_chunks) *n_chunks = ctx->fe_chunks;
   if (n_keyframes) *n_keyframes = ctx->fe_nkf;
+  return SLOAM_OK;
+}
+
+// Learned cylinder proposal weights (FP32, the layout of csrc/proposal.cuh),
+// packed once into the bf16 tensor-core operands that every slot reads.
+extern "C" int sloam_set_proposal_weights(sloam_ctx* ctx, const float* weights, int32_t n) {
+  if (!ctx || !weights || n != prop::kNumParams) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->st));
+  for (auto& s : ctx->extra) CK(cudaStreamSynchronize(s.st));
+  if (!ctx->prop_tc) CK(cudaMalloc((void**)&ctx->prop_tc, prop::kTcBytes));
+  float* w = nullptr;
+  CK(cudaMalloc((void**)&w, sizeof(float) * n));
+  cudaError_t e = cudaMemcpyAsync(w, weights, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess) {
+    prop::launch_prop_pack(w, ctx->prop_tc, ctx->st);
+    e = cudaStreamSynchronize(ctx->st);
+  }
+  cudaFree(w);
+  if (e != cudaSuccess) return fail(ctx, SLOAM_ERR_CUDA, "sloam_set_proposal_weights", e);
+  // graphs captured the slots' device state by value
+  ctx->d.prop_tc = ctx->prop_tc;
+  destroy_graphs(ctx->gx);
+  for (auto& s : ctx->extra) {
+    s.d.prop_tc = ctx->prop_tc;
+    destroy_graphs(s.gx);
+  }
   return SLOAM_OK;
 }

@@ -32,7 +32,9 @@ struct Counters {
   int32_t n_slow_px;     // projection points that took the FP64 path
   int32_t n_slow_theta;
   int32_t cc_iter_exceeded;
-  int32_t pad[11];
+  int32_t n_fallback;    // mode 2: trees that fell back to RANSAC
+  int32_t prop_err;      // mode 2: a tensor-core wait gave up
+  int32_t pad[9];
 };
 
 // Plane and cylinder records used on the device (FP64 models).
@@ -171,6 +173,17 @@ struct Dev {
   float2* lm_uv;        // [cap_cluster + cap_p] tree points on the prior axis frame
   float4* hyp;          // [cap_lm * K] circle hypotheses (cu, cv, lo2, hi2)
   int32_t* hyp_cnt;     // [cap_lm * K] inlier counts
+  // -- learned proposal (cyl_mode 2); capacities 0 in the other modes
+  const unsigned char* prop_tc;  // bf16 network weights (the context's, shared by slots)
+  float* prop_x;        // [cap_lm * S][128][3] normalised samples
+  float4* prop_f;       // [cap_lm * S] sample mean (xyz), scale (w)
+  float* prop_out;      // [cap_lm * S][8] network outputs
+  float4* phyp;         // [cap_lm * S] proposal circles (cu, cv, lo2, hi2)
+  int32_t* phyp_cnt;    // [cap_lm * S] inlier counts
+  unsigned long long* pbest;  // [cap_lm] best proposal (count << 32 | ~index)
+  int32_t* pflag;       // [cap_lm] 1: the tree falls back to RANSAC
+  int32_t* prop_err;    // &cnt->prop_err
+  int prop_cap;         // cap_lm * S (0: mode 0/1)
   double* pose_io;      // [16] in: estimate (q xyzw, t); out: T_Map_Curr, T_Delta
   Counters* cnt;
 };
@@ -192,6 +205,8 @@ struct KParams {
   double line_prob;
   uint64_t seed;
   int cyl_mode, K, ls_iters;
+  int prop_S;          // learned proposals per tree (mode 2)
+  float prop_ratio;    // fallback below this inlier ratio
   float tau, max_hyp_r;
   double tree_match_thresh, plane_match_thresh, add_new_tree_thresh;
   double min_tree_models, min_ground_models, min_planes;
@@ -233,6 +248,19 @@ int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster,
                  cudaStream_t st);
 void init_kernel_attributes();
+
+// learned cylinder proposal (proposal.cu): bf16 tensor-core operands from the
+// FP32 weights (prop::kTcBytes), and inference over n normalised 128-point
+// samples into out[n][8] (mode 0 tensor cores, 1 SIMT reference)
+namespace prop {
+int launch_prop_pack(const float* d_w, unsigned char* d_tcw, cudaStream_t st);
+int launch_prop_infer(const unsigned char* d_tcw, const float* d_x, int n, float* d_out,
+                      int* d_err, int mode, cudaStream_t st);
+// tensor-core inference over (*d_n_trees) * per_tree samples (at most cap)
+int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const int* d_n_trees,
+                            int per_tree, int cap, float* d_out, int* d_err, cudaStream_t st);
+void init_attributes();
+}  // namespace prop
 
 // host-built tables (context.cu)
 void build_px_table(const sloam_params& p, float* tab);

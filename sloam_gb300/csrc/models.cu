@@ -53,6 +53,8 @@ KParams make_kparams(const sloam_params& p) {
   k.line_prob = p.line_ransac_probability;
   k.seed = p.seed;
   k.cyl_mode = p.cyl_mode;
+  k.prop_S = p.prop_samples;
+  k.prop_ratio = p.prop_min_inlier_ratio;
   k.K = p.cyl_hypotheses;
   k.ls_iters = p.cyl_ls_iters;
   k.tau = p.cyl_inlier_thresh;
@@ -829,8 +831,10 @@ __device__ __forceinline__ Hyp make_hyp(const KParams& kp, int h, int tree_id, i
 }
 
 // Hypothesis table: one thread per (tree, hypothesis); clears the counts.
-// An invalid hypothesis gets hi2 = -1 (no point can be an inlier).
-__global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp) {
+// An invalid hypothesis gets hi2 = -1 (no point can be an inlier).  With a
+// mask (`only`), trees whose entry is 0 get no hypotheses.
+__global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp,
+                                                    const int32_t* __restrict__ only) {
   const int nl = d.cnt->n_lm, K = kp.K;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * K;
        it += gridDim.x * blockDim.x) {
@@ -838,7 +842,7 @@ __global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp) {
     d.hyp_cnt[it] = 0;
     float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
     const CylD c = d.cyl_all[l];
-    if (fit_eligible(c)) {
+    if (fit_eligible(c) && (!only || only[l])) {
       const float4* pts;
       const float2* uv;
       int n;
@@ -861,10 +865,12 @@ constexpr int kHypTile = 256;  // hypotheses staged per pass (8 per lane)
 // popcount lands in the register of the lane that owns the hypothesis
 // (lane = h % 32); per-block totals go to the (tree, hypothesis) counter.
 // A chunk that straddles trees runs once per tree.
-__global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, KParams kp) {
+__global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, const float4* __restrict__ hyp,
+                                                              int* __restrict__ hcnt, int K,
+                                                              const int32_t* __restrict__ only) {
   __shared__ float4 sh[kHypTile];
   __shared__ int sred[kCountThreads / 32][kHypTile];
-  const int nl = d.cnt->n_lm, K = kp.K;
+  const int nl = d.cnt->n_lm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const bool clusters = d.cnt->n_cluster > 0;
   const int total = clusters ? d.cnt->n_cluster : d.cnt->n_p;
@@ -880,7 +886,7 @@ __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, KParams kp) 
     }
     for (int l = lo; l < nl && seg(l) < q0 + kCountThreads; ++l) {
       const int s0 = max(q0, seg(l)), s1 = min(q0 + kCountThreads, seg(l + 1));
-      if (s1 <= s0 || !fit_eligible(d.cyl_all[l])) continue;
+      if (s1 <= s0 || !fit_eligible(d.cyl_all[l]) || (only && !only[l])) continue;
       const int q = q0 + threadIdx.x;
       const bool mine = q >= s0 && q < s1;
       float2 p = make_float2(0.f, 0.f);
@@ -888,14 +894,16 @@ __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, KParams kp) 
       for (int t0 = 0; t0 < K; t0 += kHypTile) {
         const int nt = min(kHypTile, K - t0);
         for (int i = threadIdx.x; i < kHypTile; i += blockDim.x)
-          sh[i] = i < nt ? d.hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
+          sh[i] = i < nt ? hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
         __syncthreads();
         int acc[kHypTile / 32];
 #pragma unroll
+        for (int hb = 0; hb < kHypTile / 32; ++hb) acc[hb] = 0;
+#pragma unroll
         for (int hb = 0; hb < kHypTile / 32; ++hb) {
-          acc[hb] = 0;
+          const int jn = min(32, nt - hb * 32);  // block-uniform
 #pragma unroll 8
-          for (int j = 0; j < 32; ++j) {
+          for (int j = 0; j < jn; ++j) {
             const float4 e = sh[hb * 32 + j];
             const float du = fsub(p.x, e.x), dv = fsub(p.y, e.y);
             const float d2 = fadd(fmul(du, du), fmul(dv, dv));
@@ -910,7 +918,7 @@ __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, KParams kp) 
           int s = 0;
 #pragma unroll
           for (int k = 0; k < kCountThreads / 32; ++k) s += sred[k][h];
-          if (s) atomicAdd(d.hyp_cnt + (size_t)l * K + t0 + h, s);
+          if (s) atomicAdd(hcnt + (size_t)l * K + t0 + h, s);
         }
         __syncthreads();
       }
@@ -919,14 +927,16 @@ __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, KParams kp) 
 }
 
 // Best hypothesis per tree: most inliers, lowest hypothesis on ties.
-__global__ void __launch_bounds__(256) k_cyl_best(Dev d, KParams kp) {
+__global__ void __launch_bounds__(256) k_cyl_best(Dev d, const int* __restrict__ hcnt, int K,
+                                                  unsigned long long* __restrict__ best_out,
+                                                  const int32_t* __restrict__ only) {
   __shared__ unsigned long long sk[8];
-  const int nl = d.cnt->n_lm, K = kp.K;
+  const int nl = d.cnt->n_lm;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
     unsigned long long best = 0ull;
-    if (fit_eligible(d.cyl_all[l])) {
+    if (fit_eligible(d.cyl_all[l]) && (!only || only[l])) {
       for (int h = threadIdx.x; h < K; h += blockDim.x) {
-        const int c = d.hyp_cnt[(size_t)l * K + h];
+        const int c = hcnt[(size_t)l * K + h];
         if (c > 0) {
           const unsigned long long key =
               ((unsigned long long)c << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
@@ -942,9 +952,101 @@ __global__ void __launch_bounds__(256) k_cyl_best(Dev d, KParams kp) {
     __syncthreads();
     if (threadIdx.x == 0) {
       for (int k = 1; k < (int)(blockDim.x >> 5); ++k) best = sk[k] > best ? sk[k] : best;
-      d.cyl_best[l] = best;
+      best_out[l] = best;
     }
     __syncthreads();
+  }
+}
+
+// ----------------------------------------- learned proposals (cyl_mode 2)
+// 8 (prop_S) samples of 128 points per eligible tree, drawn with
+// replacement from the tree's points (Philox keyed by tree id, sample and
+// point), centred on their mean and scaled by their RMS radius.
+__global__ void __launch_bounds__(128) k_prop_gather(Dev d, KParams kp) {
+  __shared__ float red[4];
+  const int nl = d.cnt->n_lm, S = kp.prop_S;
+  const int i = threadIdx.x;
+  auto bsum = [&](float v) {
+    v = warp_sum(v);
+    if ((i & 31) == 0) red[i >> 5] = v;
+    __syncthreads();
+    const float t = red[0] + red[1] + red[2] + red[3];
+    __syncthreads();
+    return t;
+  };
+  for (int it = blockIdx.x; it < nl * S; it += gridDim.x) {
+    const int l = it / S, j = it - l * S;
+    const CylD c = d.cyl_all[l];
+    if (!fit_eligible(c)) continue;
+    const float4* pts;
+    const float2* uv;
+    int n;
+    tree_points(d, l, &pts, &n, &uv);
+    if (n < 1) continue;
+    uint32_t u[4];
+    philox(kp.seed, (uint32_t)c.id, (uint32_t)j, 3u, (uint32_t)i, u);
+    const float4 p = pts[mulhi_idx(u[0], (uint32_t)n)];
+    const float mx = bsum(p.x) / 128.f, my = bsum(p.y) / 128.f, mz = bsum(p.z) / 128.f;
+    const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
+    const float sc = sqrtf(bsum(dx * dx + dy * dy + dz * dz) / 128.f) + 1e-6f;
+    float* x = d.prop_x + (size_t)it * 384;
+    x[3 * i] = dx / sc;
+    x[3 * i + 1] = dy / sc;
+    x[3 * i + 2] = dz / sc;
+    if (i == 0) d.prop_f[it] = make_float4(mx, my, mz, sc);
+  }
+}
+
+// Network output -> circle hypothesis on the tree's prior-axis frame: the
+// proposed axis point nearest the sample mean, projected along the prior
+// axis, and the proposed radius with the inlier band +-tau.
+__global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
+  const int nl = d.cnt->n_lm, S = kp.prop_S;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * S;
+       it += gridDim.x * blockDim.x) {
+    const int l = it / S;
+    d.phyp_cnt[it] = 0;
+    float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
+    const CylD c = d.cyl_all[l];
+    if (fit_eligible(c)) {
+      const float* o = d.prop_out + (size_t)it * 8;
+      const float4 fm = d.prop_f[it];
+      float ax = o[0], ay = o[1], az = o[2];
+      const float an = sqrtf(ax * ax + ay * ay + az * az);
+      if (an > 0.f && fabsf(az) > 1e-3f * an) {
+        ax /= an; ay /= an; az /= an;
+        const float cz = -(o[3] * ax + o[4] * ay) / az;
+        const float4 C = make_float4(fm.x + fm.w * o[3], fm.y + fm.w * o[4], fm.z + fm.w * cz, 0.f);
+        const float r = fm.w * expf(o[5]);
+        const CylFrame f = make_frame(d, c);
+        const float2 cuv = project_uv(f, C);
+        if (r > 0.f && r <= kp.max_hyp_r && isfinite(cuv.x) && isfinite(cuv.y)) {
+          const float lo = fsub(r, kp.tau), hi = fadd(r, kp.tau);
+          e = make_float4(cuv.x, cuv.y, lo > 0.0f ? fmul(lo, lo) : -1.0f, fmul(hi, hi));
+        }
+      }
+    }
+    d.phyp[it] = e;
+  }
+}
+
+// A tree whose best proposal holds fewer than prop_ratio of its points as
+// inliers falls back to the plain RANSAC hypotheses.
+__global__ void __launch_bounds__(256) k_prop_flag(Dev d, KParams kp) {
+  const int nl = d.cnt->n_lm;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
+    int flag = 0;
+    const CylD c = d.cyl_all[l];
+    if (fit_eligible(c)) {
+      const float4* pts;
+      const float2* uv;
+      int n;
+      tree_points(d, l, &pts, &n, &uv);
+      const int best = (int)(d.pbest[l] >> 32);
+      flag = (float)best < kp.prop_ratio * (float)n ? 1 : 0;
+      if (flag) atomicAdd(&d.cnt->n_fallback, 1);
+    }
+    d.pflag[l] = flag;
   }
 }
 
@@ -957,7 +1059,8 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
     CylD c = d.cyl_all[l];
-    const unsigned long long key = d.cyl_best[l];
+    const bool learned = kp.cyl_mode == 2 && !d.pflag[l];
+    const unsigned long long key = learned ? d.pbest[l] : d.cyl_best[l];
     if (c.stage != 1 || c.radius == -1.0 || key == 0ull) continue;
     const int h = (int)(0xFFFFFFFFu - (uint32_t)(key & 0xffffffffull));
     const int best_cnt = (int)(key >> 32);
@@ -966,7 +1069,18 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
     int n;
     tree_points(d, l, &pts, &n, &uvs);
     const CylFrame f = make_frame(d, c);
-    const Hyp H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return uvs[i]; });
+    Hyp H;
+    if (learned) {
+      const float4 e = d.phyp[(size_t)l * kp.prop_S + h];
+      H.cu = e.x;
+      H.cv = e.y;
+      H.lo2 = e.z;
+      H.hi2 = e.w;
+      H.r = fsub(fsqrt(e.w), kp.tau);
+      H.ok = true;
+    } else {
+      H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return uvs[i]; });
+    }
     if (threadIdx.x == 0) {
       st[0] = f.ox + (double)H.cu * f.e1x + (double)H.cv * f.e2x;
       st[1] = f.oy + (double)H.cu * f.e1y + (double)H.cv * f.e2y;
@@ -1150,21 +1264,39 @@ constexpr int kCountBlocks = 304;
 int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st) {
   k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
   k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
-  k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp);
+  k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp, nullptr);
   return 3;
 }
 int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
-  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, kp);
+  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.hyp, d.hyp_cnt, kp.K, nullptr);
   return 1;
 }
 
+// mode 1: K random 3-point circles per tree.  mode 2: prop_S network
+// proposals per tree (one tensor-core launch over every sample), their
+// inliers counted; trees below the inlier ratio run the K random circles.
+// Both end in the LS refinement of the best circle.
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream_t st) {
+  int n = 0;
   k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
-  k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp);
-  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, kp);
-  k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, kp);
+  ++n;
+  const int32_t* only = nullptr;
+  if (kp.cyl_mode == 2) {
+    k_prop_gather<<<kCountBlocks, 128, 0, st>>>(d, kp);
+    n += 1 + prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, kp.prop_S,
+                                           d.prop_cap, d.prop_out, d.prop_err, st);
+    k_prop_hyp<<<kCylBlocks, 256, 0, st>>>(d, kp);
+    k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.phyp, d.phyp_cnt, kp.prop_S, nullptr);
+    k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.phyp_cnt, kp.prop_S, d.pbest, nullptr);
+    k_prop_flag<<<kCylBlocks, 256, 0, st>>>(d, kp);
+    n += 4;
+    only = d.pflag;
+  }
+  k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp, only);
+  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.hyp, d.hyp_cnt, kp.K, only);
+  k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.hyp_cnt, kp.K, d.cyl_best, only);
   k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
-  return 5;
+  return n + 4;
 }
 
 int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st) {
@@ -1175,7 +1307,7 @@ int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st)
 int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
   int n = 1;
   k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
-  if (kp.cyl_mode == 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
+  if (kp.cyl_mode >= 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
   k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
   k_cyl_compact<<<1, 1024, 0, st>>>(d, kp);
   return n + 2;
@@ -1194,6 +1326,6 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
   return n + launch_cylinders(d, kp, from_trellis, st);
 }
 
-void init_kernel_attributes() {}
+void init_kernel_attributes() { prop::init_attributes(); }
 
 }  // namespace sg

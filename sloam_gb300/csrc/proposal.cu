@@ -1,0 +1,815 @@
+// proposal.cu — the learned cylinder proposal (network layout in
+// proposal.cuh): synthetic training clusters, FP32 training kernels
+// (forward + backward per cluster, a deterministic gradient reduction,
+// Adam), and BF16 inference -- the two dense layers (128 points x 64 -> 128
+// and 128 x 128 -> 256) on the 5th-generation tensor cores (tcgen05.mma,
+// operands in shared memory, accumulators in TMEM), with a SIMT kernel of
+// the same arithmetic as the reference it is checked against.
+//
+// Training clusters: a trunk of radius U(0.05, 0.8) m, axis tilt U(0, 15)
+// deg, 2-20 m from the sensor, the arc that faces the sensor minus an
+// occluding azimuth wedge of 0-30 % of it, radial noise sigma U(1, 5) cm,
+// 128 points; targets from the generator's own trunk.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+#include "proposal.cuh"
+
+namespace sg {
+namespace prop {
+namespace {
+
+constexpr float kPi = 3.14159265358979f;
+
+SLOAM_D float u01(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0f); }
+SLOAM_D float gauss(uint32_t a, uint32_t b) {  // Box-Muller
+  const float r = sqrtf(-2.0f * logf(fmaxf(u01(a), 1e-7f)));
+  return r * cospif(2.0f * u01(b));
+}
+
+SLOAM_D float block_sum128(float v, float* red) {  // 128 threads
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  const float t = red[0] + red[1] + red[2] + red[3];
+  __syncthreads();
+  return t;
+}
+
+// ------------------------------------------------------------ samples
+// One block (128 threads) per cluster id; thread i makes point i.
+__global__ void __launch_bounds__(128) k_prop_sample(uint64_t seed, int64_t first_id,
+                                                     float* __restrict__ X,
+                                                     float* __restrict__ T) {
+  __shared__ float red[4];
+  const int64_t g = first_id + blockIdx.x;
+  const uint32_t g0 = (uint32_t)g, g1 = (uint32_t)(g >> 32);
+  uint32_t u[4], v[4], w[4];
+  philox(seed, g0, g1, 0, 0, u);
+  philox(seed, g0, g1, 1, 0, v);
+  philox(seed, g0, g1, 2, 0, w);
+  const float r = 0.05f + 0.75f * u01(u[0]);
+  const float th = u01(u[1]) * (15.0f * kPi / 180.0f), ph = 2.0f * kPi * u01(u[2]);
+  const float D = 2.0f + 18.0f * u01(u[3]), ps = 2.0f * kPi * u01(v[0]);
+  const float sig = 0.01f + 0.04f * u01(v[1]), occ = 0.3f * u01(v[2]);
+  const float h = 1.0f + 3.0f * u01(w[0]), zb = -(1.2f + 0.8f * u01(w[1]));
+  const float ax = sinf(th) * cosf(ph), ay = sinf(th) * sinf(ph), az = cosf(th);
+  const float bx = D * cosf(ps), by = D * sinf(ps), bz = zb;
+  // frame around the axis: e1 towards the sensor (origin), e2 = a x e1
+  float sx = -bx, sy = -by, sz = -bz;
+  const float sa = sx * ax + sy * ay + sz * az;
+  sx -= sa * ax; sy -= sa * ay; sz -= sa * az;
+  const float dp = sqrtf(sx * sx + sy * sy + sz * sz);
+  const float e1x = sx / dp, e1y = sy / dp, e1z = sz / dp;
+  const float e2x = ay * e1z - az * e1y, e2y = az * e1x - ax * e1z, e2z = ax * e1y - ay * e1x;
+  const float A = acosf(fminf(1.0f, r / dp));       // visible half-arc
+  const float wdg = occ * 2.0f * A;
+  const float ws = -A + u01(v[3]) * (2.0f * A - wdg);
+  const int i = threadIdx.x;
+  uint32_t q[4];
+  philox(seed, g0, g1, 3 + i, 0, q);
+  float al = -A + u01(q[0]) * (2.0f * A - wdg);
+  if (al >= ws) al += wdg;
+  const float t = u01(q[1]) * h, rr = r + sig * gauss(q[2], q[3]);
+  const float ca = cosf(al), sn = sinf(al);
+  const float px = bx + t * ax + rr * (ca * e1x + sn * e2x);
+  const float py = by + t * ay + rr * (ca * e1y + sn * e2y);
+  const float pz = bz + t * az + rr * (ca * e1z + sn * e2z);
+  const float mx = block_sum128(px, red) / kPts, my = block_sum128(py, red) / kPts,
+              mz = block_sum128(pz, red) / kPts;
+  const float dx = px - mx, dy = py - my, dz = pz - mz;
+  const float s = sqrtf(block_sum128(dx * dx + dy * dy + dz * dz, red) / kPts) + 1e-6f;
+  float* x = X + (size_t)blockIdx.x * kPts * 3;
+  x[3 * i] = dx / s;
+  x[3 * i + 1] = dy / s;
+  x[3 * i + 2] = dz / s;
+  if (i == 0) {
+    // axis point nearest the mean, relative to the mean, in units of s
+    const float k = (mx - bx) * ax + (my - by) * ay + (mz - bz) * az;
+    float* tg = T + (size_t)blockIdx.x * kTgt;
+    tg[0] = ax; tg[1] = ay; tg[2] = az;
+    tg[3] = (bx + k * ax - mx) / s;
+    tg[4] = (by + k * ay - my) / s;
+    tg[5] = logf(r / s);
+    tg[6] = s;
+    tg[7] = r;
+  }
+}
+
+__global__ void k_prop_init(float* __restrict__ W, uint64_t seed) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kNumParams) return;
+  int fan_in = 0;
+  float gain = 1.0f;
+  if (p < kB1) fan_in = 3;
+  else if (p >= kW2 && p < kB2) fan_in = kD1;
+  else if (p >= kW3 && p < kB3) fan_in = kD2;
+  else if (p >= kW4 && p < kB4) fan_in = kD3;
+  else if (p >= kW5 && p < kB5) { fan_in = kD4; gain = 0.1f; }
+  if (!fan_in) { W[p] = 0.0f; return; }  // biases
+  uint32_t u[4];
+  philox(seed, (uint32_t)p, 0x70726f70u, 0, 0, u);
+  const float bound = gain * sqrtf(6.0f / fan_in);
+  W[p] = (2.0f * u01(u[0]) - 1.0f) * bound;
+}
+
+// ------------------------------------------------------------ training
+// One block per cluster: forward, loss, backward; the cluster's gradient
+// (every parameter, written once) goes to its own slot G[b][*].
+constexpr int kTrainThreads = 256;
+constexpr int kW2Pad = kD1 + 1;  // W2 staged transposed, [128][65]
+constexpr size_t kTrainSmemFloats = 384 + kPts * kD1 + 2 * kPts * kD2 + kD2 * kW2Pad + 256 + 256 +
+                                    128 + 8 + 128 + 256 + 8 + 64;
+
+__global__ void __launch_bounds__(kTrainThreads) k_prop_train(const float* __restrict__ W,
+                                                              const float* __restrict__ X,
+                                                              const float* __restrict__ T,
+                                                              float* __restrict__ G,
+                                                              float* __restrict__ loss) {
+  extern __shared__ float sm[];
+  float* x = sm;                       // [128][3]
+  float* a1 = x + 384;                 // [128][64]
+  float* a2 = a1 + kPts * kD1;         // [128][128]; later dA1 / dZ1 [128][64]
+  float* da2 = a2 + kPts * kD2;        // [128][128]
+  float* w2t = da2 + kPts * kD2;       // W2^T padded [128][65]
+  float* h = w2t + kD2 * kW2Pad;       // [256]
+  int* arg = reinterpret_cast<int*>(h + kD3);  // [256]
+  float* y1 = reinterpret_cast<float*>(arg + kD3);  // [128]
+  float* out = y1 + kD4;               // [8]
+  float* dy1 = out + 8;                // [128]
+  float* dh = dy1 + kD4;               // [256]
+  float* dout = dh + kD3;              // [8]
+  const int tid = threadIdx.x;
+  const int b = blockIdx.x;
+  float* g = G + (size_t)b * kNumParams;
+
+  for (int i = tid; i < 384; i += kTrainThreads) x[i] = X[(size_t)b * 384 + i];
+  for (int i = tid; i < kD1 * kD2; i += kTrainThreads) {
+    const int k = i / kD2, j = i % kD2;
+    w2t[j * kW2Pad + k] = W[kW2 + i];
+  }
+  for (int i = tid; i < kPts * kD2; i += kTrainThreads) da2[i] = 0.0f;
+  __syncthreads();
+  // layer 1
+  for (int i = tid; i < kPts * kD1; i += kTrainThreads) {
+    const int r = i / kD1, j = i % kD1;
+    const float z = W[kB1 + j] + x[3 * r] * W[kW1 + j] + x[3 * r + 1] * W[kW1 + kD1 + j] +
+                    x[3 * r + 2] * W[kW1 + 2 * kD1 + j];
+    a1[i] = fmaxf(z, 0.0f);
+  }
+  __syncthreads();
+  // layer 2: column j, 64 rows per thread in tiles of 16
+  {
+    const int j = tid & (kD2 - 1), rh = tid >> 7;
+    for (int r0 = rh * 64; r0 < rh * 64 + 64; r0 += 16) {
+      float acc[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] = W[kB2 + j];
+      for (int k = 0; k < kD1; ++k) {
+        const float w = w2t[j * kW2Pad + k];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] += a1[(r0 + q) * kD1 + k] * w;
+      }
+#pragma unroll
+      for (int q = 0; q < 16; ++q) a2[(r0 + q) * kD2 + j] = fmaxf(acc[q], 0.0f);
+    }
+  }
+  __syncthreads();
+  // layer 3 + max-pool: thread c, rows in tiles of 16
+  {
+    const int c = tid;
+    float best = -INFINITY;
+    int br = -1;
+    for (int r0 = 0; r0 < kPts; r0 += 16) {
+      float acc[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] = W[kB3 + c];
+      for (int k = 0; k < kD2; ++k) {
+        const float w = W[kW3 + k * kD3 + c];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] += a2[(r0 + q) * kD2 + k] * w;
+      }
+#pragma unroll
+      for (int q = 0; q < 16; ++q)
+        if (acc[q] > best) { best = acc[q]; br = r0 + q; }
+    }
+    h[c] = fmaxf(best, 0.0f);
+    arg[c] = best > 0.0f ? br : -1;
+  }
+  __syncthreads();
+  // head
+  if (tid < kD4) {
+    float z = W[kB4 + tid];
+    for (int c = 0; c < kD3; ++c) z += h[c] * W[kW4 + c * kD4 + tid];
+    y1[tid] = fmaxf(z, 0.0f);
+  }
+  __syncthreads();
+  if (tid < kD5) {
+    float z = W[kB5 + tid];
+    for (int j = 0; j < kD4; ++j) z += y1[j] * W[kW5 + j * kD5 + tid];
+    out[tid] = z;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const float* tg = T + (size_t)b * kTgt;
+    float L = 0.0f;
+    for (int q = 0; q < 6; ++q) {
+      const float d = out[q] - tg[q];
+      L += d * d;
+      dout[q] = 2.0f * d;
+    }
+    const float ec = (out[3] - tg[3]) * (out[3] - tg[3]) + (out[4] - tg[4]) * (out[4] - tg[4]) +
+                     (out[5] - tg[5]) * (out[5] - tg[5]);
+    const float ct = expf(-ec / 0.01f);  // confidence target: the proposal is good
+    const float p = 1.0f / (1.0f + expf(-out[6]));
+    L += 0.1f * -(ct * logf(fmaxf(p, 1e-7f)) + (1.0f - ct) * logf(fmaxf(1.0f - p, 1e-7f)));
+    dout[6] = 0.1f * (p - ct);
+    loss[b] = L;
+  }
+  __syncthreads();
+  // ---- backward: head
+  for (int i = tid; i < kD4 * kD5; i += kTrainThreads)
+    g[kW5 + i] = y1[i / kD5] * dout[i % kD5];
+  if (tid < kD5) g[kB5 + tid] = dout[tid];
+  if (tid < kD4) {
+    float s = 0.0f;
+    for (int o = 0; o < kD5; ++o) s += dout[o] * W[kW5 + tid * kD5 + o];
+    dy1[tid] = y1[tid] > 0.0f ? s : 0.0f;
+  }
+  __syncthreads();
+  for (int i = tid; i < kD3 * kD4; i += kTrainThreads) g[kW4 + i] = h[i / kD4] * dy1[i % kD4];
+  if (tid < kD4) g[kB4 + tid] = dy1[tid];
+  {
+    const int c = tid;
+    float s = 0.0f;
+    for (int j = 0; j < kD4; ++j) s += dy1[j] * W[kW4 + c * kD4 + j];
+    dh[c] = s;
+  }
+  __syncthreads();
+  // layer 3 (the max routes the gradient to one row per column)
+  {
+    const int c = tid, r = arg[c];
+    const float gc = r >= 0 ? dh[c] : 0.0f;
+    g[kB3 + c] = gc;
+    for (int k = 0; k < kD2; ++k) {
+      g[kW3 + k * kD3 + c] = r >= 0 ? a2[r * kD2 + k] * gc : 0.0f;
+      if (r >= 0 && gc != 0.0f) atomicAdd(&da2[r * kD2 + k], W[kW3 + k * kD3 + c] * gc);
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < kPts * kD2; i += kTrainThreads)
+    if (!(a2[i] > 0.0f)) da2[i] = 0.0f;  // dZ2
+  __syncthreads();
+  // layer 2: dW2[k][j] = sum_r a1[r][k] dZ2[r][j]; db2
+  {
+    const int j = tid & (kD2 - 1), kh = tid >> 7;
+    float acc[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) acc[q] = 0.0f;
+    float sb = 0.0f;
+    for (int r = 0; r < kPts; ++r) {
+      const float d = da2[r * kD2 + j];
+      sb += d;
+#pragma unroll
+      for (int q = 0; q < 32; ++q) acc[q] += a1[r * kD1 + kh * 32 + q] * d;
+    }
+#pragma unroll
+    for (int q = 0; q < 32; ++q) g[kW2 + (kh * 32 + q) * kD2 + j] = acc[q];
+    if (kh == 0) g[kB2 + j] = sb;
+  }
+  // dA1[r][k] = sum_j dZ2[r][j] W2[k][j], into the a2 region
+  float* da1 = a2;
+  {
+    const int k = tid & (kD1 - 1), rq = tid >> 6;
+    for (int r = rq * 32; r < rq * 32 + 32; ++r) {
+      float s = 0.0f;
+      for (int j = 0; j < kD2; ++j) s += da2[r * kD2 + j] * w2t[j * kW2Pad + k];
+      da1[r * kD1 + k] = s;
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < kPts * kD1; i += kTrainThreads)
+    if (!(a1[i] > 0.0f)) da1[i] = 0.0f;  // dZ1
+  __syncthreads();
+  if (tid < 3 * kD1) {
+    const int dd = tid / kD1, k = tid % kD1;
+    float s = 0.0f;
+    for (int r = 0; r < kPts; ++r) s += x[3 * r + dd] * da1[r * kD1 + k];
+    g[kW1 + dd * kD1 + k] = s;
+  } else {
+    const int k = tid - 3 * kD1;
+    float s = 0.0f;
+    for (int r = 0; r < kPts; ++r) s += da1[r * kD1 + k];
+    g[kB1 + k] = s;
+  }
+}
+
+// Mean gradient over the B slots (fixed order: deterministic).
+__global__ void k_prop_reduce(const float* __restrict__ G, int B, float* __restrict__ grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kNumParams) return;
+  float s = 0.0f;
+  for (int b = 0; b < B; ++b) s += G[(size_t)b * kNumParams + p];
+  grad[p] = s / (float)B;
+}
+
+__global__ void k_prop_adam(float* __restrict__ W, const float* __restrict__ grad,
+                            float* __restrict__ m, float* __restrict__ v, float lr, float c1,
+                            float c2) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kNumParams) return;
+  const float gr = grad[p];
+  const float mm = 0.9f * m[p] + 0.1f * gr, vv = 0.999f * v[p] + 0.001f * gr * gr;
+  m[p] = mm;
+  v[p] = vv;
+  W[p] -= lr * (mm / c1) / (sqrtf(vv / c2) + 1e-8f);
+}
+
+__global__ void k_prop_loss_mean(const float* __restrict__ loss, int B, float* __restrict__ out) {
+  __shared__ float red[32];
+  float s = 0.0f;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) s += loss[b];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    *out = t / (float)B;
+  }
+}
+
+// ----------------------------------------------------------- inference
+SLOAM_D float bfr(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+
+// BF16 operands in the tensor-core layout + bf16-rounded fp32 copies.
+__global__ void k_prop_pack(const float* __restrict__ W, unsigned char* __restrict__ tcw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __nv_bfloat16* b2 = reinterpret_cast<__nv_bfloat16*>(tcw);
+  __nv_bfloat16* b3 = reinterpret_cast<__nv_bfloat16*>(tcw + kTcW2Bytes);
+  float* f = reinterpret_cast<float*>(tcw + kTcF32Off);
+  if (i < kD1 * kD2) {  // W2[k][j] -> W2^T (j, k), K = 64
+    const int k = i / kD2, j = i % kD2;
+    b2[core_offset(j, k, kD1) / 2] = __float2bfloat16_rn(W[kW2 + i]);
+  }
+  if (i < kD2 * kD3) {  // W3[k][c] -> W3^T (c, k), K = 128
+    const int k = i / kD3, c = i % kD3;
+    b3[core_offset(c, k, kD2) / 2] = __float2bfloat16_rn(W[kW3 + i]);
+  }
+  if (i < kNumParams) f[i] = bfr(W[i]);
+}
+
+// SIMT reference of the tensor-core kernel: the same bf16 operands and
+// roundings, FP32 accumulation.  One block (128 threads) per sample.
+constexpr size_t kRefSmem = sizeof(float) * (kPts * kD1 + kPts * (kD2 + 1) + kD3 + kD4);
+
+__global__ void __launch_bounds__(128) k_prop_infer_ref(const unsigned char* __restrict__ tcw,
+                                                        const float* __restrict__ X, int S,
+                                                        float* __restrict__ out) {
+  extern __shared__ float rsm[];
+  float* a1 = rsm;                       // [128][64]
+  float* a2 = a1 + kPts * kD1;           // [128][129]
+  float* h = a2 + kPts * (kD2 + 1);      // [256]
+  float* y1 = h + kD3;                   // [128]
+  const __nv_bfloat16* b2 = reinterpret_cast<const __nv_bfloat16*>(tcw);
+  const __nv_bfloat16* b3 = reinterpret_cast<const __nv_bfloat16*>(tcw + kTcW2Bytes);
+  const float* f = reinterpret_cast<const float*>(tcw + kTcF32Off);
+  const int r = threadIdx.x;
+  for (int s = blockIdx.x; s < S; s += gridDim.x) {
+    const float* x = X + (size_t)s * kPts * 3;
+    const float x0 = x[3 * r], x1 = x[3 * r + 1], x2 = x[3 * r + 2];
+    for (int j = 0; j < kD1; ++j)
+      a1[r * kD1 + j] = bfr(fmaxf(f[kB1 + j] + x0 * f[kW1 + j] + x1 * f[kW1 + kD1 + j] +
+                                      x2 * f[kW1 + 2 * kD1 + j], 0.0f));
+    __syncthreads();
+    for (int j = 0; j < kD2; ++j) {
+      float z = 0.0f;
+      for (int k = 0; k < kD1; ++k)
+        z += a1[r * kD1 + k] * __bfloat162float(b2[core_offset(j, k, kD1) / 2]);
+      a2[r * (kD2 + 1) + j] = bfr(fmaxf(z + f[kB2 + j], 0.0f));
+    }
+    __syncthreads();
+    for (int c = r; c < kD3; c += 128) {
+      float best = 0.0f;
+      for (int q = 0; q < kPts; ++q) {
+        float z = 0.0f;
+        for (int k = 0; k < kD2; ++k)
+          z += a2[q * (kD2 + 1) + k] * __bfloat162float(b3[core_offset(c, k, kD2) / 2]);
+        best = fmaxf(best, z + f[kB3 + c]);
+      }
+      h[c] = best;
+    }
+    __syncthreads();
+    float z = f[kB4 + r];
+    for (int c = 0; c < kD3; ++c) z += h[c] * f[kW4 + c * kD4 + r];
+    y1[r] = fmaxf(z, 0.0f);
+    __syncthreads();
+    if (r < kD5) {
+      float o = f[kB5 + r];
+      for (int j = 0; j < kD4; ++j) o += y1[j] * f[kW5 + j * kD5 + r];
+      out[(size_t)s * 8 + r] = o;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------- tcgen05 primitives
+SLOAM_D uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: K-major, no swizzle; LBO = byte stride
+// between core matrices along K, SBO = along M/N; version 1 (bit 46)
+SLOAM_D uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor, kind::f16: D f32, A and B bf16, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+SLOAM_D void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+SLOAM_D void mma_commit(uint64_t* mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   saddr(mbar))
+               : "memory");
+}
+SLOAM_D void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+SLOAM_D void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+SLOAM_D void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+SLOAM_D void mbar_init(uint64_t* m, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(m)), "r"(n) : "memory");
+}
+SLOAM_D bool mbar_test(uint64_t* m, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(saddr(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+constexpr int kMbarSpin = 1 << 20;  // bounded wait (the MMAs take microseconds)
+
+#define SG_TMEM_LD32(taddr, v)                                                                 \
+  asm volatile(                                                                                \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"      \
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),   \
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),            \
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),         \
+        "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),         \
+        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),         \
+        "=r"(v[31])                                                                            \
+      : "r"(taddr))
+SLOAM_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Tensor-core inference.  One CTA per SM (its shared memory allows no
+// second), persistent over samples; 128 threads, thread r owns point r and
+// TMEM lane r.  Layer 1 and the head on CUDA cores (FP32), layers 2 and 3
+// as tcgen05.mma M=128 (N=128, K=64 then N=256, K=128), bf16 operands from
+// shared memory, fp32 accumulators in 256 TMEM columns (reused).
+constexpr int kTcThreads = 128;
+constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes, kSmA1 = kSmB3 + kTcW3Bytes,
+                   kSmA2 = kSmA1 + kPts * kD1 * 2, kSmW1 = kSmA2 + kPts * kD2 * 2,
+                   kSmPart = kSmW1 + 4 * (3 * kD1 + kD1), kSmH = kSmPart + 4 * 4 * kD3,
+                   kSmY1 = kSmH + 4 * kD3, kSmMisc = kSmY1 + 4 * kD4, kTcSmem = kSmMisc + 64;
+static_assert(kSmA1 % 128 == 0 && kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
+// the descriptors address at most: A1 [128 x 64], A2 [128 x 128], W2^T
+// [128 x 64], W3^T [256 x 128]; every core matrix lies inside its buffer
+static_assert(core_offset(kPts - 1, kD1 - 1, kD1) + 2 <= kPts * kD1 * 2, "A1 extent");
+static_assert(core_offset(kD3 - 1, kD2 - 1, kD2) + 2 <= kTcW3Bytes, "W3 extent");
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
+    const unsigned char* __restrict__ tcw, const float* __restrict__ X, int S,
+    const int* __restrict__ n_trees, int per_tree, float* __restrict__ out,
+    int* __restrict__ err) {
+  // samples: S, or n_trees * per_tree (a count on the device) when given
+  if (n_trees) S = min(S, *n_trees * per_tree);
+  if ((int)blockIdx.x >= S) return;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* w1 = reinterpret_cast<float*>(smem + kSmW1);        // W1 [3][64], b1 [64]
+  float* part = reinterpret_cast<float*>(smem + kSmPart);    // [4][256]
+  float* h = reinterpret_cast<float*>(smem + kSmH);          // [256]
+  float* y1 = reinterpret_cast<float*>(smem + kSmY1);        // [128]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8);
+  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 12);
+  const float* f = reinterpret_cast<const float*>(tcw + kTcF32Off);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // stage the bf16 weights (80 KB) and W1 / b1
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(tcw);
+    uint4* dst = reinterpret_cast<uint4*>(smem);
+    for (int i = tid; i < (kTcW2Bytes + kTcW3Bytes) / 16; i += kTcThreads) dst[i] = src[i];
+    for (int i = tid; i < 4 * kD1; i += kTcThreads) w1[i] = f[kW1 + i];
+  }
+  if (tid == 0) {
+    mbar_init(mbar, 1);
+    *abort_flag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+                     saddr(tslot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const uint32_t sA1 = saddr(smem + kSmA1), sA2 = saddr(smem + kSmA2);
+  const uint32_t sB2 = saddr(smem + kSmB2), sB3 = saddr(smem + kSmB3);
+  uint32_t phase = 0;
+
+  for (int s = blockIdx.x; s < S; s += gridDim.x) {
+    // layer 1 (row tid) -> A1 in bf16 core-matrix layout
+    {
+      const float* x = X + (size_t)s * kPts * 3;
+      const float x0 = x[3 * tid], x1 = x[3 * tid + 1], x2 = x[3 * tid + 2];
+      for (int k0 = 0; k0 < kD1; k0 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = k0 + 2 * q;
+          const float za = w1[3 * kD1 + j] + x0 * w1[j] + x1 * w1[kD1 + j] + x2 * w1[2 * kD1 + j];
+          const float zb = w1[3 * kD1 + j + 1] + x0 * w1[j + 1] + x1 * w1[kD1 + j + 1] +
+                           x2 * w1[2 * kD1 + j + 1];
+          const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
+          pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
+        }
+        *reinterpret_cast<uint4*>(smem + kSmA1 + core_offset(tid, k0, kD1)) =
+            make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0) {
+      for (int ks = 0; ks < kD1 / 16; ++ks)
+        mma_bf16(tmem, smem_desc(sA1 + ks * 256, 128, (kD1 / 8) * 128),
+                 smem_desc(sB2 + ks * 256, 128, (kD1 / 8) * 128), idesc_bf16(128, kD2), ks > 0);
+      mma_commit(mbar);
+    }
+    {
+      int it = 0;
+      while (!mbar_test(mbar, phase) && ++it < kMbarSpin) {
+      }
+      if (it >= kMbarSpin) {
+        atomicOr(err, 1);
+        *abort_flag = 1;
+      }
+      phase ^= 1u;
+    }
+    fence_after();
+    // epilogue 2: bias, ReLU, bf16 -> A2
+    for (int cc = 0; cc < kD2 / 32; ++cc) {
+      uint32_t v[32];
+      SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
+      tmem_wait_ld();
+#pragma unroll
+      for (int k0 = 0; k0 < 32; k0 += 8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = cc * 32 + k0 + 2 * q;
+          const float za = __uint_as_float(v[k0 + 2 * q]) + f[kB2 + j];
+          const float zb = __uint_as_float(v[k0 + 2 * q + 1]) + f[kB2 + j + 1];
+          const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
+          pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
+        }
+        *reinterpret_cast<uint4*>(smem + kSmA2 + core_offset(tid, cc * 32 + k0, kD2)) =
+            make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (*abort_flag) break;
+    if (tid == 0) {
+      for (int ks = 0; ks < kD2 / 16; ++ks)
+        mma_bf16(tmem, smem_desc(sA2 + ks * 256, 128, (kD2 / 8) * 128),
+                 smem_desc(sB3 + ks * 256, 128, (kD2 / 8) * 128), idesc_bf16(128, kD3), ks > 0);
+      mma_commit(mbar);
+    }
+    {
+      int it = 0;
+      while (!mbar_test(mbar, phase) && ++it < kMbarSpin) {
+      }
+      if (it >= kMbarSpin) {
+        atomicOr(err, 1);
+        *abort_flag = 1;
+      }
+      phase ^= 1u;
+    }
+    fence_after();
+    // epilogue 3: bias, ReLU, max over this warp's 32 points per column
+    for (int cc = 0; cc < kD3 / 32; ++cc) {
+      uint32_t v[32];
+      SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
+      tmem_wait_ld();
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        float m = fmaxf(__uint_as_float(v[q]) + f[kB3 + cc * 32 + q], 0.0f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == q) part[warp * kD3 + cc * 32 + q] = m;
+      }
+    }
+    fence_before();
+    __syncthreads();
+    for (int c = tid; c < kD3; c += kTcThreads)
+      h[c] = fmaxf(fmaxf(part[c], part[kD3 + c]), fmaxf(part[2 * kD3 + c], part[3 * kD3 + c]));
+    __syncthreads();
+    {
+      float z = f[kB4 + tid];
+      for (int c = 0; c < kD3; ++c) z += h[c] * f[kW4 + c * kD4 + tid];
+      y1[tid] = fmaxf(z, 0.0f);
+    }
+    __syncthreads();
+    if (tid < kD5) {
+      float o = f[kB5 + tid];
+      for (int j = 0; j < kD4; ++j) o += y1[j] * f[kW5 + j * kD5 + tid];
+      out[(size_t)s * 8 + tid] = o;
+    }
+    if (*abort_flag) break;
+    fence_before();
+    __syncthreads();
+    fence_after();
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+}
+
+int g_tc_attr = 0;
+
+}  // namespace
+
+void init_attributes() {
+  if (g_tc_attr) return;
+  cudaFuncSetAttribute(k_prop_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kTcSmem);
+  cudaFuncSetAttribute(k_prop_infer_ref, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kRefSmem);
+  g_tc_attr = 1;
+}
+
+static int sm_count() {
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const int* d_n_trees,
+                            int per_tree, int cap, float* d_out, int* d_err, cudaStream_t st) {
+  init_attributes();
+  const int grid = cap < sm_count() ? (cap > 0 ? cap : 1) : sm_count();
+  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, cap, d_n_trees, per_tree, d_out,
+                                                     d_err);
+  return 1;
+}
+
+int launch_prop_pack(const float* d_w, unsigned char* d_tcw, cudaStream_t st) {
+  k_prop_pack<<<(kNumParams + 255) / 256, 256, 0, st>>>(d_w, d_tcw);
+  return 1;
+}
+
+int launch_prop_infer(const unsigned char* d_tcw, const float* d_x, int n, float* d_out,
+                      int* d_err, int mode, cudaStream_t st) {
+  if (n <= 0) return 0;
+  init_attributes();
+  if (mode == 1) {
+    k_prop_infer_ref<<<n, 128, kRefSmem, st>>>(d_tcw, d_x, n, d_out);
+    return 1;
+  }
+  const int grid = n < sm_count() ? n : sm_count();
+  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, n, nullptr, 0, d_out, d_err);
+  return 1;
+}
+
+}  // namespace prop
+}  // namespace sg
+
+using namespace sg::prop;
+
+namespace {
+int prop_fail(const char* what, cudaError_t e) {
+  std::fprintf(stderr, "sloam proposal: %s: %s\n", what, cudaGetErrorString(e));
+  return SLOAM_ERR_CUDA;
+}
+#define PCK(call)                                  \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return prop_fail(#call, e_); \
+  } while (0)
+}  // namespace
+
+extern "C" int sloam_prop_num_params(void) { return kNumParams; }
+
+extern "C" int sloam_prop_sample(uint64_t seed, int64_t first_id, int32_t n, float* d_points,
+                                 float* d_targets) {
+  if (n < 0 || (n > 0 && (!d_points || !d_targets))) return SLOAM_ERR_ARG;
+  if (n == 0) return SLOAM_OK;
+  k_prop_sample<<<n, 128>>>(seed, first_id, d_points, d_targets);
+  PCK(cudaGetLastError());
+  PCK(cudaDeviceSynchronize());
+  return SLOAM_OK;
+}
+
+extern "C" int sloam_prop_train(const float* init, int32_t steps, int32_t batch, float lr,
+                                uint64_t seed, int64_t first_id, float* weights_out,
+                                float* loss_out) {
+  if (steps < 0 || batch < 1 || !weights_out) return SLOAM_ERR_ARG;
+  float *W = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *G = nullptr, *X = nullptr,
+        *T = nullptr, *L = nullptr, *Lm = nullptr;
+  auto release = [&]() {
+    for (float* p : {W, m, v, grad, G, X, T, L, Lm})
+      if (p) cudaFree(p);
+  };
+  const size_t np = kNumParams;
+  cudaError_t e = cudaSuccess;
+  for (auto pp : {&W, &m, &v, &grad}) {
+    if (e == cudaSuccess) e = cudaMalloc(pp, sizeof(float) * np);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&G, sizeof(float) * np * batch);
+  if (e == cudaSuccess) e = cudaMalloc(&X, sizeof(float) * 384 * batch);
+  if (e == cudaSuccess) e = cudaMalloc(&T, sizeof(float) * kTgt * batch);
+  if (e == cudaSuccess) e = cudaMalloc(&L, sizeof(float) * batch);
+  if (e == cudaSuccess) e = cudaMalloc(&Lm, sizeof(float) * (steps > 0 ? steps : 1));
+  if (e != cudaSuccess) {
+    release();
+    return prop_fail("allocation", e);
+  }
+  cudaMemset(m, 0, sizeof(float) * np);
+  cudaMemset(v, 0, sizeof(float) * np);
+  if (init)
+    e = cudaMemcpy(W, init, sizeof(float) * np, cudaMemcpyHostToDevice);
+  else
+    k_prop_init<<<(kNumParams + 255) / 256, 256>>>(W, seed);
+  const size_t smem = sizeof(float) * kTrainSmemFloats;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_prop_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  float c1 = 1.0f, c2 = 1.0f;
+  for (int s = 0; s < steps && e == cudaSuccess; ++s) {
+    k_prop_sample<<<batch, 128>>>(seed ^ 0x5a5a5a5aull, first_id + (int64_t)s * batch, X, T);
+    k_prop_train<<<batch, kTrainThreads, smem>>>(W, X, T, G, L);
+    k_prop_reduce<<<(kNumParams + 255) / 256, 256>>>(G, batch, grad);
+    c1 *= 0.9f;
+    c2 *= 0.999f;
+    k_prop_adam<<<(kNumParams + 255) / 256, 256>>>(W, grad, m, v, lr, 1.0f - c1, 1.0f - c2);
+    k_prop_loss_mean<<<1, 256>>>(L, batch, Lm + s);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(weights_out, W, sizeof(float) * np, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && loss_out && steps > 0)
+    e = cudaMemcpy(loss_out, Lm, sizeof(float) * steps, cudaMemcpyDeviceToHost);
+  release();
+  if (e != cudaSuccess) return prop_fail("training", e);
+  return SLOAM_OK;
+}
+
+extern "C" int sloam_prop_infer(const float* weights, const float* d_points, int32_t n,
+                                float* d_out, int32_t mode) {
+  if (!weights || n < 0 || (n > 0 && (!d_points || !d_out)) || mode < 0 || mode > 1)
+    return SLOAM_ERR_ARG;
+  float* W = nullptr;
+  unsigned char* tcw = nullptr;
+  int* err = nullptr;
+  cudaError_t e = cudaMalloc(&W, sizeof(float) * kNumParams);
+  if (e == cudaSuccess) e = cudaMalloc(&tcw, kTcBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(W, weights, sizeof(float) * kNumParams, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+  int herr = 0;
+  if (e == cudaSuccess) {
+    sg::prop::launch_prop_pack(W, tcw, 0);
+    sg::prop::launch_prop_infer(tcw, d_points, n, d_out, err, mode, 0);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+  }
+  if (W) cudaFree(W);
+  if (tcw) cudaFree(tcw);
+  if (err) cudaFree(err);
+  if (e != cudaSuccess) return prop_fail("inference", e);
+  return herr ? SLOAM_ERR_TIMEOUT : SLOAM_OK;
+}

@@ -17,7 +17,7 @@ EXPORTS = [
     "sloam_trellis", "sloam_compute_models", "sloam_fit_plane", "sloam_fit_cylinders",
     "sloam_run", "sloam_keyframe",
     "sloam_keyframes_device", "sloam_keyframes_host", "sloam_last_launch_count", "sloam_stream",
-    "sloam_internal_tables",
+    "sloam_internal_tables", "sloam_set_proposal_weights",
 ]
 
 _lib = None
@@ -70,6 +70,7 @@ def load(path=LIB_PATH):
                                        C.POINTER(A.Cylinder), C.c_int32, vp, vp, vp]
     L.sloam_project_mask_noalloc.argtypes = [C.POINTER(A.Params), vp, C.c_int32, vp, vp, vp, vp,
                                              vp, vp, vp, vp, vp]
+    L.sloam_set_proposal_weights.argtypes = [vp, C.POINTER(C.c_float), C.c_int32]
     L.sloam_last_launch_count.argtypes = [vp]
     L.sloam_last_launch_count.restype = C.c_int64
     L.sloam_stream.argtypes = [vp]
@@ -111,6 +112,13 @@ class Context:
         if st not in ok:
             raise SloamError(st, self.error())
         return st
+
+    def set_proposal_weights(self, w):
+        """Loads the learned-proposal weights (FP32, 75 399 values)."""
+        import numpy as np
+        w = np.ascontiguousarray(w, np.float32)
+        self.check(self.L.sloam_set_proposal_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float)),
+                                                     w.size))
 
     def launches(self):
         return int(self.L.sloam_last_launch_count(self.h))

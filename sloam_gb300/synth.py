@@ -397,3 +397,24 @@ def c3_params(forest: Forest, base=None, **kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+def cylinder_errors(forest: Forest, cyl, max_dist=0.5):
+    """Fitted cylinders (rows [root3, ray3, radius, id], map frame) against
+    the forest's trunks.  Each is matched to the trunk whose axis passes
+    nearest its root (horizontal distance at the root's height, at most
+    max_dist).  Returns (axis angle in degrees, |radius error| in m) per
+    matched cylinder."""
+    angs, rerrs = [], []
+    base, axis, rad = forest.base, forest.axis, forest.radius
+    for c in np.asarray(cyl, float).reshape(-1, 8):
+        root, ray = c[:3], c[3:6] / np.linalg.norm(c[3:6])
+        t = (root[2] - base[:, 2]) / axis[:, 2]
+        p = base + t[:, None] * axis
+        d = np.hypot(p[:, 0] - root[0], p[:, 1] - root[1])
+        k = int(np.argmin(d))
+        if d[k] > max_dist:
+            continue
+        angs.append(math.degrees(math.acos(min(1.0, abs(float(ray @ axis[k]))))))
+        rerrs.append(abs(c[6] - rad[k]))
+    return np.array(angs), np.array(rerrs)
