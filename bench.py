@@ -45,8 +45,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "keyframes/s at 64\u00d72048: learned-proposal vs plain RANSAC, equal cylinder error"
 UNIT = "keyframes/s"
-WORKLOAD = ("C2: 64x2048 keyframes, 150 trees, 400-landmark submap, 256 hyp + 3 LS per tree, "
-            "10 GN iterations; plain GPU RANSAC path (the learned proposal is not built)")
+WORKLOAD = ("C2: 64x2048 keyframes, 150 trees, 400-landmark submap, 10 GN iterations; value: "
+            "learned proposals (8 per tree, tensor-core network, RANSAC fallback below 0.6 "
+            "inlier ratio) + 3 LS; plain: 256 RANSAC hypotheses per tree + 3 LS")
 # DRAM bytes (read + write) per keyframe of the batch projection stage, summed
 # over its three kernels in one ncu capture with the caches left as they are
 # (dram__bytes_read.sum + dram__bytes_write.sum of the 8-keyframe chunk
@@ -245,41 +246,22 @@ def run_reference(args):
 
 
 # -------------------------------------------------------------- GPU leg
-def main():
-    args = parse()
-    if args.impl == "reference":
-        run_reference(args)
-        return
+def measure(args, L, A, P, forest, kfs, dev, world, mode, weights, clocks_run=None):
+    """One context in cylinder mode `mode` (1 plain RANSAC, 2 learned
+    proposals): the first scan, W warm-up and K timed batch steps."""
     import torch
-    from sloam_gb300 import build, capi as A
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = world > 1
-    if dist:
-        import torch.distributed as tdist
-        torch.cuda.set_device(local)
-        tdist.init_process_group("nccl")
-    if rank == 0:
-        build.build()
-    if dist:
-        tdist.barrier()
-    from sloam_gb300.lib import Context, load
-    L = load()
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
-
-    cfg, forest, kfs, P = workload(args.seed + rank, args.distinct)
-    P.batch_slots = args.slots
-    ctx = Context(P, device=local)
-    mapa = forest.map_cylinders()
-    mapc = A.cylinders_from_array(mapa)
-    nm = len(mapa)
-    N = P.img_w * P.img_h
+    from sloam_gb300.lib import Context
+    Pm = P.copy()
+    Pm.cyl_mode = mode
+    ctx = Context(Pm, device=dev.index or 0)
+    if mode == 2:
+        ctx.set_proposal_weights(weights)
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    nm = len(forest.radius)
+    N = Pm.img_w * Pm.img_h
     B = args.batch
-    # first scan at the true pose defines the previous-scan ground planes
     kf0 = kfs[0]
-    r = A.RunBuffers(P)
+    r = A.RunBuffers(Pm)
     ctx.check(L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), N, A.ptr(kf0.labels, C.c_uint8),
                                None, C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc, nm,
                                C.byref(r.s)))
@@ -303,13 +285,11 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    clocks = Clocks(local)
-    evs = []
-    launches = 0
-    if dist:
+    if world > 1:
+        import torch.distributed as tdist
         tdist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
+    evs, launches = [], 0
     fe_ms, fe_launches, fe_kf = 0.0, 0, 0
     host_s = 0.0  # host time to enqueue a step (the call returns before the GPU is done)
     for s in range(args.steps):
@@ -330,38 +310,117 @@ def main():
         fe_launches += nch.value
         fe_kf += nkf.value
     torch.cuda.synchronize()
+    if world > 1:
+        tdist.barrier()
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), dev)
+    return dict(ctx=ctx, P=Pm, X=X, Lb=Lb, poses=poses, mapc=mapc, nm=nm, N=N, B=B,
+                value=job_value(B, args.steps, world, total_ms), total_ms=total_ms,
+                launches=launches, fe=(fe_ms, fe_launches, fe_kf), host_s=host_s,
+                ok=int(succ.sum().item()), ncyl=float(ncyl.float().mean().item()))
+
+
+def accuracy(L, A, m, forest, kfs):
+    """Median axis / radius error of the fitted cylinders against the
+    generator's trunks over the distinct keyframes, and the trees that fell
+    back to RANSAC.  Each keyframe runs as in the batch: after the first
+    scan (keyframe 0 at its true pose), at its perturbed estimate."""
+    from sloam_gb300 import synth
+    ctx, P = m["ctx"], m["P"]
+    angs, rerrs, fb, nl = [], [], 0, 0
+    stats = (C.c_int32 * 5)()
+    kf0 = kfs[0]
+    for kf in kfs[1:]:
+        ctx.check(L.sloam_reset(ctx.h))
+        r0 = A.RunBuffers(P)
+        ctx.check(L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), m["N"],
+                                   A.ptr(kf0.labels, C.c_uint8), None,
+                                   C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), m["mapc"], m["nm"],
+                                   C.byref(r0.s)))
+        r = A.RunBuffers(P)
+        st = L.sloam_keyframe(ctx.h, A.ptr(kf.xyzi, C.c_float), m["N"],
+                              A.ptr(kf.labels, C.c_uint8), None,
+                              C.byref(A.SE3.from_qt(*kf.pose_est_qt())), m["mapc"], m["nm"],
+                              C.byref(r.s))
+        if st not in (0, A.SLOAM_ERR_NOT_CONVERGED):
+            ctx.check(st)
+        r.refresh()
+        a, e = synth.cylinder_errors(forest, r.m.cyl_array())
+        angs.append(a)
+        rerrs.append(e)
+        L.sloam_keyframe_stats(ctx.h, stats, 5)
+        fb += stats[3]
+        nl += stats[1]
+    a, e = np.concatenate(angs), np.concatenate(rerrs)
+    return {"median_axis_deg": float(np.median(a)), "median_radius_cm": float(100 * np.median(e)),
+            "cylinders_matched": int(len(a)), "keyframes": len(kfs) - 1,
+            "fallback_trees": int(fb), "valid_cylinders": int(nl)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    from sloam_gb300 import build, capi as A, proposal
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    if rank == 0:
+        build.build()
     if dist:
         tdist.barrier()
-    ck = clocks.stop()
-    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), dev)
-    value = job_value(B, args.steps, world, total_ms)
-    ok = int(succ.sum().item())
-    n_cyl = ncyl.cpu().numpy()
+    from sloam_gb300.lib import load
+    L = load()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
 
-    # per-stage breakdown of one keyframe, and the dominant kernel in isolation
+    cfg, forest, kfs, P = workload(args.seed + rank, args.distinct)
+    P.batch_slots = args.slots
+    weights = proposal.load_weights()
+    clocks = Clocks(local)
+    clocks.start()
+    learned = measure(args, L, A, P, forest, kfs, dev, world, 2, weights)
+    plain = measure(args, L, A, P, forest, kfs, dev, world, 1, weights)
+    ck = clocks.stop()
+    ctx = learned["ctx"]
+    N, B, mapc, nm = learned["N"], learned["B"], learned["mapc"], learned["nm"]
+
+    # per-stage breakdown of one keyframe, and kernels in isolation
     stages = (C.c_float * 4)()
     L.sloam_profile_stages(ctx.h, stages, 4)
-    hyp_ms = C.c_float()
-    L.sloam_time_kernel(ctx.h, 1, 20, C.byref(hyp_ms))
-    proj_ms = C.c_float()
-    L.sloam_time_kernel(ctx.h, 0, 20, C.byref(proj_ms))
+    net_ms, proj_ms, cnt_ms = C.c_float(), C.c_float(), C.c_float()
+    ctx.check(L.sloam_time_kernel(ctx.h, 2, 20, C.byref(net_ms)))
+    stats = (C.c_int32 * 5)()
+    L.sloam_keyframe_stats(ctx.h, stats, 5)
+    net_samples = stats[0] * learned["P"].prop_samples
+    ctx.check(L.sloam_time_kernel(ctx.h, 0, 20, C.byref(proj_ms)))
+    plain["ctx"].check(L.sloam_time_kernel(plain["ctx"].h, 1, 20, C.byref(cnt_ms)))
+    acc_l = accuracy(L, A, learned, forest, kfs)
+    acc_p = accuracy(L, A, plain, forest, kfs)
 
     # ---- e2e: the same keyframes through the host C ABI from pinned host
     # buffers (sloam_keyframes_host): host->device copies of every scan and
     # label array and the device->host read of every result are inside the
     # timed region.
-    hX = X.cpu().pin_memory()
-    hL = Lb.cpu().pin_memory()
+    hX = learned["X"].cpu().pin_memory()
+    hL = learned["Lb"].cpu().pin_memory()
     h_pose = np.zeros(B * 7, np.float64)
     h_succ = np.zeros(B, np.int32)
     h_ncyl = np.zeros(B, np.int32)
+    poses = learned["poses"]
 
     def e2e_step():
         ctx.check(L.sloam_keyframes_host(ctx.h, hX.data_ptr(), N, B, hL.data_ptr(), poses, mapc, nm,
                                          h_pose.ctypes.data, h_succ.ctypes.data,
                                          h_ncyl.ctypes.data))
 
-    e2e_step()  # warm-up (graph capture of the slots)
+    e2e_step()  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in range(args.e2e_steps):
@@ -381,6 +440,7 @@ def main():
     except (OSError, ValueError):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    fe_ms, fe_launches, fe_kf = learned["fe"]
     fe_bytes = 26.0 * N * fe_kf
     achieved = fe_bytes / (fe_ms / 1000.0) / 1e9 if fe_ms > 0 else None
     roofline = {
@@ -395,40 +455,62 @@ def main():
         "ms_per_launch": fe_ms / fe_launches if fe_launches else None,
         "launches_timed": fe_launches,
     }
+    # the proposal network (tensor-bound): dense bf16 FLOPs of the two
+    # tensor-core layers per 128-point sample over the isolated launch time
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    net_flops = net_samples * 2.0 * 128 * (64 * 128 + 128 * 256)
+    net_tf = net_flops / (net_ms.value / 1000.0) / 1e12 if net_ms.value > 0 else None
+    roofline_net = {
+        "bound": "tensor", "achieved": net_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+        "frac": net_tf / bf16_peak if net_tf else None, "traffic": None,
+        "kernel": f"k_prop_infer_tc, {net_samples} samples (one keyframe), alone",
+        "flops_per_launch": net_flops, "ms_per_launch": net_ms.value,
+    }
 
     # CPU baseline (rank 0, N=1): the oracle, one host thread, bounded sample
     cpu = None
     if rank == 0 and world == 1:
-        v, n_kf, dt = cpu_run_keyframes(P, forest, kfs, args.cpu_seconds, threads=1)
+        v, n_kf, dt = cpu_run_keyframes(plain["P"], forest, kfs, args.cpu_seconds, threads=1)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"{n_kf} keyframes of the same 64x2048 workload in {dt:.1f} s, "
-                         "one host thread (the reference path is single-threaded)"}
+                         "one host thread, the reference's plain path (the reference path "
+                         "is single-threaded)"}
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "metric": METRIC, "value": learned["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "ms_per_step": learned["total_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "batch_keyframes": B, "distinct_scans": args.distinct,
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{world}"},
+            "learned": {"value": learned["value"], "accuracy": acc_l,
+                        "keyframes_ok": learned["ok"],
+                        "cylinders_per_keyframe": learned["ncyl"]},
+            "plain": {"value": plain["value"], "ms_per_step": plain["total_ms"] / args.steps,
+                      "accuracy": acc_p, "keyframes_ok": plain["ok"],
+                      "cylinders_per_keyframe": plain["ncyl"],
+                      "gpu_launches": int(plain["launches"])},
+            "learned_over_plain": learned["value"] / plain["value"],
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "keyframes_ok": e2e_ok,
-                    "api": "sloam_keyframes_host, pinned host buffers"},
-            "gpu_launches": int(launches),
+                    "api": "sloam_keyframes_host, pinned host buffers, learned path"},
+            "gpu_launches": int(learned["launches"]),
             "stages_ms_per_keyframe": {"project_mask": stages[0], "trellis": stages[1],
                                        "models": stages[2], "assoc_pose": stages[3]},
-            "kernels_ms": {"k_cyl_hyp": hyp_ms.value, "k_project": proj_ms.value},
-            "keyframes_ok": ok, "cylinders_per_keyframe": float(n_cyl.mean()),
-            "host_enqueue_ms_per_step": 1000.0 * host_s / args.steps,
+            "kernels_ms": {"k_prop_infer_tc": net_ms.value, "k_project": proj_ms.value,
+                           "k_cyl_count_plain": cnt_ms.value},
+            "host_enqueue_ms_per_step": 1000.0 * learned["host_s"] / args.steps,
             "clocks": ck,
             "roofline": roofline,
+            "roofline_proposal_net": roofline_net,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    ctx.close()
+    learned["ctx"].close()
+    plain["ctx"].close()
     if dist:
         tdist.destroy_process_group()
 

@@ -1400,10 +1400,13 @@ extern "C" int sloam_profile_stages(sloam_ctx* ctx, float* ms, int n) {
   return SLOAM_OK;
 }
 
-// which: 0 = projection kernel (k_project), 1 = point-cylinder hypothesis
-// kernel (k_cyl_hyp).  Average milliseconds per launch over `reps`.
+// which: 0 = projection kernel (k_project), 1 = point-cylinder inlier
+// counting (k_cyl_count), 2 = the proposal network on the tensor cores over
+// the last keyframe's samples (cyl_mode 2).  Average milliseconds per launch
+// over `reps`.
 extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg_ms) {
-  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 1) return SLOAM_ERR_ARG;
+  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 2) return SLOAM_ERR_ARG;
+  if (which == 2 && (ctx->P.cyl_mode != 2 || !ctx->prop_tc)) return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
   Dev& d = ctx->d;
   if (int st = own_views(ctx)) return st;
@@ -1415,7 +1418,10 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
   CK(cudaEventRecord(a, ctx->st));
   for (int r = 0; r < reps; ++r) {
     if (which == 0) launch_project_kernel(d, ctx->kp, ctx->st);
-    else launch_cyl_hyp_kernel(d, ctx->kp, ctx->st);
+    else if (which == 1) launch_cyl_hyp_kernel(d, ctx->kp, ctx->st);
+    else
+      prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, ctx->kp.prop_S,
+                                    d.prop_cap, d.prop_out, d.prop_err, ctx->st);
   }
   CK(cudaEventRecord(b, ctx->st));
   CK(cudaEventSynchronize(b));
@@ -1473,5 +1479,19 @@ extern "C" int sloam_set_proposal_weights(sloam_ctx* ctx, const float* weights, 
     s.d.prop_tc = ctx->prop_tc;
     destroy_graphs(s.gx);
   }
+  return SLOAM_OK;
+}
+
+// Counts of the last single-keyframe call on the context (not part of the
+// public header): out = {landmarks, valid cylinders, valid planes, trees that
+// fell back to RANSAC (cyl_mode 2), FP64-path projection points}.
+extern "C" int sloam_keyframe_stats(const sloam_ctx* ctx, int32_t* out, int n) {
+  if (!ctx || !out || n < 5) return SLOAM_ERR_ARG;
+  const Counters& c = *ctx->h_cnt;
+  out[0] = c.n_lm;
+  out[1] = c.n_cyl;
+  out[2] = c.n_planes;
+  out[3] = c.n_fallback;
+  out[4] = c.n_slow_px;
   return SLOAM_OK;
 }

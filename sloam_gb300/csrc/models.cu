@@ -18,6 +18,7 @@
 #include <climits>
 
 #include "internal.h"
+#include "proposal.cuh"
 #include "scan_util.cuh"
 
 namespace sg {
@@ -961,19 +962,12 @@ __global__ void __launch_bounds__(256) k_cyl_best(Dev d, const int* __restrict__
 // ----------------------------------------- learned proposals (cyl_mode 2)
 // 8 (prop_S) samples of 128 points per eligible tree, drawn with
 // replacement from the tree's points (Philox keyed by tree id, sample and
-// point), centred on their mean and scaled by their RMS radius.
+// point), centred and scaled by the trimmed frame the network was trained
+// with (prop::sample_frame).
 __global__ void __launch_bounds__(128) k_prop_gather(Dev d, KParams kp) {
   __shared__ float red[4];
   const int nl = d.cnt->n_lm, S = kp.prop_S;
   const int i = threadIdx.x;
-  auto bsum = [&](float v) {
-    v = warp_sum(v);
-    if ((i & 31) == 0) red[i >> 5] = v;
-    __syncthreads();
-    const float t = red[0] + red[1] + red[2] + red[3];
-    __syncthreads();
-    return t;
-  };
   for (int it = blockIdx.x; it < nl * S; it += gridDim.x) {
     const int l = it / S, j = it - l * S;
     const CylD c = d.cyl_all[l];
@@ -986,9 +980,10 @@ __global__ void __launch_bounds__(128) k_prop_gather(Dev d, KParams kp) {
     uint32_t u[4];
     philox(kp.seed, (uint32_t)c.id, (uint32_t)j, 3u, (uint32_t)i, u);
     const float4 p = pts[mulhi_idx(u[0], (uint32_t)n)];
-    const float mx = bsum(p.x) / 128.f, my = bsum(p.y) / 128.f, mz = bsum(p.z) / 128.f;
+    float mm[3], sc;
+    prop::sample_frame(p.x, p.y, p.z, red, mm, &sc);
+    const float mx = mm[0], my = mm[1], mz = mm[2];
     const float dx = p.x - mx, dy = p.y - my, dz = p.z - mz;
-    const float sc = sqrtf(bsum(dx * dx + dy * dy + dz * dz) / 128.f) + 1e-6f;
     float* x = d.prop_x + (size_t)it * 384;
     x[3 * i] = dx / sc;
     x[3 * i + 1] = dy / sc;
@@ -1005,6 +1000,7 @@ __global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * S;
        it += gridDim.x * blockDim.x) {
     const int l = it / S;
+    if (it == l * S) d.pflag[l] = 0;
     d.phyp_cnt[it] = 0;
     float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
     const CylD c = d.cyl_all[l];
@@ -1030,38 +1026,32 @@ __global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
   }
 }
 
-// A tree whose best proposal holds fewer than prop_ratio of its points as
-// inliers falls back to the plain RANSAC hypotheses.
-__global__ void __launch_bounds__(256) k_prop_flag(Dev d, KParams kp) {
-  const int nl = d.cnt->n_lm;
-  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
-    int flag = 0;
-    const CylD c = d.cyl_all[l];
-    if (fit_eligible(c)) {
-      const float4* pts;
-      const float2* uv;
-      int n;
-      tree_points(d, l, &pts, &n, &uv);
-      const int best = (int)(d.pbest[l] >> 32);
-      flag = (float)best < kp.prop_ratio * (float)n ? 1 : 0;
-      if (flag) atomicAdd(&d.cnt->n_fallback, 1);
-    }
-    d.pflag[l] = flag;
-  }
-}
-
 // One block per tree: inliers of the best hypothesis, LS refinement.
+// pass 1: from the best RANSAC hypothesis (cyl_mode 1: every eligible tree;
+// cyl_mode 2: the trees pass 0 flagged).  pass 0 (cyl_mode 2): from the best
+// network proposal; the refined model is kept when its inliers
+// (|distance to the refined axis - radius| < tau) are at least prop_ratio
+// of the tree's points, else the tree is flagged for the RANSAC pass.
 constexpr int kLsThreads = 256;
-__global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
+__global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pass) {
+  __shared__ int s_in[kLsThreads / 32];
   __shared__ float red[20][kLsThreads / 32];
   __shared__ double st[8];  // c(3), dir(3), r, ok
   const int nl = d.cnt->n_lm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
     CylD c = d.cyl_all[l];
-    const bool learned = kp.cyl_mode == 2 && !d.pflag[l];
+    const bool learned = pass == 0;
+    if (c.stage != 1 || c.radius == -1.0) continue;
+    if (!learned && kp.cyl_mode == 2 && !d.pflag[l]) continue;
     const unsigned long long key = learned ? d.pbest[l] : d.cyl_best[l];
-    if (c.stage != 1 || c.radius == -1.0 || key == 0ull) continue;
+    if (key == 0ull) {
+      if (learned && threadIdx.x == 0) {
+        d.pflag[l] = 1;
+        atomicAdd(&d.cnt->n_fallback, 1);
+      }
+      continue;
+    }
     const int h = (int)(0xFFFFFFFFu - (uint32_t)(key & 0xffffffffull));
     const int best_cnt = (int)(key >> 32);
     const float4* pts;
@@ -1109,15 +1099,21 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
       for (int j = 0; j < 20; ++j) acc[j] = 0.f;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 q = pts[i];
-        const float2 uv = uvs[i];
-        const float du = fsub(uv.x, H.cu), dv = fsub(uv.y, H.cv);
-        const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-        if (!((d2 > H.lo2) & (d2 < H.hi2))) continue;
+        if (!learned) {
+          // the inliers of the RANSAC hypothesis, fixed over the iterations
+          const float2 uv = uvs[i];
+          const float du = fsub(uv.x, H.cu), dv = fsub(uv.y, H.cv);
+          const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+          if (!((d2 > H.lo2) & (d2 < H.hi2))) continue;
+        }
         const float wx = q.x - cx, wy = q.y - cy, wz = q.z - cz;
         const float wd = wx * dx + wy * dy + wz * dz;
         const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
         const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
         if (!(rho > 0.f)) continue;
+        // a proposal starts coarser: its inliers follow the current model,
+        // in a band of 2 tau on the first iteration and tau after it
+        if (learned && !(fabsf(rho - rf) < (itn == 0 ? 2.0f : 1.0f) * kp.tau)) continue;
         const float res = rho - rf;
         const float a1 = (px_ * b1x + py_ * b1y + pz_ * b1z) / rho;
         const float a2 = (px_ * b2x + py_ * b2y + pz_ * b2z) / rho;
@@ -1164,6 +1160,35 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp) {
         }
       }
       __syncthreads();
+    }
+    if (learned) {
+      // inliers of the refined model over all the tree's points
+      const float cx = (float)st[0], cy = (float)st[1], cz = (float)st[2];
+      const float dx = (float)st[3], dy = (float)st[4], dz = (float)st[5];
+      const float rf = (float)st[6];
+      int cnt = 0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float4 q = pts[i];
+        const float wx = q.x - cx, wy = q.y - cy, wz = q.z - cz;
+        const float wd = wx * dx + wy * dy + wz * dz;
+        const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
+        const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
+        cnt += fabsf(rho - rf) < kp.tau ? 1 : 0;
+      }
+      cnt = warp_sumi(cnt);
+      if (lane == 0) s_in[w] = cnt;
+      __syncthreads();
+      int tot = 0;
+      for (int q2 = 0; q2 < kLsThreads / 32; ++q2) tot += s_in[q2];
+      const bool keep = st[7] != 0.0 && (float)tot >= kp.prop_ratio * (float)n;
+      __syncthreads();
+      if (!keep) {
+        if (threadIdx.x == 0) {
+          d.pflag[l] = 1;
+          atomicAdd(&d.cnt->n_fallback, 1);
+        }
+        continue;
+      }
     }
     if (threadIdx.x == 0) {
       d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
@@ -1272,10 +1297,11 @@ int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
   return 1;
 }
 
-// mode 1: K random 3-point circles per tree.  mode 2: prop_S network
-// proposals per tree (one tensor-core launch over every sample), their
-// inliers counted; trees below the inlier ratio run the K random circles.
-// Both end in the LS refinement of the best circle.
+// mode 1: K random 3-point circles per tree, LS refinement of the best.
+// mode 2: prop_S network proposals per tree (one tensor-core launch over
+// every sample), inliers counted, the best LS-refined; trees whose refined
+// model holds less than prop_ratio of their points as inliers run the K
+// random circles and their LS refinement.
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream_t st) {
   int n = 0;
   k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
@@ -1288,14 +1314,14 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream
     k_prop_hyp<<<kCylBlocks, 256, 0, st>>>(d, kp);
     k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.phyp, d.phyp_cnt, kp.prop_S, nullptr);
     k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.phyp_cnt, kp.prop_S, d.pbest, nullptr);
-    k_prop_flag<<<kCylBlocks, 256, 0, st>>>(d, kp);
+    k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp, 0);
     n += 4;
     only = d.pflag;
   }
   k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp, only);
   k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.hyp, d.hyp_cnt, kp.K, only);
   k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.hyp_cnt, kp.K, d.cyl_best, only);
-  k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
+  k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp, 1);
   return n + 4;
 }
 

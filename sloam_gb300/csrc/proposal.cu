@@ -8,8 +8,10 @@
 //
 // Training clusters: a trunk of radius U(0.05, 0.8) m, axis tilt U(0, 15)
 // deg, 2-20 m from the sensor, the arc that faces the sensor minus an
-// occluding azimuth wedge of 0-30 % of it, radial noise sigma U(1, 5) cm,
-// 128 points; targets from the generator's own trunk.
+// occluding azimuth wedge of 0-30 % of it, range noise sigma U(1, 5) cm
+// along the beam, and a fraction U(0, 0.15) of range outliers moved
+// U(-1, 1) m along the beam (as segmentation keeps them in the trunk's
+// cluster); 128 points; targets from the generator's own trunk.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -30,15 +32,6 @@ SLOAM_D float u01(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0f); }
 SLOAM_D float gauss(uint32_t a, uint32_t b) {  // Box-Muller
   const float r = sqrtf(-2.0f * logf(fmaxf(u01(a), 1e-7f)));
   return r * cospif(2.0f * u01(b));
-}
-
-SLOAM_D float block_sum128(float v, float* red) {  // 128 threads
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  const float t = red[0] + red[1] + red[2] + red[3];
-  __syncthreads();
-  return t;
 }
 
 // ------------------------------------------------------------ samples
@@ -75,15 +68,25 @@ __global__ void __launch_bounds__(128) k_prop_sample(uint64_t seed, int64_t firs
   philox(seed, g0, g1, 3 + i, 0, q);
   float al = -A + u01(q[0]) * (2.0f * A - wdg);
   if (al >= ws) al += wdg;
-  const float t = u01(q[1]) * h, rr = r + sig * gauss(q[2], q[3]);
+  const float t = u01(q[1]) * h;
   const float ca = cosf(al), sn = sinf(al);
-  const float px = bx + t * ax + rr * (ca * e1x + sn * e2x);
-  const float py = by + t * ay + rr * (ca * e1y + sn * e2y);
-  const float pz = bz + t * az + rr * (ca * e1z + sn * e2z);
-  const float mx = block_sum128(px, red) / kPts, my = block_sum128(py, red) / kPts,
-              mz = block_sum128(pz, red) / kPts;
+  float px = bx + t * ax + r * (ca * e1x + sn * e2x);
+  float py = by + t * ay + r * (ca * e1y + sn * e2y);
+  float pz = bz + t * az + r * (ca * e1z + sn * e2z);
+  {
+    // range noise, and outliers, along the beam (the sensor is the origin)
+    uint32_t o[4];
+    philox(seed, g0, g1, 3 + i, 1, o);
+    const float fo = 0.15f * u01(w[2]);
+    const float dr = u01(o[0]) < fo ? 2.0f * u01(o[1]) - 1.0f : sig * gauss(q[2], q[3]);
+    const float rn = sqrtf(px * px + py * py + pz * pz);
+    const float k = (rn + dr) / rn;
+    px *= k; py *= k; pz *= k;
+  }
+  float mm[3], s;
+  sample_frame(px, py, pz, red, mm, &s);
+  const float mx = mm[0], my = mm[1], mz = mm[2];
   const float dx = px - mx, dy = py - my, dz = pz - mz;
-  const float s = sqrtf(block_sum128(dx * dx + dy * dy + dz * dz, red) / kPts) + 1e-6f;
   float* x = X + (size_t)blockIdx.x * kPts * 3;
   x[3 * i] = dx / s;
   x[3 * i + 1] = dy / s;

@@ -45,3 +45,40 @@ constexpr int kTcBytes = kTcF32Off + 4 * kNumParams;
 
 }  // namespace prop
 }  // namespace sg
+
+#include "common.cuh"
+
+namespace sg {
+namespace prop {
+
+// Centre and scale of a 128-point sample, by the 128 threads of a block
+// (thread i holds point i): mean and RMS radius, then once more over the
+// points within 2.5 RMS of that mean, so that range outliers move neither
+// much.  `red` is 4 floats of shared memory.  Used identically by the
+// training generator and by the pipeline.
+__device__ __forceinline__ float block_sum128(float v, float* red) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  const float t = red[0] + red[1] + red[2] + red[3];
+  __syncthreads();
+  return t;
+}
+__device__ __forceinline__ void sample_frame(float px, float py, float pz, float* red, float* m,
+                                             float* s) {
+  float mx = block_sum128(px, red) / kPts, my = block_sum128(py, red) / kPts,
+        mz = block_sum128(pz, red) / kPts;
+  float dx = px - mx, dy = py - my, dz = pz - mz;
+  const float s1 = sqrtf(block_sum128(dx * dx + dy * dy + dz * dz, red) / kPts);
+  const float in = (dx * dx + dy * dy + dz * dz <= 6.25f * s1 * s1) ? 1.0f : 0.0f;
+  const float n = fmaxf(block_sum128(in, red), 1.0f);
+  mx = block_sum128(in * px, red) / n;
+  my = block_sum128(in * py, red) / n;
+  mz = block_sum128(in * pz, red) / n;
+  dx = px - mx; dy = py - my; dz = pz - mz;
+  m[0] = mx; m[1] = my; m[2] = mz;
+  *s = sqrtf(block_sum128(in * (dx * dx + dy * dy + dz * dz), red) / n) + 1e-6f;
+}
+
+}  // namespace prop
+}  // namespace sg

@@ -80,6 +80,7 @@ def load(path=LIB_PATH):
     L.sloam_time_kernel.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.sloam_frontend_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32)]
+    L.sloam_keyframe_stats.argtypes = [vp, C.POINTER(C.c_int32), C.c_int]
     _lib = L
     return L
 
