@@ -108,7 +108,7 @@ typedef struct sloam_params {
                                        once (each slot owns buffers, a
                                        stream and a captured graph)       */
   int32_t prop_samples;             /* mode 2: network proposals per tree
-                                       (128-point samples)            (8) */
+                                       (128-point samples, 1..8)      (8) */
   float   prop_min_inlier_ratio;    /* mode 2: best proposal's inliers /
                                        tree points below this -> RANSAC
                                        fallback for the tree        (0.6) */

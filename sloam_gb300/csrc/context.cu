@@ -393,7 +393,7 @@ int check_params(const sloam_params& p) {
   if (p.cyl_hypotheses < 0 || p.cyl_hypotheses > 4096 || p.line_ransac_max_iter > 256) return 1;
   if (!(p.ground_retain_thresh > 0)) return 1;
   if (p.batch_slots < 0 || p.batch_slots > 64) return 1;
-  if (p.cyl_mode < 0 || p.cyl_mode > 2 || p.prop_samples < 1 || p.prop_samples > 32) return 1;
+  if (p.cyl_mode < 0 || p.cyl_mode > 2 || p.prop_samples < 1 || p.prop_samples > 8) return 1;
   return 0;
 }
 
@@ -1421,7 +1421,7 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
     else if (which == 1) launch_cyl_hyp_kernel(d, ctx->kp, ctx->st);
     else
       prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, ctx->kp.prop_S,
-                                    d.prop_cap, d.prop_out, d.prop_err, ctx->st);
+                                    d.prop_cap, d.prop_f, d.prop_out, d.prop_err, ctx->st);
   }
   CK(cudaEventRecord(b, ctx->st));
   CK(cudaEventSynchronize(b));

@@ -256,9 +256,11 @@ namespace prop {
 int launch_prop_pack(const float* d_w, unsigned char* d_tcw, cudaStream_t st);
 int launch_prop_infer(const unsigned char* d_tcw, const float* d_x, int n, float* d_out,
                       int* d_err, int mode, cudaStream_t st);
-// tensor-core inference over (*d_n_trees) * per_tree samples (at most cap)
+// tensor-core inference over (*d_n_trees) groups of per_tree samples (at
+// most cap samples); groups whose frame scale (d_frames[first].w) is 0 skip
 int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const int* d_n_trees,
-                            int per_tree, int cap, float* d_out, int* d_err, cudaStream_t st);
+                            int per_tree, int cap, const float4* d_frames, float* d_out,
+                            int* d_err, cudaStream_t st);
 void init_attributes();
 }  // namespace prop
 

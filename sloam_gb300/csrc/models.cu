@@ -971,12 +971,14 @@ __global__ void __launch_bounds__(128) k_prop_gather(Dev d, KParams kp) {
   for (int it = blockIdx.x; it < nl * S; it += gridDim.x) {
     const int l = it / S, j = it - l * S;
     const CylD c = d.cyl_all[l];
-    if (!fit_eligible(c)) continue;
     const float4* pts;
     const float2* uv;
     int n;
     tree_points(d, l, &pts, &n, &uv);
-    if (n < 1) continue;
+    if (!fit_eligible(c) || n < 1) {  // scale 0: the network skips the tree
+      if (i == 0) d.prop_f[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
     uint32_t u[4];
     philox(kp.seed, (uint32_t)c.id, (uint32_t)j, 3u, (uint32_t)i, u);
     const float4 p = pts[mulhi_idx(u[0], (uint32_t)n)];
@@ -1310,7 +1312,7 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream
   if (kp.cyl_mode == 2) {
     k_prop_gather<<<kCountBlocks, 128, 0, st>>>(d, kp);
     n += 1 + prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, kp.prop_S,
-                                           d.prop_cap, d.prop_out, d.prop_err, st);
+                                           d.prop_cap, d.prop_f, d.prop_out, d.prop_err, st);
     k_prop_hyp<<<kCylBlocks, 256, 0, st>>>(d, kp);
     k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.phyp, d.phyp_cnt, kp.prop_S, nullptr);
     k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.phyp_cnt, kp.prop_S, d.pbest, nullptr);

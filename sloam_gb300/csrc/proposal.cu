@@ -481,36 +481,72 @@ SLOAM_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: 
 // TMEM lane r.  Layer 1 and the head on CUDA cores (FP32), layers 2 and 3
 // as tcgen05.mma M=128 (N=128, K=64 then N=256, K=128), bf16 operands from
 // shared memory, fp32 accumulators in 256 TMEM columns (reused).
-constexpr int kTcThreads = 128;
-constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes, kSmA1 = kSmB3 + kTcW3Bytes,
-                   kSmA2 = kSmA1 + kPts * kD1 * 2, kSmW1 = kSmA2 + kPts * kD2 * 2,
-                   kSmPart = kSmW1 + 4 * (3 * kD1 + kD1), kSmH = kSmPart + 4 * 4 * kD3,
-                   kSmY1 = kSmH + 4 * kD3, kSmMisc = kSmY1 + 4 * kD4, kTcSmem = kSmMisc + 64;
+constexpr int kTcThreads = 256;  // two warpgroups, one sample each at a time
+constexpr int kMaxGroup = 8;     // samples per group (one tree's proposals)
+constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes,
+                   kSmA1 = kSmB3 + kTcW3Bytes,                    // [2][128 x 64] bf16
+                   kSmA2 = kSmA1 + 2 * kPts * kD1 * 2,            // [2][128 x 128] bf16
+                   kSmW1 = kSmA2 + 2 * kPts * kD2 * 2,
+                   kSmPart = kSmW1 + 4 * (3 * kD1 + kD1),         // [2][4][256]
+                   kSmH = kSmPart + 4 * 2 * 4 * kD3,              // [group][256]
+                   kSmY1 = kSmH + 4 * kMaxGroup * kD3,            // [group][128]
+                   kSmMisc = kSmY1 + 4 * kMaxGroup * kD4, kTcSmem = kSmMisc + 64;
 static_assert(kSmA1 % 128 == 0 && kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
+static_assert(kTcSmem <= 227 * 1024, "shared memory");
 // the descriptors address at most: A1 [128 x 64], A2 [128 x 128], W2^T
 // [128 x 64], W3^T [256 x 128]; every core matrix lies inside its buffer
 static_assert(core_offset(kPts - 1, kD1 - 1, kD1) + 2 <= kPts * kD1 * 2, "A1 extent");
 static_assert(core_offset(kD3 - 1, kD2 - 1, kD2) + 2 <= kTcW3Bytes, "W3 extent");
 
+SLOAM_D bool mbar_wait_bounded(uint64_t* m, uint32_t phase, int* err, int* abort_flag) {
+  int it = 0;
+  while (!mbar_test(m, phase) && ++it < kMbarSpin) {
+  }
+  if (it >= kMbarSpin) {
+    atomicOr(err, 1);
+    *abort_flag = 1;
+    return false;
+  }
+  return true;
+}
+// barrier of one warpgroup (128 threads); ids 1, 2 (0 is __syncthreads)
+SLOAM_D void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+
+// Tensor-core inference.  Persistent CTAs (one per SM at most: the shared
+// memory allows no second) over groups of `group` samples -- in the
+// pipeline one tree's proposals; groups whose frame scale is 0 (trees not
+// fitted) are skipped.  256 threads: warpgroup g (0, 1) takes samples
+// g, g + 2, ... of the group with its own operand buffers, TMEM columns
+// [256 g, 256 g + 256), mbarrier and barrier, so that one warpgroup's MMAs
+// overlap the other's CUDA-core work.  Thread r of a warpgroup owns point r
+// and TMEM lane r.  Per sample, layer 1 on CUDA cores (FP32) into bf16 A1;
+// layers 2 and 3 as tcgen05.mma M=128 (N=128, K=64, then N=256, K=128),
+// bf16 operands in shared memory, fp32 accumulators in TMEM; the column max
+// over the points by a warp max-reduction of the (non-negative) ReLU
+// outputs' bit patterns.  The head runs once per group, each weight load
+// serving every sample of the group.
 __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const unsigned char* __restrict__ tcw, const float* __restrict__ X, int S,
-    const int* __restrict__ n_trees, int per_tree, float* __restrict__ out,
-    int* __restrict__ err) {
-  // samples: S, or n_trees * per_tree (a count on the device) when given
-  if (n_trees) S = min(S, *n_trees * per_tree);
-  if ((int)blockIdx.x >= S) return;
+    const int* __restrict__ n_groups_dev, int group, const float4* __restrict__ frames,
+    float* __restrict__ out, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   float* w1 = reinterpret_cast<float*>(smem + kSmW1);        // W1 [3][64], b1 [64]
-  float* part = reinterpret_cast<float*>(smem + kSmPart);    // [4][256]
-  float* h = reinterpret_cast<float*>(smem + kSmH);          // [256]
-  float* y1 = reinterpret_cast<float*>(smem + kSmY1);        // [128]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8);
-  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 12);
+  float* h = reinterpret_cast<float*>(smem + kSmH);          // [group][256]
+  float* y1 = reinterpret_cast<float*>(smem + kSmY1);        // [group][128]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 16);
+  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 20);
   const float* f = reinterpret_cast<const float*>(tcw + kTcF32Off);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wg = tid >> 7, lt = tid & 127, wq = warp & 3;
+  float* part = reinterpret_cast<float*>(smem + kSmPart) + wg * 4 * kD3;  // [4][256]
+  unsigned char* a1b = smem + kSmA1 + wg * kPts * kD1 * 2;
+  unsigned char* a2b = smem + kSmA2 + wg * kPts * kD2 * 2;
+  // groups: ceil(S / group), or the device count of groups when given
+  int ng = (S + group - 1) / group;
+  if (n_groups_dev) ng = min(ng, *n_groups_dev);
+  if ((int)blockIdx.x >= ng) return;
 
-  // stage the bf16 weights (80 KB) and W1 / b1
   {
     const uint4* src = reinterpret_cast<const uint4*>(tcw);
     uint4* dst = reinterpret_cast<uint4*>(smem);
@@ -519,10 +555,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   }
   if (tid == 0) {
     mbar_init(mbar, 1);
+    mbar_init(mbar + 1, 1);
     *abort_flag = 0;
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
                      saddr(tslot))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -531,125 +568,138 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   fence_before();
   __syncthreads();
   fence_after();
-  const uint32_t tmem = *tslot;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-  const uint32_t sA1 = saddr(smem + kSmA1), sA2 = saddr(smem + kSmA2);
+  const uint32_t tmem = *tslot + (uint32_t)(wg * 256);
+  const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+  const uint32_t sA1 = saddr(a1b), sA2 = saddr(a2b);
   const uint32_t sB2 = saddr(smem + kSmB2), sB3 = saddr(smem + kSmB3);
+  uint64_t* mb = mbar + wg;
   uint32_t phase = 0;
 
-  for (int s = blockIdx.x; s < S; s += gridDim.x) {
-    // layer 1 (row tid) -> A1 in bf16 core-matrix layout
-    {
-      const float* x = X + (size_t)s * kPts * 3;
-      const float x0 = x[3 * tid], x1 = x[3 * tid + 1], x2 = x[3 * tid + 2];
-      for (int k0 = 0; k0 < kD1; k0 += 8) {
-        uint32_t pk[4];
+  for (int g = blockIdx.x; g < ng; g += gridDim.x) {
+    const int s0 = g * group, gs = min(group, S - s0);
+    if (frames && !(frames[s0].w > 0.0f)) continue;  // block-uniform
+    for (int k = wg; k < gs; k += 2) {
+      const int s = s0 + k;
+      // layer 1 (row lt) -> A1 in bf16 core-matrix layout
+      {
+        const float* x = X + (size_t)s * kPts * 3;
+        const float x0 = x[3 * lt], x1 = x[3 * lt + 1], x2 = x[3 * lt + 2];
+        for (int k0 = 0; k0 < kD1; k0 += 8) {
+          uint32_t pk[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int j = k0 + 2 * q;
-          const float za = w1[3 * kD1 + j] + x0 * w1[j] + x1 * w1[kD1 + j] + x2 * w1[2 * kD1 + j];
-          const float zb = w1[3 * kD1 + j + 1] + x0 * w1[j + 1] + x1 * w1[kD1 + j + 1] +
-                           x2 * w1[2 * kD1 + j + 1];
-          const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
-          pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
+          for (int q = 0; q < 4; ++q) {
+            const int j = k0 + 2 * q;
+            const float za = w1[3 * kD1 + j] + x0 * w1[j] + x1 * w1[kD1 + j] + x2 * w1[2 * kD1 + j];
+            const float zb = w1[3 * kD1 + j + 1] + x0 * w1[j + 1] + x1 * w1[kD1 + j + 1] +
+                             x2 * w1[2 * kD1 + j + 1];
+            const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
+            pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
+          }
+          *reinterpret_cast<uint4*>(a1b + core_offset(lt, k0, kD1)) =
+              make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
-        *reinterpret_cast<uint4*>(smem + kSmA1 + core_offset(tid, k0, kD1)) =
-            make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
-    }
-    fence_async_smem();
-    fence_before();
-    __syncthreads();
-    fence_after();
-    if (tid == 0) {
-      for (int ks = 0; ks < kD1 / 16; ++ks)
-        mma_bf16(tmem, smem_desc(sA1 + ks * 256, 128, (kD1 / 8) * 128),
-                 smem_desc(sB2 + ks * 256, 128, (kD1 / 8) * 128), idesc_bf16(128, kD2), ks > 0);
-      mma_commit(mbar);
-    }
-    {
-      int it = 0;
-      while (!mbar_test(mbar, phase) && ++it < kMbarSpin) {
+      fence_async_smem();
+      fence_before();
+      wg_sync(wg);
+      fence_after();
+      if (lt == 0) {
+        for (int ks = 0; ks < kD1 / 16; ++ks)
+          mma_bf16(tmem, smem_desc(sA1 + ks * 256, 128, (kD1 / 8) * 128),
+                   smem_desc(sB2 + ks * 256, 128, (kD1 / 8) * 128), idesc_bf16(128, kD2), ks > 0);
+        mma_commit(mb);
       }
-      if (it >= kMbarSpin) {
-        atomicOr(err, 1);
-        *abort_flag = 1;
-      }
+      mbar_wait_bounded(mb, phase, err, abort_flag);
       phase ^= 1u;
-    }
-    fence_after();
-    // epilogue 2: bias, ReLU, bf16 -> A2
-    for (int cc = 0; cc < kD2 / 32; ++cc) {
-      uint32_t v[32];
-      SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
-      tmem_wait_ld();
+      fence_after();
+      // epilogue 2: bias, ReLU, bf16 -> A2
+      for (int cc = 0; cc < kD2 / 32; ++cc) {
+        uint32_t v[32];
+        SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
+        tmem_wait_ld();
 #pragma unroll
-      for (int k0 = 0; k0 < 32; k0 += 8) {
-        uint32_t pk[4];
+        for (int k0 = 0; k0 < 32; k0 += 8) {
+          uint32_t pk[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int j = cc * 32 + k0 + 2 * q;
-          const float za = __uint_as_float(v[k0 + 2 * q]) + f[kB2 + j];
-          const float zb = __uint_as_float(v[k0 + 2 * q + 1]) + f[kB2 + j + 1];
-          const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
-          pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
+          for (int q = 0; q < 4; ++q) {
+            const int j = cc * 32 + k0 + 2 * q;
+            const float za = __uint_as_float(v[k0 + 2 * q]) + f[kB2 + j];
+            const float zb = __uint_as_float(v[k0 + 2 * q + 1]) + f[kB2 + j + 1];
+            const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
+            pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
+          }
+          *reinterpret_cast<uint4*>(a2b + core_offset(lt, cc * 32 + k0, kD2)) =
+              make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
-        *reinterpret_cast<uint4*>(smem + kSmA2 + core_offset(tid, cc * 32 + k0, kD2)) =
-            make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
+      fence_async_smem();
+      fence_before();
+      wg_sync(wg);
+      fence_after();
+      if (*abort_flag) break;
+      if (lt == 0) {
+        for (int ks = 0; ks < kD2 / 16; ++ks)
+          mma_bf16(tmem, smem_desc(sA2 + ks * 256, 128, (kD2 / 8) * 128),
+                   smem_desc(sB3 + ks * 256, 128, (kD2 / 8) * 128), idesc_bf16(128, kD3), ks > 0);
+        mma_commit(mb);
+      }
+      mbar_wait_bounded(mb, phase, err, abort_flag);
+      phase ^= 1u;
+      fence_after();
+      // epilogue 3: bias, ReLU; column max over this warp's 32 points
+      for (int cc = 0; cc < kD3 / 32; ++cc) {
+        uint32_t v[32];
+        SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const float a = fmaxf(__uint_as_float(v[q]) + f[kB3 + cc * 32 + q], 0.0f);
+          const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(a));
+          if (lane == q) part[wq * kD3 + cc * 32 + q] = __uint_as_float(m);
+        }
+      }
+      fence_before();
+      wg_sync(wg);
+      for (int c = lt; c < kD3; c += 128)
+        h[k * kD3 + c] =
+            fmaxf(fmaxf(part[c], part[kD3 + c]), fmaxf(part[2 * kD3 + c], part[3 * kD3 + c]));
+      if (*abort_flag) break;
+      fence_before();
+      wg_sync(wg);
+      fence_after();
     }
-    fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     if (*abort_flag) break;
-    if (tid == 0) {
-      for (int ks = 0; ks < kD2 / 16; ++ks)
-        mma_bf16(tmem, smem_desc(sA2 + ks * 256, 128, (kD2 / 8) * 128),
-                 smem_desc(sB3 + ks * 256, 128, (kD2 / 8) * 128), idesc_bf16(128, kD3), ks > 0);
-      mma_commit(mbar);
-    }
+    // head over the group: y1[k][j] = ReLU(b4 + sum_c h[k][c] W4[c][j]);
+    // warpgroup wg takes the samples k = wg (mod 2)
     {
-      int it = 0;
-      while (!mbar_test(mbar, phase) && ++it < kMbarSpin) {
-      }
-      if (it >= kMbarSpin) {
-        atomicOr(err, 1);
-        *abort_flag = 1;
-      }
-      phase ^= 1u;
-    }
-    fence_after();
-    // epilogue 3: bias, ReLU, max over this warp's 32 points per column
-    for (int cc = 0; cc < kD3 / 32; ++cc) {
-      uint32_t v[32];
-      SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
-      tmem_wait_ld();
+      const int j = lt;
+      float acc[kMaxGroup / 2];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        float m = fmaxf(__uint_as_float(v[q]) + f[kB3 + cc * 32 + q], 0.0f);
+      for (int q = 0; q < kMaxGroup / 2; ++q) acc[q] = f[kB4 + j];
+      for (int c = 0; c < kD3; ++c) {
+        const float wv = f[kW4 + c * kD4 + j];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == q) part[warp * kD3 + cc * 32 + q] = m;
+        for (int q = 0; q < kMaxGroup / 2; ++q) {
+          const int k = wg + 2 * q;
+          if (k < gs) acc[q] += h[k * kD3 + c] * wv;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kMaxGroup / 2; ++q) {
+        const int k = wg + 2 * q;
+        if (k < gs) y1[k * kD4 + j] = fmaxf(acc[q], 0.0f);
       }
     }
-    fence_before();
     __syncthreads();
-    for (int c = tid; c < kD3; c += kTcThreads)
-      h[c] = fmaxf(fmaxf(part[c], part[kD3 + c]), fmaxf(part[2 * kD3 + c], part[3 * kD3 + c]));
-    __syncthreads();
-    {
-      float z = f[kB4 + tid];
-      for (int c = 0; c < kD3; ++c) z += h[c] * f[kW4 + c * kD4 + tid];
-      y1[tid] = fmaxf(z, 0.0f);
+    for (int t = tid; t < gs * kD5; t += kTcThreads) {
+      const int k = t / kD5, o = t - k * kD5;
+      float z = f[kB5 + o];
+      for (int j = 0; j < kD4; ++j) z += y1[k * kD4 + j] * f[kW5 + j * kD5 + o];
+      out[(size_t)(s0 + k) * 8 + o] = z;
     }
-    __syncthreads();
-    if (tid < kD5) {
-      float o = f[kB5 + tid];
-      for (int j = 0; j < kD4; ++j) o += y1[j] * f[kW5 + j * kD5 + tid];
-      out[(size_t)s * 8 + tid] = o;
-    }
-    if (*abort_flag) break;
     fence_before();
     __syncthreads();
     fence_after();
@@ -658,7 +708,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   __syncthreads();
   fence_after();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(*tslot) : "memory");
 }
 
 int g_tc_attr = 0;
@@ -682,11 +732,13 @@ static int sm_count() {
 }
 
 int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const int* d_n_trees,
-                            int per_tree, int cap, float* d_out, int* d_err, cudaStream_t st) {
+                            int per_tree, int cap, const float4* d_frames, float* d_out,
+                            int* d_err, cudaStream_t st) {
   init_attributes();
-  const int grid = cap < sm_count() ? (cap > 0 ? cap : 1) : sm_count();
-  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, cap, d_n_trees, per_tree, d_out,
-                                                     d_err);
+  const int groups = (cap + per_tree - 1) / per_tree;
+  const int grid = groups < sm_count() ? (groups > 0 ? groups : 1) : sm_count();
+  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, cap, d_n_trees, per_tree,
+                                                     d_frames, d_out, d_err);
   return 1;
 }
 
@@ -703,8 +755,10 @@ int launch_prop_infer(const unsigned char* d_tcw, const float* d_x, int n, float
     k_prop_infer_ref<<<n, 128, kRefSmem, st>>>(d_tcw, d_x, n, d_out);
     return 1;
   }
-  const int grid = n < sm_count() ? n : sm_count();
-  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, n, nullptr, 0, d_out, d_err);
+  const int groups = (n + kMaxGroup - 1) / kMaxGroup;
+  const int grid = groups < sm_count() ? groups : sm_count();
+  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, n, nullptr, kMaxGroup, nullptr,
+                                                     d_out, d_err);
   return 1;
 }
 
