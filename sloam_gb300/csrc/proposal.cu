@@ -490,9 +490,11 @@ constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes,
                    kSmPart = kSmW1 + 4 * (3 * kD1 + kD1),         // [2][4][256]
                    kSmH = kSmPart + 4 * 2 * 4 * kD3,              // [group][256]
                    kSmY1 = kSmH + 4 * kMaxGroup * kD3,            // [group][128]
-                   kSmMisc = kSmY1 + 4 * kMaxGroup * kD4, kTcSmem = kSmMisc + 64;
+                   kSmBias = kSmY1 + 4 * kMaxGroup * kD4,         // b2, b3, b4, W5, b5
+                   kSmMisc = kSmBias + 4 * (kD2 + kD3 + kD4 + kD4 * kD5 + 8),
+                   kTcSmem = kSmMisc + 64;
 static_assert(kSmA1 % 128 == 0 && kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
-static_assert(kTcSmem <= 227 * 1024, "shared memory");
+static_assert(kSmMisc % 16 == 0 && kTcSmem <= 227 * 1024, "shared memory");
 // the descriptors address at most: A1 [128 x 64], A2 [128 x 128], W2^T
 // [128 x 64], W3^T [256 x 128]; every core matrix lies inside its buffer
 static_assert(core_offset(kPts - 1, kD1 - 1, kD1) + 2 <= kPts * kD1 * 2, "A1 extent");
@@ -533,6 +535,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   float* w1 = reinterpret_cast<float*>(smem + kSmW1);        // W1 [3][64], b1 [64]
   float* h = reinterpret_cast<float*>(smem + kSmH);          // [group][256]
   float* y1 = reinterpret_cast<float*>(smem + kSmY1);        // [group][128]
+  float* sb2 = reinterpret_cast<float*>(smem + kSmBias);     // b2 [128]
+  float* sb3 = sb2 + kD2;                                    // b3 [256]
+  float* sb4 = sb3 + kD3;                                    // b4 [128]
+  float* sw5 = sb4 + kD4;                                    // W5 [128][7]
+  float* sb5 = sw5 + kD4 * kD5;                              // b5 [7]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 16);
   int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 20);
@@ -552,6 +559,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     uint4* dst = reinterpret_cast<uint4*>(smem);
     for (int i = tid; i < (kTcW2Bytes + kTcW3Bytes) / 16; i += kTcThreads) dst[i] = src[i];
     for (int i = tid; i < 4 * kD1; i += kTcThreads) w1[i] = f[kW1 + i];
+    for (int i = tid; i < kD2; i += kTcThreads) sb2[i] = f[kB2 + i];
+    for (int i = tid; i < kD3; i += kTcThreads) sb3[i] = f[kB3 + i];
+    for (int i = tid; i < kD4; i += kTcThreads) sb4[i] = f[kB4 + i];
+    for (int i = tid; i < kD4 * kD5 + kD5; i += kTcThreads) sw5[i] = f[kW5 + i];  // W5, b5
   }
   if (tid == 0) {
     mbar_init(mbar, 1);
@@ -623,8 +634,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             const int j = cc * 32 + k0 + 2 * q;
-            const float za = __uint_as_float(v[k0 + 2 * q]) + f[kB2 + j];
-            const float zb = __uint_as_float(v[k0 + 2 * q + 1]) + f[kB2 + j + 1];
+            const float za = __uint_as_float(v[k0 + 2 * q]) + sb2[j];
+            const float zb = __uint_as_float(v[k0 + 2 * q + 1]) + sb2[j + 1];
             const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
             pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
           }
@@ -653,7 +664,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
         tmem_wait_ld();
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
-          const float a = fmaxf(__uint_as_float(v[q]) + f[kB3 + cc * 32 + q], 0.0f);
+          const float a = fmaxf(__uint_as_float(v[q]) + sb3[cc * 32 + q], 0.0f);
           const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(a));
           if (lane == q) part[wq * kD3 + cc * 32 + q] = __uint_as_float(m);
         }
@@ -678,7 +689,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
       const int j = lt;
       float acc[kMaxGroup / 2];
 #pragma unroll
-      for (int q = 0; q < kMaxGroup / 2; ++q) acc[q] = f[kB4 + j];
+      for (int q = 0; q < kMaxGroup / 2; ++q) acc[q] = sb4[j];
       for (int c = 0; c < kD3; ++c) {
         const float wv = f[kW4 + c * kD4 + j];
 #pragma unroll
@@ -696,8 +707,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     __syncthreads();
     for (int t = tid; t < gs * kD5; t += kTcThreads) {
       const int k = t / kD5, o = t - k * kD5;
-      float z = f[kB5 + o];
-      for (int j = 0; j < kD4; ++j) z += y1[k * kD4 + j] * f[kW5 + j * kD5 + o];
+      float z = sb5[o];
+      for (int j = 0; j < kD4; ++j) z += y1[k * kD4 + j] * sw5[j * kD5 + o];
       out[(size_t)(s0 + k) * 8 + o] = z;
     }
     fence_before();
