@@ -326,7 +326,7 @@ def accuracy(L, A, m, forest, kfs):
     scan (keyframe 0 at its true pose), at its perturbed estimate."""
     from sloam_gb300 import synth
     ctx, P = m["ctx"], m["P"]
-    angs, rerrs, fb, nl = [], [], 0, 0
+    angs, rerrs, fb, nl, slow = [], [], 0, 0, 0
     stats = (C.c_int32 * 5)()
     kf0 = kfs[0]
     for kf in kfs[1:]:
@@ -350,10 +350,12 @@ def accuracy(L, A, m, forest, kfs):
         L.sloam_keyframe_stats(ctx.h, stats, 5)
         fb += stats[3]
         nl += stats[1]
+        slow += stats[4]
     a, e = np.concatenate(angs), np.concatenate(rerrs)
     return {"median_axis_deg": float(np.median(a)), "median_radius_cm": float(100 * np.median(e)),
             "cylinders_matched": int(len(a)), "keyframes": len(kfs) - 1,
-            "fallback_trees": int(fb), "valid_cylinders": int(nl)}
+            "fallback_trees": int(fb), "valid_cylinders": int(nl),
+            "fp64_projection_points_per_keyframe": slow / max(len(kfs) - 1, 1)}
 
 
 def main():

@@ -325,6 +325,22 @@ int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t n
                          const sloam_cylinder* map, int32_t n_map, double* pose_out,
                          int32_t* success_out, int32_t* ncyl_out);
 
+/* Input ingestion (pcl::fromROSMsg at inputNode.cpp:247 and the XYZI
+ * packing of inference.cpp:374-379, on the device): n points of a
+ * sensor message with point_step bytes per point and little-endian fields
+ * at the given byte offsets (x, y, z float32; intensity per
+ * intensity_type) packed into float4 XYZI (d_xyzi [n*4]) on `stream`
+ * (a cudaStream_t, NULL = default).  Device pointers; the caller owns both
+ * buffers.  The layout of a sensor_msgs/PointCloud2 (e.g. an Ouster cloud:
+ * point_step 48, x 0, y 4, z 8, intensity 16 float32). */
+#define SLOAM_FIELD_NONE    0
+#define SLOAM_FIELD_FLOAT32 1
+#define SLOAM_FIELD_UINT16  2
+#define SLOAM_FIELD_UINT8   3
+int sloam_pack_points(const void* d_points, int32_t n, int32_t point_step, int32_t off_x,
+                      int32_t off_y, int32_t off_z, int32_t off_i, int32_t intensity_type,
+                      float* d_xyzi, void* stream);
+
 /* Weights of the learned cylinder proposal (cyl_mode 2; no reference
  * counterpart): n = 75399 FP32 values of the point-set network
  * (shared MLP 3-64-128-256, max-pool, head 256-128-7, row-major W[in][out]

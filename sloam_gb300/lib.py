@@ -17,7 +17,7 @@ EXPORTS = [
     "sloam_trellis", "sloam_compute_models", "sloam_fit_plane", "sloam_fit_cylinders",
     "sloam_run", "sloam_keyframe",
     "sloam_keyframes_device", "sloam_keyframes_host", "sloam_last_launch_count", "sloam_stream",
-    "sloam_internal_tables", "sloam_set_proposal_weights",
+    "sloam_internal_tables", "sloam_set_proposal_weights", "sloam_pack_points",
 ]
 
 _lib = None
@@ -71,6 +71,8 @@ def load(path=LIB_PATH):
     L.sloam_project_mask_noalloc.argtypes = [C.POINTER(A.Params), vp, C.c_int32, vp, vp, vp, vp,
                                              vp, vp, vp, vp, vp]
     L.sloam_set_proposal_weights.argtypes = [vp, C.POINTER(C.c_float), C.c_int32]
+    L.sloam_pack_points.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.c_int32, C.c_int32, vp, vp]
     L.sloam_last_launch_count.argtypes = [vp]
     L.sloam_last_launch_count.restype = C.c_int64
     L.sloam_stream.argtypes = [vp]
