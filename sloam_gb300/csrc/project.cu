@@ -177,80 +177,119 @@ __device__ __forceinline__ uint8_t pixel_label(const FrontRef& f, int pix, int p
   return (uint8_t)f.pkey[pix];
 }
 
-// Thread o is pixel o and point o.  Pixel: range image and mask from the
+// The label stage works in blocks of 1024 pixels / points (the ground
+// bits, 32 per word, and the per-block ground counts); 256 threads take 4
+// each, at a stride of 256, all loads issued before use.
+constexpr int kLabelThreads = 256, kLabelPer = 4;
+static_assert(kLabelThreads * kLabelPer == 1024, "label block");
+
+// Index o is pixel o and point o.  Pixel: range image and mask from the
 // winner.  Point: maskCloud -- the organised tree cloud (with the Ouster
 // destagger as a gather: even rows take x,y,z from column c-32 for c >= 32
 // and keep their own intensity; inference.cpp:200-228) and the ground bit,
 // both from the label of the point's pixel.
 template <bool kBatch>
-__global__ void __launch_bounds__(1024) k_label(Dev d, KParams kp, const FrontRef* refs, int kf0,
-                                                int point_labels) {
+__global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, const FrontRef* refs,
+                                                         int kf0, int point_labels) {
   __shared__ int sm[33];
   const FrontRef f = front<kBatch>(d, refs, kf0);
   const int N = d.N, W = kp.img_w;
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  bool ground = false;
-  if (o < N) {
-    const unsigned long long key = f.pkey[o];
-    float r = 0.0f;
-    uint8_t m = 0;
-    if (key != ~0ull) {
-      r = __uint_as_float((uint32_t)(key >> 32));
-      if (point_labels) m = (uint8_t)key;
+  const int o0 = blockIdx.x * 1024 + threadIdx.x;
+  const float nan = __int_as_float(0x7fc00000);
+  unsigned long long key[kLabelPer];
+  int pix[kLabelPer], spix[kLabelPer];
+  float4 src[kLabelPer], sq[kLabelPer];
+  bool stag[kLabelPer];
+  uint8_t min_[kLabelPer];
+#pragma unroll
+  for (int j = 0; j < kLabelPer; ++j) {
+    const int o = o0 + j * kLabelThreads;
+    key[j] = ~0ull;
+    pix[j] = 0;
+    stag[j] = false;
+    if (o < N) {
+      key[j] = f.pkey[o];
+      pix[j] = f.pix[o];
+      src[j] = f.xyzi[o];
+      min_[j] = point_labels ? 0 : f.mask_in[o];
+      const int row = o / W, c = o - row * W;
+      stag[j] = kp.do_destagger && (row & 1) == 0 && c >= 32;
+      if (stag[j]) {
+        spix[j] = f.pix[o - 32];
+        sq[j] = f.xyzi[o - 32];
+      }
     }
-    if (!point_labels) m = f.mask_in[o];
-    f.range_img[o] = r;
-    f.mask[o] = m;
-
-    const uint8_t mo = pixel_label(f, f.pix[o], point_labels);
-    ground = (mo == 1);
-    const float nan = __int_as_float(0x7fc00000);
-    const float4* X = f.xyzi;
-    float4 src = X[o];
-    float4 t = (mo == 255) ? src : make_float4(nan, nan, nan, 0.0f);
-    const int row = o / W, c = o - row * W;
-    if (kp.do_destagger && (row & 1) == 0 && c >= 32) {
-      const int s = o - 32;
-      const uint8_t ms = pixel_label(f, f.pix[s], point_labels);
-      float4 q = X[s];
-      t.x = (ms == 255) ? q.x : nan;
-      t.y = (ms == 255) ? q.y : nan;
-      t.z = (ms == 255) ? q.z : nan;
-    }
-    f.tree[o] = t;
   }
-  const unsigned b = __ballot_sync(0xffffffffu, ground);
-  if ((threadIdx.x & 31) == 0 && o < N + 31) f.gbits[o >> 5] = b;
+  int cnt = 0;
+#pragma unroll
+  for (int j = 0; j < kLabelPer; ++j) {
+    const int o = o0 + j * kLabelThreads;
+    bool ground = false;
+    if (o < N) {
+      float r = 0.0f;
+      uint8_t m = 0;
+      if (key[j] != ~0ull) {
+        r = __uint_as_float((uint32_t)(key[j] >> 32));
+        if (point_labels) m = (uint8_t)key[j];
+      }
+      if (!point_labels) m = min_[j];
+      f.range_img[o] = r;
+      f.mask[o] = m;
+      const uint8_t mo = pixel_label(f, pix[j], point_labels);
+      ground = (mo == 1);
+      float4 t = (mo == 255) ? src[j] : make_float4(nan, nan, nan, 0.0f);
+      if (stag[j]) {
+        const uint8_t ms = pixel_label(f, spix[j], point_labels);
+        t.x = (ms == 255) ? sq[j].x : nan;
+        t.y = (ms == 255) ? sq[j].y : nan;
+        t.z = (ms == 255) ? sq[j].z : nan;
+      }
+      f.tree[o] = t;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, ground);
+    if ((threadIdx.x & 31) == 0 && o < N + 31) f.gbits[o >> 5] = b;
+    cnt += ground ? 1 : 0;
+  }
   int total;
-  block_excl_scan(ground ? 1 : 0, sm, &total);
+  block_excl_scan(cnt, sm, &total);
   if (threadIdx.x == 0) f.blk[blockIdx.x] = total;
 }
 
-// Ordered compaction of the ground points (point order); re-arms the pixel
-// keys for the next scan.
+// Ordered compaction of the ground points (point order: the 4 slices of a
+// block in turn); re-arms the pixel keys for the next scan.
 template <bool kBatch>
-__global__ void __launch_bounds__(1024) k_ground_compact(Dev d, const FrontRef* refs, int kf0) {
+__global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const FrontRef* refs,
+                                                                  int kf0) {
   __shared__ int sm[33];
   const FrontRef f = front<kBatch>(d, refs, kf0);
   const int N = d.N;
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned b = (o < N + 31) ? f.gbits[o >> 5] : 0u;
-  const bool g = o < N && ((b >> (threadIdx.x & 31)) & 1u);
-  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (g) v = f.xyzi[o];  // issued before the prefix sums
-  if (o < N) f.pkey[o] = ~0ull;
-  const int base = block_sum_prefix(f.blk, blockIdx.x, sm);
-  int total;
-  const int ex = block_excl_scan(g ? 1 : 0, sm, &total);
-  const int pos = base + ex;
-  if (g) {
-    f.ground_idx[pos] = o;
-    if (pos < d.cap_ground) f.ground[pos] = v;
+  const int o0 = blockIdx.x * 1024 + threadIdx.x;
+  bool g[kLabelPer];
+  float4 v[kLabelPer];
+#pragma unroll
+  for (int j = 0; j < kLabelPer; ++j) {
+    const int o = o0 + j * kLabelThreads;
+    const unsigned b = (o < N + 31) ? f.gbits[o >> 5] : 0u;
+    g[j] = o < N && ((b >> (threadIdx.x & 31)) & 1u);
+    v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g[j]) v[j] = f.xyzi[o];  // issued before the prefix sums
+    if (o < N) f.pkey[o] = ~0ull;
+  }
+  int run = block_sum_prefix(f.blk, blockIdx.x, sm);
+#pragma unroll
+  for (int j = 0; j < kLabelPer; ++j) {
+    const int o = o0 + j * kLabelThreads;
+    int total;
+    const int pos = run + block_excl_scan(g[j] ? 1 : 0, sm, &total);
+    if (g[j]) {
+      f.ground_idx[pos] = o;
+      if (pos < d.cap_ground) f.ground[pos] = v[j];
+    }
+    run += total;
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-    const int n = base + total;
-    *fe_slot<kBatch>(d, f, 0) = n < d.cap_ground ? n : d.cap_ground;
-    if (n > d.cap_ground) atomicOr(fe_slot<kBatch>(d, f, 1), 1);
+    *fe_slot<kBatch>(d, f, 0) = run < d.cap_ground ? run : d.cap_ground;
+    if (run > d.cap_ground) atomicOr(fe_slot<kBatch>(d, f, 1), 1);
   }
 }
 
@@ -295,8 +334,8 @@ int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
 }
 int launch_project_rest(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st) {
   const int g1k = front_blocks(d.N);
-  k_label<false><<<g1k, 1024, 0, st>>>(d, kp, nullptr, 0, point_labels ? 1 : 0);
-  k_ground_compact<false><<<g1k, 1024, 0, st>>>(d, nullptr, 0);
+  k_label<false><<<g1k, kLabelThreads, 0, st>>>(d, kp, nullptr, 0, point_labels ? 1 : 0);
+  k_ground_compact<false><<<g1k, kLabelThreads, 0, st>>>(d, nullptr, 0);
   return 2;
 }
 
@@ -310,8 +349,8 @@ int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, 
   if (nkf <= 0) return 0;
   const dim3 g256((d.N + 255) / 256, nkf), g1k(front_blocks(d.N), nkf);
   k_project<true><<<g256, 256, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
-  k_label<true><<<g1k, 1024, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
-  k_ground_compact<true><<<g1k, 1024, 0, st>>>(d, refs, kf0);
+  k_label<true><<<g1k, kLabelThreads, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
+  k_ground_compact<true><<<g1k, kLabelThreads, 0, st>>>(d, refs, kf0);
   return 3;
 }
 
