@@ -7,11 +7,14 @@
 // round-to-nearest, unfused, in the reference's order; yaw and pitch are the
 // correctly rounded float atan2/asin.  Yaw enters the column through a double
 // expression, so the column is read from an exact boundary table built on the
-// host (px_tab[k] = smallest float yaw whose column is >= k).  The fast path
-// evaluates atan2f/asinf in FP32 and accepts the result when a +-1.2e-6
-// relative margin (about 10 ulp, above the documented error of the CUDA
-// functions) cannot change the pixel; otherwise the point takes the FP64
-// path.  The row likewise comes from an exact boundary table of the pitch.
+// host (px_tab[k] = smallest float yaw whose column is >= k).  The first try
+// evaluates yaw and pitch with the FP32 polynomials of fastpoly.cuh (at most
+// 4.9e-7 relative from the correctly rounded angle), reads the table entry
+// the column/row formula estimates, and accepts it when the whole +-1.2e-6
+// relative margin (about 10 ulp) lies inside that entry; otherwise the
+// column takes the FP64 path and the row the library asinf under the same
+// margin, then FP64.  The row likewise comes from an exact boundary table of
+// the pitch.
 // The nearest point wins its pixel: 64-bit atomicMin on
 // range bits (32) : point index (24) : point label (8), ties to the lowest
 // index; the label rides in the key so the winner's label needs no gather.
@@ -22,6 +25,7 @@
 // keyframe's FrontRef.
 #include "internal.h"
 #include "scan_util.cuh"
+#include "fastpoly.cuh"
 
 namespace sg {
 
@@ -36,6 +40,14 @@ __device__ __forceinline__ int table_index(const float* __restrict__ tab, float 
   while (k < n - 1 && v >= __ldg(tab + k + 1)) ++k;
   while (k > 0 && v < __ldg(tab + k)) --k;
   return k;
+}
+// Entry k = the estimate e truncated into [0, n-1] when the whole interval
+// [v - m, v + m] lies in it (tab[k] <= v - m and v + m < tab[k+1]), else
+// -1: two loads and no search.
+__device__ __forceinline__ int table_guess(const float* __restrict__ tab, float v, float m,
+                                           float e, int n) {
+  const int k = min(n - 1, max(0, __float2int_rz(e)));
+  return (__ldg(tab + k) <= v - m && v + m < __ldg(tab + k + 1)) ? k : -1;
 }
 // The index of v when the whole interval [v - m, v + m] has it, else -1.
 __device__ __forceinline__ int table_index_margin(const float* __restrict__ tab, float v,
@@ -82,20 +94,21 @@ __device__ __forceinline__ int32_t* fe_slot(const Dev& d, const FrontRef& f, int
   return which == 0 ? &d.cnt->n_ground : which == 1 ? &d.cnt->overflow : &d.cnt->n_slow_px;
 }
 
-// Pixel keys are combined before the atomics: one atomicMin per distinct
-// pixel per warp, and for pixel (0, W-1) -- where every no-return (NaN)
-// point lands -- one per block through shared memory.  The minimum is the
-// same, so the winner is unchanged.
+// In an organised scan the points of a warp fall on distinct pixels, so each
+// point makes its own 64-bit atomicMin.  Pixel (H-1, W-1), where every
+// no-return (NaN) point lands, is the exception: its keys are reduced over
+// the warp (two full-warp min reductions), kept as a running minimum per
+// warp, and sent by one atomic per block.  The minimum is the same, so the
+// winner is unchanged.
 template <bool kBatch>
 __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontRef* refs,
                                                  int kf0, int point_labels) {
-  __shared__ unsigned long long hot_min;
+  __shared__ unsigned long long hot_w[8];
   const FrontRef f = front<kBatch>(d, refs, kf0);
   const int N = d.N, W = kp.img_w, H = kp.img_h;
   const int hot = N - 1;  // the pixel of NaN points: row H - 1, column W - 1
   const int lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) hot_min = ~0ull;
-  __syncthreads();
+  unsigned long long hot_acc = ~0ull;  // this warp's least key at `hot`
   int slow = 0;
   for (int i0 = blockIdx.x * blockDim.x; i0 < N; i0 += gridDim.x * blockDim.x) {
     const int i = i0 + threadIdx.x;
@@ -107,64 +120,65 @@ __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontR
       const uint32_t lab = point_labels ? f.plabel[i] : 0u;
       const float x = p.x, y = p.y, z = p.z;
       const float range = fsqrt(fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z)));
-      // ---- column
-      int px;
-      {
-        float yaw = -atan2f(y, x);
-        // NaN in, NaN out on both paths: no-return points stay on the fast path.
-        const bool nan_in = isnan(x) || isnan(y);
-        if (nan_in) {
-          px = W - 1;
-        } else {
-          px = -1;
-          if (!(isinf(x) || isinf(y) || x == 0.0f || y == 0.0f))
-            px = table_index_margin(d.px_tab, yaw, fmaxf(fabsf(yaw) * 1.2e-6f, 1e-30f),
-                                    col_estimate(yaw, W), W);
-          if (px < 0) {
-            yaw = -(float)atan2((double)y, (double)x);
-            px = table_index(d.px_tab, yaw, col_estimate(yaw, W), W);
-            ++slow;
-          }
+      // ---- first try: own polynomial angles, the table entry the formula
+      // estimates, accepted when the margin interval lies inside it
+      const bool nan_xy = isnan(x) || isnan(y);
+      const float mx = fmaxf(fabsf(x), fabsf(y)), mn = fminf(fabsf(x), fabsf(y));
+      const float yaw0 = -atan2_poly(y, x);
+      int px = (mn >= 1e-18f && mx <= 1e18f)
+                   ? table_guess(d.px_tab, yaw0, fmaxf(fabsf(yaw0) * 1.2e-6f, 1e-30f),
+                                 col_estimate(yaw0, W), W)
+                   : -1;
+      px = nan_xy ? W - 1 : px;  // NaN in, NaN out: column W - 1
+      const float q = fdiv(z, range);
+      const float aq = fabsf(q);
+      const float pitch0 = asin05_poly(q);
+      int g = aq <= 0.5f ? table_guess(d.py_tab, pitch0, fmaxf(fabsf(pitch0) * 1.2e-6f, 1e-30f),
+                                       row_estimate(pitch0, kp), H)
+                         : -1;
+      g = isnan(q) ? 0 : g;  // NaN: row H - 1
+      // ---- exact column: correctly rounded yaw from FP64
+      if (px < 0) {
+        const float yaw = -(float)atan2((double)y, (double)x);
+        px = table_index(d.px_tab, yaw, col_estimate(yaw, W), W);
+        ++slow;
+      }
+      // ---- exact row: the library asinf under the same margin, else FP64
+      if (g < 0) {
+        if (aq < 1.0f) {
+          const float pitch = asinf(q);
+          g = table_index_margin(d.py_tab, pitch, fmaxf(fabsf(pitch) * 1.2e-6f, 1e-30f),
+                                 row_estimate(pitch, kp), H);
+        }
+        if (g < 0) {
+          const float pitch = (float)asin((double)q);
+          g = table_index(d.py_tab, pitch, row_estimate(pitch, kp), H);
+          ++slow;
         }
       }
-      // ---- row
-      int py;
-      {
-        const float q = fdiv(z, range);
-        float pitch = asinf(q);
-        if (isnan(q)) {
-          py = H - 1;
-        } else {
-          int g = -1;
-          if (fabsf(q) < 1.0f)
-            g = table_index_margin(d.py_tab, pitch, fmaxf(fabsf(pitch) * 1.2e-6f, 1e-30f),
-                                   row_estimate(pitch, kp), H);
-          if (g < 0) {
-            pitch = (float)asin((double)q);
-            g = table_index(d.py_tab, pitch, row_estimate(pitch, kp), H);
-            ++slow;
-          }
-          py = H - 1 - g;
-        }
-      }
+      const int py = H - 1 - g;
       pix = py * W + px;
       f.pix[i] = pix;
       key = ((unsigned long long)range_key(range) << 32) | ((uint32_t)i << 8) | lab;
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, pix);
-    const uint32_t hi = (uint32_t)(key >> 32);
-    const uint32_t hmin = __reduce_min_sync(peers, hi);
-    const uint32_t lmin = __reduce_min_sync(peers, hi == hmin ? (uint32_t)key : 0xffffffffu);
-    if (valid && lane == __ffs(peers) - 1) {
+    const bool at_hot = valid && pix == hot;
+    if (valid && !at_hot) atomicMin(f.pkey + pix, key);
+    if (__any_sync(0xffffffffu, at_hot)) {
+      const uint32_t hi = at_hot ? (uint32_t)(key >> 32) : 0xffffffffu;
+      const uint32_t hmin = __reduce_min_sync(0xffffffffu, hi);
+      const uint32_t lmin =
+          __reduce_min_sync(0xffffffffu, (at_hot && hi == hmin) ? (uint32_t)key : 0xffffffffu);
       const unsigned long long kmin = ((unsigned long long)hmin << 32) | lmin;
-      if (pix == hot)
-        atomicMin(&hot_min, kmin);
-      else
-        atomicMin(f.pkey + pix, kmin);
+      hot_acc = kmin < hot_acc ? kmin : hot_acc;
     }
   }
+  if (lane == 0) hot_w[threadIdx.x >> 5] = hot_acc;
   __syncthreads();
-  if (threadIdx.x == 0 && hot_min != ~0ull) atomicMin(f.pkey + hot, hot_min);
+  if (threadIdx.x == 0) {
+    unsigned long long m = hot_w[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = hot_w[w] < m ? hot_w[w] : m;
+    if (m != ~0ull) atomicMin(f.pkey + hot, m);
+  }
   slow = warp_sumi(slow);
   if (lane == 0 && slow) atomicAdd(fe_slot<kBatch>(d, f, 2), slow);
 }
