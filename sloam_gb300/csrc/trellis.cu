@@ -41,45 +41,131 @@ __device__ __forceinline__ uint32_t cc_find(volatile uint32_t* P, uint32_t x) {
   return x;
 }
 
-__global__ void __launch_bounds__(256) k_cc_init(Dev d) {
-  const float4* __restrict__ tree = d.in->tree;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.N; p += gridDim.x * blockDim.x)
-    d.parent[p] = isfinite(tree[p].x) ? (uint32_t)p : kInvalid;
+// Union of the components of u and v in parent array P (roots are the
+// minimum index: the larger root is linked under the smaller by CAS).
+// Returns false when the retry limit ran out.
+template <typename T, typename Find>
+__device__ __forceinline__ bool cc_union(T* P, T u, T v, Find find) {
+  for (int it = 0; it < kCCIterLimit; ++it) {
+    T ru = find(u), rv = find(v);
+    if (ru == rv) return true;
+    if (ru > rv) { const T t = ru; ru = rv; rv = t; }
+    const T old = atomicCAS(P + rv, rv, ru);
+    if (old == rv) return true;
+    u = ru;
+    v = old;
+  }
+  return false;
 }
 
-__global__ void __launch_bounds__(256) k_cc_union(Dev d, float thr) {
-  volatile uint32_t* P = d.parent;
+// a3, first level: one block per 32 x 32 pixel tile, one warp per tile row
+// (lane = column).  Horizontal runs come from one ballot: every valid pixel
+// points at the first pixel of its run.  Vertical neighbours then join the
+// run roots in a shared-memory union-find, once per stretch of overlapping
+// runs (where the pixel, or its upper neighbour, starts a run, or the left
+// pair was not joined vertically).  Roots are minimum pixel indices (local
+// indices are row-major like global ones); each pixel writes the global index
+// of its tile root to the global parent array.
+constexpr int kCCTile = 32;
+
+__global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr) {
+  __shared__ int lp[kCCTile * kCCTile];
+  __shared__ float4 pt[kCCTile * kCCTile];
+  __shared__ unsigned vbits[kCCTile], hbits[kCCTile];
   const float4* __restrict__ tree = d.in->tree;
-  const int W = d.W;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < d.N; p += gridDim.x * blockDim.x) {
-    if (d.parent[p] == kInvalid) continue;
-    const float4 a = tree[p];
-    const int col = p % W;
-    for (int e = 0; e < 2; ++e) {
-      int q;
-      if (e == 0) {
-        if (col == 0) continue;
-        q = p - 1;
-      } else {
-        if (p < W) continue;
-        q = p - W;
-      }
-      const float4 b = tree[q];
-      if (!isfinite(b.x) || !cc_close(a, b, thr)) continue;
-      uint32_t u = (uint32_t)p, v = (uint32_t)q;
-      int it = 0;
-      for (; it < kCCIterLimit; ++it) {
-        uint32_t ru = cc_find(P, u), rv = cc_find(P, v);
-        if (ru == rv) break;
-        if (ru > rv) { uint32_t t = ru; ru = rv; rv = t; }
-        const uint32_t old = atomicCAS(d.parent + rv, rv, ru);
-        if (old == rv) break;
-        u = ru;
-        v = old;
-      }
-      if (it == kCCIterLimit) atomicOr(&d.cnt->cc_iter_exceeded, 1);
+  const int W = d.W, H = d.H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int tiles_x = (W + kCCTile - 1) / kCCTile;
+  const int r0 = (blockIdx.x / tiles_x) * kCCTile, c0 = (blockIdx.x % tiles_x) * kCCTile;
+  for (int row = warp; row < kCCTile; row += nwarp) {
+    const int r = r0 + row, c = c0 + lane;
+    float4 a = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+    if (r < H && c < W) a = tree[r * W + c];
+    pt[row * kCCTile + lane] = a;
+    const bool v = isfinite(a.x);
+    const unsigned vb = __ballot_sync(0xffffffffu, v);
+    // left neighbour: the previous lane's point
+    const float lx = __shfl_up_sync(0xffffffffu, a.x, 1), ly = __shfl_up_sync(0xffffffffu, a.y, 1),
+                lz = __shfl_up_sync(0xffffffffu, a.z, 1);
+    const bool h = v && lane > 0 && ((vb >> (lane - 1)) & 1u) &&
+                   cc_close(a, make_float4(lx, ly, lz, 0.f), thr);
+    const unsigned hb = __ballot_sync(0xffffffffu, h);
+    const unsigned starts = vb & ~hb;
+    const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+    lp[row * kCCTile + lane] = v ? row * kCCTile + (31 - __clz(starts & upto)) : -1;
+    if (lane == 0) {
+      vbits[row] = vb;
+      hbits[row] = hb;
     }
   }
+  __syncthreads();
+  volatile int* P = lp;
+  auto find = [P](int x) {
+    int p = P[x];
+    while (p != x) {
+      const int gp = P[p];
+      if (gp != p) P[x] = gp;  // path halving: parents only ever decrease
+      x = p;
+      p = P[x];
+    }
+    return x;
+  };
+  bool ok = true;
+  for (int row = 1 + warp; row < kCCTile; row += nwarp) {
+    const int l = row * kCCTile + lane;
+    const unsigned vb = vbits[row], vbu = vbits[row - 1];
+    bool up = ((vb & vbu) >> lane) & 1u;
+    if (up) up = cc_close(pt[l], pt[l - kCCTile], thr);
+    const unsigned ub = __ballot_sync(0xffffffffu, up);
+    const bool joined_left = lane > 0 && ((hbits[row] >> lane) & 1u) &&
+                             ((hbits[row - 1] >> lane) & 1u) && ((ub >> (lane - 1)) & 1u);
+    if (up && !joined_left) ok &= cc_union(lp, l, l - kCCTile, find);
+  }
+  if (!ok) atomicOr(&d.cnt->cc_iter_exceeded, 1);
+  __syncthreads();
+  for (int l = threadIdx.x; l < kCCTile * kCCTile; l += blockDim.x) {
+    const int r = r0 + l / kCCTile, c = c0 + l % kCCTile;
+    if (r >= H || c >= W) continue;
+    uint32_t g = kInvalid;
+    if (P[l] >= 0) {
+      const int root = find(l);
+      g = (uint32_t)((r0 + root / kCCTile) * W + c0 + root % kCCTile);
+    }
+    d.parent[r * W + c] = g;
+  }
+}
+
+// a3, second level: pixel pairs across tile borders (left neighbour across a
+// vertical border, upper neighbour across a horizontal one) join in the
+// global parent array.
+__global__ void __launch_bounds__(256) k_cc_border(Dev d, float thr) {
+  const float4* __restrict__ tree = d.in->tree;
+  const int W = d.W, H = d.H;
+  const int nv = ((W + kCCTile - 1) / kCCTile - 1) * H;
+  const int nh = ((H + kCCTile - 1) / kCCTile - 1) * W;
+  uint32_t* P = d.parent;
+  auto find = [P](uint32_t x) { return cc_find(P, x); };
+  bool ok = true;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nv + nh; t += gridDim.x * blockDim.x) {
+    int p, q;
+    if (t < nv) {
+      const int k = t / H + 1, r = t - (k - 1) * H;
+      p = r * W + k * kCCTile;
+      q = p - 1;
+    } else {
+      const int u = t - nv, k = u / W + 1, c = u - (k - 1) * W;
+      p = k * kCCTile * W + c;
+      q = p - W;
+    }
+    if (P[p] == kInvalid || P[q] == kInvalid) continue;
+    if (!cc_close(tree[p], tree[q], thr)) continue;
+    ok &= cc_union(P, (uint32_t)p, (uint32_t)q, find);
+  }
+  if (!ok) atomicOr(&d.cnt->cc_iter_exceeded, 1);
+}
+
+int cc_border_pairs(int W, int H) {
+  return ((W + kCCTile - 1) / kCCTile - 1) * H + ((H + kCCTile - 1) / kCCTile - 1) * W;
 }
 
 // Roots -> per-block counts; every valid pixel stores its root in label[].
@@ -233,6 +319,118 @@ __device__ __forceinline__ bool zless(float4 a, int ia, float4 b, int ib) {
   return ia < ib;
 }
 
+// Order-preserving key of a float (x < y <=> key(x) < key(y); -0 and +0
+// equal, as the float comparison has them).
+__device__ __forceinline__ uint32_t fkey(float v) {
+  if (v == 0.0f) v = 0.0f;
+  const uint32_t u = __float_as_uint(v);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Value of the element at position k of the stable order by value of the
+// warp's n (<= 32 * kVtxSlots) keys, slot s of lane l holding element
+// 32 s + l: warp quickselect (pivot = a pseudo-random remaining candidate,
+// counts by ballot; each round removes the pivot's key, so at most n
+// rounds), then the k'-th element, in index order, among those with the
+// selected key -- the element the rank count (b < a, or b == a and k < j)
+// puts at position k.
+constexpr int kVtxSlots = kVtxCap / 32;
+__device__ __forceinline__ float warp_select(const uint32_t (&key)[kVtxSlots],
+                                             const float (&val)[kVtxSlots], int n, int k,
+                                             int lane) {
+  const int ns = (n + 31) >> 5;
+  unsigned cb[kVtxSlots];  // remaining candidates, one ballot word per slot
+  int nc = n;
+#pragma unroll
+  for (int s = 0; s < kVtxSlots; ++s) {
+    const int left = n - 32 * s;
+    cb[s] = left >= 32 ? 0xffffffffu : left > 0 ? ((1u << left) - 1u) : 0u;
+  }
+  unsigned seed = 0x2545f491u;
+  uint32_t K = 0;
+  for (int round = 0; round <= n; ++round) {
+    seed = seed * 1664525u + 1013904223u;
+    int r = (int)(((unsigned long long)(seed >> 8) * (unsigned)nc) >> 24);
+    uint32_t piv = 0;
+#pragma unroll
+    for (int s = 0; s < kVtxSlots; ++s) {
+      if (s < ns) {
+        const int c = __popc(cb[s]);
+        if (r >= 0 && r < c) {  // warp-uniform
+          unsigned e = cb[s];
+          for (int q = 0; q < r; ++q) e &= e - 1;
+          piv = __shfl_sync(0xffffffffu, key[s], __ffs(e) - 1);
+        }
+        r -= c;
+      }
+    }
+    int cl = 0, ce = 0;
+    unsigned lt[kVtxSlots], gt[kVtxSlots];
+#pragma unroll
+    for (int s = 0; s < kVtxSlots; ++s) {
+      lt[s] = gt[s] = 0u;
+      if (s < ns) {
+        const bool in = (cb[s] >> lane) & 1u;
+        lt[s] = __ballot_sync(0xffffffffu, in && key[s] < piv);
+        const unsigned eq = __ballot_sync(0xffffffffu, in && key[s] == piv);
+        gt[s] = cb[s] & ~lt[s] & ~eq;
+        cl += __popc(lt[s]);
+        ce += __popc(eq);
+      }
+    }
+    if (k < cl) {
+#pragma unroll
+      for (int s = 0; s < kVtxSlots; ++s) cb[s] = lt[s];
+      nc = cl;
+    } else if (k < cl + ce) {
+      K = piv;
+      k -= cl;
+      break;
+    } else {
+#pragma unroll
+      for (int s = 0; s < kVtxSlots; ++s) cb[s] = gt[s];
+      k -= cl + ce;
+      nc -= cl + ce;
+    }
+  }
+  float out = 0.0f;
+#pragma unroll
+  for (int s = 0; s < kVtxSlots; ++s) {
+    if (s < ns) {
+      const unsigned eq = __ballot_sync(0xffffffffu, s * 32 + lane < n && key[s] == K);
+      const int c = __popc(eq);
+      if (k >= 0 && k < c) {  // warp-uniform
+        unsigned e = eq;
+        for (int q = 0; q < k; ++q) e &= e - 1;  // drop the k lowest set bits
+        out = __shfl_sync(0xffffffffu, val[s], __ffs(e) - 1);
+      }
+      k -= c;
+    }
+  }
+  return out;
+}
+
+// Warp bitonic sort of m (power of two, <= kVtxCap) indices in shared memory
+// by `less`; indices >= n are placed last.
+template <typename Less>
+__device__ __forceinline__ void warp_bitonic(int* a, int m, int n, int lane, Less less) {
+  auto lt = [&](int x, int y) { return x < n && (y >= n || less(x, y)); };
+  for (int k = 2; k <= m; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = lane; t < (m >> 1); t += 32) {
+        const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i | j;
+        const int x = a[i], y = a[l];
+        const bool up = (i & k) == 0;
+        if (up ? lt(y, x) : lt(x, y)) {
+          a[i] = y;
+          a[l] = x;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // One warp per (candidate, row) bucket with > min_beam points.
 __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
   __shared__ float4 spts[kVtxWarps][kVtxCap];
@@ -259,6 +457,52 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
     __syncwarp();
     auto pt = [&](int j) -> float4 { return inshm ? P[j] : tree[d.bucket[off + j]]; };
     const int mid = n / 2;  // (int)(n / 2.0)
+    if (inshm && n > 64) {
+      // medians by quickselect; kept points in (z, y, x, column) order
+      // by a bitonic sort -- the same elements and order as the rank counts
+      // below, in O(n log^2 n) instead of O(n^2)
+      uint32_t kx[kVtxSlots], ky[kVtxSlots], kz[kVtxSlots];
+      float vx[kVtxSlots], vy[kVtxSlots], vz[kVtxSlots];
+#pragma unroll
+      for (int s = 0; s < kVtxSlots; ++s) {
+        const int j = s * 32 + lane;
+        const float4 a = j < n ? P[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        vx[s] = a.x; vy[s] = a.y; vz[s] = a.z;
+        kx[s] = fkey(a.x); ky[s] = fkey(a.y); kz[s] = fkey(a.z);
+      }
+      const float mx = warp_select(kx, vx, n, mid, lane);
+      const float my = warp_select(ky, vy, n, mid, lane);
+      const float mz = warp_select(kz, vz, n, mid, lane);
+      int m = 32;
+      while (m < n) m <<= 1;
+      int* idx = srank[w];
+      int nkept = 0;
+      for (int j = lane; j < m; j += 32) {
+        bool keep = false;
+        if (j < n) {
+          const float4 a = P[j];
+          keep = pcl_euclid(a.x, a.y, a.z, mx, my, mz) < kp.max_d_centroid;
+        }
+        idx[j] = keep ? j : n;
+        nkept += __popc(__ballot_sync(0xffffffffu, keep));  // m is a multiple of 32
+      }
+      __syncwarp();
+      warp_bitonic(idx, m, n, lane, [&](int x, int y) { return zless(P[x], x, P[y], y); });
+      for (int r = lane; r < nkept; r += 32) d.kept[off + r] = P[idx[r]];
+      if (lane == 0) {
+        const bool valid = nkept > 1;
+        double rad = 0.0;
+        if (valid) {
+          const float4 a = P[idx[0]], b = P[idx[nkept - 1]];
+          rad = (double)pcl_euclid(a.x, a.y, a.z, b.x, b.y, b.z);
+        }
+        d.vmed[it] = make_float4(mx, my, mz, 0.0f);
+        d.vrad[it] = rad;
+        d.vkept[it] = valid ? nkept : 0;
+      }
+      __syncwarp();
+      continue;
+    }
     // per-axis medians by rank
     float mx = __int_as_float(0x7fc00000), my = mx, mz = mx;
     for (int j = lane; j < n; j += 32) {
@@ -516,8 +760,9 @@ __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   const int N = d.N;
   const int g256 = (N + 255) / 256, g1k = (N + 1023) / 1024;
-  k_cc_init<<<g256, 256, 0, st>>>(d);
-  k_cc_union<<<g256, 256, 0, st>>>(d, kp.cc_thr);
+  const int tiles = ((d.W + kCCTile - 1) / kCCTile) * ((d.H + kCCTile - 1) / kCCTile);
+  k_cc_local<<<tiles, 256, 0, st>>>(d, kp.cc_thr);
+  k_cc_border<<<(cc_border_pairs(d.W, d.H) + 255) / 256 + 1, 256, 0, st>>>(d, kp.cc_thr);
   k_cc_flatten<<<g1k, 1024, 0, st>>>(d);
   k_cc_rank<<<g1k, 1024, 0, st>>>(d);
   k_cc_label<<<g256, 256, 0, st>>>(d);
