@@ -476,19 +476,14 @@ constexpr int kMbarSpin = 1 << 20;  // bounded wait (the MMAs take microseconds)
       : "r"(taddr))
 SLOAM_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Tensor-core inference.  One CTA per SM (its shared memory allows no
-// second), persistent over samples; 128 threads, thread r owns point r and
-// TMEM lane r.  Layer 1 and the head on CUDA cores (FP32), layers 2 and 3
-// as tcgen05.mma M=128 (N=128, K=64 then N=256, K=128), bf16 operands from
-// shared memory, fp32 accumulators in 256 TMEM columns (reused).
+// Shared-memory layout of the tensor-core inference kernel below.
 constexpr int kTcThreads = 256;  // two warpgroups, one sample each at a time
 constexpr int kMaxGroup = 8;     // samples per group (one tree's proposals)
 constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes,
                    kSmA1 = kSmB3 + kTcW3Bytes,                    // [2][128 x 64] bf16
                    kSmA2 = kSmA1 + 2 * kPts * kD1 * 2,            // [2][128 x 128] bf16
                    kSmW1 = kSmA2 + 2 * kPts * kD2 * 2,
-                   kSmPart = kSmW1 + 4 * (3 * kD1 + kD1),         // [2][4][256]
-                   kSmH = kSmPart + 4 * 2 * 4 * kD3,              // [group][256]
+                   kSmH = kSmW1 + 4 * (3 * kD1 + kD1),            // [group][256]
                    kSmY1 = kSmH + 4 * kMaxGroup * kD3,            // [group][128]
                    kSmBias = kSmY1 + 4 * kMaxGroup * kD4,         // b2, b3, b4, W5, b5
                    kSmMisc = kSmBias + 4 * (kD2 + kD3 + kD4 + kD4 * kD5 + 8),
@@ -520,13 +515,14 @@ SLOAM_D void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : 
 // fitted) are skipped.  256 threads: warpgroup g (0, 1) takes samples
 // g, g + 2, ... of the group with its own operand buffers, TMEM columns
 // [256 g, 256 g + 256), mbarrier and barrier, so that one warpgroup's MMAs
-// overlap the other's CUDA-core work.  Thread r of a warpgroup owns point r
-// and TMEM lane r.  Per sample, layer 1 on CUDA cores (FP32) into bf16 A1;
-// layers 2 and 3 as tcgen05.mma M=128 (N=128, K=64, then N=256, K=128),
-// bf16 operands in shared memory, fp32 accumulators in TMEM; the column max
-// over the points by a warp max-reduction of the (non-negative) ReLU
-// outputs' bit patterns.  The head runs once per group, each weight load
-// serving every sample of the group.
+// overlap the other's CUDA-core work.  Per sample, layer 1 on CUDA cores
+// (FP32, thread r = point r) into bf16 A1; layer 2 as tcgen05.mma M=128
+// points, N=128, K=64 (TMEM lane r = point r) into bf16 A2; layer 3
+// transposed, M=128 features (two halves of W3^T), N=128 points, K=128, so
+// that TMEM lane r holds feature r of a half and the max over the points is
+// a register reduction of the thread's own row.  bf16 operands in shared
+// memory, fp32 accumulators in TMEM.  The head runs once per group, each
+// weight load serving every sample of the group.
 __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const unsigned char* __restrict__ tcw, const float* __restrict__ X, int S,
     const int* __restrict__ n_groups_dev, int group, const float4* __restrict__ frames,
@@ -544,9 +540,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 16);
   int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 20);
   const float* f = reinterpret_cast<const float*>(tcw + kTcF32Off);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const int wg = tid >> 7, lt = tid & 127, wq = warp & 3;
-  float* part = reinterpret_cast<float*>(smem + kSmPart) + wg * 4 * kD3;  // [4][256]
   unsigned char* a1b = smem + kSmA1 + wg * kPts * kD1 * 2;
   unsigned char* a2b = smem + kSmA2 + wg * kPts * kD2 * 2;
   // groups: ceil(S / group), or the device count of groups when given
@@ -648,32 +643,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
       wg_sync(wg);
       fence_after();
       if (*abort_flag) break;
+      // layer 3 transposed: D^T[feature][point] = W3^T[feature][:] . A2[point][:],
+      // two M = 128 feature halves (A = W3^T rows, B = A2), N = 128 points,
+      // into TMEM columns [128 half, 128 half + 128)
       if (lt == 0) {
-        for (int ks = 0; ks < kD2 / 16; ++ks)
-          mma_bf16(tmem, smem_desc(sA2 + ks * 256, 128, (kD2 / 8) * 128),
-                   smem_desc(sB3 + ks * 256, 128, (kD2 / 8) * 128), idesc_bf16(128, kD3), ks > 0);
+        for (int hf = 0; hf < 2; ++hf)
+          for (int ks = 0; ks < kD2 / 16; ++ks)
+            mma_bf16(tmem + hf * kPts,
+                     smem_desc(sB3 + hf * (kPts * kD2 * 2) + ks * 256, 128, (kD2 / 8) * 128),
+                     smem_desc(sA2 + ks * 256, 128, (kD2 / 8) * 128), idesc_bf16(128, kPts),
+                     ks > 0);
         mma_commit(mb);
       }
       mbar_wait_bounded(mb, phase, err, abort_flag);
       phase ^= 1u;
       fence_after();
-      // epilogue 3: bias, ReLU; column max over this warp's 32 points
-      for (int cc = 0; cc < kD3 / 32; ++cc) {
-        uint32_t v[32];
-        SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
-        tmem_wait_ld();
+      // epilogue 3: thread (lane row) = feature; max over the 128 points in
+      // registers, then bias and ReLU (both monotone, so max then bias/ReLU
+      // equals the max of the biased ReLU outputs)
+#pragma unroll 1
+      for (int hf = 0; hf < 2; ++hf) {
+        float m = -INFINITY;
+#pragma unroll 1
+        for (int cc = 0; cc < kPts / 32; ++cc) {
+          uint32_t v[32];
+          SG_TMEM_LD32(tmem + lane_base + hf * kPts + cc * 32, v);
+          tmem_wait_ld();
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
-          const float a = fmaxf(__uint_as_float(v[q]) + sb3[cc * 32 + q], 0.0f);
-          const uint32_t m = __reduce_max_sync(0xffffffffu, __float_as_uint(a));
-          if (lane == q) part[wq * kD3 + cc * 32 + q] = __uint_as_float(m);
+          for (int q = 0; q < 32; ++q) m = fmaxf(m, __uint_as_float(v[q]));
         }
+        const int c = hf * kPts + lt;
+        h[k * kD3 + c] = fmaxf(m + sb3[c], 0.0f);
       }
-      fence_before();
-      wg_sync(wg);
-      for (int c = lt; c < kD3; c += 128)
-        h[k * kD3 + c] =
-            fmaxf(fmaxf(part[c], part[kD3 + c]), fmaxf(part[2 * kD3 + c], part[3 * kD3 + c]));
       if (*abort_flag) break;
       fence_before();
       wg_sync(wg);
@@ -723,6 +724,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
 }
 
 int g_tc_attr = 0;
+constexpr int kTreeCtas = 48;
 
 }  // namespace
 
@@ -746,8 +748,12 @@ int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const 
                             int per_tree, int cap, const float4* d_frames, float* d_out,
                             int* d_err, cudaStream_t st) {
   init_attributes();
+  // persistent CTAs over the trees: at most kTreeCtas, each of which needs
+  // a whole SM's shared memory, so that the many CTAs of a large capacity
+  // do not each wait for an empty SM only to exit
   const int groups = (cap + per_tree - 1) / per_tree;
-  const int grid = groups < sm_count() ? (groups > 0 ? groups : 1) : sm_count();
+  const int lim = sm_count() < kTreeCtas ? sm_count() : kTreeCtas;
+  const int grid = groups < lim ? (groups > 0 ? groups : 1) : lim;
   k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, cap, d_n_trees, per_tree,
                                                      d_frames, d_out, d_err);
   return 1;
