@@ -231,6 +231,7 @@ __device__ void euler_two_vectors(d3 a, d3 b, double* ang) {
 
 constexpr int kBinCap = 4096;   // keys of one bin staged in shared memory
 constexpr int kPlaneThreads = 512;
+constexpr int kScatterWarps = 4;
 
 __device__ void bitonic_sort(unsigned long long* a, int n2) {
   for (int k = 2; k <= n2; k <<= 1) {
@@ -269,27 +270,37 @@ __device__ void fit_plane_block(At at, int n, float* cen, double* red, PlaneD& o
     cen[2] = (float)((double)sz / (double)n);
   }
   __syncthreads();
-  double s[6] = {0, 0, 0, 0, 0, 0};
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const float4 p = at(i);
-    const double a0 = (double)fsub(p.x, cen[0]), a1 = (double)fsub(p.y, cen[1]),
-                 a2 = (double)fsub(p.z, cen[2]);
-    s[0] += a0 * a0; s[1] += a0 * a1; s[2] += a0 * a2;
-    s[3] += a1 * a1; s[4] += a1 * a2; s[5] += a2 * a2;
-  }
+  // FP64 scatter by the first kScatterWarps warps only: every FP64 warp
+  // instruction and warp reduction costs the same pipe time whatever the
+  // number of points, so fewer warps cost less
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int j = 0; j < 6; ++j) {
-    const double v = warp_sumd(s[j]);
-    if (lane == 0) red[j * 32 + w] = v;
+  if (w < kScatterWarps) {
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < n; i += 32 * kScatterWarps) {
+      const float4 p = at(i);
+      const double a0 = (double)fsub(p.x, cen[0]), a1 = (double)fsub(p.y, cen[1]),
+                   a2 = (double)fsub(p.z, cen[2]);
+      s[0] += a0 * a0; s[1] += a0 * a1; s[2] += a0 * a2;
+      s[3] += a1 * a1; s[4] += a1 * a2; s[5] += a2 * a2;
+    }
+    for (int j = 0; j < 6; ++j) {
+      const double v = warp_sumd(s[j]);
+      if (lane == 0) red[j * 32 + w] = v;
+    }
   }
   __syncthreads();
+  // sum j over the warps by lane j of warp 0 (the order of one thread's sum)
+  if (w == 0) {
+    if (lane < 6) {
+      double t = 0;
+      for (int q = 0; q < kScatterWarps; ++q) t += red[lane * 32 + q];
+      red[lane * 32 + 31] = t;  // slot 31: at most 16 warps write partials
+    }
+    __syncwarp();
+  }
   if (threadIdx.x == 0) {
     double S6[6];
-    for (int j = 0; j < 6; ++j) {
-      double t = 0;
-      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[j * 32 + q];
-      S6[j] = t;
-    }
+    for (int j = 0; j < 6; ++j) S6[j] = red[j * 32 + 31];
     const float S[9] = {(float)S6[0], (float)S6[1], (float)S6[2], (float)S6[1], (float)S6[3],
                         (float)S6[4], (float)S6[2], (float)S6[4], (float)S6[5]};
     float ev[3], V[9];
@@ -379,22 +390,7 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
   if (enough) {
     fit_plane_block([&](int i) { return ground[(uint32_t)keys[i]]; }, kk, cen, red, out);
     if (threadIdx.x == 0) {
-      const d3 nrm = mk3(out.plane[0], out.plane[1], out.plane[2]);
-      // gates (sloam.cpp:394-408): normal in the map frame = R n
-      sloam_se3 pe;
-      for (int j = 0; j < 4; ++j) pe.q[j] = d.pose_io[j];
-      for (int j = 0; j < 3; ++j) pe.t[j] = d.pose_io[4 + j];
-      const Pose T = pose_from(pe);
-      const d3 nw = rot3(T.R, nrm);
-      double ang[3];
-      euler_two_vectors(mk3(0, 0, 1), nw, ang);
-      const double PI = 3.14159265358979323846;
-      const bool angle_ok = (ang[0] < 0.1 && ang[1] < 0.1 && ang[2] < 0.1) ||
-                            (PI - fabs(ang[0]) < 0.1 && PI - fabs(ang[1]) < 0.1 &&
-                             PI - fabs(ang[2]) < 0.1);
-      const bool height_ok =
-          xform(T, mk3(out.centroid[0], out.centroid[1], out.centroid[2])).z < T.t.z;
-      out.valid = angle_ok && height_ok;
+      out.valid = 1;  // fitted; the gates follow in k_plane_compact
       d.plane_all[b] = out;
     }
     for (int i = threadIdx.x; i < kp.G; i += blockDim.x)
@@ -427,12 +423,33 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane_points(Dev d, KParams k
   }
 }
 
+// Gates of a fitted bin plane (sloam.cpp:394-408): the normal in the map
+// frame (R n) within 0.1 rad of +-z by its Euler angles, and the centroid
+// below the sensor.  FP64, one bin per thread.
+__device__ bool plane_gates(const Dev& d, const PlaneD& pl) {
+  const d3 nrm = mk3(pl.plane[0], pl.plane[1], pl.plane[2]);
+  sloam_se3 pe;
+  for (int j = 0; j < 4; ++j) pe.q[j] = d.pose_io[j];
+  for (int j = 0; j < 3; ++j) pe.t[j] = d.pose_io[4 + j];
+  const Pose T = pose_from(pe);
+  const d3 nw = rot3(T.R, nrm);
+  double ang[3];
+  euler_two_vectors(mk3(0, 0, 1), nw, ang);
+  const double PI = 3.14159265358979323846;
+  const bool angle_ok = (ang[0] < 0.1 && ang[1] < 0.1 && ang[2] < 0.1) ||
+                        (PI - fabs(ang[0]) < 0.1 && PI - fabs(ang[1]) < 0.1 &&
+                         PI - fabs(ang[2]) < 0.1);
+  const bool height_ok =
+      xform(T, mk3(pl.centroid[0], pl.centroid[1], pl.centroid[2])).z < T.t.z;
+  return angle_ok && height_ok;
+}
+
 __global__ void __launch_bounds__(1024) k_plane_compact(Dev d, KParams kp) {
   __shared__ int sm[33];
   int base = 0;
   for (int b0 = 0; b0 < d.n_bins; b0 += blockDim.x) {
     const int b = b0 + threadIdx.x;
-    const bool v = b < d.n_bins && d.plane_all[b].valid;
+    const bool v = b < d.n_bins && d.plane_all[b].valid && plane_gates(d, d.plane_all[b]);
     int total;
     const int ex = block_excl_scan(v ? 1 : 0, sm, &total);
     if (v) {
@@ -1034,11 +1051,30 @@ __global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
 // network proposal; the refined model is kept when its inliers
 // (|distance to the refined axis - radius| < tau) are at least prop_ratio
 // of the tree's points, else the tree is flagged for the RANSAC pass.
+// Normal frame of the LS model st (centre st[0..2], unit direction
+// st[3..5], radius st[6]): b1 = dir x t / |dir x t| (t = x unless
+// |dir_x| >= 0.9, then y), b2 = dir x b1, in double into st[8..13], and the
+// float copies every thread uses into sf.
+__device__ __forceinline__ void ls_frame(double* st, float* sf) {
+  const d3 dd = mk3(st[3], st[4], st[5]);
+  const d3 t = fabs(dd.x) < 0.9 ? mk3(1, 0, 0) : mk3(0, 1, 0);
+  d3 b1 = cross3(dd, t);
+  b1 = scl3(1.0 / norm3(b1), b1);
+  const d3 b2 = cross3(dd, b1);
+  st[8] = b1.x; st[9] = b1.y; st[10] = b1.z;
+  st[11] = b2.x; st[12] = b2.y; st[13] = b2.z;
+  for (int j = 0; j < 6; ++j) sf[j] = (float)st[j];
+  sf[6] = (float)b1.x; sf[7] = (float)b1.y; sf[8] = (float)b1.z;
+  sf[9] = (float)b2.x; sf[10] = (float)b2.y; sf[11] = (float)b2.z;
+  sf[12] = (float)st[6];
+}
 constexpr int kLsThreads = 256;
 __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pass) {
   __shared__ int s_in[kLsThreads / 32];
   __shared__ float red[20][kLsThreads / 32];
-  __shared__ double st[8];  // c(3), dir(3), r, ok
+  __shared__ double st[14];  // c(3), dir(3), r, ok, b1(3), b2(3)
+  __shared__ double ssum[20];
+  __shared__ float sf[13];   // c(3), dir(3), b1(3), b2(3), r as float
   const int nl = d.cnt->n_lm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
@@ -1081,21 +1117,17 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pa
       st[3] = f.ax / an; st[4] = f.ay / an; st[5] = f.az / an;
       st[6] = H.r;
       st[7] = 1.0;
+      ls_frame(st, sf);
     }
     __syncthreads();
     for (int itn = 0; itn < kp.ls_iters; ++itn) {
       if (st[7] == 0.0) break;
-      const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
-      const double r = st[6];
-      const d3 t = fabs(dd.x) < 0.9 ? mk3(1, 0, 0) : mk3(0, 1, 0);
-      d3 b1 = cross3(dd, t);
-      b1 = scl3(1.0 / norm3(b1), b1);
-      const d3 b2 = cross3(dd, b1);
-      const float cx = (float)cc.x, cy = (float)cc.y, cz = (float)cc.z;
-      const float dx = (float)dd.x, dy = (float)dd.y, dz = (float)dd.z;
-      const float b1x = (float)b1.x, b1y = (float)b1.y, b1z = (float)b1.z;
-      const float b2x = (float)b2.x, b2y = (float)b2.y, b2z = (float)b2.z;
-      const float rf = (float)r;
+      // the model and its normal frame, as floats (computed once by thread 0)
+      const float cx = sf[0], cy = sf[1], cz = sf[2];
+      const float dx = sf[3], dy = sf[4], dz = sf[5];
+      const float b1x = sf[6], b1y = sf[7], b1z = sf[8];
+      const float b2x = sf[9], b2y = sf[10], b2z = sf[11];
+      const float rf = sf[12];
       float acc[20];
 #pragma unroll
       for (int j = 0; j < 20; ++j) acc[j] = 0.f;
@@ -1134,13 +1166,22 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pa
         if (lane == 0) red[j][w] = v;
       }
       __syncthreads();
+      // sum j over the warps by lane j of warp 0 (the same order as one
+      // thread summing them)
+      if (w == 0) {
+        if (lane < 20) {
+          double t2 = 0;
+          for (int q2 = 0; q2 < kLsThreads / 32; ++q2) t2 += red[lane][q2];
+          ssum[lane] = t2;
+        }
+        __syncwarp();
+      }
       if (threadIdx.x == 0) {
         double s[20];
-        for (int j = 0; j < 20; ++j) {
-          double t2 = 0;
-          for (int q2 = 0; q2 < kLsThreads / 32; ++q2) t2 += red[j][q2];
-          s[j] = t2;
-        }
+        for (int j = 0; j < 20; ++j) s[j] = ssum[j];
+        const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
+        const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
+        const double r = st[6];
         double Hm[25], g[5], x[5];
         int k = 0;
         for (int p = 0; p < 5; ++p)
@@ -1157,6 +1198,7 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pa
           st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
           st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
           st[6] = r + x[4];
+          ls_frame(st, sf);
         } else {
           st[7] = 0.0;
         }
@@ -1165,9 +1207,9 @@ __global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pa
     }
     if (learned) {
       // inliers of the refined model over all the tree's points
-      const float cx = (float)st[0], cy = (float)st[1], cz = (float)st[2];
-      const float dx = (float)st[3], dy = (float)st[4], dz = (float)st[5];
-      const float rf = (float)st[6];
+      const float cx = sf[0], cy = sf[1], cz = sf[2];
+      const float dx = sf[3], dy = sf[4], dz = sf[5];
+      const float rf = sf[12];
       int cnt = 0;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 q = pts[i];
