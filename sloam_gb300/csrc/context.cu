@@ -365,6 +365,7 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.plane_match = c.take<int32_t>(d.n_bins);
   d.match_out = c.take<int32_t>(d.cap_lm);
   d.map_pts = c.take<double>((size_t)d.cap_map * 9);
+  d.map_f = c.take<float4>((size_t)d.cap_map * 3);
   d.res_tab = c.take<float>(((size_t)d.cap_lm * d.F + (size_t)d.n_bins * d.G) * 12);
   d.lm_uv = c.take<float2>((size_t)d.cap_cluster + d.cap_p);  // cluster | vertex points
   d.hyp = c.take<float4>((size_t)d.cap_lm * std::max(d.K, 1));

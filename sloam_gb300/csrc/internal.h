@@ -169,6 +169,7 @@ struct Dev {
   int32_t* plane_match; // [n_bins]
   int32_t* match_out;   // [cap_lm] matchModels result
   double* map_pts;      // [cap_map*9] map axis points at z = 0, 3, 6
+  float4* map_f;        // [cap_map*3] the same as floats, then max |coordinate|
   float* res_tab;       // [(cap_lm*F + n_bins*G) * 12] residual table of the pose solve
   float2* lm_uv;        // [cap_cluster + cap_p] tree points on the prior axis frame
   float4* hyp;          // [cap_lm * K] circle hypotheses (cu, cv, lo2, hi2)

@@ -88,23 +88,104 @@ __global__ void __launch_bounds__(256) k_map_prep(Dev d) {
     const sloam_cylinder& m = map[k];
     d3 pts[3];
     axis_points(mk3(m.root[0], m.root[1], m.root[2]), mk3(m.ray[0], m.ray[1], m.ray[2]), pts);
+    float f[12];
+    float cmax = 0.0f;
     for (int j = 0; j < 3; ++j) {
       d.map_pts[9 * k + 3 * j] = pts[j].x;
       d.map_pts[9 * k + 3 * j + 1] = pts[j].y;
       d.map_pts[9 * k + 3 * j + 2] = pts[j].z;
+      f[3 * j] = (float)pts[j].x;
+      f[3 * j + 1] = (float)pts[j].y;
+      f[3 * j + 2] = (float)pts[j].z;
+      cmax = fmaxf(cmax, fmaxf(fabsf(f[3 * j]), fmaxf(fabsf(f[3 * j + 1]), fabsf(f[3 * j + 2]))));
     }
+    f[9] = cmax;  // NaN coordinates make every bound NaN: never a candidate
+    if (!(cmax < INFINITY)) f[9] = __int_as_float(0x7fc00000);
+    f[10] = f[11] = 0.0f;
+    for (int j = 0; j < 3; ++j)
+      d.map_f[3 * (size_t)k + j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
   }
 }
 
-// argmin over the map of the distance to a (projected) current cylinder
-__device__ __forceinline__ void map_argmin(const Dev& d, d3 root, d3 ray, double init, double& bd,
-                                           int& bi, double* sv, int* si) {
+// The current cylinder's axis points, shared by the block (written by one
+// thread): FP64, FP32 copies and their max |coordinate|.
+struct AxisPts {
+  double tp[9];
+  float tf[9];
+  float tmax;
+};
+
+__device__ __forceinline__ void set_axis_pts(AxisPts* a, d3 root, d3 ray) {
   d3 tp[3];
   axis_points(root, ray, tp);
+  float cmax = 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    a->tp[3 * k] = tp[k].x; a->tp[3 * k + 1] = tp[k].y; a->tp[3 * k + 2] = tp[k].z;
+    a->tf[3 * k] = (float)tp[k].x; a->tf[3 * k + 1] = (float)tp[k].y;
+    a->tf[3 * k + 2] = (float)tp[k].z;
+    cmax = fmaxf(cmax, fmaxf(fabsf(a->tf[3 * k]), fmaxf(fabsf(a->tf[3 * k + 1]),
+                                                         fabsf(a->tf[3 * k + 2]))));
+  }
+  a->tmax = cmax < INFINITY ? cmax : __int_as_float(0x7fc00000);
+}
+
+// FP32 axis distance of map entry k (its three float4 records) and a bound
+// on |it - the exact distance|: coordinates rounded to float (u = 2^-24 each)
+// move each of the three norms by at most sqrt(3) u (|m| + |t|)max, the float
+// differences, squares, sums, root and mean add a few u relative; the bound
+// takes 3e-7 * (2 (|m|max + |t|max) + 8 d) (about 2x these).  NaN or
+// infinite inputs give a NaN bound.
+__device__ __forceinline__ float axis_dist_f(const float4* mf, const float* tf, float tmax,
+                                             float* eps) {
+  const float4 a = mf[0], b = mf[1], c = mf[2];
+  const float m[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+  float acc = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float dx = m[3 * k] - tf[3 * k], dy = m[3 * k + 1] - tf[3 * k + 1],
+                dz = m[3 * k + 2] - tf[3 * k + 2];
+    acc += sqrtf(dx * dx + dy * dy + dz * dz);
+  }
+  const float dist = acc * (1.0f / 3.0f);
+  *eps = 3e-7f * (2.0f * (c.y + tmax) + 8.0f * dist);
+  return dist;
+}
+
+// argmin over the map of the distance to the current cylinder whose axis
+// points are in *a: the smallest FP64 distance below `init`, first index on
+// ties (bi = 0 when none), exactly as an FP64 scan of the whole map.  The
+// FP64 distance is evaluated only for entries whose FP32 lower bound
+// (distance - eps) is at most the smallest FP32 upper bound (distance + eps,
+// or init): the exact minimum and every entry tied with it are among them.
+__device__ void map_argmin(const Dev& d, const AxisPts* a, double init, double& bd, int& bi,
+                           double* sv, int* si, float* su) {
+  const int n_map = d.in->n_map;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float tf[9];
+#pragma unroll
+  for (int j = 0; j < 9; ++j) tf[j] = a->tf[j];
+  const float tmax = a->tmax;
+  float U = (float)init * (1.0f + 1e-6f);
+  for (int k = threadIdx.x; k < n_map; k += blockDim.x) {
+    float eps;
+    const float df = axis_dist_f(d.map_f + 3 * (size_t)k, tf, tmax, &eps);
+    U = fminf(U, df + eps);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) U = fminf(U, __shfl_xor_sync(0xffffffffu, U, o));
+  if (lane == 0) su[w] = U;
+  __syncthreads();
+  U = su[0];
+  for (int q = 1; q < (int)(blockDim.x >> 5); ++q) U = fminf(U, su[q]);
   bd = init;
   bi = 0;
-  const int n_map = d.in->n_map;
   for (int k = threadIdx.x; k < n_map; k += blockDim.x) {
+    float eps;
+    const float df = axis_dist_f(d.map_f + 3 * (size_t)k, tf, tmax, &eps);
+    if (!(df - eps <= U)) continue;
+    d3 tp[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) tp[j] = mk3(a->tp[3 * j], a->tp[3 * j + 1], a->tp[3 * j + 2]);
     const double dist = axis_dist(d.map_pts + 9 * (size_t)k, tp);
     if (dist < bd) { bd = dist; bi = k; }
   }
@@ -114,16 +195,22 @@ __device__ __forceinline__ void map_argmin(const Dev& d, d3 root, d3 ray, double
 __global__ void __launch_bounds__(kAssocThreads) k_assoc(Dev d, KParams kp) {
   __shared__ double sv[kAssocThreads / 32];
   __shared__ int si[kAssocThreads / 32];
+  __shared__ float su[kAssocThreads / 32];
+  __shared__ AxisPts ax;
   const int nc = d.cnt->n_cyl, np = d.cnt->n_planes, nprev = d.cnt->n_prev;
   const Pose T = pose_at(d.pose_io);
   for (int it = blockIdx.x; it < nc + np; it += gridDim.x) {
     double bd;
     int bi;
     if (it < nc) {
-      const CylD c = d.cyls[it];
-      d3 root = mk3(c.root[0], c.root[1], c.root[2]), ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
-      cyl_project(T, root, ray);
-      map_argmin(d, root, ray, kp.tree_match_thresh + 100, bd, bi, sv, si);
+      if (threadIdx.x == 0) {
+        const CylD c = d.cyls[it];
+        d3 root = mk3(c.root[0], c.root[1], c.root[2]), ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
+        cyl_project(T, root, ray);
+        set_axis_pts(&ax, root, ray);
+      }
+      __syncthreads();
+      map_argmin(d, &ax, kp.tree_match_thresh + 100, bd, bi, sv, si, su);
       if (threadIdx.x == 0)
         d.cyl_match[it] = (d.in->n_map > 0 && bd < kp.tree_match_thresh) ? bi : -1;
     } else {
@@ -491,6 +578,8 @@ __global__ void __launch_bounds__(kAssocThreads) k_finalize(Dev d, KParams kp, i
                                                             int update) {
   __shared__ double sv[kAssocThreads / 32];
   __shared__ int si[kAssocThreads / 32];
+  __shared__ float su[kAssocThreads / 32];
+  __shared__ AxisPts ax;
   const int nc = d.cnt->n_cyl, np = d.cnt->n_planes;
   if (first) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -519,22 +608,25 @@ __global__ void __launch_bounds__(kAssocThreads) k_finalize(Dev d, KParams kp, i
     if (threadIdx.x == 0 && update) d.cnt->n_prev = np;
   }
   for (int c = blockIdx.x; c < nc; c += gridDim.x) {
-    CylD C = d.cyls[c];
-    d3 root = mk3(C.root[0], C.root[1], C.root[2]), ray = mk3(C.ray[0], C.ray[1], C.ray[2]);
-    cyl_project(T, root, ray);
+    if (threadIdx.x == 0) {
+      CylD C = d.cyls[c];
+      d3 root = mk3(C.root[0], C.root[1], C.root[2]), ray = mk3(C.ray[0], C.ray[1], C.ray[2]);
+      cyl_project(T, root, ray);
+      set_axis_pts(&ax, root, ray);
+      C.root[0] = root.x; C.root[1] = root.y; C.root[2] = root.z;
+      C.ray[0] = ray.x; C.ray[1] = ray.y; C.ray[2] = ray.z;
+      d.cyls[c] = C;
+    }
+    __syncthreads();
     int out = -1;
     if (!first) {
       double bd;
       int bi;
-      map_argmin(d, root, ray, kp.tree_match_thresh + 100, bd, bi, sv, si);
+      map_argmin(d, &ax, kp.tree_match_thresh + 100, bd, bi, sv, si, su);
       out = (d.in->n_map > 0 && bd < kp.add_new_tree_thresh) ? bi : -1;
     }
-    if (threadIdx.x == 0) {
-      C.root[0] = root.x; C.root[1] = root.y; C.root[2] = root.z;
-      C.ray[0] = ray.x; C.ray[1] = ray.y; C.ray[2] = ray.z;
-      d.cyls[c] = C;
-      d.match_out[c] = out;
-    }
+    if (threadIdx.x == 0) d.match_out[c] = out;
+    __syncthreads();
   }
 }
 
