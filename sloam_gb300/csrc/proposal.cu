@@ -477,19 +477,23 @@ constexpr int kMbarSpin = 1 << 20;  // bounded wait (the MMAs take microseconds)
 SLOAM_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Shared-memory layout of the tensor-core inference kernel below.
-constexpr int kTcThreads = 256;  // two warpgroups, one sample each at a time
+constexpr int kTcWg = 4;                // warpgroups, one sample each at a time
+constexpr int kTcThreads = 128 * kTcWg;
 constexpr int kMaxGroup = 8;     // samples per group (one tree's proposals)
+// Per warpgroup one 32 KB operand buffer: A1 [128 x 64] at its start while
+// layer 2 runs, then A2 [128 x 128] (written once the layer-2 MMAs, which
+// read A1, have completed).
 constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes,
-                   kSmA1 = kSmB3 + kTcW3Bytes,                    // [2][128 x 64] bf16
-                   kSmA2 = kSmA1 + 2 * kPts * kD1 * 2,            // [2][128 x 128] bf16
-                   kSmW1 = kSmA2 + 2 * kPts * kD2 * 2,
+                   kSmA2 = kSmB3 + kTcW3Bytes,                    // [wg][128 x 128] bf16
+                   kSmW1 = kSmA2 + kTcWg * kPts * kD2 * 2,
                    kSmH = kSmW1 + 4 * (3 * kD1 + kD1),            // [group][256]
                    kSmY1 = kSmH + 4 * kMaxGroup * kD3,            // [group][128]
                    kSmBias = kSmY1 + 4 * kMaxGroup * kD4,         // b2, b3, b4, W5, b5
                    kSmMisc = kSmBias + 4 * (kD2 + kD3 + kD4 + kD4 * kD5 + 8),
                    kTcSmem = kSmMisc + 64;
-static_assert(kSmA1 % 128 == 0 && kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
+static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
 static_assert(kSmMisc % 16 == 0 && kTcSmem <= 227 * 1024, "shared memory");
+static_assert(kPts * kD1 * 2 <= kPts * kD2 * 2, "A1 inside the A2 buffer");
 // the descriptors address at most: A1 [128 x 64], A2 [128 x 128], W2^T
 // [128 x 64], W3^T [256 x 128]; every core matrix lies inside its buffer
 static_assert(core_offset(kPts - 1, kD1 - 1, kD1) + 2 <= kPts * kD1 * 2, "A1 extent");
@@ -506,16 +510,28 @@ SLOAM_D bool mbar_wait_bounded(uint64_t* m, uint32_t phase, int* err, int* abort
   }
   return true;
 }
-// barrier of one warpgroup (128 threads); ids 1, 2 (0 is __syncthreads)
+// barrier of one warpgroup (128 threads); ids 1..kTcWg (0 is __syncthreads)
 SLOAM_D void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+// the same barrier, returning the OR of p over the warpgroup: a decision
+// every thread of the warpgroup takes alike
+SLOAM_D bool wg_any(int wg, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, d;\n\tsetp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred d, %2, 128, q;\n\tselp.u32 %0, 1, 0, d;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(1 + wg)
+      : "memory");
+  return r != 0;
+}
 
 // Tensor-core inference.  Persistent CTAs (one per SM at most: the shared
 // memory allows no second) over groups of `group` samples -- in the
 // pipeline one tree's proposals; groups whose frame scale is 0 (trees not
-// fitted) are skipped.  256 threads: warpgroup g (0, 1) takes samples
-// g, g + 2, ... of the group with its own operand buffers, TMEM columns
-// [256 g, 256 g + 256), mbarrier and barrier, so that one warpgroup's MMAs
-// overlap the other's CUDA-core work.  Per sample, layer 1 on CUDA cores
+// fitted) are skipped.  512 threads: warpgroup g (0..3) takes samples
+// g, g + 4 of the group with its own operand buffer, TMEM columns
+// [128 g, 128 g + 128), mbarrier and barrier, so that one warpgroup's MMAs
+// overlap the others' CUDA-core work.  Per sample, layer 1 on CUDA cores
 // (FP32, thread r = point r) into bf16 A1; layer 2 as tcgen05.mma M=128
 // points, N=128, K=64 (TMEM lane r = point r) into bf16 A2; layer 3
 // transposed, M=128 features (two halves of W3^T), N=128 points, K=128, so
@@ -536,14 +552,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   float* sb4 = sb3 + kD3;                                    // b4 [128]
   float* sw5 = sb4 + kD4;                                    // W5 [128][7]
   float* sb5 = sw5 + kD4 * kD5;                              // b5 [7]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 16);
-  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 20);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [kTcWg]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8 * kTcWg);
+  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 8 * kTcWg + 4);
   const float* f = reinterpret_cast<const float*>(tcw + kTcF32Off);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int wg = tid >> 7, lt = tid & 127, wq = warp & 3;
-  unsigned char* a1b = smem + kSmA1 + wg * kPts * kD1 * 2;
   unsigned char* a2b = smem + kSmA2 + wg * kPts * kD2 * 2;
+  unsigned char* a1b = a2b;
   // groups: ceil(S / group), or the device count of groups when given
   int ng = (S + group - 1) / group;
   if (n_groups_dev) ng = min(ng, *n_groups_dev);
@@ -560,8 +576,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     for (int i = tid; i < kD4 * kD5 + kD5; i += kTcThreads) sw5[i] = f[kW5 + i];  // W5, b5
   }
   if (tid == 0) {
-    mbar_init(mbar, 1);
-    mbar_init(mbar + 1, 1);
+    for (int q = 0; q < kTcWg; ++q) mbar_init(mbar + q, 1);
     *abort_flag = 0;
   }
   if (warp == 0) {
@@ -574,7 +589,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   fence_before();
   __syncthreads();
   fence_after();
-  const uint32_t tmem = *tslot + (uint32_t)(wg * 256);
+  const uint32_t tmem = *tslot + (uint32_t)(wg * 128);  // 128 columns per warpgroup
   const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
   const uint32_t sA1 = saddr(a1b), sA2 = saddr(a2b);
   const uint32_t sB2 = saddr(smem + kSmB2), sB3 = saddr(smem + kSmB3);
@@ -584,7 +599,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   for (int g = blockIdx.x; g < ng; g += gridDim.x) {
     const int s0 = g * group, gs = min(group, S - s0);
     if (frames && !(frames[s0].w > 0.0f)) continue;  // block-uniform
-    for (int k = wg; k < gs; k += 2) {
+    for (int k = wg; k < gs; k += kTcWg) {
       const int s = s0 + k;
       // layer 1 (row lt) -> A1 in bf16 core-matrix layout
       {
@@ -640,68 +655,69 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
       }
       fence_async_smem();
       fence_before();
-      wg_sync(wg);
+      if (wg_any(wg, *abort_flag != 0)) break;  // uniform over the warpgroup
       fence_after();
-      if (*abort_flag) break;
       // layer 3 transposed: D^T[feature][point] = W3^T[feature][:] . A2[point][:],
-      // two M = 128 feature halves (A = W3^T rows, B = A2), N = 128 points,
-      // into TMEM columns [128 half, 128 half + 128)
-      if (lt == 0) {
-        for (int hf = 0; hf < 2; ++hf)
+      // one M = 128 feature half at a time (A = W3^T rows, B = A2, N = 128
+      // points) into the warpgroup's 128 TMEM columns.  Thread (TMEM lane)
+      // = feature: the max over the points is a register reduction of its
+      // row, then bias and ReLU (both monotone, so max then bias/ReLU equals
+      // the max of the biased ReLU outputs).
+      bool ab = false;
+      for (int hf = 0; hf < 2 && !ab; ++hf) {
+        if (lt == 0) {
           for (int ks = 0; ks < kD2 / 16; ++ks)
-            mma_bf16(tmem + hf * kPts,
+            mma_bf16(tmem,
                      smem_desc(sB3 + hf * (kPts * kD2 * 2) + ks * 256, 128, (kD2 / 8) * 128),
                      smem_desc(sA2 + ks * 256, 128, (kD2 / 8) * 128), idesc_bf16(128, kPts),
                      ks > 0);
-        mma_commit(mb);
-      }
-      mbar_wait_bounded(mb, phase, err, abort_flag);
-      phase ^= 1u;
-      fence_after();
-      // epilogue 3: thread (lane row) = feature; max over the 128 points in
-      // registers, then bias and ReLU (both monotone, so max then bias/ReLU
-      // equals the max of the biased ReLU outputs)
-#pragma unroll 1
-      for (int hf = 0; hf < 2; ++hf) {
+          mma_commit(mb);
+        }
+        mbar_wait_bounded(mb, phase, err, abort_flag);
+        phase ^= 1u;
+        fence_after();
         float m = -INFINITY;
 #pragma unroll 1
         for (int cc = 0; cc < kPts / 32; ++cc) {
           uint32_t v[32];
-          SG_TMEM_LD32(tmem + lane_base + hf * kPts + cc * 32, v);
+          SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
           tmem_wait_ld();
 #pragma unroll
           for (int q = 0; q < 32; ++q) m = fmaxf(m, __uint_as_float(v[q]));
         }
         const int c = hf * kPts + lt;
         h[k * kD3 + c] = fmaxf(m + sb3[c], 0.0f);
+        // barrier: the next half's MMAs (or the next sample's) overwrite
+        // these columns
+        fence_before();
+        ab = wg_any(wg, *abort_flag != 0);
+        fence_after();
       }
-      if (*abort_flag) break;
-      fence_before();
-      wg_sync(wg);
-      fence_after();
+      if (ab) break;
     }
     fence_before();
-    __syncthreads();
+    const int ab_all = __syncthreads_or(*abort_flag != 0);
     fence_after();
-    if (*abort_flag) break;
+    if (ab_all) break;
     // head over the group: y1[k][j] = ReLU(b4 + sum_c h[k][c] W4[c][j]);
-    // warpgroup wg takes the samples k = wg (mod 2)
+    // warpgroup wg takes the samples k = wg (mod kTcWg)
     {
+      constexpr int kPer = kMaxGroup / kTcWg;
       const int j = lt;
-      float acc[kMaxGroup / 2];
+      float acc[kPer];
 #pragma unroll
-      for (int q = 0; q < kMaxGroup / 2; ++q) acc[q] = sb4[j];
+      for (int q = 0; q < kPer; ++q) acc[q] = sb4[j];
       for (int c = 0; c < kD3; ++c) {
         const float wv = f[kW4 + c * kD4 + j];
 #pragma unroll
-        for (int q = 0; q < kMaxGroup / 2; ++q) {
-          const int k = wg + 2 * q;
+        for (int q = 0; q < kPer; ++q) {
+          const int k = wg + kTcWg * q;
           if (k < gs) acc[q] += h[k * kD3 + c] * wv;
         }
       }
 #pragma unroll
-      for (int q = 0; q < kMaxGroup / 2; ++q) {
-        const int k = wg + 2 * q;
+      for (int q = 0; q < kPer; ++q) {
+        const int k = wg + kTcWg * q;
         if (k < gs) y1[k * kD4 + j] = fmaxf(acc[q], 0.0f);
       }
     }
