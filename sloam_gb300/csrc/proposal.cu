@@ -494,6 +494,8 @@ constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes,
 static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
 static_assert(kSmMisc % 16 == 0 && kTcSmem <= 227 * 1024, "shared memory");
 static_assert(kPts * kD1 * 2 <= kPts * kD2 * 2, "A1 inside the A2 buffer");
+static_assert(kD3 * kD4 * 2 <= kTcWg * kPts * kD2 * 2, "bf16 W4 inside the operand buffers");
+static_assert((kTcF32Off + 4 * kW4) % 8 == 0, "W4 float2 alignment");
 // the descriptors address at most: A1 [128 x 64], A2 [128 x 128], W2^T
 // [128 x 64], W3^T [256 x 128]; every core matrix lies inside its buffer
 static_assert(core_offset(kPts - 1, kD1 - 1, kD1) + 2 <= kPts * kD1 * 2, "A1 extent");
@@ -699,16 +701,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const int ab_all = __syncthreads_or(*abort_flag != 0);
     fence_after();
     if (ab_all) break;
+    // W4 into the operand buffers, free until the next group's layer 1: its
+    // values are bf16 (rounded when packed), so the bf16 copy is exact
+    __nv_bfloat162* w4s = reinterpret_cast<__nv_bfloat162*>(smem + kSmA2);
+    {
+      const float2* w4g = reinterpret_cast<const float2*>(f + kW4);
+#pragma unroll 4
+      for (int i = tid; i < kD3 * kD4 / 2; i += kTcThreads) {
+        const float2 v = w4g[i];
+        w4s[i] = __floats2bfloat162_rn(v.x, v.y);
+      }
+    }
+    __syncthreads();
     // head over the group: y1[k][j] = ReLU(b4 + sum_c h[k][c] W4[c][j]);
     // warpgroup wg takes the samples k = wg (mod kTcWg)
     {
       constexpr int kPer = kMaxGroup / kTcWg;
       const int j = lt;
+      const __nv_bfloat16* w4h = reinterpret_cast<const __nv_bfloat16*>(w4s);
       float acc[kPer];
 #pragma unroll
       for (int q = 0; q < kPer; ++q) acc[q] = sb4[j];
+#pragma unroll 8
       for (int c = 0; c < kD3; ++c) {
-        const float wv = f[kW4 + c * kD4 + j];
+        const float wv = __bfloat162float(w4h[c * kD4 + j]);
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
           const int k = wg + kTcWg * q;
