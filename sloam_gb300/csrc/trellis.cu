@@ -334,11 +334,23 @@ __device__ __forceinline__ uint32_t fkey(float v) {
 // rounds), then the k'-th element, in index order, among those with the
 // selected key -- the element the rank count (b < a, or b == a and k < j)
 // puts at position k.
-constexpr int kVtxSlots = kVtxCap / 32;
-__device__ __forceinline__ float warp_select(const uint32_t (&key)[kVtxSlots],
-                                             const float (&val)[kVtxSlots], int n, int k,
-                                             int lane) {
+constexpr int kVtxSlots = 4;          // the sort path takes buckets of <= 128 points
+constexpr int kVtxSortMax = 32 * kVtxSlots;
+__device__ __forceinline__ float warp_select(const float4* P, int axis, int n, int k, int lane) {
   const int ns = (n + 31) >> 5;
+  uint32_t key[kVtxSlots];
+  float val[kVtxSlots];
+#pragma unroll
+  for (int s = 0; s < kVtxSlots; ++s) {
+    const int j = s * 32 + lane;
+    float v = 0.0f;
+    if (j < n) {
+      const float4 a = P[j];
+      v = axis == 0 ? a.x : axis == 1 ? a.y : a.z;
+    }
+    val[s] = v;
+    key[s] = fkey(v);
+  }
   unsigned cb[kVtxSlots];  // remaining candidates, one ballot word per slot
   int nc = n;
 #pragma unroll
@@ -457,22 +469,13 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
     __syncwarp();
     auto pt = [&](int j) -> float4 { return inshm ? P[j] : tree[d.bucket[off + j]]; };
     const int mid = n / 2;  // (int)(n / 2.0)
-    if (inshm && n > 64) {
+    if (inshm && n > 32 && n <= kVtxSortMax) {
       // medians by quickselect; kept points in (z, y, x, column) order
       // by a bitonic sort -- the same elements and order as the rank counts
       // below, in O(n log^2 n) instead of O(n^2)
-      uint32_t kx[kVtxSlots], ky[kVtxSlots], kz[kVtxSlots];
-      float vx[kVtxSlots], vy[kVtxSlots], vz[kVtxSlots];
-#pragma unroll
-      for (int s = 0; s < kVtxSlots; ++s) {
-        const int j = s * 32 + lane;
-        const float4 a = j < n ? P[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        vx[s] = a.x; vy[s] = a.y; vz[s] = a.z;
-        kx[s] = fkey(a.x); ky[s] = fkey(a.y); kz[s] = fkey(a.z);
-      }
-      const float mx = warp_select(kx, vx, n, mid, lane);
-      const float my = warp_select(ky, vy, n, mid, lane);
-      const float mz = warp_select(kz, vz, n, mid, lane);
+      const float mx = warp_select(P, 0, n, mid, lane);
+      const float my = warp_select(P, 1, n, mid, lane);
+      const float mz = warp_select(P, 2, n, mid, lane);
       int m = 32;
       while (m < n) m <<= 1;
       int* idx = srank[w];
