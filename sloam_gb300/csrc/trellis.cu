@@ -168,71 +168,88 @@ int cc_border_pairs(int W, int H) {
   return ((W + kCCTile - 1) / kCCTile - 1) * H + ((H + kCCTile - 1) / kCCTile - 1) * W;
 }
 
+// The whole-image passes below take blocks of 1024 pixels with 256 threads,
+// 4 slices of 256 pixels in turn (so raster order within a block is slice
+// order, then thread order).
+constexpr int kCCThreads = 256, kCCSlices = 4;
+static_assert(kCCThreads * kCCSlices == 1024, "CC block");
+
 // Roots -> per-block counts; every valid pixel stores its root in label[].
-__global__ void __launch_bounds__(1024) k_cc_flatten(Dev d) {
+__global__ void __launch_bounds__(kCCThreads) k_cc_flatten(Dev d) {
   __shared__ int sm[33];
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  bool root = false;
-  if (p < d.N) {
-    const uint32_t par = d.parent[p];
-    if (par != kInvalid) {
-      const uint32_t r = cc_find(d.parent, (uint32_t)p);
-      d.label[p] = r;
-      root = (r == (uint32_t)p);
-    } else {
-      d.label[p] = kInvalid;
+  int roots = 0;
+#pragma unroll
+  for (int j = 0; j < kCCSlices; ++j) {
+    const int p = blockIdx.x * 1024 + j * kCCThreads + threadIdx.x;
+    if (p < d.N) {
+      const uint32_t par = d.parent[p];
+      if (par != kInvalid) {
+        const uint32_t r = cc_find(d.parent, (uint32_t)p);
+        d.label[p] = r;
+        roots += r == (uint32_t)p ? 1 : 0;
+      } else {
+        d.label[p] = kInvalid;
+      }
     }
   }
   int total;
-  block_excl_scan(root ? 1 : 0, sm, &total);
+  block_excl_scan(roots, sm, &total);
   if (threadIdx.x == 0) d.blk[blockIdx.x] = total;
 }
 
 // Rank of each root in raster order = the component label.
-__global__ void __launch_bounds__(1024) k_cc_rank(Dev d) {
+__global__ void __launch_bounds__(kCCThreads) k_cc_rank(Dev d) {
   __shared__ int sm[33];
-  const int base = block_sum_prefix(d.blk, blockIdx.x, sm);
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool root = p < d.N && d.label[p] == (uint32_t)p;
-  int total;
-  const int ex = block_excl_scan(root ? 1 : 0, sm, &total);
-  if (root) {
-    const int r = base + ex;
-    d.rank[p] = (uint32_t)r;
-    d.comp_size[r] = 0;
-    d.comp_cmin[r] = INT_MAX;
-    d.comp_cmax[r] = -1;
+  int base = block_sum_prefix(d.blk, blockIdx.x, sm);
+#pragma unroll
+  for (int j = 0; j < kCCSlices; ++j) {
+    const int p = blockIdx.x * 1024 + j * kCCThreads + threadIdx.x;
+    const bool root = p < d.N && d.label[p] == (uint32_t)p;
+    int total;
+    const int ex = block_excl_scan(root ? 1 : 0, sm, &total);
+    if (root) {
+      const int r = base + ex;
+      d.rank[p] = (uint32_t)r;
+      d.comp_size[r] = 0;
+      d.comp_cmin[r] = INT_MAX;
+      d.comp_cmax[r] = -1;
+    }
+    base += total;
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) d.cnt->n_comp = base + total;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) d.cnt->n_comp = base;
 }
 
 // Final labels + component size and column span (warp-aggregated atomics).
-__global__ void __launch_bounds__(256) k_cc_label(Dev d) {
+__global__ void __launch_bounds__(kCCThreads) k_cc_label(Dev d) {
   const int W = d.W;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t l = kInvalid;
-  if (p < d.N) {
-    const uint32_t r = d.label[p];
-    if (r != kInvalid) {
-      l = d.rank[r];
-      d.label[p] = l;
-    }
-  }
-  const bool valid = l != kInvalid;
-  const unsigned act = __ballot_sync(0xffffffffu, valid);
-  if (!valid) return;
-  const unsigned peers = __match_any_sync(act, l);
   const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  if (lane == leader) {
-    const int last = 31 - __clz(peers);
-    const int p0 = p, p1 = p + (last - lane);
-    int c0 = p0 % W, c1 = p1 % W;
-    // a warp may straddle two rows (W % 32 != 0): fall back to per-lane span
-    if (p0 / W != p1 / W) { c0 = 0; c1 = W - 1; }
-    atomicAdd(d.comp_size + l, __popc(peers));
-    atomicMin(d.comp_cmin + l, c0);
-    atomicMax(d.comp_cmax + l, c1);
+#pragma unroll
+  for (int j = 0; j < kCCSlices; ++j) {
+    const int p = blockIdx.x * 1024 + j * kCCThreads + threadIdx.x;
+    uint32_t l = kInvalid;
+    if (p < d.N) {
+      const uint32_t r = d.label[p];
+      if (r != kInvalid) {
+        l = d.rank[r];
+        d.label[p] = l;
+      }
+    }
+    const bool valid = l != kInvalid;
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      const unsigned peers = __match_any_sync(act, l);
+      const int leader = __ffs(peers) - 1;
+      if (lane == leader) {
+        const int last = 31 - __clz(peers);
+        const int p0 = p, p1 = p + (last - lane);
+        int c0 = p0 % W, c1 = p1 % W;
+        // a warp may straddle two rows (W % 32 != 0): fall back to per-lane span
+        if (p0 / W != p1 / W) { c0 = 0; c1 = W - 1; }
+        atomicAdd(d.comp_size + l, __popc(peers));
+        atomicMin(d.comp_cmin + l, c0);
+        atomicMax(d.comp_cmax + l, c1);
+      }
+    }
   }
 }
 
@@ -762,13 +779,13 @@ __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
 
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   const int N = d.N;
-  const int g256 = (N + 255) / 256, g1k = (N + 1023) / 1024;
+  const int g1k = (N + 1023) / 1024;
   const int tiles = ((d.W + kCCTile - 1) / kCCTile) * ((d.H + kCCTile - 1) / kCCTile);
   k_cc_local<<<tiles, 256, 0, st>>>(d, kp.cc_thr);
   k_cc_border<<<(cc_border_pairs(d.W, d.H) + 255) / 256 + 1, 256, 0, st>>>(d, kp.cc_thr);
-  k_cc_flatten<<<g1k, 1024, 0, st>>>(d);
-  k_cc_rank<<<g1k, 1024, 0, st>>>(d);
-  k_cc_label<<<g256, 256, 0, st>>>(d);
+  k_cc_flatten<<<g1k, kCCThreads, 0, st>>>(d);
+  k_cc_rank<<<g1k, kCCThreads, 0, st>>>(d);
+  k_cc_label<<<g1k, kCCThreads, 0, st>>>(d);
   k_cands<<<1, 1024, 0, st>>>(d, kp.min_cluster);
   // warp-per-item kernels stride over the (candidate, row) items: one wave
   // of 1216 warps on the 152 SMs, leaving room for concurrent keyframes
