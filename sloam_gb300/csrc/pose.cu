@@ -65,18 +65,30 @@ __device__ __forceinline__ void cyl_project(const Pose& T, d3& root, d3& ray) {
   ray = sub3(other, root);
 }
 
-// block-wide argmin (value, then index)
+// block-wide argmin (value, then index) of non-negative, non-NaN doubles:
+// their bit patterns order as unsigned integers, so the comparisons need no
+// FP64 instruction
 __device__ __forceinline__ void block_argmin(double& v, int& i, double* sv, int* si) {
-  warp_argmin(v, i);
+  unsigned long long key = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+    if (ok < key || (ok == key && oi < i)) {
+      key = ok;
+      i = oi;
+    }
+  }
+  unsigned long long* sk = reinterpret_cast<unsigned long long*>(sv);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) { sv[w] = v; si[w] = i; }
+  if (lane == 0) { sk[w] = key; si[w] = i; }
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int k = 1; k < (int)(blockDim.x >> 5); ++k)
-      if (sv[k] < sv[0] || (sv[k] == sv[0] && si[k] < si[0])) { sv[0] = sv[k]; si[0] = si[k]; }
+      if (sk[k] < sk[0] || (sk[k] == sk[0] && si[k] < si[0])) { sk[0] = sk[k]; si[0] = si[k]; }
   }
   __syncthreads();
-  v = sv[0];
+  v = __longlong_as_double((long long)sk[0]);
   i = si[0];
   __syncthreads();
 }
@@ -197,8 +209,12 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(Dev d, KParams kp) {
   __shared__ int si[kAssocThreads / 32];
   __shared__ float su[kAssocThreads / 32];
   __shared__ AxisPts ax;
+  __shared__ Pose sT;
+  __shared__ double sc[3];
   const int nc = d.cnt->n_cyl, np = d.cnt->n_planes, nprev = d.cnt->n_prev;
-  const Pose T = pose_at(d.pose_io);
+  if (threadIdx.x == 0) sT = pose_at(d.pose_io);  // FP64 once per block
+  __syncthreads();
+  const Pose& T = sT;
   for (int it = blockIdx.x; it < nc + np; it += gridDim.x) {
     double bd;
     int bi;
@@ -215,8 +231,13 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(Dev d, KParams kp) {
         d.cyl_match[it] = (d.in->n_map > 0 && bd < kp.tree_match_thresh) ? bi : -1;
     } else {
       const int p = it - nc;
-      const PlaneD P = d.planes[p];
-      const d3 c = xform(T, mk3(P.centroid[0], P.centroid[1], P.centroid[2]));
+      if (threadIdx.x == 0) {
+        const PlaneD P = d.planes[p];
+        const d3 c0 = xform(T, mk3(P.centroid[0], P.centroid[1], P.centroid[2]));
+        sc[0] = c0.x; sc[1] = c0.y; sc[2] = c0.z;
+      }
+      __syncthreads();
+      const d3 c = mk3(sc[0], sc[1], sc[2]);
       bd = kp.plane_match_thresh + 100;
       bi = 0;
       for (int k = threadIdx.x; k < nprev; k += blockDim.x) {
@@ -593,7 +614,10 @@ __global__ void __launch_bounds__(kAssocThreads) k_finalize(Dev d, KParams kp, i
   } else if (d.cnt->status == SLOAM_ERR_NO_MODELS) {
     return;
   }
-  const Pose T = pose_at(d.pose_io + (first ? 0 : 7));
+  __shared__ Pose sT;
+  if (threadIdx.x == 0) sT = pose_at(d.pose_io + (first ? 0 : 7));  // FP64 once per block
+  __syncthreads();
+  const Pose& T = sT;
   if (blockIdx.x == 0) {
     for (int p = threadIdx.x; p < np; p += blockDim.x) {
       PlaneD P = d.planes[p];
