@@ -173,6 +173,28 @@ SLOAM_HD void matmul3(const double* A, const double* B, double* C) {
       T[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] + A[3 * i + 2] * B[6 + j];
   for (int k = 0; k < 9; ++k) C[k] = T[k];
 }
+// Row r of exp([w]x) = I + A K + B K^2, K = [w]x, K^2 = w w^T - |w|^2 I;
+// A = sin(t)/t, B = (1 - cos(t))/t^2 by their Taylor series for t < 0.1
+// (truncation < 3e-14 relative; multiplications by the series' reciprocal
+// constants), else the library functions.
+SLOAM_HD void so3_exp_row(d3 w, int r, double* out) {
+  const double th2 = dot3(w, w);
+  double A, B;
+  if (th2 < 1e-2) {
+    A = 1.0 - th2 * (1.0 / 6.0) * (1.0 - th2 * (1.0 / 20.0) * (1.0 - th2 * (1.0 / 42.0)));
+    B = 0.5 - th2 * (1.0 / 24.0) * (1.0 - th2 * (1.0 / 30.0) * (1.0 - th2 * (1.0 / 56.0)));
+  } else {
+    const double th = sqrt(th2);
+    A = sin(th) / th;
+    B = (1.0 - cos(th)) / th2;
+  }
+  const double wv[3] = {w.x, w.y, w.z};
+  // K row r: r = 0: (0, -wz, wy); r = 1: (wz, 0, -wx); r = 2: (-wy, wx, 0)
+  const double K[3][3] = {{0.0, -w.z, w.y}, {w.z, 0.0, -w.x}, {-w.y, w.x, 0.0}};
+  for (int k = 0; k < 3; ++k)
+    out[k] = (r == k ? 1.0 : 0.0) + A * K[r][k] + B * (wv[r] * wv[k] - (r == k ? th2 : 0.0));
+}
+
 SLOAM_HD void so3_exp(d3 w, double* R) {
   const double th2 = dot3(w, w);
   double A, B;

@@ -428,10 +428,12 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
   if (!kp.two_step) {
     if (!(tchk && gchk)) return;
     // ---------------------------------------------------------- joint
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int itn = 0; itn < kp.gn_iters; ++itn) {
-      if (threadIdx.x == 0) {
-        for (int k = 0; k < 9; ++k) sR[k] = (float)s_R[k];
-        for (int k = 0; k < 3; ++k) sT[k] = (float)s_t[k];
+      // float copies of the pose, one lane per entry
+      if (w == 0 && lane < 12) {
+        if (lane < 9) sR[lane] = (float)s_R[lane];
+        else sT[lane - 9] = (float)s_t[lane - 9];
       }
       __syncthreads();
       float acc[27];
@@ -459,23 +461,36 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
         }
       }
       reduce_normal<27>(acc, red, s_out);
-      if (threadIdx.x == 0) {
-        double Hm[36], g[6], x[6];
-        int k = 0;
-        for (int a = 0; a < 6; ++a)
-          for (int b = a; b < 6; ++b) {
-            Hm[6 * a + b] = s_out[k];
-            Hm[6 * b + a] = s_out[k];
-            ++k;
+      // FP64 6x6 solve on one lane; the SE(3) update R <- exp([x0..2]) R,
+      // t <- t + x3..5 on nine lanes of the same warp (each FP64 warp
+      // instruction costs the pipe the same for one lane or nine)
+      if (w == 0) {
+        if (lane == 0) {
+          double Hm[36], g[6], x[6];
+          int k = 0;
+          for (int a = 0; a < 6; ++a)
+            for (int b = a; b < 6; ++b) {
+              Hm[6 * a + b] = s_out[k];
+              Hm[6 * b + a] = s_out[k];
+              ++k;
+            }
+          for (int a = 0; a < 6; ++a) g[a] = -s_out[21 + a];
+          if (s_ok && chol_solve(6, Hm, g, x)) {
+            for (int a = 0; a < 6; ++a) s_x[a] = x[a];
+          } else {
+            s_ok = 0;
           }
-        for (int a = 0; a < 6; ++a) g[a] = -s_out[21 + a];
-        if (s_ok && chol_solve(6, Hm, g, x)) {
-          double dR[9];
-          so3_exp(mk3(x[0], x[1], x[2]), dR);
-          matmul3(dR, s_R, s_R);
-          s_t[0] += x[3]; s_t[1] += x[4]; s_t[2] += x[5];
-        } else {
-          s_ok = 0;
+        }
+        __syncwarp();
+        if (s_ok && lane < 9) {
+          const int r = lane / 3, c = lane - 3 * r;
+          double dRr[3];
+          so3_exp_row(mk3(s_x[0], s_x[1], s_x[2]), r, dRr);
+          const double v = dRr[0] * s_R[c] + dRr[1] * s_R[3 + c] + dRr[2] * s_R[6 + c];
+          const double tn = lane < 3 ? s_t[lane] + s_x[3 + lane] : 0.0;
+          __syncwarp(0x1ffu);
+          s_R[lane] = v;
+          if (lane < 3) s_t[lane] = tn;
         }
       }
       __syncthreads();
