@@ -371,6 +371,46 @@ int sloam_project_mask_noalloc(const sloam_params* params, const float* d_xyzi, 
                                int32_t* d_ground_idx, int32_t* d_n_ground,
                                float* d_tree_cloud, void* stream);
 
+/* ---- Map manager on the GPU (MapManager, mapManager.h:7-10) ------------
+ * The landmark map, its hit counts, the submap query and the update stay
+ * in device memory.  getSubmap (mapManager.cpp:41-68): the k nearest map
+ * roots to (x, y, 1) - squared distances summed in double and rounded to
+ * float, ties to the lower map index; the reference's k is 100 (:54) - of
+ * which those among the `recent` most recently added (200, :60) form the
+ * submap, in distance order.  updateMap (mapManager.cpp:8-28): each
+ * cylinder in order; no match appends it with one hit, a match overwrites
+ * the matched entry and adds a hit. */
+typedef struct sloam_mapmgr sloam_mapmgr;
+
+/* MapManager::MapManager (mapManager.cpp:3): an empty map of up to
+ * `capacity` landmarks on `device`. */
+int sloam_mapmgr_create(int32_t device, int32_t capacity, int32_t k, int32_t recent,
+                        sloam_mapmgr** out);
+int sloam_mapmgr_destroy(sloam_mapmgr* mm);
+/* Map size, size of the last submap, and 1 when an append found the map
+ * full (the cylinder was dropped). */
+int sloam_mapmgr_size(sloam_mapmgr* mm, int32_t* n, int32_t* n_submap, int32_t* overflow);
+/* MapManager::getMap (mapManager.cpp:30-39), with the hit counts: up to
+ * `cap` entries into host arrays; *n = the map size. */
+int sloam_mapmgr_read(sloam_mapmgr* mm, sloam_cylinder* models, int32_t* hits, int32_t cap,
+                      int32_t* n);
+/* Replaces the map by n host entries. */
+int sloam_mapmgr_load(sloam_mapmgr* mm, const sloam_cylinder* models, const int32_t* hits,
+                      int32_t n);
+/* MapManager::getSubmap at (x, y): the submap into host arrays (its map
+ * indices too, NULL skips), *n_out = its size. */
+int sloam_mapmgr_submap(sloam_mapmgr* mm, double x, double y, sloam_cylinder* out,
+                        int32_t* map_index, int32_t cap, int32_t* n_out);
+/* One keyframe of SLOAMNode::runSLOAMNode with the device map
+ * (sloamNode.cpp:197-236): getSubmap at the pose's (x, y), RunSloam on it
+ * (as sloam_keyframe, with the submap as the map), then updateMap with the
+ * keyframe's cylinders and matches when the status is SLOAM_OK or
+ * SLOAM_ERR_NOT_CONVERGED.  A later keyframe whose submap is empty returns
+ * SLOAM_ERR_EMPTY_MAP and leaves the map unchanged (sloamNode.cpp:199). */
+int sloam_keyframe_mapped(sloam_ctx* ctx, sloam_mapmgr* mm, const float* xyzi, int32_t n,
+                          const uint8_t* point_labels, const uint8_t* mask_image,
+                          const sloam_se3* pose, sloam_run_out* out);
+
 /* Returns the number of kernels launched by the last call (for accounting). */
 int64_t sloam_last_launch_count(const sloam_ctx* ctx);
 

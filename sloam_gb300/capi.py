@@ -363,6 +363,12 @@ class RunBuffers:
         self.m.s.n_cylinders = self.s.models.n_cylinders
 
 
+def cylinders_to_array(arr, n):
+    """The first n of a ctypes array of Cylinder -> (n,8) [root3, ray3, radius, id]."""
+    return np.array([[*c.root, *c.ray, c.radius, c.id] for c in arr[:n]],
+                    np.float64).reshape(n, 8)
+
+
 def cylinders_from_array(a):
     """(n,8) [root3, ray3, radius, id] -> ctypes array of Cylinder."""
     n = len(a)

@@ -1042,6 +1042,54 @@ extern "C" int sloam_keyframe(sloam_ctx* ctx, const float* xyzi, int32_t n,
   return status;
 }
 
+extern "C" int sloam_keyframe_mapped(sloam_ctx* ctx, sloam_mapmgr* mm, const float* xyzi,
+                                     int32_t n, const uint8_t* point_labels,
+                                     const uint8_t* mask_image, const sloam_se3* pose,
+                                     sloam_run_out* out) {
+  if (!ctx || !mm || !xyzi || !pose || !out || (!point_labels && !mask_image))
+    return SLOAM_ERR_ARG;
+  if (sg::mapmgr_device(mm) != ctx->device)
+    return fail(ctx, SLOAM_ERR_ARG, "the map manager is on another device");
+  cudaSetDevice(ctx->device);
+  if (int g_ = need_weights(ctx)) return g_;
+  Dev& d = ctx->d;
+  const sg::MapMgrDev& m = sg::mapmgr_dev(mm);
+  if (n != d.N) return fail(ctx, SLOAM_ERR_ARG, "n must equal img_h * img_w");
+  if (m.k > d.cap_map) return fail(ctx, SLOAM_ERR_CAPACITY, "submap size k exceeds max_map");
+  const bool first = ctx->first_scan;
+  CK(cudaMemcpyAsync(d.buf_xyzi, xyzi, 16 * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+  if (point_labels)
+    CK(cudaMemcpyAsync(d.buf_plabel, point_labels, n, cudaMemcpyHostToDevice, ctx->st));
+  else
+    CK(cudaMemcpyAsync(d.buf_mask_in, mask_image, n, cudaMemcpyHostToDevice, ctx->st));
+  int st = set_inputs(ctx, d.buf_xyzi, d.buf_plabel, d.buf_mask_in, m.sub, 0);
+  if (st) return st;
+  if ((st = upload_pose(ctx, pose))) return st;
+  // getSubmap on the device; map and n_map of the input block follow it
+  sg::launch_mm_submap(m, pose->t[0], pose->t[1], d.in, ctx->st);
+  int32_t n_sub = 0;
+  CK(cudaMemcpyAsync(&ctx->h_cnt->pad[0], m.state + 1, 4, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  n_sub = ctx->h_cnt->pad[0];
+  if (!first && n_sub == 0) {
+    out->success = 0;
+    return fail(ctx, SLOAM_ERR_EMPTY_MAP, "not the first scan but the submap is empty");
+  }
+  if ((st = run_keyframe_graph(ctx, first, point_labels != nullptr, true))) return st;
+  int nk = ctx->last_launches;
+  nk += sg::launch_mm_update(m, d, first ? 1 : 0, ctx->st);
+  ctx->last_launches = nk + 1;
+  if ((st = sync_counters(ctx))) return st;
+  ctx->first_scan = false;
+  const int status = first ? SLOAM_OK : ctx->h_cnt->status;
+  if (status == SLOAM_ERR_NO_MODELS) {
+    out->success = 0;
+    return fail(ctx, SLOAM_ERR_NO_MODELS, "no ground or landmark models found");
+  }
+  if ((st = download_run(ctx, out, first))) return st;
+  return status;
+}
+
 namespace sg {
 // per-keyframe outputs of a device batch
 __global__ void k_batch_out(Counters* c, const double* pose_io, double* pose_out,

@@ -265,6 +265,26 @@ int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const 
 void init_attributes();
 }  // namespace prop
 
+// Device view of a map manager (mapmgr.cu): the map, hit counts, scratch,
+// the last submap and its map indices; state = {n, n_submap, overflow}.
+struct MapMgrDev {
+  int cap, k, recent;
+  sloam_cylinder* models;  // [cap]
+  int32_t* hits;           // [cap]
+  float* dist;             // [cap] squared distances of the last query
+  sloam_cylinder* sub;     // [k]
+  int32_t* sub_idx;        // [k] map index of each submap entry
+  int32_t* slot;           // [k] rank -> map index scratch
+  int32_t* state;          // [4]
+};
+// submap query at (x, y); with d_in, also points the keyframe input block's
+// map at the submap (map, n_map written on the device)
+int launch_mm_submap(const MapMgrDev& m, double x, double y, InPtrs* d_in, cudaStream_t st);
+// map update with the keyframe's cylinders and matches (reads its status)
+int launch_mm_update(const MapMgrDev& m, const Dev& d, int first, cudaStream_t st);
+const MapMgrDev& mapmgr_dev(const sloam_mapmgr* mm);
+int mapmgr_device(const sloam_mapmgr* mm);
+
 // host-built tables (context.cu)
 void build_px_table(const sloam_params& p, float* tab);
 void build_py_table(const sloam_params& p, float* tab);

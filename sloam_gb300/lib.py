@@ -18,6 +18,8 @@ EXPORTS = [
     "sloam_run", "sloam_keyframe",
     "sloam_keyframes_device", "sloam_keyframes_host", "sloam_last_launch_count", "sloam_stream",
     "sloam_internal_tables", "sloam_set_proposal_weights", "sloam_pack_points",
+    "sloam_mapmgr_create", "sloam_mapmgr_destroy", "sloam_mapmgr_size", "sloam_mapmgr_read",
+    "sloam_mapmgr_load", "sloam_mapmgr_submap", "sloam_keyframe_mapped",
 ]
 
 _lib = None
@@ -73,6 +75,19 @@ def load(path=LIB_PATH):
     L.sloam_set_proposal_weights.argtypes = [vp, C.POINTER(C.c_float), C.c_int32]
     L.sloam_pack_points.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_int32, vp, vp]
+    L.sloam_mapmgr_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                      C.POINTER(vp)]
+    L.sloam_mapmgr_destroy.argtypes = [vp]
+    L.sloam_mapmgr_size.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32)]
+    L.sloam_mapmgr_read.argtypes = [vp, C.POINTER(A.Cylinder), C.POINTER(C.c_int32), C.c_int32,
+                                    C.POINTER(C.c_int32)]
+    L.sloam_mapmgr_load.argtypes = [vp, C.POINTER(A.Cylinder), C.POINTER(C.c_int32), C.c_int32]
+    L.sloam_mapmgr_submap.argtypes = [vp, C.c_double, C.c_double, C.POINTER(A.Cylinder),
+                                      C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]
+    L.sloam_keyframe_mapped.argtypes = [vp, vp, C.POINTER(C.c_float), C.c_int32,
+                                        C.POINTER(C.c_uint8), C.POINTER(C.c_uint8),
+                                        C.POINTER(A.SE3), C.POINTER(A.RunOut)]
     L.sloam_last_launch_count.argtypes = [vp]
     L.sloam_last_launch_count.restype = C.c_int64
     L.sloam_stream.argtypes = [vp]
@@ -128,3 +143,67 @@ class Context:
 
     def stream(self):
         return self.L.sloam_stream(self.h)
+
+
+class DeviceMapManager:
+    """The map manager on the GPU (sloam_mapmgr_*): map, hit counts, submap
+    query and update in device memory."""
+
+    def __init__(self, capacity=100000, k=100, recent=200, device=0):
+        self.L = load()
+        h = C.c_void_p()
+        st = self.L.sloam_mapmgr_create(device, capacity, k, recent, C.byref(h))
+        if st:
+            raise SloamError(st, "sloam_mapmgr_create failed")
+        self.h = h
+        self.capacity = capacity
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sloam_mapmgr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def size(self):
+        n, s, o = C.c_int32(), C.c_int32(), C.c_int32()
+        st = self.L.sloam_mapmgr_size(self.h, C.byref(n), C.byref(s), C.byref(o))
+        if st:
+            raise SloamError(st)
+        return n.value, s.value, o.value
+
+    def read(self):
+        """(models [n, 8] = root3, ray3, radius, id; hits [n])."""
+        import numpy as np
+        n = self.size()[0]
+        arr = (A.Cylinder * max(1, n))()
+        hits = np.zeros(max(1, n), np.int32)
+        got = C.c_int32()
+        st = self.L.sloam_mapmgr_read(self.h, arr, hits.ctypes.data_as(C.POINTER(C.c_int32)),
+                                      n, C.byref(got))
+        if st:
+            raise SloamError(st)
+        return A.cylinders_to_array(arr, n), hits[:n]
+
+    def load(self, models, hits):
+        import numpy as np
+        n = len(models)
+        arr = A.cylinders_from_array(np.asarray(models, np.float64).reshape(-1, 8))
+        h = np.ascontiguousarray(hits, np.int32)
+        st = self.L.sloam_mapmgr_load(self.h, arr, h.ctypes.data_as(C.POINTER(C.c_int32)), n)
+        if st:
+            raise SloamError(st)
+
+    def submap(self, x, y, cap=4096):
+        """(submap models [m, 8], their map indices [m])."""
+        import numpy as np
+        arr = (A.Cylinder * cap)()
+        idx = np.zeros(cap, np.int32)
+        n = C.c_int32()
+        st = self.L.sloam_mapmgr_submap(self.h, x, y, arr, idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        cap, C.byref(n))
+        if st:
+            raise SloamError(st)
+        m = n.value
+        return A.cylinders_to_array(arr, m), idx[:m]

@@ -268,12 +268,14 @@ def _compose(Ra, ta, Rb, tb):
     return Ra @ Rb, Ra @ tb + ta
 
 
-def run(keyframe, P, poses, odo, scans, submap_k):
+def run(keyframe, P, poses, odo, scans, submap_k, mm=None):
     """Runs the sequence through keyframe(P, xyzi, labels, (R, t), map) ->
     (status, success, (R, t), cylinders, matches); returns the estimated
-    trajectory and the wall time."""
+    trajectory and the wall time.  `mm`: the host map manager to use (a new
+    one with k = submap_k by default)."""
     from . import capi as A
-    mm = MapManager(k=submap_k)
+    if mm is None:
+        mm = MapManager(k=submap_k)
     est = [poses[0]]
     t0 = time.perf_counter()
     for k in range(len(poses)):
@@ -288,6 +290,30 @@ def run(keyframe, P, poses, odo, scans, submap_k):
             mm.update(cyl, matches)
         if k > 0:
             est.append(pose if (st == 0 and ok) else guess)
+    return est, time.perf_counter() - t0
+
+
+def run_mapped(ctx, mm, P, poses, odo, scans):
+    """The same sequence through sloam_keyframe_mapped: the map manager on
+    the GPU (getSubmap, RunSloam, updateMap without the map leaving the
+    device).  Returns the estimated trajectory and the wall time."""
+    from . import capi as A
+    est = [poses[0]]
+    t0 = time.perf_counter()
+    for k in range(len(poses)):
+        if k == 0:
+            guess = poses[0]
+        else:
+            guess = _compose(est[-1][0], est[-1][1], *odo[k - 1])
+        xyzi, lab = scans[k]
+        r = A.RunBuffers(P)
+        st = ctx.L.sloam_keyframe_mapped(
+            ctx.h, mm.h, A.ptr(xyzi, C.c_float), len(xyzi), A.ptr(lab, C.c_uint8), None,
+            C.byref(A.SE3.from_qt(synth.quat_from_R(guess[0]), guess[1])), C.byref(r.s))
+        r.refresh()
+        q, t = r.s.T_Map_Curr.qt()
+        if k > 0:
+            est.append((synth.R_from_quat(q), t) if (st == 0 and r.s.success) else guess)
     return est, time.perf_counter() - t0
 
 
