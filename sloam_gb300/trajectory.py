@@ -391,6 +391,7 @@ def main():
     res = {"config": {"keyframes": a.kf, "H": a.h, "W": a.w, "trees": a.trees,
                       "submap": a.submap, "gn_iters": 15, "seed": a.seed,
                       "scene_seconds": gen_s}}
+    ests = {}
     for name, mode in (("gpu_plain", 1), ("gpu_learned", 2)):
         P = params(a.h, a.w, mode, submap=a.submap)
         ctx = Context(P)
@@ -398,7 +399,22 @@ def main():
             ctx.set_proposal_weights(proposal.load_weights())
         est, dt = run(gpu_keyframe_fn(ctx), P, poses, odo, scans, a.submap)
         res[name] = dict(drift(poses, est), seconds=dt, keyframes_per_s=a.kf / dt)
+        ests[name] = est
         ctx.close()
+    # the plain path with the map manager on the GPU (sloam_keyframe_mapped)
+    from .lib import DeviceMapManager
+    P = params(a.h, a.w, 1, submap=a.submap)
+    ctx = Context(P)
+    dm = DeviceMapManager(capacity=max(4 * a.trees, 4096), k=a.submap, recent=200)
+    est, dt = run_mapped(ctx, dm, P, poses, odo, scans)
+    dev_t = max(float(np.abs(np.asarray(e[1]) - np.asarray(h[1])).max())
+                for e, h in zip(est, ests["gpu_plain"]))
+    res["gpu_plain_device_map"] = dict(drift(poses, est), seconds=dt,
+                                       keyframes_per_s=a.kf / dt,
+                                       max_translation_diff_vs_host_map_m=dev_t,
+                                       map_size=dm.size()[0])
+    dm.close()
+    ctx.close()
     if a.oracle:
         from oracle import loader
         L = loader.lib()
