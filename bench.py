@@ -50,9 +50,9 @@ WORKLOAD = ("C2: 64x2048 keyframes, 150 trees, 400-landmark submap, 10 GN iterat
             "inlier ratio) + 3 LS; plain: 256 RANSAC hypotheses per tree + 3 LS")
 # DRAM bytes (read + write) per keyframe of the batch projection stage, summed
 # over its three kernels in one ncu capture with the caches left as they are
-# (dram__bytes_read.sum + dram__bytes_write.sum of the 8-keyframe chunk
-# launches: 6.05 and 6.50 MB per keyframe in two chunks).
-FRONT_TRAFFIC_PER_KF = 6.28e6
+# (dram__bytes_read.sum + dram__bytes_write.sum of two 16-keyframe chunk
+# launches: 4.15 and 6.43 MB per keyframe).
+FRONT_TRAFFIC_PER_KF = 5.29e6
 
 
 def max_over_ranks(x, device=None):
@@ -434,7 +434,8 @@ def main():
     e2e_ok = int(h_succ.sum())
 
     # ---- roofline: the batch projection stage (HBM-bound), per launch group
-    # of 8 keyframes; algorithmic bytes = 26 B per point.
+    # (16 keyframes per launch with the inputs in device memory);
+    # algorithmic bytes = 26 B per point.
     peaks, peak_src = {}, "fallback"
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))

@@ -204,7 +204,12 @@ extern "C" int sloam_internal_tables(const sloam_params* p, float* px_tab, float
 
 // ================================================================ context
 // Keyframes per batch projection launch.
-constexpr int kFrontChunk = 8;
+// Keyframes per batch projection launch: 16 when the scans are already in
+// device memory (fewer, longer launches; the chunk's scans, pixels and keys
+// still fit in L2), 8 when they stream from host memory (uploads of the next
+// chunk overlap the projection of this one and the keyframes of the last).
+constexpr int kFrontChunkHost = 8, kFrontChunkDevice = 16;
+constexpr int kFrontChunkMax = kFrontChunkDevice;
 
 // Captured keyframe graphs of one slot, keyed
 // [first scan][point labels][state update][projection done by a batch launch].
@@ -248,8 +253,9 @@ struct sloam_ctx {
   cudaStream_t fe_st = nullptr;
   void* fb = nullptr;            // [fb_cap] per-keyframe projection buffers
   size_t fb_stride = 0;          // bytes per keyframe
-  int32_t* fb_pix = nullptr;     // [kFrontChunk * N] point pixels of the chunk in flight
-  unsigned long long* fb_pkey = nullptr;  // [kFrontChunk * N] pixel keys, kept all-ones
+  int32_t* fb_pix = nullptr;     // [kFrontChunkMax * N] point pixels of the chunk in flight
+  unsigned long long* fb_pkey = nullptr;  // [kFrontChunkMax * N] pixel keys, kept all-ones
+  int fe_chunk = kFrontChunkHost;         // keyframes per projection launch of this batch
   int fb_cap = 0;
   bool fb_upload = false;        // the buffers include scan upload space
   FrontRef* d_refs = nullptr;    // [fb_cap]
@@ -525,7 +531,10 @@ int set_inputs(sloam_ctx* ctx, const float4* xyzi, const uint8_t* pl, const uint
   h.tree = ctx->d.tree;
   h.ground = ctx->d.ground;
   h.fe = nullptr;
+  h.tflag = nullptr;
+  h.gidx = nullptr;
   h.n_map = n_map;
+  h.destag = 0;
   CK(cudaMemcpyAsync(ctx->d.in, &h, sizeof(InPtrs), cudaMemcpyHostToDevice, ctx->st));
   // the pinned block must stay unchanged until the copy ran
   CK(cudaStreamSynchronize(ctx->st));
@@ -1143,11 +1152,14 @@ FrontSlice front_slice(const Dev& d, char* base, bool upload, size_t* bytes) {
   FrontSlice s;
   s.f.range_img = c.take<float>(N);
   s.f.mask = c.take<uint8_t>(N);
-  s.f.tree = c.take<float4>(N);
+  // the tree cloud and the ground list stay views of the scan: a tree flag
+  // per point and the ground point indices (no 16 B copies per point)
+  s.f.tree = nullptr;
+  s.f.tflag = c.take<uint8_t>(N);
   s.f.gbits = c.take<uint32_t>(front_gbits_words(N));
   s.f.blk = c.take<int32_t>(front_blocks(N));
   s.f.ground_idx = c.take<int32_t>(N);
-  s.f.ground = c.take<float4>(d.cap_ground);
+  s.f.ground = nullptr;
   if (upload) {
     s.up_xyzi = c.take<float4>(N);
     s.up_plabel = c.take<uint8_t>(N);
@@ -1184,7 +1196,7 @@ int grow_front(sloam_ctx* ctx, int nkf, bool upload) {
   size_t stride = 0;
   front_slice(ctx->d, nullptr, upload, &stride);
   CK(cudaMalloc(&ctx->fb, stride * cap));
-  const size_t sn = (size_t)kFrontChunk * ctx->d.N;
+  const size_t sn = (size_t)kFrontChunkMax * ctx->d.N;
   CK(cudaMalloc((void**)&ctx->fb_pix, sizeof(int32_t) * sn));
   CK(cudaMalloc((void**)&ctx->fb_pkey, sizeof(unsigned long long) * sn));
   CK(cudaMemsetAsync(ctx->fb_pkey, 0xFF, sizeof(unsigned long long) * sn, ctx->fe_st));
@@ -1253,13 +1265,14 @@ void fill_pose(sloam_ctx* ctx, int k, const sloam_se3& p) {
 void fill_batch(sloam_ctx* ctx, int nkf, const float* xyzi, const uint8_t* labels,
                 const sloam_se3* poses, const sloam_cylinder* d_map, int n_map) {
   const int n = ctx->d.N;
+  ctx->fe_chunk = xyzi ? kFrontChunkDevice : kFrontChunkHost;
   for (int k = 0; k < nkf; ++k) {
     FrontSlice s = front_slice(ctx->d, (char*)ctx->fb + ctx->fb_stride * k, ctx->fb_upload,
                                nullptr);
     FrontRef& f = ctx->h_refs[k];
     f = s.f;
-    f.pix = ctx->fb_pix + (size_t)(k % kFrontChunk) * n;
-    f.pkey = ctx->fb_pkey + (size_t)(k % kFrontChunk) * n;
+    f.pix = ctx->fb_pix + (size_t)(k % ctx->fe_chunk) * n;
+    f.pkey = ctx->fb_pkey + (size_t)(k % ctx->fe_chunk) * n;
     f.xyzi = xyzi ? reinterpret_cast<const float4*>(xyzi) + (size_t)k * n : s.up_xyzi;
     f.plabel = labels ? labels + (size_t)k * n : s.up_plabel;
     f.mask_in = nullptr;
@@ -1269,11 +1282,13 @@ void fill_batch(sloam_ctx* ctx, int nkf, const float* xyzi, const uint8_t* label
     h.plabel = f.plabel;
     h.mask_in = nullptr;
     h.map = d_map;
-    h.tree = f.tree;
-    h.ground = f.ground;
+    h.tree = nullptr;
+    h.ground = nullptr;
     h.fe = f.fe;
+    h.tflag = f.tflag;
+    h.gidx = f.ground_idx;
     h.n_map = n_map;
-    h.pad = 0;
+    h.destag = ctx->kp.do_destagger ? 1 : 0;
     fill_pose(ctx, k, poses[k]);
   }
 }
@@ -1287,7 +1302,8 @@ int batch_run(sloam_ctx* ctx, int nkf, const float* h_xyzi, const uint8_t* h_lab
               double* pose_out, int32_t* success_out, int32_t* ncyl_out, int64_t* launches) {
   const int n = ctx->d.N;
   const int S = 1 + (int)ctx->extra.size();
-  const int nch = (nkf + kFrontChunk - 1) / kFrontChunk;
+  const int chunk = ctx->fe_chunk;
+  const int nch = (nkf + chunk - 1) / chunk;
   while ((int)ctx->ev_fe.size() < 2 * nch) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
@@ -1298,7 +1314,7 @@ int batch_run(sloam_ctx* ctx, int nkf, const float* h_xyzi, const uint8_t* h_lab
   CK(cudaMemsetAsync(ctx->fb_fe, 0, sizeof(int32_t) * 4 * nkf, ctx->fe_st));
   ctx->fe_chunks = 0;
   for (int c = 0; c < nch; ++c) {
-    const int kf0 = c * kFrontChunk, nc = std::min(kFrontChunk, nkf - kf0);
+    const int kf0 = c * chunk, nc = std::min(chunk, nkf - kf0);
     if (h_xyzi) {
       for (int k = kf0; k < kf0 + nc; ++k) {
         FrontRef& f = ctx->h_refs[k];
@@ -1421,6 +1437,9 @@ int own_views(sloam_ctx* ctx) {
   h.tree = ctx->d.tree;
   h.ground = ctx->d.ground;
   h.fe = nullptr;
+  h.tflag = nullptr;
+  h.gidx = nullptr;
+  h.destag = 0;
   CK(cudaMemcpy(ctx->d.in, &h, sizeof(h), cudaMemcpyHostToDevice));
   return SLOAM_OK;
 }

@@ -68,12 +68,58 @@ struct InPtrs {
   const uint8_t* plabel;
   const uint8_t* mask_in;
   const sloam_cylinder* map;
-  const float4* tree;
-  const float4* ground;
+  const float4* tree;      // organised tree cloud, or null: derived (TreeView)
+  const float4* ground;    // ground list, or null: xyzi[gidx[i]] (GroundView)
   const int32_t* fe;
+  const uint8_t* tflag;    // per point: its pixel's label is the tree label
+  const int32_t* gidx;     // ground list as point indices
   int32_t n_map;
-  int32_t pad;
+  int32_t destag;          // Ouster destagger applied to the derived tree cloud
 };
+
+// The organised tree cloud of maskCloud(..., 255, true) + _destaggerCloud
+// (inference.cpp:200-273): materialised, or from the scan and the per-point
+// tree flag exactly as the projection's label pass would write it -- x, y, z
+// of the point (of point p - 32 on even rows at column >= 32 when
+// destaggered) if that point's pixel is a tree pixel, else NaN; the
+// intensity of the point itself if its pixel is a tree pixel, else 0.
+struct TreeView {
+  const float4* tree;
+  const float4* xyzi;
+  const uint8_t* flag;
+  int W;
+  int destag;
+  __device__ __forceinline__ float4 operator[](int p) const {
+    if (tree) return tree[p];
+    const float nan = __int_as_float(0x7fc00000);
+    const bool f = flag[p] != 0;
+    float4 t = f ? xyzi[p] : make_float4(nan, nan, nan, 0.0f);
+    if (destag) {
+      const int row = p / W, c = p - row * W;
+      if ((row & 1) == 0 && c >= 32) {
+        const bool fs = flag[p - 32] != 0;
+        const float4 s = fs ? xyzi[p - 32] : make_float4(nan, nan, nan, 0.0f);
+        t.x = s.x; t.y = s.y; t.z = s.z;
+      }
+    }
+    return t;
+  }
+};
+// The ground list of maskCloud(..., 1): materialised, or as point indices.
+struct GroundView {
+  const float4* ground;
+  const float4* xyzi;
+  const int32_t* idx;
+  __device__ __forceinline__ float4 operator[](int i) const {
+    return ground ? ground[i] : xyzi[idx[i]];
+  }
+};
+__device__ __forceinline__ TreeView tree_view(const InPtrs* in, int W) {
+  return TreeView{in->tree, in->xyzi, in->tflag, W, in->destag};
+}
+__device__ __forceinline__ GroundView ground_view(const InPtrs* in) {
+  return GroundView{in->ground, in->xyzi, in->gidx};
+}
 
 // One keyframe's projection buffers (a1-a2).  A batch launch reads an array
 // of these, one per keyframe, indexed by blockIdx.y.
@@ -85,11 +131,12 @@ struct FrontRef {
   unsigned long long* pkey;
   float* range_img;
   uint8_t* mask;
-  float4* tree;
+  float4* tree;      // materialised tree cloud (one keyframe on the context)
+  uint8_t* tflag;    // per-point tree flag (batch keyframes)
   uint32_t* gbits;
   int32_t* blk;
   int32_t* ground_idx;
-  float4* ground;
+  float4* ground;    // materialised ground list, or null (batch keyframes)
   int32_t* fe;  // {n_ground, overflow, n_slow_px, pad}
 };
 

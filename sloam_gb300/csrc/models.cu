@@ -103,7 +103,7 @@ __device__ __forceinline__ int warp_bin_add(int* hist, int bin, int lane) {
 
 __global__ void __launch_bounds__(256) k_gbin(Dev d, KParams kp) {
   __shared__ int hist[kMaxBins];
-  const float4* __restrict__ ground = d.in->ground;
+  const GroundView ground = ground_view(d.in);
   const int n = d.cnt->n_ground;
   if (blockIdx.x * blockDim.x >= n) return;
   const int lane = threadIdx.x & 31;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(1024) k_gbin_scan(Dev d) {
 // (k_plane orders every bin by key).
 __global__ void __launch_bounds__(256) k_gbin_scatter(Dev d) {
   __shared__ int hist[kMaxBins];
-  const float4* __restrict__ ground = d.in->ground;
+  const GroundView ground = ground_view(d.in);
   const int n = d.cnt->n_ground;
   if (blockIdx.x * blockDim.x >= n) return;
   const int lane = threadIdx.x & 31;
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
   __shared__ float cen[3];
   __shared__ unsigned long long sel_prefix;
   __shared__ int sel_k, s_cnt;
-  const float4* __restrict__ ground = d.in->ground;
+  const GroundView ground = ground_view(d.in);
   const int b = blockIdx.x;
   if (b >= d.n_bins) return;
   const int off = d.bin_off[b], n = d.bin_off[b + 1] - off;

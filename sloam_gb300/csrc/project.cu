@@ -80,6 +80,7 @@ __device__ __forceinline__ FrontRef front(const Dev& d, const FrontRef* refs, in
   f.range_img = d.range_img;
   f.mask = d.mask;
   f.tree = d.tree;
+  f.tflag = nullptr;
   f.gbits = d.gbits;
   f.blk = d.blk;
   f.ground_idx = d.ground_idx;
@@ -198,10 +199,12 @@ constexpr int kLabelThreads = 256, kLabelPer = 4;
 static_assert(kLabelThreads * kLabelPer == 1024, "label block");
 
 // Index o is pixel o and point o.  Pixel: range image and mask from the
-// winner.  Point: maskCloud -- the organised tree cloud (with the Ouster
-// destagger as a gather: even rows take x,y,z from column c-32 for c >= 32
-// and keep their own intensity; inference.cpp:200-228) and the ground bit,
-// both from the label of the point's pixel.
+// winner.  Point: maskCloud -- the ground bit and the organised tree cloud,
+// both from the label of the point's pixel.  One keyframe on the context
+// materialises the tree cloud (with the Ouster destagger as a gather: even
+// rows take x,y,z from column c-32 for c >= 32 and keep their own
+// intensity; inference.cpp:200-228); a batch keyframe writes a tree flag per
+// point, from which TreeView derives the same values.
 template <bool kBatch>
 __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, const FrontRef* refs,
                                                          int kf0, int point_labels) {
@@ -224,13 +227,15 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
     if (o < N) {
       key[j] = f.pkey[o];
       pix[j] = f.pix[o];
-      src[j] = f.xyzi[o];
       min_[j] = point_labels ? 0 : f.mask_in[o];
-      const int row = o / W, c = o - row * W;
-      stag[j] = kp.do_destagger && (row & 1) == 0 && c >= 32;
-      if (stag[j]) {
-        spix[j] = f.pix[o - 32];
-        sq[j] = f.xyzi[o - 32];
+      if (!kBatch) {  // the materialised tree cloud needs the points
+        src[j] = f.xyzi[o];
+        const int row = o / W, c = o - row * W;
+        stag[j] = kp.do_destagger && (row & 1) == 0 && c >= 32;
+        if (stag[j]) {
+          spix[j] = f.pix[o - 32];
+          sq[j] = f.xyzi[o - 32];
+        }
       }
     }
   }
@@ -251,14 +256,19 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
       f.mask[o] = m;
       const uint8_t mo = pixel_label(f, pix[j], point_labels);
       ground = (mo == 1);
-      float4 t = (mo == 255) ? src[j] : make_float4(nan, nan, nan, 0.0f);
-      if (stag[j]) {
-        const uint8_t ms = pixel_label(f, spix[j], point_labels);
-        t.x = (ms == 255) ? sq[j].x : nan;
-        t.y = (ms == 255) ? sq[j].y : nan;
-        t.z = (ms == 255) ? sq[j].z : nan;
+      if (kBatch) {
+        // the tree cloud stays a view: this flag + the scan (TreeView)
+        f.tflag[o] = mo == 255 ? 1 : 0;
+      } else {
+        float4 t = (mo == 255) ? src[j] : make_float4(nan, nan, nan, 0.0f);
+        if (stag[j]) {
+          const uint8_t ms = pixel_label(f, spix[j], point_labels);
+          t.x = (ms == 255) ? sq[j].x : nan;
+          t.y = (ms == 255) ? sq[j].y : nan;
+          t.z = (ms == 255) ? sq[j].z : nan;
+        }
+        f.tree[o] = t;
       }
-      f.tree[o] = t;
     }
     const unsigned b = __ballot_sync(0xffffffffu, ground);
     if ((threadIdx.x & 31) == 0 && o < N + 31) f.gbits[o >> 5] = b;
@@ -270,7 +280,8 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
 }
 
 // Ordered compaction of the ground points (point order: the 4 slices of a
-// block in turn); re-arms the pixel keys for the next scan.
+// block in turn): their indices, and for one keyframe on the context their
+// points too; re-arms the pixel keys for the next scan.
 template <bool kBatch>
 __global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const FrontRef* refs,
                                                                   int kf0) {
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const F
     const unsigned b = (o < N + 31) ? f.gbits[o >> 5] : 0u;
     g[j] = o < N && ((b >> (threadIdx.x & 31)) & 1u);
     v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (g[j]) v[j] = f.xyzi[o];  // issued before the prefix sums
+    if (!kBatch && g[j]) v[j] = f.xyzi[o];  // issued before the prefix sums
     if (o < N) f.pkey[o] = ~0ull;
   }
   int run = block_sum_prefix(f.blk, blockIdx.x, sm);
@@ -297,7 +308,8 @@ __global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const F
     const int pos = run + block_excl_scan(g[j] ? 1 : 0, sm, &total);
     if (g[j]) {
       f.ground_idx[pos] = o;
-      if (pos < d.cap_ground) f.ground[pos] = v[j];
+      // batch keyframes keep the ground list as indices (GroundView)
+      if (!kBatch && pos < d.cap_ground) f.ground[pos] = v[j];
     }
     run += total;
   }

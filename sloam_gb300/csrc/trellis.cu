@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr) {
   __shared__ int lp[kCCTile * kCCTile];
   __shared__ float4 pt[kCCTile * kCCTile];
   __shared__ unsigned vbits[kCCTile], hbits[kCCTile];
-  const float4* __restrict__ tree = d.in->tree;
+  const TreeView tree = tree_view(d.in, d.W);
   const int W = d.W, H = d.H;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int tiles_x = (W + kCCTile - 1) / kCCTile;
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr) {
 // vertical border, upper neighbour across a horizontal one) join in the
 // global parent array.
 __global__ void __launch_bounds__(256) k_cc_border(Dev d, float thr) {
-  const float4* __restrict__ tree = d.in->tree;
+  const TreeView tree = tree_view(d.in, d.W);
   const int W = d.W, H = d.H;
   const int nv = ((W + kCCTile - 1) / kCCTile - 1) * H;
   const int nh = ((H + kCCTile - 1) / kCCTile - 1) * W;
@@ -464,7 +464,7 @@ __device__ __forceinline__ void warp_bitonic(int* a, int m, int n, int lane, Les
 __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
   __shared__ float4 spts[kVtxWarps][kVtxCap];
   __shared__ int srank[kVtxWarps][kVtxCap];
-  const float4* __restrict__ tree = d.in->tree;
+  const TreeView tree = tree_view(d.in, d.W);
   const int H = d.H;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nitems = d.cnt->n_cand * H;
@@ -750,7 +750,7 @@ __global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
 // vertex for the kept points, one thread per bucket slot for the cluster
 // points (raster order; the candidate of a slot found by binary search).
 __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
-  const float4* __restrict__ tree = d.in->tree;
+  const TreeView tree = tree_view(d.in, d.W);
   const int H = d.H;
   const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;

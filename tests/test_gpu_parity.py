@@ -318,13 +318,16 @@ def _check_batch(po, succ, ncyl, order, ref):
         assert int(succ[k]) == ok
 
 
-def test_keyframes_batches_match_single():
+@pytest.mark.parametrize("destagger", [0, 1])
+def test_keyframes_batches_match_single(destagger):
     """Batches through the device and the host entry points: 37 keyframes
     (several batch projection launches, the last one partial) over five
-    slots, each result bit-identical to the keyframe run alone."""
+    slots, each result bit-identical to the keyframe run alone.  The batch
+    keeps the tree cloud and the ground list as views of the scan (tree
+    flags, ground indices); the keyframe alone materialises them."""
     import torch
     cfg, forest, kfs = H.scene("C2", seed=0, n_kf=3)
-    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1)
+    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1, do_destagger=destagger)
     P.batch_slots = 5
     mapa = forest.map_cylinders()
     mapc = A.cylinders_from_array(mapa)
