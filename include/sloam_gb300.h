@@ -112,6 +112,14 @@ typedef struct sloam_params {
   float   prop_min_inlier_ratio;    /* mode 2: best proposal's inliers /
                                        tree points below this -> RANSAC
                                        fallback for the tree        (0.6) */
+  int32_t pose_solver;              /* 0 = Gauss-Newton, gn_iters fixed
+                                       iterations (0) ; 1 = trust-region
+                                       Levenberg-Marquardt with the solver
+                                       settings the reference gives Ceres
+                                       (sloam.cpp:91-97: at most
+                                       lm_max_iters iterations, default
+                                       trust-region options)              */
+  int32_t lm_max_iters;             /* max_num_iterations (sloam.cpp:92) (50) */
 } sloam_params;
 
 void sloam_params_default(sloam_params* p);

@@ -1225,9 +1225,13 @@ void matmul3(const double* A, const double* B, double* C) {
   std::memcpy(C, T, sizeof(T));
 }
 
+bool optimize_joint_lm(const sloam_params& P, const SE3& est, const std::vector<CylRes>& cr,
+                       const std::vector<PlaneRes>& pr, SE3& out);
+
 // OptimizePose (joint, quaternion + translation), sloam.cpp:174-255.
 bool optimize_joint(const sloam_params& P, const SE3& est, const std::vector<CylRes>& cr,
                     const std::vector<PlaneRes>& pr, SE3& out) {
+  if (P.pose_solver == 1) return optimize_joint_lm(P, est, cr, pr, out);
   V3 a = est.t;
   double R[9];
   std::memcpy(R, est.R, sizeof(R));
@@ -1317,12 +1321,209 @@ void aa_rotate_jac(const double* r, V3 p, V3& out, double Jr3[9]) {
   }
 }
 
+// ---- a10 with pose_solver 1: trust-region Levenberg-Marquardt ----------
+// The solver settings the reference gives Ceres (sloam.cpp:91-97,
+// 149-155: at most max_num_iterations = 50, the rest default), restated
+// from Ceres' documented behaviour:
+//  - cost 1/2 sum rho(r^2), Huber rho with delta = huber_delta; residuals
+//    and Jacobian rows rescaled by sqrt(rho'), which for a loss with
+//    rho'' <= 0 (Huber) is the whole robust correction: H = sum w J J^T,
+//    g = sum w J r with w = rho'(r^2) (the IRLS weight of the GN path);
+//  - Jacobi scaling: column i scaled by 1 / (1 + sqrt(H_ii));
+//  - LM step: (Hs + D / radius) ds = -gs, D = diag(Hs) clamped to
+//    [1e-6, 1e32]; predicted decrease -(g.d + d.H.d / 2);
+//  - ratio = actual / predicted decrease; a step is taken when it is above
+//    1e-3: radius /= max(1/3, 1 - (2 ratio - 1)^3) (at most 1e16) and the
+//    shrink factor returns to 2; otherwise radius /= factor, factor *= 2
+//    (stop below 1e-32);
+//  - stop when |g|_inf <= 1e-10, when |step| <= 1e-8 (|x| + 1e-8), when a
+//    step changes the cost by at most 1e-6 of it (not taken), or after
+//    lm_max_iters iterations; initial radius 1e4.
+// The joint mode's quaternion is stepped as Ceres' quaternion plus does,
+// q <- [cos|d|, sin|d| d/|d|] q: a rotation by 2|d|, so its step is half
+// the rotation vector of the GN path.
+struct LMLin {
+  double cost = 0.0;
+  double H[36] = {0};
+  double g[6] = {0};
+};
+
+inline double huber_rho(double r, double delta) {
+  const double s2 = r * r;
+  return s2 <= delta * delta ? s2 : 2.0 * delta * std::fabs(r) - delta * delta;
+}
+
+template <int N, typename State, typename Lin, typename Plus, typename XNorm>
+void lm_minimize(int max_iters, State& x, Lin lin, Plus plus, XNorm xnorm) {
+  LMLin L = lin(x);
+  double radius = 1e4, factor = 2.0;
+  auto gmax = [](const LMLin& l) {
+    double m = 0.0;
+    for (int i = 0; i < N; ++i) m = std::max(m, std::fabs(l.g[i]));
+    return m;
+  };
+  if (gmax(L) <= 1e-10) return;
+  for (int it = 0; it < max_iters; ++it) {
+    double sc[N], A[N * N], b[N], ds[N], d[N];
+    for (int i = 0; i < N; ++i) sc[i] = 1.0 / (1.0 + std::sqrt(L.H[i * N + i]));
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) A[i * N + j] = sc[i] * L.H[i * N + j] * sc[j];
+    for (int i = 0; i < N; ++i) {
+      const double dg = std::min(std::max(A[i * N + i], 1e-6), 1e32);
+      A[i * N + i] += dg / radius;
+      b[i] = -sc[i] * L.g[i];
+    }
+    if (!chol_solve(N, A, b, ds)) {
+      radius /= factor;
+      factor *= 2.0;
+      if (radius < 1e-32) return;
+      continue;
+    }
+    double step2 = 0.0, gd = 0.0, dHd = 0.0;
+    for (int i = 0; i < N; ++i) {
+      d[i] = sc[i] * ds[i];
+      step2 += d[i] * d[i];
+    }
+    for (int i = 0; i < N; ++i) {
+      gd += L.g[i] * d[i];
+      for (int j = 0; j < N; ++j) dHd += d[i] * L.H[i * N + j] * d[j];
+    }
+    const double model = -(gd + 0.5 * dHd);
+    if (std::sqrt(step2) <= 1e-8 * (xnorm(x) + 1e-8)) return;
+    const State xn = plus(x, d);
+    const LMLin Ln = lin(xn);
+    if (std::fabs(L.cost - Ln.cost) <= 1e-6 * L.cost) return;
+    const double ratio = (L.cost - Ln.cost) / model;
+    if (model > 0.0 && ratio > 1e-3) {
+      x = xn;
+      L = Ln;
+      const double t = 2.0 * ratio - 1.0;
+      radius = std::min(1e16, radius / std::max(1.0 / 3.0, 1.0 - t * t * t));
+      factor = 2.0;
+      if (gmax(L) <= 1e-10) return;
+    } else {
+      radius /= factor;
+      factor *= 2.0;
+      if (radius < 1e-32) return;
+    }
+  }
+}
+
+struct JointState {
+  double R[9];
+  V3 t;  // in the frame anchored at the estimate's translation
+};
+
+bool optimize_joint_lm(const sloam_params& P, const SE3& est, const std::vector<CylRes>& cr,
+                       const std::vector<PlaneRes>& pr, SE3& out) {
+  const V3 a = est.t;
+  JointState x;
+  std::memcpy(x.R, est.R, sizeof(x.R));
+  x.t = V3{0, 0, 0};
+  std::vector<CylRes> C = cr;
+  std::vector<PlaneRes> Pl = pr;
+  for (auto& m : C) m.root = m.root - a;
+  for (auto& m : Pl) m.d = m.d + dot(m.n, a);
+  const double delta = P.huber_delta;
+  auto lin = [&](const JointState& s) {
+    LMLin L;
+    auto acc = [&](double res, V3 Jl, V3 q) {
+      const V3 Jw = cross(q, Jl);
+      const double J[6] = {2 * Jw.x, 2 * Jw.y, 2 * Jw.z, Jl.x, Jl.y, Jl.z};
+      const double w = huber_w(res, delta);
+      L.cost += 0.5 * huber_rho(res, delta);
+      for (int i = 0; i < 6; ++i) {
+        L.g[i] += w * J[i] * res;
+        for (int j = 0; j < 6; ++j) L.H[6 * i + j] += w * J[i] * J[j];
+      }
+    };
+    for (auto& m : C) {
+      V3 q = rot(s.R, m.p), lp = q + s.t, J;
+      double r = cyl_res(m, lp, J);
+      acc(r, J, q);
+    }
+    for (auto& m : Pl) {
+      V3 q = rot(s.R, m.p), lp = q + s.t, J;
+      double r = plane_res(m, lp, J);
+      acc(r, J, q);
+    }
+    return L;
+  };
+  auto plus = [](const JointState& s, const double* d) {
+    JointState n;
+    double dR[9];
+    so3_exp({2 * d[0], 2 * d[1], 2 * d[2]}, dR);
+    matmul3(dR, s.R, n.R);
+    n.t = s.t + V3{d[3], d[4], d[5]};
+    return n;
+  };
+  auto xnorm = [&](const JointState& s) {
+    const V3 ta = s.t + a;
+    return std::sqrt(1.0 + dot(ta, ta));
+  };
+  lm_minimize<6>(P.lm_max_iters, x, lin, plus, xnorm);
+  std::memcpy(out.R, x.R, sizeof(x.R));
+  out.t = x.t + a;
+  return true;
+}
+
+struct SubsetState {
+  double v[6];
+};
+
+template <typename ResT>
+bool optimize_subset_lm(const sloam_params& P, double x[6], const int free_idx[3],
+                        const std::vector<ResT>& res, V3 a) {
+  const double delta = P.huber_delta;
+  SubsetState st;
+  for (int i = 0; i < 6; ++i) st.v[i] = x[i];
+  auto lin = [&](const SubsetState& s) {
+    LMLin L;
+    for (const auto& m0 : res) {
+      ResT m = m0;
+      V3 q, Jl;
+      double J3[9];
+      aa_rotate_jac(s.v + 3, m.p, q, J3);
+      V3 lp = q + V3{s.v[0] - a.x, s.v[1] - a.y, s.v[2] - a.z};
+      double r;
+      if constexpr (std::is_same<ResT, CylRes>::value) r = cyl_res(m, lp, Jl);
+      else r = plane_res(m, lp, Jl);
+      const double Jfull[6] = {Jl.x, Jl.y, Jl.z,
+                               Jl.x * J3[0] + Jl.y * J3[3] + Jl.z * J3[6],
+                               Jl.x * J3[1] + Jl.y * J3[4] + Jl.z * J3[7],
+                               Jl.x * J3[2] + Jl.y * J3[5] + Jl.z * J3[8]};
+      const double J[3] = {Jfull[free_idx[0]], Jfull[free_idx[1]], Jfull[free_idx[2]]};
+      const double w = huber_w(r, delta);
+      L.cost += 0.5 * huber_rho(r, delta);
+      for (int i = 0; i < 3; ++i) {
+        L.g[i] += w * J[i] * r;
+        for (int j = 0; j < 3; ++j) L.H[3 * i + j] += w * J[i] * J[j];
+      }
+    }
+    return L;
+  };
+  auto plus = [&](const SubsetState& s, const double* d) {
+    SubsetState n = s;
+    for (int i = 0; i < 3; ++i) n.v[free_idx[i]] += d[i];
+    return n;
+  };
+  auto xnorm = [](const SubsetState& s) {
+    double q = 0.0;
+    for (int i = 0; i < 6; ++i) q += s.v[i] * s.v[i];
+    return std::sqrt(q);
+  };
+  lm_minimize<3>(P.lm_max_iters, st, lin, plus, xnorm);
+  for (int i = 0; i < 6; ++i) x[i] = st.v[i];
+  return true;
+}
+
 // OptimizeXYYaw / OptimizeZRollPitch, sloam.cpp:55-172: the 6-vector
 // (tx,ty,tz,rx,ry,rz) with angle-axis rotation, `free` the three optimised
 // entries.  Returns false if a solve fails.
 template <typename ResT>
 bool optimize_subset(const sloam_params& P, double x[6], const int free_idx[3],
                      const std::vector<ResT>& res, V3 a) {
+  if (P.pose_solver == 1) return optimize_subset_lm(P, x, free_idx, res, a);
   const double delta = P.huber_delta;
   for (int it = 0; it < P.gn_iters; ++it) {
     double H[9] = {0}, g[3] = {0};

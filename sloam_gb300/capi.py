@@ -81,6 +81,8 @@ class Params(C.Structure):
         ("batch_slots", C.c_int32),
         ("prop_samples", C.c_int32),
         ("prop_min_inlier_ratio", C.c_float),
+        ("pose_solver", C.c_int32),
+        ("lm_max_iters", C.c_int32),
     ]
 
     def copy(self):
@@ -153,6 +155,8 @@ def default_params(**overrides):
     p.batch_slots = 8
     p.prop_samples = 8
     p.prop_min_inlier_ratio = 0.6
+    p.pose_solver = 0
+    p.lm_max_iters = 50
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)

@@ -75,6 +75,8 @@ extern "C" void sloam_params_default(sloam_params* p) {
   p->batch_slots = 8;
   p->prop_samples = 8;
   p->prop_min_inlier_ratio = 0.6f;
+  p->pose_solver = 0;
+  p->lm_max_iters = 50;
 }
 
 // sizeof() of every ABI struct, for binding checks.
@@ -401,6 +403,8 @@ int check_params(const sloam_params& p) {
   if (!(p.ground_retain_thresh > 0)) return 1;
   if (p.batch_slots < 0 || p.batch_slots > 64) return 1;
   if (p.cyl_mode < 0 || p.cyl_mode > 2 || p.prop_samples < 1 || p.prop_samples > 8) return 1;
+  if (p.pose_solver < 0 || p.pose_solver > 1 || p.lm_max_iters < 1 || p.lm_max_iters > 1000)
+    return 1;
   return 0;
 }
 

@@ -260,6 +260,7 @@ struct KParams {
   double min_tree_models, min_ground_models, min_planes;
   int two_step;
   int gn_iters;
+  int pose_lm, lm_iters;  // trust-region LM instead of fixed GN iterations
   double huber;
 };
 

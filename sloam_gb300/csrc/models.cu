@@ -68,6 +68,8 @@ KParams make_kparams(const sloam_params& p) {
   k.min_planes = p.min_planes;
   k.two_step = p.two_step_optim;
   k.gn_iters = p.gn_iters;
+  k.pose_lm = p.pose_solver == 1 ? 1 : 0;
+  k.lm_iters = p.lm_max_iters;
   k.huber = p.huber_delta;
   return k;
 }

@@ -380,9 +380,107 @@ __device__ __forceinline__ void reduce_normal(const float* acc, float (*red)[kGN
   __syncthreads();
 }
 
+// ---- pose_solver 1: trust-region Levenberg-Marquardt (the rules of the
+// oracle's lm_minimize: the solver settings the reference gives Ceres,
+// sloam.cpp:91-97, 149-155).  The bookkeeping runs on one thread in FP64;
+// the residual passes use the whole block.
+template <int N>
+struct LMDev {
+  double H[N * N], g[N], cost;  // linearisation at the current point
+  double radius, factor, model;
+  double d[N];                  // the step proposed last
+  int done;
+};
+__device__ __forceinline__ float huber_rho_f(float r, float delta) {
+  const float a = fabsf(r);
+  return a <= delta ? r * r : 2.0f * delta * a - delta * delta;
+}
+// H (upper triangle, row by row), g and the cost from a block reduction;
+// `sc` scales the parameters (the joint mode steps half rotation vectors)
+template <int N>
+__device__ void lm_load(LMDev<N>& L, const double* s_out, const double* sc) {
+  int k = 0;
+  for (int a = 0; a < N; ++a)
+    for (int b = a; b < N; ++b) {
+      L.H[N * a + b] = L.H[N * b + a] = sc[a] * s_out[k] * sc[b];
+      ++k;
+    }
+  for (int a = 0; a < N; ++a) L.g[a] = sc[a] * s_out[k + a];
+  L.cost = s_out[k + N];
+}
+template <int N>
+__device__ bool lm_gsmall(const LMDev<N>& L) {
+  double m = 0.0;
+  for (int i = 0; i < N; ++i) m = fmax(m, fabs(L.g[i]));
+  return m <= 1e-10;
+}
+// One proposal: 1 = a candidate step in L.d, -1 = the damped system failed
+// (the radius shrank), 0 = stopped (step below the parameter tolerance, or
+// the radius below 1e-32).
+template <int N>
+__device__ int lm_propose(LMDev<N>& L, double xnorm) {
+  double sc[N], A[N * N], b[N], ds[N];
+  for (int i = 0; i < N; ++i) sc[i] = 1.0 / (1.0 + sqrt(L.H[i * N + i]));
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) A[i * N + j] = sc[i] * L.H[i * N + j] * sc[j];
+  for (int i = 0; i < N; ++i) {
+    const double dg = fmin(fmax(A[i * N + i], 1e-6), 1e32);
+    A[i * N + i] += dg / L.radius;
+    b[i] = -sc[i] * L.g[i];
+  }
+  if (!chol_solve(N, A, b, ds)) {
+    L.radius /= L.factor;
+    L.factor *= 2.0;
+    return L.radius < 1e-32 ? 0 : -1;
+  }
+  double step2 = 0.0, gd = 0.0, dHd = 0.0;
+  for (int i = 0; i < N; ++i) {
+    L.d[i] = sc[i] * ds[i];
+    step2 += L.d[i] * L.d[i];
+  }
+  for (int i = 0; i < N; ++i) {
+    gd += L.g[i] * L.d[i];
+    for (int j = 0; j < N; ++j) dHd += L.d[i] * L.H[i * N + j] * L.d[j];
+  }
+  L.model = -(gd + 0.5 * dHd);
+  if (sqrt(step2) <= 1e-8 * (xnorm + 1e-8)) return 0;
+  return 1;
+}
+// The candidate's linearisation in s_out: true when the step is taken;
+// sets L.done when the solve stops.
+template <int N>
+__device__ bool lm_decide(LMDev<N>& L, const double* s_out, const double* sc) {
+  LMDev<N> C;
+  lm_load<N>(C, s_out, sc);
+  if (fabs(L.cost - C.cost) <= 1e-6 * L.cost) {
+    L.done = 1;
+    return false;
+  }
+  const double ratio = (L.cost - C.cost) / L.model;
+  if (L.model > 0.0 && ratio > 1e-3) {
+    for (int i = 0; i < N * N; ++i) L.H[i] = C.H[i];
+    for (int i = 0; i < N; ++i) L.g[i] = C.g[i];
+    L.cost = C.cost;
+    const double t = 2.0 * ratio - 1.0;
+    L.radius = fmin(1e16, L.radius / fmax(1.0 / 3.0, 1.0 - t * t * t));
+    L.factor = 2.0;
+    if (lm_gsmall<N>(L)) L.done = 1;
+    return true;
+  }
+  L.radius /= L.factor;
+  L.factor *= 2.0;
+  if (L.radius < 1e-32) L.done = 1;
+  return false;
+}
+
+template <bool kLM>
 __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
-  __shared__ float red[27][kGN / 32];
-  __shared__ double s_out[27];
+  __shared__ float red[28][kGN / 32];
+  __shared__ double s_out[28];
+  __shared__ LMDev<6> lm6;
+  __shared__ LMDev<3> lm3;
+  __shared__ double c_R[9], c_t[3], c_x[6];
+  __shared__ int s_flag;
   __shared__ float sR[9], sT[3], sRj[9], sJr[9];
   __shared__ double s_R[9], s_t[3], s_x[6], s_anchor[3];
   __shared__ int s_ok, s_checks[2];
@@ -427,8 +525,91 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
   const float delta = (float)kp.huber;
   if (!kp.two_step) {
     if (!(tchk && gchk)) return;
-    // ---------------------------------------------------------- joint
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (kLM) {
+      // ------------------------------------------ joint, trust-region LM
+      const double sc6[6] = {2.0, 2.0, 2.0, 1.0, 1.0, 1.0};  // d = omega / 2
+      auto pass = [&]() {  // cost, H, g at (sR, sT)
+        float acc[28];
+#pragma unroll
+        for (int j = 0; j < 28; ++j) acc[j] = 0.f;
+        for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
+          const float* e = d.res_tab + (size_t)kResStride * i;
+          if (e[0] == 0.f) continue;
+          const float px = e[1], py = e[2], pz = e[3];
+          const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
+          const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
+          const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
+          float Jl[3];
+          const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
+          const float J[6] = {qy * Jl[2] - qz * Jl[1], qz * Jl[0] - qx * Jl[2],
+                              qx * Jl[1] - qy * Jl[0], Jl[0], Jl[1], Jl[2]};
+          const float wgt = huber_w(res, delta);
+          int k = 0;
+#pragma unroll
+          for (int a = 0; a < 6; ++a) {
+            const float wa = wgt * J[a];
+#pragma unroll
+            for (int b = a; b < 6; ++b) acc[k++] += wa * J[b];
+            acc[21 + a] += wa * res;
+          }
+          acc[27] += 0.5f * huber_rho_f(res, delta);
+        }
+        reduce_normal<28>(acc, red, s_out);
+      };
+      if (w == 0 && lane < 12) {
+        if (lane < 9) sR[lane] = (float)s_R[lane];
+        else sT[lane - 9] = (float)s_t[lane - 9];
+      }
+      __syncthreads();
+      pass();
+      if (threadIdx.x == 0) {
+        lm_load<6>(lm6, s_out, sc6);
+        lm6.radius = 1e4;
+        lm6.factor = 2.0;
+        lm6.done = lm_gsmall<6>(lm6) ? 1 : 0;
+      }
+      __syncthreads();
+      for (int itn = 0; itn < kp.lm_iters; ++itn) {
+        if (threadIdx.x == 0) {
+          int r = 0;
+          if (!lm6.done) {
+            const double ta[3] = {s_t[0] + s_anchor[0], s_t[1] + s_anchor[1], s_t[2] + s_anchor[2]};
+            r = lm_propose<6>(lm6, sqrt(1.0 + ta[0] * ta[0] + ta[1] * ta[1] + ta[2] * ta[2]));
+          }
+          if (r == 1) {
+            double dR[9];
+            so3_exp(mk3(2.0 * lm6.d[0], 2.0 * lm6.d[1], 2.0 * lm6.d[2]), dR);
+            matmul3(dR, s_R, c_R);
+            for (int k = 0; k < 3; ++k) c_t[k] = s_t[k] + lm6.d[3 + k];
+            for (int k = 0; k < 9; ++k) sR[k] = (float)c_R[k];
+            for (int k = 0; k < 3; ++k) sT[k] = (float)c_t[k];
+          }
+          s_flag = r;
+        }
+        __syncthreads();
+        const int r = s_flag;
+        if (r == 1) {
+          pass();
+          if (threadIdx.x == 0 && lm_decide<6>(lm6, s_out, sc6)) {
+            for (int k = 0; k < 9; ++k) s_R[k] = c_R[k];
+            for (int k = 0; k < 3; ++k) s_t[k] = c_t[k];
+          }
+        }
+        __syncthreads();
+        if (r == 0) break;
+      }
+      if (threadIdx.x == 0) {
+        d.cnt->success = 1;
+        Pose T;
+        for (int k = 0; k < 9; ++k) T.R[k] = s_R[k];
+        T.t = mk3(s_t[0] + s_anchor[0], s_t[1] + s_anchor[1], s_t[2] + s_anchor[2]);
+        pose_store(d.pose_io + 7, T);
+        pose_store(d.pose_io + 14, T);
+      }
+      return;
+    }
+    // ---------------------------------------------------------- joint
     for (int itn = 0; itn < kp.gn_iters; ++itn) {
       // float copies of the pose, one lane per entry
       if (w == 0 && lane < 12) {
@@ -529,62 +710,149 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
     __syncthreads();
     const int lo = step == 0 ? 0 : nc * kp.F;
     const int hi = step == 0 ? nc * kp.F : nitems;
-    for (int itn = 0; itn < kp.gn_iters && s_ok; ++itn) {
-      if (threadIdx.x == 0) {
+    if (kLM) {
+      // ------------------------------------- subset, trust-region LM
+      const double sc3[3] = {1.0, 1.0, 1.0};
+      auto set_point = [&](const double* xv) {  // thread 0: the pass's matrices at xv
         double Rm[9], Rj[9], Jr[9];
-        aa_mats(s_x + 3, Rm, Rj, Jr);
+        aa_mats(xv + 3, Rm, Rj, Jr);
         for (int k = 0; k < 9; ++k) {
           sR[k] = (float)Rm[k];
           sRj[k] = (float)Rj[k];
           sJr[k] = (float)Jr[k];
         }
-        for (int k = 0; k < 3; ++k) sT[k] = (float)(s_x[k] - s_anchor[k]);
-      }
-      __syncthreads();
-      float acc[9];
+        for (int k = 0; k < 3; ++k) sT[k] = (float)(xv[k] - s_anchor[k]);
+      };
+      auto pass = [&]() {  // cost, H, g of the free entries at (sR, sRj, sJr, sT)
+        float acc[10];
 #pragma unroll
-      for (int j = 0; j < 9; ++j) acc[j] = 0.f;
-      // residuals i == threadIdx.x (mod kGN): the entries this thread built
-      for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
-        if (i < lo || i >= hi) continue;
-        const float* e = d.res_tab + (size_t)kResStride * i;
-        if (e[0] == 0.f) continue;
-        const float px = e[1], py = e[2], pz = e[3];
-        const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
-        const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
-        const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
-        float Jl[3];
-        const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
-        // d lp / d r_k = -Rj (p x Jr[:,k])
-        float Jfull[6] = {Jl[0], Jl[1], Jl[2], 0.f, 0.f, 0.f};
+        for (int j = 0; j < 10; ++j) acc[j] = 0.f;
+        for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
+          if (i < lo || i >= hi) continue;
+          const float* e = d.res_tab + (size_t)kResStride * i;
+          if (e[0] == 0.f) continue;
+          const float px = e[1], py = e[2], pz = e[3];
+          const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
+          const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
+          const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
+          float Jl[3];
+          const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
+          float Jfull[6] = {Jl[0], Jl[1], Jl[2], 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const float vx = sJr[k], vy = sJr[3 + k], vz = sJr[6 + k];
-          const float cx = py * vz - pz * vy, cy = pz * vx - px * vz, cz = px * vy - py * vx;
-          const float mx = -(sRj[0] * cx + sRj[1] * cy + sRj[2] * cz);
-          const float my = -(sRj[3] * cx + sRj[4] * cy + sRj[5] * cz);
-          const float mz = -(sRj[6] * cx + sRj[7] * cy + sRj[8] * cz);
-          Jfull[3 + k] = Jl[0] * mx + Jl[1] * my + Jl[2] * mz;
+          for (int k = 0; k < 3; ++k) {
+            const float vx = sJr[k], vy = sJr[3 + k], vz = sJr[6 + k];
+            const float cx = py * vz - pz * vy, cy = pz * vx - px * vz, cz = px * vy - py * vx;
+            const float mx = -(sRj[0] * cx + sRj[1] * cy + sRj[2] * cz);
+            const float my = -(sRj[3] * cx + sRj[4] * cy + sRj[5] * cz);
+            const float mz = -(sRj[6] * cx + sRj[7] * cy + sRj[8] * cz);
+            Jfull[3 + k] = Jl[0] * mx + Jl[1] * my + Jl[2] * mz;
+          }
+          const float J[3] = {Jfull[f0], Jfull[f1], Jfull[f2]};
+          const float wgt = huber_w(res, delta);
+          acc[0] += wgt * J[0] * J[0]; acc[1] += wgt * J[0] * J[1]; acc[2] += wgt * J[0] * J[2];
+          acc[3] += wgt * J[1] * J[1]; acc[4] += wgt * J[1] * J[2]; acc[5] += wgt * J[2] * J[2];
+          acc[6] += wgt * J[0] * res; acc[7] += wgt * J[1] * res; acc[8] += wgt * J[2] * res;
+          acc[9] += 0.5f * huber_rho_f(res, delta);
         }
-        const float J[3] = {Jfull[f0], Jfull[f1], Jfull[f2]};
-        const float wgt = huber_w(res, delta);
-        acc[0] += wgt * J[0] * J[0]; acc[1] += wgt * J[0] * J[1]; acc[2] += wgt * J[0] * J[2];
-        acc[3] += wgt * J[1] * J[1]; acc[4] += wgt * J[1] * J[2]; acc[5] += wgt * J[2] * J[2];
-        acc[6] += wgt * J[0] * res; acc[7] += wgt * J[1] * res; acc[8] += wgt * J[2] * res;
-      }
-      reduce_normal<9>(acc, red, s_out);
-      if (threadIdx.x == 0) {
-        const double Hm[9] = {s_out[0], s_out[1], s_out[2], s_out[1], s_out[3],
-                              s_out[4], s_out[2], s_out[4], s_out[5]};
-        const double g[3] = {-s_out[6], -s_out[7], -s_out[8]};
-        double x[3];
-        if (chol_solve(3, Hm, g, x)) {
-          s_x[f0] += x[0]; s_x[f1] += x[1]; s_x[f2] += x[2];
-        } else {
-          s_ok = 0;
-        }
-      }
+        reduce_normal<10>(acc, red, s_out);
+      };
+      if (threadIdx.x == 0 && s_ok) set_point(s_x);
       __syncthreads();
+      if (s_ok) {
+        pass();
+        if (threadIdx.x == 0) {
+          lm_load<3>(lm3, s_out, sc3);
+          lm3.radius = 1e4;
+          lm3.factor = 2.0;
+          lm3.done = lm_gsmall<3>(lm3) ? 1 : 0;
+        }
+        __syncthreads();
+        for (int itn = 0; itn < kp.lm_iters; ++itn) {
+          if (threadIdx.x == 0) {
+            int r = 0;
+            if (!lm3.done) {
+              double xn = 0.0;
+              for (int k = 0; k < 6; ++k) xn += s_x[k] * s_x[k];
+              r = lm_propose<3>(lm3, sqrt(xn));
+            }
+            if (r == 1) {
+              for (int k = 0; k < 6; ++k) c_x[k] = s_x[k];
+              c_x[f0] += lm3.d[0];
+              c_x[f1] += lm3.d[1];
+              c_x[f2] += lm3.d[2];
+              set_point(c_x);
+            }
+            s_flag = r;
+          }
+          __syncthreads();
+          const int r = s_flag;
+          if (r == 1) {
+            pass();
+            if (threadIdx.x == 0 && lm_decide<3>(lm3, s_out, sc3))
+              for (int k = 0; k < 6; ++k) s_x[k] = c_x[k];
+          }
+          __syncthreads();
+          if (r == 0) break;
+        }
+      }
+    } else {
+      for (int itn = 0; itn < kp.gn_iters && s_ok; ++itn) {
+        if (threadIdx.x == 0) {
+          double Rm[9], Rj[9], Jr[9];
+          aa_mats(s_x + 3, Rm, Rj, Jr);
+          for (int k = 0; k < 9; ++k) {
+            sR[k] = (float)Rm[k];
+            sRj[k] = (float)Rj[k];
+            sJr[k] = (float)Jr[k];
+          }
+          for (int k = 0; k < 3; ++k) sT[k] = (float)(s_x[k] - s_anchor[k]);
+        }
+        __syncthreads();
+        float acc[9];
+  #pragma unroll
+        for (int j = 0; j < 9; ++j) acc[j] = 0.f;
+        // residuals i == threadIdx.x (mod kGN): the entries this thread built
+        for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
+          if (i < lo || i >= hi) continue;
+          const float* e = d.res_tab + (size_t)kResStride * i;
+          if (e[0] == 0.f) continue;
+          const float px = e[1], py = e[2], pz = e[3];
+          const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
+          const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
+          const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
+          float Jl[3];
+          const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
+          // d lp / d r_k = -Rj (p x Jr[:,k])
+          float Jfull[6] = {Jl[0], Jl[1], Jl[2], 0.f, 0.f, 0.f};
+  #pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float vx = sJr[k], vy = sJr[3 + k], vz = sJr[6 + k];
+            const float cx = py * vz - pz * vy, cy = pz * vx - px * vz, cz = px * vy - py * vx;
+            const float mx = -(sRj[0] * cx + sRj[1] * cy + sRj[2] * cz);
+            const float my = -(sRj[3] * cx + sRj[4] * cy + sRj[5] * cz);
+            const float mz = -(sRj[6] * cx + sRj[7] * cy + sRj[8] * cz);
+            Jfull[3 + k] = Jl[0] * mx + Jl[1] * my + Jl[2] * mz;
+          }
+          const float J[3] = {Jfull[f0], Jfull[f1], Jfull[f2]};
+          const float wgt = huber_w(res, delta);
+          acc[0] += wgt * J[0] * J[0]; acc[1] += wgt * J[0] * J[1]; acc[2] += wgt * J[0] * J[2];
+          acc[3] += wgt * J[1] * J[1]; acc[4] += wgt * J[1] * J[2]; acc[5] += wgt * J[2] * J[2];
+          acc[6] += wgt * J[0] * res; acc[7] += wgt * J[1] * res; acc[8] += wgt * J[2] * res;
+        }
+        reduce_normal<9>(acc, red, s_out);
+        if (threadIdx.x == 0) {
+          const double Hm[9] = {s_out[0], s_out[1], s_out[2], s_out[1], s_out[3],
+                                s_out[4], s_out[2], s_out[4], s_out[5]};
+          const double g[3] = {-s_out[6], -s_out[7], -s_out[8]};
+          double x[3];
+          if (chol_solve(3, Hm, g, x)) {
+            s_x[f0] += x[0]; s_x[f1] += x[1]; s_x[f2] += x[2];
+          } else {
+            s_ok = 0;
+          }
+        }
+        __syncthreads();
+      }
     }
     if (step == 0) {
       if (s_ok) { out_tree[0] = s_x[0]; out_tree[1] = s_x[1]; out_tree[2] = s_x[5]; }
@@ -678,7 +946,10 @@ int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update, cu
   }
   k_map_prep<<<16, 256, 0, st>>>(d);
   k_assoc<<<96, kAssocThreads, 0, st>>>(d, kp);
-  k_gn<<<1, kGN, 0, st>>>(d, kp);
+  if (kp.pose_lm)
+    k_gn<true><<<1, kGN, 0, st>>>(d, kp);
+  else
+    k_gn<false><<<1, kGN, 0, st>>>(d, kp);
   k_finalize<<<64, kAssocThreads, 0, st>>>(d, kp, 0, update ? 1 : 0);
   return 4;
 }
