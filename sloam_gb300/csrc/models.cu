@@ -356,28 +356,61 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
         __syncthreads();
         const unsigned long long pre = sel_prefix;
         const unsigned long long hmask = shift == 56 ? 0ull : (~0ull << (shift + 8));
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-          const unsigned long long v = src[i];
-          if ((v & hmask) == pre) atomicAdd(hist + ((v >> shift) & 255u), 1u);
+        // the keys of a bin share their high bytes (nearby z), so the
+        // histogram increments are combined per warp and digit
+        for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+          const int i = i0 + threadIdx.x;
+          int dg = -1;
+          if (i < n) {
+            const unsigned long long v = src[i];
+            if ((v & hmask) == pre) dg = (int)((v >> shift) & 255u);
+          }
+          const unsigned peers = __match_any_sync(0xffffffffu, dg);
+          if (dg >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+            atomicAdd(hist + dg, (unsigned)__popc(peers));
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-          int rem = sel_k, dg = 0;
-          for (; dg < 256; ++dg) {
-            if (rem <= (int)hist[dg]) break;
-            rem -= hist[dg];
+        // the digit where the running count reaches sel_k: warp 0, 8 bins a
+        // lane, a scan of the lane sums, then the owning lane's 8 bins
+        if (threadIdx.x < 32) {
+          const int ln = threadIdx.x;
+          unsigned c[8], sum = 0;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            c[j] = hist[ln * 8 + j];
+            sum += c[j];
           }
-          sel_prefix = pre | ((unsigned long long)dg << shift);
-          sel_k = rem;
+          unsigned incl = sum;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (ln >= o) incl += y;
+          }
+          const int rem = sel_k;
+          if (rem > (int)(incl - sum) && rem <= (int)incl) {
+            int r = rem - (int)(incl - sum), dg = ln * 8;
+            for (int j = 0; j < 8; ++j, ++dg) {
+              if (r <= (int)c[j]) break;
+              r -= (int)c[j];
+            }
+            sel_prefix = pre | ((unsigned long long)dg << shift);
+            sel_k = r;
+          }
         }
         __syncthreads();
       }
       const unsigned long long T = sel_prefix;  // k-th smallest (keys unique)
       if (threadIdx.x == 0) s_cnt = 0;
       __syncthreads();
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const unsigned long long v = src[i];
-        if (v <= T) keys[atomicAdd(&s_cnt, 1)] = v;
+      // the k keys <= T, one counter update per warp (sorted below)
+      for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool take = i < n && src[i] <= T;
+        const unsigned b = __ballot_sync(0xffffffffu, take);
+        int base = 0;
+        if ((threadIdx.x & 31) == 0 && b) base = atomicAdd(&s_cnt, __popc(b));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (take) keys[base + __popc(b & ((1u << (threadIdx.x & 31)) - 1u))] = src[i];
       }
       __syncthreads();
       int n2 = 1;
