@@ -103,7 +103,7 @@ __device__ __forceinline__ int warp_bin_add(int* hist, int bin, int lane) {
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(256) k_gbin(Dev d, KParams kp) {
+__global__ void __launch_bounds__(256, 8) k_gbin(Dev d, KParams kp) {
   __shared__ int hist[kMaxBins];
   const GroundView ground = ground_view(d.in);
   const int n = d.cnt->n_ground;
@@ -317,7 +317,7 @@ __device__ void fit_plane_block(At at, int n, float* cen, double* red, PlaneD& o
 }
 
 // One block per bin: retained points, plane model, gates, features.
-__global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
+__global__ void __launch_bounds__(kPlaneThreads, 3) k_plane(Dev d, KParams kp) {
   __shared__ unsigned long long keys[kBinCap];
   __shared__ unsigned int hist[256];
   __shared__ double red[6 * 32];
@@ -374,14 +374,9 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
         // lane, a scan of the lane sums, then the owning lane's 8 bins
         if (threadIdx.x < 32) {
           const int ln = threadIdx.x;
-          unsigned c[8], sum = 0;
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            c[j] = hist[ln * 8 + j];
-            sum += c[j];
-          }
+          unsigned sum = 0;
+          for (int j = 0; j < 8; ++j) sum += hist[ln * 8 + j];
           unsigned incl = sum;
-#pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
             if (ln >= o) incl += y;
@@ -390,8 +385,9 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane(Dev d, KParams kp) {
           if (rem > (int)(incl - sum) && rem <= (int)incl) {
             int r = rem - (int)(incl - sum), dg = ln * 8;
             for (int j = 0; j < 8; ++j, ++dg) {
-              if (r <= (int)c[j]) break;
-              r -= (int)c[j];
+              const int cj = (int)hist[dg];
+              if (r <= cj) break;
+              r -= cj;
             }
             sel_prefix = pre | ((unsigned long long)dg << shift);
             sel_k = r;
