@@ -1100,7 +1100,7 @@ __device__ __forceinline__ void ls_frame(double* st, float* sf) {
   sf[12] = (float)st[6];
 }
 constexpr int kLsThreads = 256;
-__global__ void __launch_bounds__(kLsThreads) k_cyl_ls(Dev d, KParams kp, int pass) {
+__global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int pass) {
   __shared__ int s_in[kLsThreads / 32];
   __shared__ float red[20][kLsThreads / 32];
   __shared__ double st[14];  // c(3), dir(3), r, ok, b1(3), b2(3)
