@@ -73,3 +73,34 @@ def test_mapped_sequence_matches_host_map_manager():
     assert list(hits) == host_mm.hits
     assert dm.size()[2] == 0
     dm.close()
+
+
+def test_mapped_keyframe_refuses_an_empty_submap():
+    """A later keyframe whose submap is empty returns SLOAM_ERR_EMPTY_MAP
+    (the reference's early return, sloamNode.cpp:199-203) and leaves the
+    device map as it was."""
+    import ctypes as C
+    from sloam_gb300 import capi as A, synth
+    from sloam_gb300.lib import Context, DeviceMapManager
+    cfg = synth.C2
+    forest, kfs = synth.scene(cfg, seed=0, n_kf=2)
+    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1)
+    ctx = Context(P)
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    kf0 = kfs[0]
+    r = A.RunBuffers(P)
+    ctx.check(ctx.L.sloam_keyframe(ctx.h, A.ptr(kf0.xyzi, C.c_float), len(kf0.xyzi),
+                                   A.ptr(kf0.labels, C.c_uint8), None,
+                                   C.byref(A.SE3.from_qt(*kf0.pose_gt_qt())), mapc,
+                                   len(forest.radius), C.byref(r.s)))
+    dm = DeviceMapManager(capacity=1024, k=100, recent=200)
+    kf = kfs[1]
+    r = A.RunBuffers(P)
+    st = ctx.L.sloam_keyframe_mapped(ctx.h, dm.h, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                     A.ptr(kf.labels, C.c_uint8), None,
+                                     C.byref(A.SE3.from_qt(*kf.pose_est_qt())), C.byref(r.s))
+    assert st == A.SLOAM_ERR_EMPTY_MAP
+    assert r.s.success == 0
+    assert dm.size() == (0, 0, 0)
+    dm.close()
+    ctx.close()
