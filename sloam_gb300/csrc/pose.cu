@@ -380,6 +380,69 @@ __device__ __forceinline__ void reduce_normal(const float* acc, float (*red)[kGN
   __syncthreads();
 }
 
+// Cholesky solve of the 6x6 normal equations H x = -g by one warp (all 32
+// lanes call it): lanes 0..20 hold the lower triangle of H row by row (lane
+// i(i+1)/2 + j holds H_ij, j <= i), lanes 21..26 the right-hand side.
+// Column k: the pivot's reciprocal square root (every lane computes it:
+// an FP64 warp instruction costs the pipe the same for one lane or 32),
+// L_ik scaled on their lanes, y_k = b_k / L_kk, then the trailing entries and
+// right-hand sides updated together, one fma per lane.  Back substitution
+// one unknown at a time.  The same eliminations as chol_solve in the same
+// order (the back substitution sums in the opposite order).  `H` is the
+// upper triangle row by row (H_ab, a <= b), as the block reduction leaves
+// it.  Returns false (on every lane) when a pivot is not positive or x is
+// not finite; lane 21 + i writes x[i].
+__device__ bool warp_chol_solve6(const double* H, const double* g, double* x) {
+  const int lane = threadIdx.x & 31;
+  int ri = -1, rj = -1;  // this lane's matrix entry (ri, rj), or rhs row ri (rj = -1)
+  double v = 0.0;
+  if (lane < 21) {
+    int i = 0;
+    while ((i + 1) * (i + 2) / 2 <= lane) ++i;
+    ri = i;
+    rj = lane - i * (i + 1) / 2;
+    const int a = rj, b = ri;  // upper index of (a, b), a <= b
+    v = H[a * 6 - a * (a - 1) / 2 + (b - a)];
+  } else if (lane < 27) {
+    ri = lane - 21;
+    v = -g[ri];
+  }
+  double inv[6];
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double piv = __shfl_sync(0xffffffffu, v, k * (k + 1) / 2 + k);
+    ok = ok && piv > 0.0;
+    inv[k] = rsqrt(piv);
+    if (ri == k && rj == k) v = piv * inv[k];          // L_kk
+    else if (rj == k && ri > k) v *= inv[k];           // L_ik
+    else if (rj < 0 && ri == k) v *= inv[k];           // y_k
+    // trailing update: matrix (i, j), k < j <= i: -= L_ik L_jk;
+    // rhs i > k: -= L_ik y_k
+    int s1 = 0, s2 = 0;
+    const bool upd = (rj > k) || (rj < 0 && ri > k);
+    if (upd) {
+      s1 = ri * (ri + 1) / 2 + k;
+      s2 = rj >= 0 ? rj * (rj + 1) / 2 + k : 21 + k;
+    }
+    const double a1 = __shfl_sync(0xffffffffu, v, s1);
+    const double a2 = __shfl_sync(0xffffffffu, v, s2);
+    if (upd) v = fma(-a1, a2, v);
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    if (rj < 0 && ri == i) v *= inv[i];                // x_i
+    const double xi = __shfl_sync(0xffffffffu, v, 21 + i);
+    const int src = (rj < 0 && ri >= 0 && ri < i) ? i * (i + 1) / 2 + ri : 0;
+    const double lij = __shfl_sync(0xffffffffu, v, src);
+    if (rj < 0 && ri >= 0 && ri < i) v = fma(-lij, xi, v);
+  }
+  const bool fin = rj >= 0 || ri < 0 || isfinite(v);
+  ok = ok && __all_sync(0xffffffffu, fin);
+  if (rj < 0 && ri >= 0) x[ri] = v;
+  return ok;
+}
+
 // ---- pose_solver 1: trust-region Levenberg-Marquardt (the rules of the
 // oracle's lm_minimize: the solver settings the reference gives Ceres,
 // sloam.cpp:91-97, 149-155).  The bookkeeping runs on one thread in FP64;
@@ -526,7 +589,7 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
   if (!kp.two_step) {
     if (!(tchk && gchk)) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (kLM) {
+    if constexpr (kLM) {
       // ------------------------------------------ joint, trust-region LM
       const double sc6[6] = {2.0, 2.0, 2.0, 1.0, 1.0, 1.0};  // d = omega / 2
       auto pass = [&]() {  // cost, H, g at (sR, sT)
@@ -608,88 +671,77 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
         pose_store(d.pose_io + 14, T);
       }
       return;
-    }
-    // ---------------------------------------------------------- joint
-    for (int itn = 0; itn < kp.gn_iters; ++itn) {
-      // float copies of the pose, one lane per entry
-      if (w == 0 && lane < 12) {
-        if (lane < 9) sR[lane] = (float)s_R[lane];
-        else sT[lane - 9] = (float)s_t[lane - 9];
-      }
-      __syncthreads();
-      float acc[27];
-#pragma unroll
-      for (int j = 0; j < 27; ++j) acc[j] = 0.f;
-      for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
-        const float* e = d.res_tab + (size_t)kResStride * i;
-        if (e[0] == 0.f) continue;
-        const float px = e[1], py = e[2], pz = e[3];
-        const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
-        const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
-        const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
-        float Jl[3];
-        const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
-        const float J[6] = {qy * Jl[2] - qz * Jl[1], qz * Jl[0] - qx * Jl[2],
-                            qx * Jl[1] - qy * Jl[0], Jl[0], Jl[1], Jl[2]};
-        const float wgt = huber_w(res, delta);
-        int k = 0;
-#pragma unroll
-        for (int a = 0; a < 6; ++a) {
-          const float wa = wgt * J[a];
-#pragma unroll
-          for (int b = a; b < 6; ++b) acc[k++] += wa * J[b];
-          acc[21 + a] += wa * res;
+    } else {
+      // ---------------------------------------------------------- joint
+      for (int itn = 0; itn < kp.gn_iters; ++itn) {
+        // float copies of the pose, one lane per entry
+        if (w == 0 && lane < 12) {
+          if (lane < 9) sR[lane] = (float)s_R[lane];
+          else sT[lane - 9] = (float)s_t[lane - 9];
         }
-      }
-      reduce_normal<27>(acc, red, s_out);
-      // FP64 6x6 solve on one lane; the SE(3) update R <- exp([x0..2]) R,
-      // t <- t + x3..5 on nine lanes of the same warp (each FP64 warp
-      // instruction costs the pipe the same for one lane or nine)
-      if (w == 0) {
-        if (lane == 0) {
-          double Hm[36], g[6], x[6];
+        __syncthreads();
+        float acc[27];
+  #pragma unroll
+        for (int j = 0; j < 27; ++j) acc[j] = 0.f;
+        for (int i = threadIdx.x; i < nitems; i += blockDim.x) {
+          const float* e = d.res_tab + (size_t)kResStride * i;
+          if (e[0] == 0.f) continue;
+          const float px = e[1], py = e[2], pz = e[3];
+          const float qx = sR[0] * px + sR[1] * py + sR[2] * pz;
+          const float qy = sR[3] * px + sR[4] * py + sR[5] * pz;
+          const float qz = sR[6] * px + sR[7] * py + sR[8] * pz;
+          float Jl[3];
+          const float res = residual_eval(e, qx + sT[0], qy + sT[1], qz + sT[2], Jl);
+          const float J[6] = {qy * Jl[2] - qz * Jl[1], qz * Jl[0] - qx * Jl[2],
+                              qx * Jl[1] - qy * Jl[0], Jl[0], Jl[1], Jl[2]};
+          const float wgt = huber_w(res, delta);
           int k = 0;
-          for (int a = 0; a < 6; ++a)
-            for (int b = a; b < 6; ++b) {
-              Hm[6 * a + b] = s_out[k];
-              Hm[6 * b + a] = s_out[k];
-              ++k;
-            }
-          for (int a = 0; a < 6; ++a) g[a] = -s_out[21 + a];
-          if (s_ok && chol_solve(6, Hm, g, x)) {
-            for (int a = 0; a < 6; ++a) s_x[a] = x[a];
-          } else {
-            s_ok = 0;
+  #pragma unroll
+          for (int a = 0; a < 6; ++a) {
+            const float wa = wgt * J[a];
+  #pragma unroll
+            for (int b = a; b < 6; ++b) acc[k++] += wa * J[b];
+            acc[21 + a] += wa * res;
           }
         }
-        __syncwarp();
-        if (s_ok && lane < 9) {
-          const int r = lane / 3, c = lane - 3 * r;
-          double dRr[3];
-          so3_exp_row(mk3(s_x[0], s_x[1], s_x[2]), r, dRr);
-          const double v = dRr[0] * s_R[c] + dRr[1] * s_R[3 + c] + dRr[2] * s_R[6 + c];
-          const double tn = lane < 3 ? s_t[lane] + s_x[3 + lane] : 0.0;
-          __syncwarp(0x1ffu);
-          s_R[lane] = v;
-          if (lane < 3) s_t[lane] = tn;
+        reduce_normal<27>(acc, red, s_out);
+        // FP64 6x6 solve by warp 0; the SE(3) update R <- exp([x0..2]) R,
+        // t <- t + x3..5 on nine lanes of the same warp (each FP64 warp
+        // instruction costs the pipe the same for one lane or nine)
+        if (w == 0) {
+          // H x = -g (s_out: H's upper triangle, then g) on the whole warp
+          const bool solved = s_ok && warp_chol_solve6(s_out, s_out + 21, s_x);
+          __syncwarp();
+          if (lane == 0 && !solved) s_ok = 0;
+          __syncwarp();
+          if (s_ok && lane < 9) {
+            const int r = lane / 3, c = lane - 3 * r;
+            double dRr[3];
+            so3_exp_row(mk3(s_x[0], s_x[1], s_x[2]), r, dRr);
+            const double v = dRr[0] * s_R[c] + dRr[1] * s_R[3 + c] + dRr[2] * s_R[6 + c];
+            const double tn = lane < 3 ? s_t[lane] + s_x[3 + lane] : 0.0;
+            __syncwarp(0x1ffu);
+            s_R[lane] = v;
+            if (lane < 3) s_t[lane] = tn;
+          }
+        }
+        __syncthreads();
+        if (!s_ok) break;
+      }
+      if (threadIdx.x == 0) {
+        d.cnt->success = s_ok;
+        if (s_ok) {
+          Pose T;
+          for (int k = 0; k < 9; ++k) T.R[k] = s_R[k];
+          T.t = mk3(s_t[0] + s_anchor[0], s_t[1] + s_anchor[1], s_t[2] + s_anchor[2]);
+          pose_store(d.pose_io + 7, T);
+          pose_store(d.pose_io + 14, T);
+        } else {
+          d.cnt->status = SLOAM_ERR_NOT_CONVERGED;
         }
       }
-      __syncthreads();
-      if (!s_ok) break;
+      return;
     }
-    if (threadIdx.x == 0) {
-      d.cnt->success = s_ok;
-      if (s_ok) {
-        Pose T;
-        for (int k = 0; k < 9; ++k) T.R[k] = s_R[k];
-        T.t = mk3(s_t[0] + s_anchor[0], s_t[1] + s_anchor[1], s_t[2] + s_anchor[2]);
-        pose_store(d.pose_io + 7, T);
-        pose_store(d.pose_io + 14, T);
-      } else {
-        d.cnt->status = SLOAM_ERR_NOT_CONVERGED;
-      }
-    }
-    return;
   }
   // -------------------------------------------------------- two-step
   double rpy[3];
@@ -710,7 +762,7 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
     __syncthreads();
     const int lo = step == 0 ? 0 : nc * kp.F;
     const int hi = step == 0 ? nc * kp.F : nitems;
-    if (kLM) {
+    if constexpr (kLM) {
       // ------------------------------------- subset, trust-region LM
       const double sc3[3] = {1.0, 1.0, 1.0};
       auto set_point = [&](const double* xv) {  // thread 0: the pass's matrices at xv
