@@ -213,6 +213,72 @@ SLOAM_HD void so3_exp(d3 w, double* R) {
   for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0 ? 1.0 : 0.0) + A * K[i] + B * K2[i];
 }
 
+// Cholesky solve of N x N normal equations H x = -g (N <= 6) by one warp
+// (all 32 lanes call it): lanes 0..T-1 (T = N(N+1)/2) hold the lower
+// triangle of H row by row (lane i(i+1)/2 + j holds H_ij, j <= i), lanes
+// T..T+N-1 the right-hand side.  Column k: the pivot's reciprocal square
+// root (every lane computes it: an FP64 warp instruction costs the pipe the
+// same for one lane or 32), L_ik scaled on their lanes, y_k = b_k / L_kk,
+// then the trailing entries and right-hand sides updated together, one fma
+// per lane.  Back substitution one unknown at a time.  The same eliminations
+// as chol_solve in the same order (the back substitution sums in the
+// opposite order).  `H` is the upper triangle row by row (H_ab, a <= b).
+// Returns false (on every lane) when a pivot is not positive or x is not
+// finite; lane T + i writes x[i].
+template <int N>
+__device__ bool warp_chol_solve(const double* H, const double* g, double* x) {
+  constexpr int T = N * (N + 1) / 2;
+  static_assert(T + N <= 32, "one warp");
+  const int lane = threadIdx.x & 31;
+  int ri = -1, rj = -1;  // this lane's matrix entry (ri, rj), or rhs row ri (rj = -1)
+  double v = 0.0;
+  if (lane < T) {
+    int i = 0;
+    while ((i + 1) * (i + 2) / 2 <= lane) ++i;
+    ri = i;
+    rj = lane - i * (i + 1) / 2;
+    const int a = rj, b = ri;  // upper index of (a, b), a <= b
+    v = H[a * N - a * (a - 1) / 2 + (b - a)];
+  } else if (lane < T + N) {
+    ri = lane - T;
+    v = -g[ri];
+  }
+  double inv[N];
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const double piv = __shfl_sync(0xffffffffu, v, k * (k + 1) / 2 + k);
+    ok = ok && piv > 0.0;
+    inv[k] = rsqrt(piv);
+    if (ri == k && rj == k) v = piv * inv[k];          // L_kk
+    else if (rj == k && ri > k) v *= inv[k];           // L_ik
+    else if (rj < 0 && ri == k) v *= inv[k];           // y_k
+    // trailing update: matrix (i, j), k < j <= i: -= L_ik L_jk;
+    // rhs i > k: -= L_ik y_k
+    int s1 = 0, s2 = 0;
+    const bool upd = (rj > k) || (rj < 0 && ri > k);
+    if (upd) {
+      s1 = ri * (ri + 1) / 2 + k;
+      s2 = rj >= 0 ? rj * (rj + 1) / 2 + k : T + k;
+    }
+    const double a1 = __shfl_sync(0xffffffffu, v, s1);
+    const double a2 = __shfl_sync(0xffffffffu, v, s2);
+    if (upd) v = fma(-a1, a2, v);
+  }
+#pragma unroll
+  for (int i = N - 1; i >= 0; --i) {
+    if (rj < 0 && ri == i) v *= inv[i];                // x_i
+    const double xi = __shfl_sync(0xffffffffu, v, T + i);
+    const int src = (rj < 0 && ri >= 0 && ri < i) ? i * (i + 1) / 2 + ri : 0;
+    const double lij = __shfl_sync(0xffffffffu, v, src);
+    if (rj < 0 && ri >= 0 && ri < i) v = fma(-lij, xi, v);
+  }
+  const bool fin = rj >= 0 || ri < 0 || isfinite(v);
+  ok = ok && __all_sync(0xffffffffu, fin);
+  if (rj < 0 && ri >= 0) x[ri] = v;
+  return ok;
+}
+
 // Cholesky solve of an n x n SPD system (n <= 6, row-major), FP64.  One
 // reciprocal square root per pivot; everything else multiplies (the FP64
 // divide and square root are long dependent sequences on this part).

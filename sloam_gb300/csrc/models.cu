@@ -1105,6 +1105,7 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
   __shared__ float red[20][kLsThreads / 32];
   __shared__ double st[14];  // c(3), dir(3), r, ok, b1(3), b2(3)
   __shared__ double ssum[20];
+  __shared__ double sxls[5];
   __shared__ float sf[13];   // c(3), dir(3), b1(3), b2(3), r as float
   const int nl = d.cnt->n_lm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1206,32 +1207,26 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
           ssum[lane] = t2;
         }
         __syncwarp();
-      }
-      if (threadIdx.x == 0) {
-        double s[20];
-        for (int j = 0; j < 20; ++j) s[j] = ssum[j];
-        const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
-        const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
-        const double r = st[6];
-        double Hm[25], g[5], x[5];
-        int k = 0;
-        for (int p = 0; p < 5; ++p)
-          for (int q2 = p; q2 < 5; ++q2) {
-            Hm[5 * p + q2] = s[k];
-            Hm[5 * q2 + p] = s[k];
-            ++k;
+        // the 5x5 normal equations (ssum: upper triangle, then J^T r) on
+        // the warp; the model update on lane 0
+        const bool solved = warp_chol_solve<5>(ssum, ssum + 15, sxls);
+        __syncwarp();
+        if (lane == 0) {
+          if (solved) {
+            const double* x = sxls;
+            const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
+            const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
+            const double r = st[6];
+            d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
+            d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
+            d2 = scl3(1.0 / norm3(d2), d2);
+            st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
+            st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
+            st[6] = r + x[4];
+            ls_frame(st, sf);
+          } else {
+            st[7] = 0.0;
           }
-        for (int p = 0; p < 5; ++p) g[p] = -s[15 + p];
-        if (chol_solve(5, Hm, g, x)) {
-          d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
-          d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
-          d2 = scl3(1.0 / norm3(d2), d2);
-          st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
-          st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
-          st[6] = r + x[4];
-          ls_frame(st, sf);
-        } else {
-          st[7] = 0.0;
         }
       }
       __syncthreads();

@@ -380,69 +380,6 @@ __device__ __forceinline__ void reduce_normal(const float* acc, float (*red)[kGN
   __syncthreads();
 }
 
-// Cholesky solve of the 6x6 normal equations H x = -g by one warp (all 32
-// lanes call it): lanes 0..20 hold the lower triangle of H row by row (lane
-// i(i+1)/2 + j holds H_ij, j <= i), lanes 21..26 the right-hand side.
-// Column k: the pivot's reciprocal square root (every lane computes it:
-// an FP64 warp instruction costs the pipe the same for one lane or 32),
-// L_ik scaled on their lanes, y_k = b_k / L_kk, then the trailing entries and
-// right-hand sides updated together, one fma per lane.  Back substitution
-// one unknown at a time.  The same eliminations as chol_solve in the same
-// order (the back substitution sums in the opposite order).  `H` is the
-// upper triangle row by row (H_ab, a <= b), as the block reduction leaves
-// it.  Returns false (on every lane) when a pivot is not positive or x is
-// not finite; lane 21 + i writes x[i].
-__device__ bool warp_chol_solve6(const double* H, const double* g, double* x) {
-  const int lane = threadIdx.x & 31;
-  int ri = -1, rj = -1;  // this lane's matrix entry (ri, rj), or rhs row ri (rj = -1)
-  double v = 0.0;
-  if (lane < 21) {
-    int i = 0;
-    while ((i + 1) * (i + 2) / 2 <= lane) ++i;
-    ri = i;
-    rj = lane - i * (i + 1) / 2;
-    const int a = rj, b = ri;  // upper index of (a, b), a <= b
-    v = H[a * 6 - a * (a - 1) / 2 + (b - a)];
-  } else if (lane < 27) {
-    ri = lane - 21;
-    v = -g[ri];
-  }
-  double inv[6];
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const double piv = __shfl_sync(0xffffffffu, v, k * (k + 1) / 2 + k);
-    ok = ok && piv > 0.0;
-    inv[k] = rsqrt(piv);
-    if (ri == k && rj == k) v = piv * inv[k];          // L_kk
-    else if (rj == k && ri > k) v *= inv[k];           // L_ik
-    else if (rj < 0 && ri == k) v *= inv[k];           // y_k
-    // trailing update: matrix (i, j), k < j <= i: -= L_ik L_jk;
-    // rhs i > k: -= L_ik y_k
-    int s1 = 0, s2 = 0;
-    const bool upd = (rj > k) || (rj < 0 && ri > k);
-    if (upd) {
-      s1 = ri * (ri + 1) / 2 + k;
-      s2 = rj >= 0 ? rj * (rj + 1) / 2 + k : 21 + k;
-    }
-    const double a1 = __shfl_sync(0xffffffffu, v, s1);
-    const double a2 = __shfl_sync(0xffffffffu, v, s2);
-    if (upd) v = fma(-a1, a2, v);
-  }
-#pragma unroll
-  for (int i = 5; i >= 0; --i) {
-    if (rj < 0 && ri == i) v *= inv[i];                // x_i
-    const double xi = __shfl_sync(0xffffffffu, v, 21 + i);
-    const int src = (rj < 0 && ri >= 0 && ri < i) ? i * (i + 1) / 2 + ri : 0;
-    const double lij = __shfl_sync(0xffffffffu, v, src);
-    if (rj < 0 && ri >= 0 && ri < i) v = fma(-lij, xi, v);
-  }
-  const bool fin = rj >= 0 || ri < 0 || isfinite(v);
-  ok = ok && __all_sync(0xffffffffu, fin);
-  if (rj < 0 && ri >= 0) x[ri] = v;
-  return ok;
-}
-
 // ---- pose_solver 1: trust-region Levenberg-Marquardt (the rules of the
 // oracle's lm_minimize: the solver settings the reference gives Ceres,
 // sloam.cpp:91-97, 149-155).  The bookkeeping runs on one thread in FP64;
@@ -710,7 +647,7 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
         // instruction costs the pipe the same for one lane or nine)
         if (w == 0) {
           // H x = -g (s_out: H's upper triangle, then g) on the whole warp
-          const bool solved = s_ok && warp_chol_solve6(s_out, s_out + 21, s_x);
+          const bool solved = s_ok && warp_chol_solve<6>(s_out, s_out + 21, s_x);
           __syncwarp();
           if (lane == 0 && !solved) s_ok = 0;
           __syncwarp();
