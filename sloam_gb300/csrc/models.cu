@@ -457,6 +457,46 @@ __global__ void __launch_bounds__(kPlaneThreads) k_plane_points(Dev d, KParams k
 // Gates of a fitted bin plane (sloam.cpp:394-408): the normal in the map
 // frame (R n) within 0.1 rad of +-z by its Euler angles, and the centroid
 // below the sensor.  FP64, one bin per thread.
+// euler_two_vectors((0, 0, 1), b) in FP32 with the same steps (CUDA's float
+// atan2, hypot, sin, cos): angles within about 1e-6 rad of the FP64 ones.
+// Returns false when the gate's decision could differ from the FP64 one: b
+// nearly opposite to z (the FP64 path takes its other formula), the first
+// angle within `eps` of 0 or of +-pi (its branch and wrap), or an angle
+// within `eps` of a gate threshold (0.1, pi - 0.1).
+__device__ bool euler_z_to_f(d3 b, float eps, float* ang) {
+  const float nb = sqrtf((float)b.x * (float)b.x + (float)b.y * (float)b.y +
+                         (float)b.z * (float)b.z);
+  const float vx = (float)b.x / nb, vy = (float)b.y / nb, vz = (float)b.z / nb;
+  const float c = vz;
+  if (!(c > -1.0f + 1e-5f)) return false;
+  const float s = sqrtf((1.0f + c) * 2.0f), invs = 1.0f / s;
+  const float qx = -vy * invs, qy = vx * invs, qz = 0.0f, qw = s * 0.5f;
+  const float tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
+  const float twx = tx * qw, twy = ty * qw, twz = tz * qw;
+  const float txx = tx * qx, txy = ty * qx, txz = tz * qx;
+  const float tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+  const float M00 = 1 - (tyy + tzz), M01 = txy - twz, M02 = txz + twy;
+  const float M10 = txy + twz, M11 = 1 - (txx + tzz);
+  const float M20 = txz - twy, M21 = tyz + twx, M22 = 1 - (txx + tyy), M12 = tyz - twx;
+  const float PIf = 3.14159265f;
+  float r0 = atan2f(M12, M22);
+  if (fabsf(r0) < eps || fabsf(PIf - fabsf(r0)) < eps) return false;
+  const float c2 = hypotf(M00, M01);
+  float r1;
+  if (r0 > 0) {
+    r0 -= PIf;
+    r1 = atan2f(-M02, -c2);
+  } else {
+    r1 = atan2f(-M02, c2);
+  }
+  const float s1 = sinf(r0), c1 = cosf(r0);
+  const float r2 = atan2f(s1 * M20 - c1 * M10, c1 * M11 - s1 * M21);
+  ang[0] = -r0; ang[1] = -r1; ang[2] = -r2;
+  for (int i = 0; i < 3; ++i)
+    if (fabsf(ang[i] - 0.1f) < eps || fabsf(PIf - fabsf(ang[i]) - 0.1f) < eps) return false;
+  return true;
+}
+
 __device__ bool plane_gates(const Dev& d, const PlaneD& pl) {
   const d3 nrm = mk3(pl.plane[0], pl.plane[1], pl.plane[2]);
   sloam_se3 pe;
@@ -464,12 +504,23 @@ __device__ bool plane_gates(const Dev& d, const PlaneD& pl) {
   for (int j = 0; j < 3; ++j) pe.t[j] = d.pose_io[4 + j];
   const Pose T = pose_from(pe);
   const d3 nw = rot3(T.R, nrm);
-  double ang[3];
-  euler_two_vectors(mk3(0, 0, 1), nw, ang);
   const double PI = 3.14159265358979323846;
-  const bool angle_ok = (ang[0] < 0.1 && ang[1] < 0.1 && ang[2] < 0.1) ||
-                        (PI - fabs(ang[0]) < 0.1 && PI - fabs(ang[1]) < 0.1 &&
-                         PI - fabs(ang[2]) < 0.1);
+  // the angle gate from FP32 angles where their decision is certain (a
+  // 1e-4 rad margin, about 100 times their error), else from FP64
+  bool angle_ok;
+  float af[3];
+  if (euler_z_to_f(nw, 1e-4f, af)) {
+    const float PIf = 3.14159265f;
+    angle_ok = (af[0] < 0.1f && af[1] < 0.1f && af[2] < 0.1f) ||
+               (PIf - fabsf(af[0]) < 0.1f && PIf - fabsf(af[1]) < 0.1f &&
+                PIf - fabsf(af[2]) < 0.1f);
+  } else {
+    double ang[3];
+    euler_two_vectors(mk3(0, 0, 1), nw, ang);
+    angle_ok = (ang[0] < 0.1 && ang[1] < 0.1 && ang[2] < 0.1) ||
+               (PI - fabs(ang[0]) < 0.1 && PI - fabs(ang[1]) < 0.1 &&
+                PI - fabs(ang[2]) < 0.1);
+  }
   const bool height_ok =
       xform(T, mk3(pl.centroid[0], pl.centroid[1], pl.centroid[2])).z < T.t.z;
   return angle_ok && height_ok;
