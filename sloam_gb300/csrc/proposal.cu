@@ -365,6 +365,41 @@ __global__ void k_prop_pack(const float* __restrict__ W, unsigned char* __restri
     b3[core_offset(c, k, kD2) / 2] = __float2bfloat16_rn(W[kW3 + i]);
   }
   if (i < kNumParams) f[i] = bfr(W[i]);
+  if (i < kD3 * kD4) {  // W4[c][j] -> bf16 at ((c / 8) * 128 + j) * 8 + c % 8
+    __nv_bfloat16* b4 = reinterpret_cast<__nv_bfloat16*>(tcw + kTcW4Off);
+    const int c = i / kD4, j = i % kD4;
+    b4[((c >> 3) * kD4 + j) * 8 + (c & 7)] = __float2bfloat16_rn(W[kW4 + i]);
+  }
+  if (i < kSmallFloats) {  // W1 / b1 as float4 rows, b2, b3, b4, b5, pad, W5
+    float v = 0.0f;
+    if (i < kSfB2) {
+      const int j = i >> 2, q = i & 3;
+      v = W[q < 3 ? kW1 + q * kD1 + j : kB1 + j];
+    } else if (i < kSfB3) {
+      v = W[kB2 + i - kSfB2];
+    } else if (i < kSfB4) {
+      v = W[kB3 + i - kSfB3];
+    } else if (i < kSfB5) {
+      v = W[kB4 + i - kSfB4];
+    } else if (i < kSfB5 + kD5) {
+      v = W[kB5 + i - kSfB5];
+    } else if (i >= kSfW5) {
+      v = W[kW5 + i - kSfW5];
+    }
+    reinterpret_cast<float*>(tcw + kTcSmallOff)[i] = bfr(v);
+  }
+  if (i < kD2 * kK2x) {  // W2^T | b2 (128 x 80), K-major core matrices
+    const int j = i / kK2x, k = i % kK2x;
+    const float v = k < kD1 ? W[kW2 + k * kD2 + j] : (k == kD1 ? W[kB2 + j] : 0.0f);
+    reinterpret_cast<__nv_bfloat16*>(tcw + kTcB2xOff)[core_offset(j, k, kK2x) / 2] =
+        __float2bfloat16_rn(v);
+  }
+  if (i < kD1 * kK1) {  // B1 (64 x 16): W1 rows for the hi, mid, lo terms, b1
+    const int j = i / kK1, k = i % kK1;
+    const float v = k < 9 ? W[kW1 + (k % 3) * kD1 + j] : (k == 9 ? W[kB1 + j] : 0.0f);
+    reinterpret_cast<__nv_bfloat16*>(tcw + kTcB1Off)[core_offset(j, k, kK1) / 2] =
+        __float2bfloat16_rn(v);
+  }
 }
 
 // SIMT reference of the tensor-core kernel: the same bf16 operands and
@@ -480,25 +515,36 @@ SLOAM_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: 
 constexpr int kTcWg = 4;                // warpgroups, one sample each at a time
 constexpr int kTcThreads = 128 * kTcWg;
 constexpr int kMaxGroup = 8;     // samples per group (one tree's proposals)
-// Per warpgroup one 32 KB operand buffer: A1 [128 x 64] at its start while
-// layer 2 runs, then A2 [128 x 128] (written once the layer-2 MMAs, which
-// read A1, have completed).
-constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcW2Bytes,
-                   kSmA2 = kSmB3 + kTcW3Bytes,                    // [wg][128 x 128] bf16
-                   kSmW1 = kSmA2 + kTcWg * kPts * kD2 * 2,
-                   kSmH = kSmW1 + 4 * (3 * kD1 + kD1),            // [group][256]
-                   kSmY1 = kSmH + 4 * kMaxGroup * kD3,            // [group][128]
-                   kSmBias = kSmY1 + 4 * kMaxGroup * kD4,         // b2, b3, b4, W5, b5
-                   kSmMisc = kSmBias + 4 * (kD2 + kD3 + kD4 + kD4 * kD5 + 8),
+// Per warpgroup one 32 KB operand buffer: A1 [128 x 80] (the ones column
+// at 64 carries b2) at its start and A0 [128 x 16] (layer-1 input) after
+// it while layers 1 and 2 run, then A2 [128 x 128] (written once the
+// layer-2 MMAs, which read A1, have completed).  The operand buffers hold
+// the head's partial sums and outputs between groups.  W2^T | b2, W3^T, B1
+// and the biases arrive by bulk copy from the packed device layout.
+constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcB2xBytes,
+                   kSmA2 = kSmB3 + kTcW3Bytes,                    // [wg][32 KB]
+                   kSmB1 = kSmA2 + kTcWg * kPts * kD2 * 2,        // [64 x 16] bf16
+                   kSmSmall = kSmB1 + kTcB1Bytes,                 // b3, b4, b5
+                   kSmallCopy = 4 * (kSfW5 - kSfB3),
+                   kSmH = kSmSmall + kSmallCopy,                  // [group][256]
+                   kSmMisc = kSmH + 4 * kMaxGroup * kD3,
                    kTcSmem = kSmMisc + 64;
-static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0, "operand alignment");
-static_assert(kSmMisc % 16 == 0 && kTcSmem <= 227 * 1024, "shared memory");
-static_assert(kPts * kD1 * 2 <= kPts * kD2 * 2, "A1 inside the A2 buffer");
-static_assert(kD3 * kD4 * 2 <= kTcWg * kPts * kD2 * 2, "bf16 W4 inside the operand buffers");
-static_assert((kTcF32Off + 4 * kW4) % 8 == 0, "W4 float2 alignment");
-// the descriptors address at most: A1 [128 x 64], A2 [128 x 128], W2^T
-// [128 x 64], W3^T [256 x 128]; every core matrix lies inside its buffer
-static_assert(core_offset(kPts - 1, kD1 - 1, kD1) + 2 <= kPts * kD1 * 2, "A1 extent");
+constexpr uint32_t kOpA0 = kPts * kK2x * 2;                       // A0 inside the buffer
+static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0 && kSmB1 % 128 == 0, "operand alignment");
+static_assert(kSmSmall % 16 == 0 && kSmH % 16 == 0 && kSmMisc % 16 == 0 && kOpA0 % 128 == 0,
+              "16-byte alignment");
+static_assert(kTcSmem <= 227 * 1024, "shared memory");
+static_assert(kOpA0 + kPts * kK1 * 2 <= kPts * kD2 * 2, "A1 and A0 inside the A2 buffer");
+static_assert(2 * kTcWg * kMaxGroup * kD4 * 4 <= kTcWg * kPts * kD2 * 2,
+              "head partial sums and outputs inside the operand buffers");
+static_assert(kD3 == kTcWg * 64, "head: one quarter of the inputs per warpgroup");
+// the descriptors address at most: A0 [128 x 16], A1 [128 x 80], A2
+// [128 x 128], B1 [64 x 16], W2^T | b2 [128 x 80], W3^T [256 x 128]; every
+// core matrix lies inside its buffer
+static_assert(core_offset(kPts - 1, kK1 - 1, kK1) + 2 <= kPts * kK1 * 2, "A0 extent");
+static_assert(core_offset(kPts - 1, kK2x - 1, kK2x) + 2 <= kOpA0, "A1 extent");
+static_assert(core_offset(kD1 - 1, kK1 - 1, kK1) + 2 <= kTcB1Bytes, "B1 extent");
+static_assert(core_offset(kD2 - 1, kK2x - 1, kK2x) + 2 <= kTcB2xBytes, "W2 extent");
 static_assert(core_offset(kD3 - 1, kD2 - 1, kD2) + 2 <= kTcW3Bytes, "W3 extent");
 
 SLOAM_D bool mbar_wait_bounded(uint64_t* m, uint32_t phase, int* err, int* abort_flag) {
@@ -511,6 +557,31 @@ SLOAM_D bool mbar_wait_bounded(uint64_t* m, uint32_t phase, int* err, int* abort
     return false;
   }
   return true;
+}
+SLOAM_D void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(m)),
+               "r"(bytes)
+               : "memory");
+}
+// bulk copy global -> shared (16-byte aligned, size a multiple of 16),
+// completing on the mbarrier's transaction count
+SLOAM_D void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(dst),
+      "l"((uint64_t)__cvta_generic_to_global(src)), "r"(bytes), "r"(saddr(bar))
+      : "memory");
+}
+// ReLU, round to bf16 and pack: lo in the low half, hi in the high half
+SLOAM_D uint32_t relu_bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+SLOAM_D float max3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
 }
 // barrier of one warpgroup (128 threads); ids 1..kTcWg (0 is __syncthreads)
 SLOAM_D void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
@@ -533,53 +604,55 @@ SLOAM_D bool wg_any(int wg, bool p) {
 // fitted) are skipped.  512 threads: warpgroup g (0..3) takes samples
 // g, g + 4 of the group with its own operand buffer, TMEM columns
 // [128 g, 128 g + 128), mbarrier and barrier, so that one warpgroup's MMAs
-// overlap the others' CUDA-core work.  Per sample, layer 1 on CUDA cores
-// (FP32, thread r = point r) into bf16 A1; layer 2 as tcgen05.mma M=128
-// points, N=128, K=64 (TMEM lane r = point r) into bf16 A2; layer 3
-// transposed, M=128 features (two halves of W3^T), N=128 points, K=128, so
-// that TMEM lane r holds feature r of a half and the max over the points is
-// a register reduction of the thread's own row.  bf16 operands in shared
-// memory, fp32 accumulators in TMEM.  The head runs once per group, each
-// weight load serving every sample of the group.
+// overlap the others' CUDA-core work.  Per sample (thread r = point r):
+// layer 1 as one tcgen05.mma M=128 points, N=64, K=16 -- each FP32
+// coordinate split exactly into three bf16 terms (hi + mid + lo) against
+// W1 repeated three times, and a ones column against b1 -- then ReLU and
+// bf16 into A1; layer 2 as M=128 points, N=128, K=80 (A1's ones column
+// against b2); ReLU and bf16 into A2; layer 3 transposed, M=128 features
+// (two halves of W3^T), N=128 points, K=128, so that TMEM lane r holds
+// feature r of a half and the max over the points is a register reduction
+// of the thread's own row.  bf16 operands in shared memory, fp32
+// accumulators in TMEM.  The head runs once per group: thread (g, j) sums
+// inputs [64 g, 64 g + 64) of output j for every sample of the group, from
+// W4 in bf16 read once per CTA and group, and the four partial sums meet in
+// shared memory; one warp per (sample, output) for the last layer.
 __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const unsigned char* __restrict__ tcw, const float* __restrict__ X, int S,
     const int* __restrict__ n_groups_dev, int group, const float4* __restrict__ frames,
     float* __restrict__ out, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  float* w1 = reinterpret_cast<float*>(smem + kSmW1);        // W1 [3][64], b1 [64]
+  const float* sb3 = reinterpret_cast<const float*>(smem + kSmSmall);  // b3, b4, b5
+  const float* sb4 = sb3 + (kSfB4 - kSfB3);
+  const float* sb5 = sb3 + (kSfB5 - kSfB3);
+  const float* w5g = reinterpret_cast<const float*>(tcw + kTcSmallOff) + kSfW5;  // [128][7]
   float* h = reinterpret_cast<float*>(smem + kSmH);          // [group][256]
-  float* y1 = reinterpret_cast<float*>(smem + kSmY1);        // [group][128]
-  float* sb2 = reinterpret_cast<float*>(smem + kSmBias);     // b2 [128]
-  float* sb3 = sb2 + kD2;                                    // b3 [256]
-  float* sb4 = sb3 + kD3;                                    // b4 [128]
-  float* sw5 = sb4 + kD4;                                    // W5 [128][7]
-  float* sb5 = sw5 + kD4 * kD5;                              // b5 [7]
+  float* part = reinterpret_cast<float*>(smem + kSmA2);      // [wg][group][128], head only
+  float* y1 = part + kTcWg * kMaxGroup * kD4;                // [group][128], head only
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [kTcWg]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8 * kTcWg);
-  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 8 * kTcWg + 4);
-  const float* f = reinterpret_cast<const float*>(tcw + kTcF32Off);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  uint64_t* lbar = mbar + kTcWg;                                 // the bulk copies
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8 * kTcWg + 8);
+  int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 8 * kTcWg + 12);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid >> 7, lt = tid & 127, wq = warp & 3;
   unsigned char* a2b = smem + kSmA2 + wg * kPts * kD2 * 2;
   unsigned char* a1b = a2b;
+  unsigned char* a0b = a2b + kOpA0;
   // groups: ceil(S / group), or the device count of groups when given
   int ng = (S + group - 1) / group;
   if (n_groups_dev) ng = min(ng, *n_groups_dev);
   if ((int)blockIdx.x >= ng) return;
 
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(tcw);
-    uint4* dst = reinterpret_cast<uint4*>(smem);
-    for (int i = tid; i < (kTcW2Bytes + kTcW3Bytes) / 16; i += kTcThreads) dst[i] = src[i];
-    for (int i = tid; i < 4 * kD1; i += kTcThreads) w1[i] = f[kW1 + i];
-    for (int i = tid; i < kD2; i += kTcThreads) sb2[i] = f[kB2 + i];
-    for (int i = tid; i < kD3; i += kTcThreads) sb3[i] = f[kB3 + i];
-    for (int i = tid; i < kD4; i += kTcThreads) sb4[i] = f[kB4 + i];
-    for (int i = tid; i < kD4 * kD5 + kD5; i += kTcThreads) sw5[i] = f[kW5 + i];  // W5, b5
-  }
   if (tid == 0) {
     for (int q = 0; q < kTcWg; ++q) mbar_init(mbar + q, 1);
+    mbar_init(lbar, 1);
     *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(lbar, kTcB2xBytes + kTcW3Bytes + kTcB1Bytes + kSmallCopy);
+    bulk_load(saddr(smem + kSmB2), tcw + kTcB2xOff, kTcB2xBytes, lbar);
+    bulk_load(saddr(smem + kSmB3), tcw + kTcW2Bytes, kTcW3Bytes, lbar);
+    bulk_load(saddr(smem + kSmB1), tcw + kTcB1Off, kTcB1Bytes, lbar);
+    bulk_load(saddr(smem + kSmSmall), tcw + kTcSmallOff + 4 * kSfB3, kSmallCopy, lbar);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
@@ -587,14 +660,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   fence_before();
   __syncthreads();
   fence_after();
+  mbar_wait_bounded(lbar, 0, err, abort_flag);
+  if (__syncthreads_or(*abort_flag != 0)) {
+    // the copies may still be in flight: wait for them (bounded) before the
+    // shared memory is given up
+    mbar_wait_bounded(lbar, 0, err, abort_flag);
+    ng = 0;
+  }
   const uint32_t tmem = *tslot + (uint32_t)(wg * 128);  // 128 columns per warpgroup
   const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
-  const uint32_t sA1 = saddr(a1b), sA2 = saddr(a2b);
-  const uint32_t sB2 = saddr(smem + kSmB2), sB3 = saddr(smem + kSmB3);
+  const uint32_t sA0 = saddr(a0b), sA1 = saddr(a1b), sA2 = saddr(a2b);
+  const uint32_t sB1 = saddr(smem + kSmB1), sB2 = saddr(smem + kSmB2),
+                 sB3 = saddr(smem + kSmB3);
   uint64_t* mb = mbar + wg;
   uint32_t phase = 0;
 
@@ -603,56 +683,83 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     if (frames && !(frames[s0].w > 0.0f)) continue;  // block-uniform
     for (int k = wg; k < gs; k += kTcWg) {
       const int s = s0 + k;
-      // layer 1 (row lt) -> A1 in bf16 core-matrix layout
+      // A0 row lt: x = hi + mid + lo in bf16 (exact), then 1 (b1)
       {
         const float* x = X + (size_t)s * kPts * 3;
-        const float x0 = x[3 * lt], x1 = x[3 * lt + 1], x2 = x[3 * lt + 2];
-        for (int k0 = 0; k0 < kD1; k0 += 8) {
-          uint32_t pk[4];
+        uint32_t t[9];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int j = k0 + 2 * q;
-            const float za = w1[3 * kD1 + j] + x0 * w1[j] + x1 * w1[kD1 + j] + x2 * w1[2 * kD1 + j];
-            const float zb = w1[3 * kD1 + j + 1] + x0 * w1[j + 1] + x1 * w1[kD1 + j + 1] +
-                             x2 * w1[2 * kD1 + j + 1];
-            const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
-            pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
-          }
-          *reinterpret_cast<uint4*>(a1b + core_offset(lt, k0, kD1)) =
-              make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        for (int d = 0; d < 3; ++d) {
+          const float v = x[3 * lt + d];
+          const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+          const float r1 = v - __bfloat162float(hi);
+          const __nv_bfloat16 mi = __float2bfloat16_rn(r1);
+          const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mi));
+          t[d] = __bfloat16_as_ushort(hi);
+          t[3 + d] = __bfloat16_as_ushort(mi);
+          t[6 + d] = __bfloat16_as_ushort(lo);
         }
+        *reinterpret_cast<uint4*>(a0b + core_offset(lt, 0, kK1)) =
+            make_uint4(t[0] | (t[1] << 16), t[2] | (t[3] << 16), t[4] | (t[5] << 16),
+                       t[6] | (t[7] << 16));
+        *reinterpret_cast<uint4*>(a0b + core_offset(lt, 8, kK1)) =
+            make_uint4(t[8] | (0x3F80u << 16), 0u, 0u, 0u);
       }
       fence_async_smem();
       fence_before();
       wg_sync(wg);
       fence_after();
       if (lt == 0) {
-        for (int ks = 0; ks < kD1 / 16; ++ks)
-          mma_bf16(tmem, smem_desc(sA1 + ks * 256, 128, (kD1 / 8) * 128),
-                   smem_desc(sB2 + ks * 256, 128, (kD1 / 8) * 128), idesc_bf16(128, kD2), ks > 0);
+        mma_bf16(tmem, smem_desc(sA0, 128, (kK1 / 8) * 128), smem_desc(sB1, 128, (kK1 / 8) * 128),
+                 idesc_bf16(128, kD1), 0);
         mma_commit(mb);
       }
       mbar_wait_bounded(mb, phase, err, abort_flag);
       phase ^= 1u;
       fence_after();
-      // epilogue 2: bias, ReLU, bf16 -> A2
+      // epilogue 1: ReLU, bf16 -> A1 columns 0..63; column 64 = 1 (b2)
+#pragma unroll
+      for (int cc = 0; cc < kD1 / 32; ++cc) {
+        uint32_t v[32];
+        SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int k0 = 0; k0 < 32; k0 += 8) {
+          uint4 pk;
+          pk.x = relu_bf16x2(__uint_as_float(v[k0]), __uint_as_float(v[k0 + 1]));
+          pk.y = relu_bf16x2(__uint_as_float(v[k0 + 2]), __uint_as_float(v[k0 + 3]));
+          pk.z = relu_bf16x2(__uint_as_float(v[k0 + 4]), __uint_as_float(v[k0 + 5]));
+          pk.w = relu_bf16x2(__uint_as_float(v[k0 + 6]), __uint_as_float(v[k0 + 7]));
+          *reinterpret_cast<uint4*>(a1b + core_offset(lt, cc * 32 + k0, kK2x)) = pk;
+        }
+      }
+      *reinterpret_cast<uint4*>(a1b + core_offset(lt, kD1, kK2x)) = make_uint4(0x3F80u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(a1b + core_offset(lt, kD1 + 8, kK2x)) = make_uint4(0u, 0u, 0u, 0u);
+      fence_async_smem();
+      fence_before();
+      wg_sync(wg);
+      fence_after();
+      if (lt == 0) {
+        for (int ks = 0; ks < kK2x / 16; ++ks)
+          mma_bf16(tmem, smem_desc(sA1 + ks * 256, 128, (kK2x / 8) * 128),
+                   smem_desc(sB2 + ks * 256, 128, (kK2x / 8) * 128), idesc_bf16(128, kD2), ks > 0);
+        mma_commit(mb);
+      }
+      mbar_wait_bounded(mb, phase, err, abort_flag);
+      phase ^= 1u;
+      fence_after();
+      // epilogue 2: ReLU, bf16 -> A2 (b2 came with the MMA)
       for (int cc = 0; cc < kD2 / 32; ++cc) {
         uint32_t v[32];
         SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
         tmem_wait_ld();
 #pragma unroll
         for (int k0 = 0; k0 < 32; k0 += 8) {
-          uint32_t pk[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int j = cc * 32 + k0 + 2 * q;
-            const float za = __uint_as_float(v[k0 + 2 * q]) + sb2[j];
-            const float zb = __uint_as_float(v[k0 + 2 * q + 1]) + sb2[j + 1];
-            const __nv_bfloat162 v2 = __floats2bfloat162_rn(fmaxf(za, 0.f), fmaxf(zb, 0.f));
-            pk[q] = *reinterpret_cast<const uint32_t*>(&v2);
-          }
-          *reinterpret_cast<uint4*>(a2b + core_offset(lt, cc * 32 + k0, kD2)) =
-              make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          uint4 pk;
+          pk.x = relu_bf16x2(__uint_as_float(v[k0]), __uint_as_float(v[k0 + 1]));
+          pk.y = relu_bf16x2(__uint_as_float(v[k0 + 2]), __uint_as_float(v[k0 + 3]));
+          pk.z = relu_bf16x2(__uint_as_float(v[k0 + 4]), __uint_as_float(v[k0 + 5]));
+          pk.w = relu_bf16x2(__uint_as_float(v[k0 + 6]), __uint_as_float(v[k0 + 7]));
+          *reinterpret_cast<uint4*>(a2b + core_offset(lt, cc * 32 + k0, kD2)) = pk;
         }
       }
       fence_async_smem();
@@ -685,7 +792,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
           SG_TMEM_LD32(tmem + lane_base + cc * 32, v);
           tmem_wait_ld();
 #pragma unroll
-          for (int q = 0; q < 32; ++q) m = fmaxf(m, __uint_as_float(v[q]));
+          for (int q = 0; q < 32; q += 2)
+            m = max3f(m, __uint_as_float(v[q]), __uint_as_float(v[q + 1]));
         }
         const int c = hf * kPts + lt;
         h[k * kD3 + c] = fmaxf(m + sb3[c], 0.0f);
@@ -701,48 +809,63 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const int ab_all = __syncthreads_or(*abort_flag != 0);
     fence_after();
     if (ab_all) break;
-    // W4 into the operand buffers, free until the next group's layer 1: its
-    // values are bf16 (rounded when packed), so the bf16 copy is exact
-    __nv_bfloat162* w4s = reinterpret_cast<__nv_bfloat162*>(smem + kSmA2);
+    // head: y1[k][j] = ReLU(b4[j] + sum_c h[k][c] W4[c][j]); thread (wg, j)
+    // sums c in [64 wg, 64 wg + 64) for every sample k of the group
     {
-      const float2* w4g = reinterpret_cast<const float2*>(f + kW4);
-#pragma unroll 4
-      for (int i = tid; i < kD3 * kD4 / 2; i += kTcThreads) {
-        const float2 v = w4g[i];
-        w4s[i] = __floats2bfloat162_rn(v.x, v.y);
-      }
-    }
-    __syncthreads();
-    // head over the group: y1[k][j] = ReLU(b4 + sum_c h[k][c] W4[c][j]);
-    // warpgroup wg takes the samples k = wg (mod kTcWg)
-    {
-      constexpr int kPer = kMaxGroup / kTcWg;
       const int j = lt;
-      const __nv_bfloat16* w4h = reinterpret_cast<const __nv_bfloat16*>(w4s);
-      float acc[kPer];
+      const uint4* w4g = reinterpret_cast<const uint4*>(tcw + kTcW4Off) + (size_t)(wg * 8) * kD4 + j;
+      uint4 wv[8];
 #pragma unroll
-      for (int q = 0; q < kPer; ++q) acc[q] = sb4[j];
-#pragma unroll 8
-      for (int c = 0; c < kD3; ++c) {
-        const float wv = __bfloat162float(w4h[c * kD4 + j]);
+      for (int cb = 0; cb < 8; ++cb) wv[cb] = __ldg(w4g + cb * kD4);
+      float acc[kMaxGroup];
 #pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-          const int k = wg + kTcWg * q;
-          if (k < gs) acc[q] += h[k * kD3 + c] * wv;
+      for (int k = 0; k < kMaxGroup; ++k) acc[k] = 0.0f;
+#pragma unroll
+      for (int cb = 0; cb < 8; ++cb) {
+        const uint32_t u[4] = {wv[cb].x, wv[cb].y, wv[cb].z, wv[cb].w};
+        float w[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          w[2 * q] = __uint_as_float(u[q] << 16);
+          w[2 * q + 1] = __uint_as_float(u[q] & 0xffff0000u);
+        }
+        const int c0 = wg * 64 + cb * 8;
+#pragma unroll
+        for (int k = 0; k < kMaxGroup; ++k) {
+          const float4 ha = *reinterpret_cast<const float4*>(h + k * kD3 + c0);
+          const float4 hb = *reinterpret_cast<const float4*>(h + k * kD3 + c0 + 4);
+          float a = acc[k];
+          a += ha.x * w[0];
+          a += ha.y * w[1];
+          a += ha.z * w[2];
+          a += ha.w * w[3];
+          a += hb.x * w[4];
+          a += hb.y * w[5];
+          a += hb.z * w[6];
+          a += hb.w * w[7];
+          acc[k] = a;
         }
       }
 #pragma unroll
-      for (int q = 0; q < kPer; ++q) {
-        const int k = wg + kTcWg * q;
-        if (k < gs) y1[k * kD4 + j] = fmaxf(acc[q], 0.0f);
-      }
+      for (int k = 0; k < kMaxGroup; ++k) part[(wg * kMaxGroup + k) * kD4 + j] = acc[k];
     }
     __syncthreads();
-    for (int t = tid; t < gs * kD5; t += kTcThreads) {
-      const int k = t / kD5, o = t - k * kD5;
-      float z = sb5[o];
-      for (int j = 0; j < kD4; ++j) z += y1[k * kD4 + j] * sw5[j * kD5 + o];
-      out[(size_t)(s0 + k) * 8 + o] = z;
+    for (int t = tid; t < gs * kD4; t += kTcThreads) {
+      const int k = t / kD4, j = t - k * kD4;
+      float z = sb4[j];
+#pragma unroll
+      for (int q = 0; q < kTcWg; ++q) z += part[(q * kMaxGroup + k) * kD4 + j];
+      y1[k * kD4 + j] = fmaxf(z, 0.0f);
+    }
+    __syncthreads();
+    // last layer: one warp per (sample, output)
+    for (int p = warp; p < gs * kD5; p += kTcThreads / 32) {
+      const int k = p / kD5, o = p - k * kD5;
+      float z = 0.0f;
+#pragma unroll
+      for (int j = lane; j < kD4; j += 32) z += y1[k * kD4 + j] * __ldg(w5g + j * kD5 + o);
+      z = warp_sum(z);
+      if (lane == 0) out[(size_t)(s0 + k) * 8 + o] = z + sb5[o];
     }
     fence_before();
     __syncthreads();

@@ -36,12 +36,36 @@ __host__ __device__ constexpr uint32_t core_offset(int r, int k, int K) {
   return (uint32_t)(((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 // bf16 inference weights, one device block: W2^T (128 x 64) and W3^T
-// (256 x 128) in the core-matrix layout, then fp32 copies of W1, b1, b2,
-// b3, W4, b4, W5, b5 rounded to bf16 values.
+// (256 x 128) in the core-matrix layout; fp32 copies of all parameters
+// rounded to bf16 values (parameter order); W4 in bf16, element (c, j) at
+// ((c / 8) * 128 + j) * 8 + c % 8, so that one 16-byte load gives head
+// output j eight consecutive inputs; the small fp32 block (W1 and b1 as
+// float4 (w0j, w1j, w2j, b1j), b2, b3, b4, b5 (+1 pad), W5); and the
+// tensor-core kernel's own operands: W2^T extended by b2 as column 64
+// (128 x 80, K = 80: A1 carries a ones column there) and B1 (64 x 16): W1
+// rows 0-2 repeated three times (for the three bf16 terms of each FP32
+// coordinate) and b1 as column 9, so that layer 1 is one MMA.
 constexpr int kTcW2Bytes = kD2 * kD1 * 2;           // 16 KB
 constexpr int kTcW3Bytes = kD3 * kD2 * 2;           // 64 KB
 constexpr int kTcF32Off = kTcW2Bytes + kTcW3Bytes;  // fp32 part after the bf16 operands
-constexpr int kTcBytes = kTcF32Off + 4 * kNumParams;
+constexpr int kTcW4Off = (kTcF32Off + 4 * kNumParams + 15) / 16 * 16;
+constexpr int kTcW4Bytes = kD3 * kD4 * 2;           // 64 KB
+constexpr int kTcSmallOff = kTcW4Off + kTcW4Bytes;
+constexpr int kSfW1 = 0, kSfB2 = kSfW1 + 4 * kD1, kSfB3 = kSfB2 + kD2, kSfB4 = kSfB3 + kD3,
+              kSfB5 = kSfB4 + kD4, kSfW5 = kSfB5 + 8,
+              kSmallFloats = kSfW5 + kD4 * kD5;     // float offsets in the small block
+constexpr int kTcSmallBytes = 4 * kSmallFloats;
+constexpr int kK2x = kD1 + 16;                      // layer-2 K with the bias column
+constexpr int kK1 = 16;                             // layer-1 K: 3 x 3 terms + bias
+constexpr int kTcB2xOff = kTcSmallOff + kTcSmallBytes;
+constexpr int kTcB2xBytes = kD2 * kK2x * 2;         // 20 KB
+constexpr int kTcB1Off = kTcB2xOff + kTcB2xBytes;
+constexpr int kTcB1Bytes = kD1 * kK1 * 2;           // 2 KB
+constexpr int kTcBytes = kTcB1Off + kTcB1Bytes;
+static_assert(kTcW4Off % 16 == 0 && kTcSmallOff % 16 == 0 && kTcSmallBytes % 16 == 0 &&
+                  kTcB2xOff % 16 == 0 && kTcB1Off % 16 == 0 && kTcW2Bytes % 16 == 0 &&
+                  kTcW3Bytes % 16 == 0 && (4 * kSfB3) % 16 == 0 && (4 * kSfW5) % 16 == 0,
+              "bulk-copy alignment");
 
 }  // namespace prop
 }  // namespace sg
