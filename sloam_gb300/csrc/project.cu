@@ -23,6 +23,8 @@
 // (inputs read through the context's input block, so a captured graph can be
 // replayed on new inputs), or a batch of keyframes, blockIdx.y selecting the
 // keyframe's FrontRef.
+#include <algorithm>
+
 #include "internal.h"
 #include "scan_util.cuh"
 #include "fastpoly.cuh"
@@ -111,14 +113,30 @@ __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontR
   const int lane = threadIdx.x & 31;
   unsigned long long hot_acc = ~0ull;  // this warp's least key at `hot`
   int slow = 0;
-  for (int i0 = blockIdx.x * blockDim.x; i0 < N; i0 += gridDim.x * blockDim.x) {
+  // a grid of resident blocks: each thread walks its points at the grid's
+  // stride, the next point's loads issued before this point's arithmetic
+  const int stride = gridDim.x * blockDim.x;
+  float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t lab_next = 0u;
+  {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) {
+      p_next = f.xyzi[i];
+      lab_next = point_labels ? f.plabel[i] : 0u;
+    }
+  }
+  for (int i0 = blockIdx.x * blockDim.x; i0 < N; i0 += stride) {
     const int i = i0 + threadIdx.x;
     const bool valid = i < N;
     int pix = -1;
     unsigned long long key = ~0ull;
+    const float4 p = p_next;
+    const uint32_t lab = lab_next;
+    if (i + stride < N) {
+      p_next = f.xyzi[i + stride];  // kept in L2 for k_label
+      lab_next = point_labels ? f.plabel[i + stride] : 0u;
+    }
     if (valid) {
-      const float4 p = f.xyzi[i];  // kept in L2 for k_label
-      const uint32_t lab = point_labels ? f.plabel[i] : 0u;
       const float x = p.x, y = p.y, z = p.z;
       const float range = fsqrt(fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z)));
       // ---- first try: own polynomial angles, the table entry the formula
@@ -345,6 +363,23 @@ __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_c
 
 }  // namespace
 
+// Blocks per keyframe of a batch projection launch: the resident blocks of
+// the whole GPU shared among the launch's keyframes (each thread then walks
+// several points), at most one point per thread.
+static int project_blocks_per_kf(int N, int nkf) {
+  static int resident = 0;
+  if (!resident) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project<true>, 256, 0);
+    resident = std::max(1, sms) * std::max(1, per_sm);
+  }
+  const int full = (N + 255) / 256;
+  const int share = (resident + nkf - 1) / std::max(1, nkf);
+  return std::max(1, std::min(full, share));
+}
+
 size_t front_gbits_words(int N) { return (size_t)((N + 1023) / 1024) * 32 + 32; }
 int front_blocks(int N) { return (N + 1023) / 1024; }
 
@@ -373,7 +408,7 @@ int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStrea
 int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, int kf0,
                          int nkf, bool point_labels, cudaStream_t st) {
   if (nkf <= 0) return 0;
-  const dim3 g256((d.N + 255) / 256, nkf), g1k(front_blocks(d.N), nkf);
+  const dim3 g256(project_blocks_per_kf(d.N, nkf), nkf), g1k(front_blocks(d.N), nkf);
   k_project<true><<<g256, 256, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
   k_label<true><<<g1k, kLabelThreads, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
   k_ground_compact<true><<<g1k, kLabelThreads, 0, st>>>(d, refs, kf0);
