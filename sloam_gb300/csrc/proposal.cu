@@ -365,11 +365,13 @@ __global__ void k_prop_pack(const float* __restrict__ W, unsigned char* __restri
     b3[core_offset(c, k, kD2) / 2] = __float2bfloat16_rn(W[kW3 + i]);
   }
   if (i < kNumParams) f[i] = bfr(W[i]);
-  if (i < kD3 * kD4) {  // W4[c][j] -> bf16 at ((c / 8) * 128 + j) * 8 + c % 8
+  if (i < kD3 * kD4) {  // W4[c][j] -> W4^T (j, c), K = 256
     __nv_bfloat16* b4 = reinterpret_cast<__nv_bfloat16*>(tcw + kTcW4Off);
     const int c = i / kD4, j = i % kD4;
-    b4[((c >> 3) * kD4 + j) * 8 + (c & 7)] = __float2bfloat16_rn(W[kW4 + i]);
+    b4[core_offset(j, c, kD3) / 2] = __float2bfloat16_rn(W[kW4 + i]);
   }
+  if (i < kD4 * kD5)  // W5 [128][7] in bf16
+    reinterpret_cast<__nv_bfloat16*>(tcw + kTcW5hOff)[i] = __float2bfloat16_rn(W[kW5 + i]);
   if (i < kSmallFloats) {  // W1 / b1 as float4 rows, b2, b3, b4, b5, pad, W5
     float v = 0.0f;
     if (i < kSfB2) {
@@ -518,34 +520,43 @@ constexpr int kMaxGroup = 8;     // samples per group (one tree's proposals)
 // Per warpgroup one 32 KB operand buffer: A1 [128 x 80] (the ones column
 // at 64 carries b2) at its start and A0 [128 x 16] (layer-1 input) after
 // it while layers 1 and 2 run, then A2 [128 x 128] (written once the
-// layer-2 MMAs, which read A1, have completed).  The operand buffers hold
-// the head's partial sums and outputs between groups.  W2^T | b2, W3^T, B1
-// and the biases arrive by bulk copy from the packed device layout.
+// layer-2 MMAs, which read A1, have completed).  Between groups the
+// operand buffers hold the head's W4^T (64 KB, bulk copy) and outputs.
+// W2^T | b2, W3^T, B1, the biases and W5 arrive by bulk copy from the
+// packed device layout.  Ht [16 x 256] is the head's B operand: the
+// max-pooled features of sample k split exactly into bf16 hi (row k) and
+// lo (row 8 + k) terms.
 constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcB2xBytes,
                    kSmA2 = kSmB3 + kTcW3Bytes,                    // [wg][32 KB]
                    kSmB1 = kSmA2 + kTcWg * kPts * kD2 * 2,        // [64 x 16] bf16
-                   kSmSmall = kSmB1 + kTcB1Bytes,                 // b3, b4, b5
+                   kSmHt = kSmB1 + kTcB1Bytes,                    // [16 x 256] bf16
+                   kSmSmall = kSmHt + 2 * kMaxGroup * kD3 * 2,    // b3, b4, b5
                    kSmallCopy = 4 * (kSfW5 - kSfB3),
-                   kSmH = kSmSmall + kSmallCopy,                  // [group][256]
-                   kSmMisc = kSmH + 4 * kMaxGroup * kD3,
+                   kSmW5h = kSmSmall + kSmallCopy,                // W5 [128][7] bf16
+                   kSmMisc = kSmW5h + kTcW5hBytes,
                    kTcSmem = kSmMisc + 64;
 constexpr uint32_t kOpA0 = kPts * kK2x * 2;                       // A0 inside the buffer
-static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0 && kSmB1 % 128 == 0, "operand alignment");
-static_assert(kSmSmall % 16 == 0 && kSmH % 16 == 0 && kSmMisc % 16 == 0 && kOpA0 % 128 == 0,
+constexpr uint32_t kOpY1 = kTcW4Bytes;                            // head outputs, after W4^T
+static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0 && kSmB1 % 128 == 0 && kSmHt % 128 == 0,
+              "operand alignment");
+static_assert(kSmSmall % 16 == 0 && kSmW5h % 16 == 0 && kSmMisc % 16 == 0 && kOpA0 % 128 == 0,
               "16-byte alignment");
 static_assert(kTcSmem <= 227 * 1024, "shared memory");
 static_assert(kOpA0 + kPts * kK1 * 2 <= kPts * kD2 * 2, "A1 and A0 inside the A2 buffer");
-static_assert(2 * kTcWg * kMaxGroup * kD4 * 4 <= kTcWg * kPts * kD2 * 2,
-              "head partial sums and outputs inside the operand buffers");
-static_assert(kD3 == kTcWg * 64, "head: one quarter of the inputs per warpgroup");
+static_assert(kOpY1 + kMaxGroup * kD4 * 4 <= kTcWg * kPts * kD2 * 2,
+              "W4^T and the head outputs inside the operand buffers");
+static_assert(2 * kMaxGroup == 16, "head MMA: N = 16 (hi and lo rows of 8 samples)");
 // the descriptors address at most: A0 [128 x 16], A1 [128 x 80], A2
-// [128 x 128], B1 [64 x 16], W2^T | b2 [128 x 80], W3^T [256 x 128]; every
-// core matrix lies inside its buffer
+// [128 x 128], B1 [64 x 16], W2^T | b2 [128 x 80], W3^T [256 x 128], W4^T
+// [128 x 256], Ht [16 x 256]; every core matrix lies inside its buffer
 static_assert(core_offset(kPts - 1, kK1 - 1, kK1) + 2 <= kPts * kK1 * 2, "A0 extent");
 static_assert(core_offset(kPts - 1, kK2x - 1, kK2x) + 2 <= kOpA0, "A1 extent");
 static_assert(core_offset(kD1 - 1, kK1 - 1, kK1) + 2 <= kTcB1Bytes, "B1 extent");
 static_assert(core_offset(kD2 - 1, kK2x - 1, kK2x) + 2 <= kTcB2xBytes, "W2 extent");
 static_assert(core_offset(kD3 - 1, kD2 - 1, kD2) + 2 <= kTcW3Bytes, "W3 extent");
+static_assert(core_offset(kD4 - 1, kD3 - 1, kD3) + 2 <= kTcW4Bytes, "W4 extent");
+static_assert(core_offset(2 * kMaxGroup - 1, kD3 - 1, kD3) + 2 <= 2 * kMaxGroup * kD3 * 2,
+              "Ht extent");
 
 SLOAM_D bool mbar_wait_bounded(uint64_t* m, uint32_t phase, int* err, int* abort_flag) {
   int it = 0;
@@ -604,7 +615,8 @@ SLOAM_D bool wg_any(int wg, bool p) {
 // fitted) are skipped.  512 threads: warpgroup g (0..3) takes samples
 // g, g + 4 of the group with its own operand buffer, TMEM columns
 // [128 g, 128 g + 128), mbarrier and barrier, so that one warpgroup's MMAs
-// overlap the others' CUDA-core work.  Per sample (thread r = point r):
+// overlap the others' CUDA-core work; its next sample's points are loaded
+// while it works on the current one.  Per sample (thread r = point r):
 // layer 1 as one tcgen05.mma M=128 points, N=64, K=16 -- each FP32
 // coordinate split exactly into three bf16 terms (hi + mid + lo) against
 // W1 repeated three times, and a ones column against b1 -- then ReLU and
@@ -612,11 +624,11 @@ SLOAM_D bool wg_any(int wg, bool p) {
 // against b2); ReLU and bf16 into A2; layer 3 transposed, M=128 features
 // (two halves of W3^T), N=128 points, K=128, so that TMEM lane r holds
 // feature r of a half and the max over the points is a register reduction
-// of the thread's own row.  bf16 operands in shared memory, fp32
-// accumulators in TMEM.  The head runs once per group: thread (g, j) sums
-// inputs [64 g, 64 g + 64) of output j for every sample of the group, from
-// W4 in bf16 read once per CTA and group, and the four partial sums meet in
-// shared memory; one warp per (sample, output) for the last layer.
+// of the thread's own row; bias and ReLU, and the feature goes to Ht as
+// bf16 hi and lo terms.  The head is one MMA per group, M=128 outputs,
+// N=16 (hi and lo of 8 samples), K=256, A = W4^T; then bias and ReLU, and
+// one warp per (sample, output) for the last layer.  bf16 operands in
+// shared memory, fp32 accumulators in TMEM.
 __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const unsigned char* __restrict__ tcw, const float* __restrict__ X, int S,
     const int* __restrict__ n_groups_dev, int group, const float4* __restrict__ frames,
@@ -625,12 +637,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   const float* sb3 = reinterpret_cast<const float*>(smem + kSmSmall);  // b3, b4, b5
   const float* sb4 = sb3 + (kSfB4 - kSfB3);
   const float* sb5 = sb3 + (kSfB5 - kSfB3);
-  const float* w5g = reinterpret_cast<const float*>(tcw + kTcSmallOff) + kSfW5;  // [128][7]
-  float* h = reinterpret_cast<float*>(smem + kSmH);          // [group][256]
-  float* part = reinterpret_cast<float*>(smem + kSmA2);      // [wg][group][128], head only
-  float* y1 = part + kTcWg * kMaxGroup * kD4;                // [group][128], head only
+  const __nv_bfloat16* sw5 = reinterpret_cast<const __nv_bfloat16*>(smem + kSmW5h);
+  unsigned char* htb = smem + kSmHt;
+  float* y1 = reinterpret_cast<float*>(smem + kSmA2 + kOpY1);  // [group][128], head only
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [kTcWg]
-  uint64_t* lbar = mbar + kTcWg;                                 // the bulk copies
+  uint64_t* lbar = mbar + kTcWg;  // bulk copies and the head MMA
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8 * kTcWg + 8);
   int* abort_flag = reinterpret_cast<int*>(smem + kSmMisc + 8 * kTcWg + 12);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -642,17 +653,34 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   int ng = (S + group - 1) / group;
   if (n_groups_dev) ng = min(ng, *n_groups_dev);
   if ((int)blockIdx.x >= ng) return;
+  // this warpgroup's next sample and its point (row lt), loaded ahead
+  int pf_s = -1;
+  float px0 = 0.f, px1 = 0.f, px2 = 0.f;
+  auto prefetch = [&](int s) {
+    pf_s = s;
+    if (s >= 0) {
+      const float* x = X + (size_t)s * kPts * 3 + 3 * lt;
+      px0 = x[0];
+      px1 = x[1];
+      px2 = x[2];
+    }
+  };
+  {
+    const int s = blockIdx.x * group + wg;
+    prefetch(wg < min(group, S - (int)blockIdx.x * group) ? s : -1);
+  }
 
   if (tid == 0) {
     for (int q = 0; q < kTcWg; ++q) mbar_init(mbar + q, 1);
     mbar_init(lbar, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    mbar_expect_tx(lbar, kTcB2xBytes + kTcW3Bytes + kTcB1Bytes + kSmallCopy);
+    mbar_expect_tx(lbar, kTcB2xBytes + kTcW3Bytes + kTcB1Bytes + kSmallCopy + kTcW5hBytes);
     bulk_load(saddr(smem + kSmB2), tcw + kTcB2xOff, kTcB2xBytes, lbar);
     bulk_load(saddr(smem + kSmB3), tcw + kTcW2Bytes, kTcW3Bytes, lbar);
     bulk_load(saddr(smem + kSmB1), tcw + kTcB1Off, kTcB1Bytes, lbar);
     bulk_load(saddr(smem + kSmSmall), tcw + kTcSmallOff + 4 * kSfB3, kSmallCopy, lbar);
+    bulk_load(saddr(smem + kSmW5h), tcw + kTcW5hOff, kTcW5hBytes, lbar);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
@@ -663,33 +691,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   fence_before();
   __syncthreads();
   fence_after();
-  mbar_wait_bounded(lbar, 0, err, abort_flag);
+  uint32_t lph = 0;  // parity of lbar's next phase
+  mbar_wait_bounded(lbar, lph, err, abort_flag);
+  lph ^= 1u;
   if (__syncthreads_or(*abort_flag != 0)) {
     // the copies may still be in flight: wait for them (bounded) before the
     // shared memory is given up
     mbar_wait_bounded(lbar, 0, err, abort_flag);
     ng = 0;
   }
-  const uint32_t tmem = *tslot + (uint32_t)(wg * 128);  // 128 columns per warpgroup
+  const uint32_t tmem0 = *tslot;
+  const uint32_t tmem = tmem0 + (uint32_t)(wg * 128);  // 128 columns per warpgroup
   const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
   const uint32_t sA0 = saddr(a0b), sA1 = saddr(a1b), sA2 = saddr(a2b);
   const uint32_t sB1 = saddr(smem + kSmB1), sB2 = saddr(smem + kSmB2),
-                 sB3 = saddr(smem + kSmB3);
+                 sB3 = saddr(smem + kSmB3), sW4 = saddr(smem + kSmA2), sHt = saddr(htb);
   uint64_t* mb = mbar + wg;
   uint32_t phase = 0;
 
   for (int g = blockIdx.x; g < ng; g += gridDim.x) {
     const int s0 = g * group, gs = min(group, S - s0);
-    if (frames && !(frames[s0].w > 0.0f)) continue;  // block-uniform
+    if (frames && !(frames[s0].w > 0.0f)) {  // block-uniform
+      const int g2 = g + gridDim.x;
+      if (g2 < ng && wg < min(group, S - g2 * group)) prefetch(g2 * group + wg);
+      continue;
+    }
     for (int k = wg; k < gs; k += kTcWg) {
       const int s = s0 + k;
+      if (pf_s != s) prefetch(s);
+      const float x0 = px0, x1 = px1, x2 = px2;
+      {  // the next sample of this warpgroup: in this group, else the next group's
+        const int g2 = g + gridDim.x;
+        if (k + kTcWg < gs) prefetch(s + kTcWg);
+        else if (g2 < ng && wg < min(group, S - g2 * group)) prefetch(g2 * group + wg);
+      }
       // A0 row lt: x = hi + mid + lo in bf16 (exact), then 1 (b1)
       {
-        const float* x = X + (size_t)s * kPts * 3;
+        const float xv[3] = {x0, x1, x2};
         uint32_t t[9];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          const float v = x[3 * lt + d];
+          const float v = xv[d];
           const __nv_bfloat16 hi = __float2bfloat16_rn(v);
           const float r1 = v - __bfloat162float(hi);
           const __nv_bfloat16 mi = __float2bfloat16_rn(r1);
@@ -795,8 +837,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
           for (int q = 0; q < 32; q += 2)
             m = max3f(m, __uint_as_float(v[q]), __uint_as_float(v[q + 1]));
         }
+        // feature c of sample k -> Ht rows k (hi) and 8 + k (lo)
         const int c = hf * kPts + lt;
-        h[k * kD3 + c] = fmaxf(m + sb3[c], 0.0f);
+        const float hv = fmaxf(m + sb3[c], 0.0f);
+        const __nv_bfloat16 hh = __float2bfloat16_rn(hv);
+        const __nv_bfloat16 hl = __float2bfloat16_rn(hv - __bfloat162float(hh));
+        *reinterpret_cast<__nv_bfloat16*>(htb + core_offset(k, c, kD3)) = hh;
+        *reinterpret_cast<__nv_bfloat16*>(htb + core_offset(kMaxGroup + k, c, kD3)) = hl;
+        fence_async_smem();
         // barrier: the next half's MMAs (or the next sample's) overwrite
         // these columns
         fence_before();
@@ -809,63 +857,75 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     const int ab_all = __syncthreads_or(*abort_flag != 0);
     fence_after();
     if (ab_all) break;
-    // head: y1[k][j] = ReLU(b4[j] + sum_c h[k][c] W4[c][j]); thread (wg, j)
-    // sums c in [64 wg, 64 wg + 64) for every sample k of the group
+    // head: W4^T into the operand buffers (free: every MMA that read them
+    // has completed), then D[j][n] = W4^T[j][:] . Ht[n][:] into warpgroup
+    // 0's TMEM columns 0..15
+    if (tid == 0) {
+      mbar_expect_tx(lbar, kTcW4Bytes);
+      bulk_load(sW4, tcw + kTcW4Off, kTcW4Bytes, lbar);
+      mbar_wait_bounded(lbar, lph, err, abort_flag);
+      fence_after();
+      if (!*abort_flag) {
+        for (int ks = 0; ks < kD3 / 16; ++ks)
+          mma_bf16(tmem0, smem_desc(sW4 + ks * 256, 128, (kD3 / 8) * 128),
+                   smem_desc(sHt + ks * 256, 128, (kD3 / 8) * 128), idesc_bf16(128, 2 * kMaxGroup),
+                   ks > 0);
+        mma_commit(lbar);
+      }
+    }
+    fence_before();
+    if (__syncthreads_or(*abort_flag != 0)) {
+      // the copy may still be in flight (its wait timed out): wait for it
+      // (bounded) before the shared memory is given up
+      if (tid == 0) mbar_wait_bounded(lbar, lph, err, abort_flag);
+      __syncthreads();
+      break;
+    }
+    lph ^= 1u;
+    mbar_wait_bounded(lbar, lph, err, abort_flag);  // the head MMA
+    lph ^= 1u;
+    fence_after();
+    if (wg == 0) {
+      // lane j = output j: y1[k][j] = ReLU(b4[j] + hi part + lo part)
+      uint32_t v[32];
+      SG_TMEM_LD32(tmem0 + lane_base, v);
+      tmem_wait_ld();
+      const float b = sb4[lt];
+#pragma unroll
+      for (int k = 0; k < kMaxGroup; ++k)
+        if (k < gs)
+          y1[k * kD4 + lt] =
+              fmaxf(b + (__uint_as_float(v[k]) + __uint_as_float(v[kMaxGroup + k])), 0.0f);
+    }
+    fence_before();
+    if (__syncthreads_or(*abort_flag != 0)) break;
+    fence_after();
+    // last layer: warp w takes the (sample, output) pairs w + 16 i, i < 4,
+    // side by side
     {
-      const int j = lt;
-      const uint4* w4g = reinterpret_cast<const uint4*>(tcw + kTcW4Off) + (size_t)(wg * 8) * kD4 + j;
-      uint4 wv[8];
+      constexpr int kPairW = (kMaxGroup * kD5 + kTcThreads / 32 - 1) / (kTcThreads / 32);
+      float z[kPairW];
 #pragma unroll
-      for (int cb = 0; cb < 8; ++cb) wv[cb] = __ldg(w4g + cb * kD4);
-      float acc[kMaxGroup];
+      for (int i = 0; i < kPairW; ++i) {
+        const int p = warp + i * (kTcThreads / 32);
+        z[i] = 0.0f;
+        if (p < gs * kD5) {
+          const int k = p / kD5, o = p - k * kD5;
 #pragma unroll
-      for (int k = 0; k < kMaxGroup; ++k) acc[k] = 0.0f;
-#pragma unroll
-      for (int cb = 0; cb < 8; ++cb) {
-        const uint32_t u[4] = {wv[cb].x, wv[cb].y, wv[cb].z, wv[cb].w};
-        float w[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          w[2 * q] = __uint_as_float(u[q] << 16);
-          w[2 * q + 1] = __uint_as_float(u[q] & 0xffff0000u);
-        }
-        const int c0 = wg * 64 + cb * 8;
-#pragma unroll
-        for (int k = 0; k < kMaxGroup; ++k) {
-          const float4 ha = *reinterpret_cast<const float4*>(h + k * kD3 + c0);
-          const float4 hb = *reinterpret_cast<const float4*>(h + k * kD3 + c0 + 4);
-          float a = acc[k];
-          a += ha.x * w[0];
-          a += ha.y * w[1];
-          a += ha.z * w[2];
-          a += ha.w * w[3];
-          a += hb.x * w[4];
-          a += hb.y * w[5];
-          a += hb.z * w[6];
-          a += hb.w * w[7];
-          acc[k] = a;
+          for (int j = lane; j < kD4; j += 32)
+            z[i] += y1[k * kD4 + j] * __bfloat162float(sw5[j * kD5 + o]);
         }
       }
 #pragma unroll
-      for (int k = 0; k < kMaxGroup; ++k) part[(wg * kMaxGroup + k) * kD4 + j] = acc[k];
-    }
-    __syncthreads();
-    for (int t = tid; t < gs * kD4; t += kTcThreads) {
-      const int k = t / kD4, j = t - k * kD4;
-      float z = sb4[j];
+      for (int i = 0; i < kPairW; ++i) z[i] = warp_sum(z[i]);
 #pragma unroll
-      for (int q = 0; q < kTcWg; ++q) z += part[(q * kMaxGroup + k) * kD4 + j];
-      y1[k * kD4 + j] = fmaxf(z, 0.0f);
-    }
-    __syncthreads();
-    // last layer: one warp per (sample, output)
-    for (int p = warp; p < gs * kD5; p += kTcThreads / 32) {
-      const int k = p / kD5, o = p - k * kD5;
-      float z = 0.0f;
-#pragma unroll
-      for (int j = lane; j < kD4; j += 32) z += y1[k * kD4 + j] * __ldg(w5g + j * kD5 + o);
-      z = warp_sum(z);
-      if (lane == 0) out[(size_t)(s0 + k) * 8 + o] = z + sb5[o];
+      for (int i = 0; i < kPairW; ++i) {
+        const int p = warp + i * (kTcThreads / 32);
+        if (lane == 0 && p < gs * kD5) {
+          const int k = p / kD5, o = p - k * kD5;
+          out[(size_t)(s0 + k) * 8 + o] = z[i] + sb5[o];
+        }
+      }
     }
     fence_before();
     __syncthreads();

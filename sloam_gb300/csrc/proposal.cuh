@@ -37,14 +37,13 @@ __host__ __device__ constexpr uint32_t core_offset(int r, int k, int K) {
 }
 // bf16 inference weights, one device block: W2^T (128 x 64) and W3^T
 // (256 x 128) in the core-matrix layout; fp32 copies of all parameters
-// rounded to bf16 values (parameter order); W4 in bf16, element (c, j) at
-// ((c / 8) * 128 + j) * 8 + c % 8, so that one 16-byte load gives head
-// output j eight consecutive inputs; the small fp32 block (W1 and b1 as
-// float4 (w0j, w1j, w2j, b1j), b2, b3, b4, b5 (+1 pad), W5); and the
-// tensor-core kernel's own operands: W2^T extended by b2 as column 64
-// (128 x 80, K = 80: A1 carries a ones column there) and B1 (64 x 16): W1
-// rows 0-2 repeated three times (for the three bf16 terms of each FP32
-// coordinate) and b1 as column 9, so that layer 1 is one MMA.
+// rounded to bf16 values (parameter order); W4^T (128 x 256) in the
+// core-matrix layout; the small fp32 block (W1 and b1 as float4 (w0j, w1j,
+// w2j, b1j), b2, b3, b4, b5 (+1 pad), W5); and the tensor-core kernel's
+// own operands: W2^T extended by b2 as column 64 (128 x 80, K = 80: A1
+// carries a ones column there), B1 (64 x 16): W1 rows 0-2 repeated three
+// times (for the three bf16 terms of each FP32 coordinate) and b1 as
+// column 9, so that layer 1 is one MMA; and W5 in bf16 ([128][7]).
 constexpr int kTcW2Bytes = kD2 * kD1 * 2;           // 16 KB
 constexpr int kTcW3Bytes = kD3 * kD2 * 2;           // 64 KB
 constexpr int kTcF32Off = kTcW2Bytes + kTcW3Bytes;  // fp32 part after the bf16 operands
@@ -61,10 +60,13 @@ constexpr int kTcB2xOff = kTcSmallOff + kTcSmallBytes;
 constexpr int kTcB2xBytes = kD2 * kK2x * 2;         // 20 KB
 constexpr int kTcB1Off = kTcB2xOff + kTcB2xBytes;
 constexpr int kTcB1Bytes = kD1 * kK1 * 2;           // 2 KB
-constexpr int kTcBytes = kTcB1Off + kTcB1Bytes;
+constexpr int kTcW5hOff = kTcB1Off + kTcB1Bytes;
+constexpr int kTcW5hBytes = kD4 * kD5 * 2;          // 1792 B
+constexpr int kTcBytes = kTcW5hOff + kTcW5hBytes;
 static_assert(kTcW4Off % 16 == 0 && kTcSmallOff % 16 == 0 && kTcSmallBytes % 16 == 0 &&
-                  kTcB2xOff % 16 == 0 && kTcB1Off % 16 == 0 && kTcW2Bytes % 16 == 0 &&
-                  kTcW3Bytes % 16 == 0 && (4 * kSfB3) % 16 == 0 && (4 * kSfW5) % 16 == 0,
+                  kTcB2xOff % 16 == 0 && kTcB1Off % 16 == 0 && kTcW5hOff % 16 == 0 &&
+                  kTcW5hBytes % 16 == 0 && kTcW2Bytes % 16 == 0 && kTcW3Bytes % 16 == 0 &&
+                  kTcW4Bytes % 16 == 0 && (4 * kSfB3) % 16 == 0 && (4 * kSfW5) % 16 == 0,
               "bulk-copy alignment");
 
 }  // namespace prop
