@@ -233,6 +233,9 @@ __device__ void euler_two_vectors(d3 a, d3 b, double* ang) {
 
 constexpr int kBinCap = 4096;   // keys of one bin staged in shared memory
 constexpr int kPlaneThreads = 512;
+constexpr int kPlaneStage = kBinCap / 2;  // retained points that fit over the keys as float4
+constexpr int kSelCap = 256;              // retained keys sorted apart from the bin
+static_assert(kPlaneStage % kPlaneThreads == 0, "whole passes");
 constexpr int kScatterWarps = 4;
 
 __device__ void bitonic_sort(unsigned long long* a, int n2) {
@@ -316,14 +319,109 @@ __device__ void fit_plane_block(At at, int n, float* cen, double* red, PlaneD& o
   }
 }
 
+// Block-wide radix select: the k-th smallest (k >= 1) of n distinct 64-bit
+// keys at(0..n-1), 8 bits at a time from the top; it stops once the chosen
+// digit prefix holds a single key and finds that key.  Every thread calls
+// it and gets the key.  The keys of a bin share their high bytes (nearby
+// z), so histogram increments are combined per warp and digit.
+struct SelState {
+  unsigned long long prefix, found;
+  int k, unique;
+};
+template <typename At>
+__device__ unsigned long long radix_select(At at, int n, int k, unsigned* hist, SelState* ss) {
+  if (threadIdx.x == 0) {
+    ss->prefix = 0;
+    ss->k = k;
+    ss->unique = 0;
+  }
+  __syncthreads();
+  int shift = 56;
+  for (; shift >= 0; shift -= 8) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const unsigned long long pre = ss->prefix;
+    const unsigned long long hmask = shift == 56 ? 0ull : (~0ull << (shift + 8));
+    for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+      const int i = i0 + threadIdx.x;
+      int dg = -1;
+      if (i < n) {
+        const unsigned long long v = at(i);
+        if ((v & hmask) == pre) dg = (int)((v >> shift) & 255u);
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, dg);
+      if (dg >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+        atomicAdd(hist + dg, (unsigned)__popc(peers));
+    }
+    __syncthreads();
+    // the digit where the running count reaches k: warp 0, 8 bins a lane, a
+    // scan of the lane sums, then the owning lane's 8 bins
+    if (threadIdx.x < 32) {
+      const int ln = threadIdx.x;
+      unsigned sum = 0;
+      for (int j = 0; j < 8; ++j) sum += hist[ln * 8 + j];
+      unsigned incl = sum;
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (ln >= o) incl += y;
+      }
+      const int rem = ss->k;
+      if (rem > (int)(incl - sum) && rem <= (int)incl) {
+        int r = rem - (int)(incl - sum), dg = ln * 8;
+        for (int j = 0; j < 8; ++j, ++dg) {
+          const int cj = (int)hist[dg];
+          if (r <= cj) break;
+          r -= cj;
+        }
+        ss->prefix = pre | ((unsigned long long)dg << shift);
+        ss->k = r;
+        ss->unique = hist[dg] == 1u;
+      }
+    }
+    __syncthreads();
+    if (ss->unique) break;  // block-uniform
+  }
+  if (shift < 0) return ss->prefix;  // every byte chosen: the key itself
+  const unsigned long long m = ~0ull << shift, pre = ss->prefix;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned long long v = at(i);
+    if ((v & m) == pre) ss->found = v;  // exactly one key
+  }
+  __syncthreads();
+  return ss->found;
+}
+// The keys <= T of at(0..n-1) into out[0 ..), in any order; one counter
+// update per warp.
+template <typename At>
+__device__ void take_le(At at, int n, unsigned long long T, unsigned long long* out, int* cnt) {
+  if (threadIdx.x == 0) *cnt = 0;
+  __syncthreads();
+  for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    unsigned long long v = 0;
+    bool take = false;
+    if (i < n) {
+      v = at(i);
+      take = v <= T;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, take);
+    int base = 0;
+    if ((threadIdx.x & 31) == 0 && b) base = atomicAdd(cnt, __popc(b));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (take) out[base + __popc(b & ((1u << (threadIdx.x & 31)) - 1u))] = v;
+  }
+  __syncthreads();
+}
+
 // One block per bin: retained points, plane model, gates, features.
 __global__ void __launch_bounds__(kPlaneThreads, 3) k_plane(Dev d, KParams kp) {
   __shared__ unsigned long long keys[kBinCap];
   __shared__ unsigned int hist[256];
   __shared__ double red[6 * 32];
   __shared__ float cen[3];
-  __shared__ unsigned long long sel_prefix;
-  __shared__ int sel_k, s_cnt;
+  __shared__ unsigned long long sel[kSelCap];
+  __shared__ SelState ss;
+  __shared__ int s_cnt;
   const GroundView ground = ground_view(d.in);
   const int b = blockIdx.x;
   if (b >= d.n_bins) return;
@@ -337,7 +435,22 @@ __global__ void __launch_bounds__(kPlaneThreads, 3) k_plane(Dev d, KParams kp) {
   // the retained set sorted by (z, index); without retention, by index
   int kk = k;
   if (n > 0 && k > 0) {
-    if (n <= kBinCap) {
+    if (n <= kBinCap && retain && k <= kSelCap) {
+      // the k lowest of the staged keys: select the k-th, take the keys at
+      // or below it, sort those k (distinct keys: the same set and order as
+      // sorting all n)
+      for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = src[i];
+      __syncthreads();
+      auto at = [&](int i) { return keys[i]; };
+      const unsigned long long T = radix_select(at, n, k, hist, &ss);
+      take_le(at, n, T, sel, &s_cnt);
+      int m2 = 1;
+      while (m2 < k) m2 <<= 1;
+      for (int i = k + threadIdx.x; i < m2; i += blockDim.x) sel[i] = ~0ull;
+      __syncthreads();
+      bitonic_sort(sel, m2);
+      for (int i = threadIdx.x; i < k; i += blockDim.x) keys[i] = sel[i];
+    } else if (n <= kBinCap) {
       int n2 = 1;
       while (n2 < n) n2 <<= 1;
       for (int i = threadIdx.x; i < n2; i += blockDim.x)
@@ -348,67 +461,10 @@ __global__ void __launch_bounds__(kPlaneThreads, 3) k_plane(Dev d, KParams kp) {
       if (threadIdx.x == 0) atomicOr(&d.cnt->overflow, 8);
       kk = 0;
     } else {
-      // radix select of the k-th smallest 64-bit key, 8 bits at a time
-      if (threadIdx.x == 0) { sel_prefix = 0; sel_k = k; }
-      __syncthreads();
-      for (int shift = 56; shift >= 0; shift -= 8) {
-        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
-        __syncthreads();
-        const unsigned long long pre = sel_prefix;
-        const unsigned long long hmask = shift == 56 ? 0ull : (~0ull << (shift + 8));
-        // the keys of a bin share their high bytes (nearby z), so the
-        // histogram increments are combined per warp and digit
-        for (int i0 = 0; i0 < n; i0 += blockDim.x) {
-          const int i = i0 + threadIdx.x;
-          int dg = -1;
-          if (i < n) {
-            const unsigned long long v = src[i];
-            if ((v & hmask) == pre) dg = (int)((v >> shift) & 255u);
-          }
-          const unsigned peers = __match_any_sync(0xffffffffu, dg);
-          if (dg >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
-            atomicAdd(hist + dg, (unsigned)__popc(peers));
-        }
-        __syncthreads();
-        // the digit where the running count reaches sel_k: warp 0, 8 bins a
-        // lane, a scan of the lane sums, then the owning lane's 8 bins
-        if (threadIdx.x < 32) {
-          const int ln = threadIdx.x;
-          unsigned sum = 0;
-          for (int j = 0; j < 8; ++j) sum += hist[ln * 8 + j];
-          unsigned incl = sum;
-          for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (ln >= o) incl += y;
-          }
-          const int rem = sel_k;
-          if (rem > (int)(incl - sum) && rem <= (int)incl) {
-            int r = rem - (int)(incl - sum), dg = ln * 8;
-            for (int j = 0; j < 8; ++j, ++dg) {
-              const int cj = (int)hist[dg];
-              if (r <= cj) break;
-              r -= cj;
-            }
-            sel_prefix = pre | ((unsigned long long)dg << shift);
-            sel_k = r;
-          }
-        }
-        __syncthreads();
-      }
-      const unsigned long long T = sel_prefix;  // k-th smallest (keys unique)
-      if (threadIdx.x == 0) s_cnt = 0;
-      __syncthreads();
-      // the k keys <= T, one counter update per warp (sorted below)
-      for (int i0 = 0; i0 < n; i0 += blockDim.x) {
-        const int i = i0 + threadIdx.x;
-        const bool take = i < n && src[i] <= T;
-        const unsigned b = __ballot_sync(0xffffffffu, take);
-        int base = 0;
-        if ((threadIdx.x & 31) == 0 && b) base = atomicAdd(&s_cnt, __popc(b));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (take) keys[base + __popc(b & ((1u << (threadIdx.x & 31)) - 1u))] = src[i];
-      }
-      __syncthreads();
+      // the same from global memory, the k keys sorted in the key array
+      auto at = [&](int i) { return src[i]; };
+      const unsigned long long T = radix_select(at, n, k, hist, &ss);
+      take_le(at, n, T, keys, &s_cnt);
       int n2 = 1;
       while (n2 < k) n2 <<= 1;
       for (int i = k + threadIdx.x; i < n2; i += blockDim.x) keys[i] = ~0ull;
@@ -418,10 +474,36 @@ __global__ void __launch_bounds__(kPlaneThreads, 3) k_plane(Dev d, KParams kp) {
   }
   __syncthreads();
   const bool enough = kk > 0 && kk >= kp.G && kk >= 3;
-  if (enough) {
-    fit_plane_block([&](int i) { return ground[(uint32_t)keys[i]]; }, kk, cen, red, out);
+  if (enough && kk <= kPlaneStage) {
+    // the retained points gathered once into shared memory (over the key
+    // array: every key is read into registers before the first point is
+    // written), so that the sequential centroid, the scatter and the
+    // features read shared memory instead of two dependent global loads
+    float4* sp = reinterpret_cast<float4*>(keys);
+    uint32_t gi[kPlaneStage / kPlaneThreads];
+#pragma unroll
+    for (int q = 0; q < kPlaneStage / kPlaneThreads; ++q) {
+      const int i = threadIdx.x + q * kPlaneThreads;
+      gi[q] = i < kk ? (uint32_t)keys[i] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kPlaneStage / kPlaneThreads; ++q) {
+      const int i = threadIdx.x + q * kPlaneThreads;
+      if (i < kk) sp[i] = ground[gi[q]];
+    }
+    __syncthreads();
+    fit_plane_block([&](int i) { return sp[i]; }, kk, cen, red, out);
     if (threadIdx.x == 0) {
       out.valid = 1;  // fitted; the gates follow in k_plane_compact
+      d.plane_all[b] = out;
+    }
+    for (int i = threadIdx.x; i < kp.G; i += blockDim.x)
+      d.plane_feat_all[(size_t)b * kp.G + i] = sp[i];
+  } else if (enough) {
+    fit_plane_block([&](int i) { return ground[(uint32_t)keys[i]]; }, kk, cen, red, out);
+    if (threadIdx.x == 0) {
+      out.valid = 1;
       d.plane_all[b] = out;
     }
     for (int i = threadIdx.x; i < kp.G; i += blockDim.x)
