@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(1024) k_gbin_scan(Dev d) {
 }
 
 // Scatter of (z key, index) into the bins; the order inside a bin is free
-// (k_plane orders every bin by key).
+// (k_plane orders the keys it retains).
 __global__ void __launch_bounds__(256) k_gbin_scatter(Dev d) {
   __shared__ int hist[kMaxBins];
   const GroundView ground = ground_view(d.in);

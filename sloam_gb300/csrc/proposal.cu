@@ -1,10 +1,10 @@
 // proposal.cu — the learned cylinder proposal (network layout in
 // proposal.cuh): synthetic training clusters, FP32 training kernels
 // (forward + backward per cluster, a deterministic gradient reduction,
-// Adam), and BF16 inference -- the two dense layers (128 points x 64 -> 128
-// and 128 x 128 -> 256) on the 5th-generation tensor cores (tcgen05.mma,
-// operands in shared memory, accumulators in TMEM), with a SIMT kernel of
-// the same arithmetic as the reference it is checked against.
+// Adam), and BF16 inference -- every layer of the shared MLP and the head
+// on the 5th-generation tensor cores (tcgen05.mma, operands in shared
+// memory by bulk copy, accumulators in TMEM), with a SIMT kernel of the same
+// bf16 operands as the reference it is checked against.
 //
 // Training clusters: a trunk of radius U(0.05, 0.8) m, axis tilt U(0, 15)
 // deg, 2-20 m from the sensor, the arc that faces the sensor minus an
