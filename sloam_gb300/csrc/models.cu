@@ -103,43 +103,57 @@ __device__ __forceinline__ int warp_bin_add(int* hist, int bin, int lane) {
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(256, 8) k_gbin(Dev d, KParams kp) {
+// The ground binning kernels take kGbinPer points per thread (slices of 256
+// in point order), all of their loads issued before use.
+constexpr int kGbinPer = 4;
+constexpr int kGbinSpan = 256 * kGbinPer;
+
+__global__ void __launch_bounds__(256, 5) k_gbin(Dev d, KParams kp) {
   __shared__ int hist[kMaxBins];
   const GroundView ground = ground_view(d.in);
   const int n = d.cnt->n_ground;
-  if (blockIdx.x * blockDim.x >= n) return;
+  if (blockIdx.x * kGbinSpan >= n) return;
   const int lane = threadIdx.x & 31;
   for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x) hist[b] = 0;
   __syncthreads();
   int slow = 0;
-  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
-    const int i = i0 + threadIdx.x;
-    int bin = -1;
-    if (i < n) {
-      const float4 p = ground[i];
-      const float dx = fsub(0.0f, p.x), dy = fsub(0.0f, p.y);
-      const float r = fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
-      if (r >= d.r_lo && r <= d.r_hi) {
-        const float y = fsub(p.y, 0.0f), x = fsub(p.x, 0.0f);
-        float th = atan2f(y, x);
-        int tb;
-        bool need = !(isfinite(x) && isfinite(y)) || x == 0.0f || y == 0.0f;
-        if (!need) {
-          const float m = fmaxf(fabsf(th) * 1.2e-6f, 1e-30f);
-          tb = bin_from_table(d.tb_tab, th - m, kp.Tb);
-          need = tb != bin_from_table(d.tb_tab, th + m, kp.Tb);
-        }
-        if (need) {
-          th = (float)atan2((double)y, (double)x);
-          tb = bin_from_table(d.tb_tab, th, kp.Tb);
-          ++slow;
-        }
-        const int rb = bin_from_table(d.rb_tab, r, kp.Rb);
-        bin = rb * kp.Tb + tb;
-      }
-      d.bin_of[i] = bin;
+  for (int i0 = blockIdx.x * kGbinSpan; i0 < n; i0 += gridDim.x * kGbinSpan) {
+    float4 pts[kGbinPer];
+#pragma unroll
+    for (int u = 0; u < kGbinPer; ++u) {
+      const int i = i0 + u * 256 + threadIdx.x;
+      if (i < n) pts[u] = ground[i];
     }
-    warp_bin_add(hist, bin, lane);
+#pragma unroll
+    for (int u = 0; u < kGbinPer; ++u) {
+      const int i = i0 + u * 256 + threadIdx.x;
+      int bin = -1;
+      if (i < n) {
+        const float4 p = pts[u];
+        const float dx = fsub(0.0f, p.x), dy = fsub(0.0f, p.y);
+        const float r = fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
+        if (r >= d.r_lo && r <= d.r_hi) {
+          const float y = fsub(p.y, 0.0f), x = fsub(p.x, 0.0f);
+          float th = atan2f(y, x);
+          int tb;
+          bool need = !(isfinite(x) && isfinite(y)) || x == 0.0f || y == 0.0f;
+          if (!need) {
+            const float m = fmaxf(fabsf(th) * 1.2e-6f, 1e-30f);
+            tb = bin_from_table(d.tb_tab, th - m, kp.Tb);
+            need = tb != bin_from_table(d.tb_tab, th + m, kp.Tb);
+          }
+          if (need) {
+            th = (float)atan2((double)y, (double)x);
+            tb = bin_from_table(d.tb_tab, th, kp.Tb);
+            ++slow;
+          }
+          const int rb = bin_from_table(d.rb_tab, r, kp.Rb);
+          bin = rb * kp.Tb + tb;
+        }
+        d.bin_of[i] = bin;
+      }
+      warp_bin_add(hist, bin, lane);
+    }
   }
   __syncthreads();
   for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x)
@@ -171,20 +185,36 @@ __global__ void __launch_bounds__(256) k_gbin_scatter(Dev d) {
   __shared__ int hist[kMaxBins];
   const GroundView ground = ground_view(d.in);
   const int n = d.cnt->n_ground;
-  if (blockIdx.x * blockDim.x >= n) return;
+  if (blockIdx.x * kGbinSpan >= n) return;
   const int lane = threadIdx.x & 31;
-  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
-    const int i = i0 + threadIdx.x;
+  for (int i0 = blockIdx.x * kGbinSpan; i0 < n; i0 += gridDim.x * kGbinSpan) {
+    int bin[kGbinPer], local[kGbinPer];
+    float z[kGbinPer];
+#pragma unroll
+    for (int u = 0; u < kGbinPer; ++u) {
+      const int i = i0 + u * 256 + threadIdx.x;
+      bin[u] = -1;
+      z[u] = 0.0f;
+      if (i < n) {
+        bin[u] = d.bin_of[i];
+        z[u] = ground[i].z;
+      }
+    }
     for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x) hist[b] = 0;
     __syncthreads();
-    const int bin = i < n ? d.bin_of[i] : -1;
-    const int local = warp_bin_add(hist, bin, lane);
+#pragma unroll
+    for (int u = 0; u < kGbinPer; ++u) local[u] = warp_bin_add(hist, bin[u], lane);
     __syncthreads();
     for (int b = threadIdx.x; b < d.n_bins; b += blockDim.x)
       if (hist[b]) hist[b] = atomicAdd(d.bin_cnt + b, hist[b]);
     __syncthreads();
-    if (bin >= 0)
-      d.bin_keys[hist[bin] + local] = ((unsigned long long)zkey(ground[i].z) << 32) | (uint32_t)i;
+#pragma unroll
+    for (int u = 0; u < kGbinPer; ++u) {
+      const int i = i0 + u * 256 + threadIdx.x;
+      if (bin[u] >= 0)
+        d.bin_keys[hist[bin[u]] + local[u]] =
+            ((unsigned long long)zkey(z[u]) << 32) | (uint32_t)i;
+    }
     __syncthreads();
   }
 }
@@ -1545,7 +1575,7 @@ int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStr
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
   int n = 0;
   k_zero_bins<<<1, 256, 0, st>>>(d);
-  const int gg = (d.cap_ground + 255) / 256;
+  const int gg = (d.cap_ground + kGbinSpan - 1) / kGbinSpan;
   k_gbin<<<gg < 1 ? 1 : gg, 256, 0, st>>>(d, kp);
   k_gbin_scan<<<1, 1024, 0, st>>>(d);
   k_gbin_scatter<<<gg < 1 ? 1 : gg, 256, 0, st>>>(d);
