@@ -39,7 +39,8 @@ __host__ __device__ constexpr uint32_t core_offset(int r, int k, int K) {
 // (256 x 128) in the core-matrix layout; fp32 copies of all parameters
 // rounded to bf16 values (parameter order); W4^T (128 x 256) in the
 // core-matrix layout; the small fp32 block (W1 and b1 as float4 (w0j, w1j,
-// w2j, b1j), b2, b3, b4, b5 (+1 pad), W5); and the tensor-core kernel's
+// w2j, b1j), b2, b3, b4, b5 (+1 pad), W5, of which the tensor-core kernel
+// copies b3, b4 and b5; the rest is spare); and the tensor-core kernel's
 // own operands: W2^T extended by b2 as column 64 (128 x 80, K = 80: A1
 // carries a ones column there), B1 (64 x 16): W1 rows 0-2 repeated three
 // times (for the three bf16 terms of each FP32 coordinate) and b1 as
