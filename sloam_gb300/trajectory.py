@@ -2,10 +2,9 @@
 through a forest on piecewise-planar terrain, each keyframe run the way
 SLOAMNode::run does it (sloamNode.cpp:186-282): pose estimate = previous
 estimated pose composed with an odometry increment, submap query, keyframe,
-map update.  Reports drift against ground truth for the GPU path (plain
-RANSAC and learned proposals) and for the CPU restatement of the reference.
-
-    python -m sloam_gb300.trajectory --kf 200 --h 128 --w 2048
+map update.  The scene generator, the host map manager, the keyframe loop
+and the drift figures live here; `trajectory_run.py` (beside `bench.py`)
+runs them on the GPU path and on the CPU restatement of the reference.
 
 Scenes (configuration 5 of the benchmark set): 200 keyframes of 128x2048,
 1 m per keyframe, yaw rate at most 15 deg per keyframe, a 1 000-tree forest
@@ -14,9 +13,7 @@ on a triangulated height field (planar facets, slope at most 20 deg), a
 with PyTorch on the device given (the GPU for full size), a data generator
 only.
 """
-import argparse
 import ctypes as C
-import json
 import math
 import time
 
@@ -346,93 +343,9 @@ def gpu_keyframe_fn(ctx):
     return kf
 
 
-def oracle_keyframe_fn(L, s):
-    from . import capi as A
-
-    def kf(P, xyzi, lab, pose, mp):
-        r = A.RunBuffers(P)
-        mapc = A.cylinders_from_array(mp) if len(mp) else None
-        st = L.oracle_keyframe(s, A.ptr(xyzi, C.c_float), len(xyzi), A.ptr(lab, C.c_uint8), None,
-                               C.byref(A.SE3.from_qt(synth.quat_from_R(pose[0]), pose[1])), mapc,
-                               len(mp), C.byref(r.s))
-        r.refresh()
-        q, t = r.s.T_Map_Curr.qt()
-        n = r.s.models.n_cylinders
-        return st, r.s.success, (synth.R_from_quat(q), t), r.m.cyl_array()[:n], r.matches[:n]
-    return kf
-
-
 def params(H, W, cyl_mode, gn_iters=15, submap=1000):
     cfg = synth.SceneConfig(H=H, W=W, disc=30.0)
     # the reference's default two-step pose (sloam.yaml): on slopes above the
     # 0.1 rad plane gate the trees alone still fix x, y and yaw
     return synth.preset_params(cfg, two_step_optim=1, cyl_mode=cyl_mode, gn_iters=gn_iters,
                                max_map=max(submap, 128), batch_slots=1)
-
-
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--kf", type=int, default=200)
-    ap.add_argument("--h", type=int, default=128)
-    ap.add_argument("--w", type=int, default=2048)
-    ap.add_argument("--trees", type=int, default=1000)
-    ap.add_argument("--submap", type=int, default=1000)
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--oracle", type=int, default=1, help="also run the CPU restatement")
-    ap.add_argument("--out", default=None)
-    a = ap.parse_args()
-    import torch
-    from . import proposal
-    from .lib import Context
-    dev = "cuda" if torch.cuda.is_available() else "cpu"
-    t0 = time.perf_counter()
-    poses, odo, forest, terrain, scans = scene(a.seed, a.kf, a.h, a.w, a.trees, dev)
-    gen_s = time.perf_counter() - t0
-    res = {"config": {"keyframes": a.kf, "H": a.h, "W": a.w, "trees": a.trees,
-                      "submap": a.submap, "gn_iters": 15, "seed": a.seed,
-                      "scene_seconds": gen_s}}
-    ests = {}
-    for name, mode in (("gpu_plain", 1), ("gpu_learned", 2)):
-        P = params(a.h, a.w, mode, submap=a.submap)
-        ctx = Context(P)
-        if mode == 2:
-            ctx.set_proposal_weights(proposal.load_weights())
-        est, dt = run(gpu_keyframe_fn(ctx), P, poses, odo, scans, a.submap)
-        res[name] = dict(drift(poses, est), seconds=dt, keyframes_per_s=a.kf / dt)
-        ests[name] = est
-        ctx.close()
-    # the plain path with the map manager on the GPU (sloam_keyframe_mapped)
-    from .lib import DeviceMapManager
-    P = params(a.h, a.w, 1, submap=a.submap)
-    ctx = Context(P)
-    dm = DeviceMapManager(capacity=max(4 * a.trees, 4096), k=a.submap, recent=200)
-    est, dt = run_mapped(ctx, dm, P, poses, odo, scans)
-    dev_t = max(float(np.abs(np.asarray(e[1]) - np.asarray(h[1])).max())
-                for e, h in zip(est, ests["gpu_plain"]))
-    res["gpu_plain_device_map"] = dict(drift(poses, est), seconds=dt,
-                                       keyframes_per_s=a.kf / dt,
-                                       max_translation_diff_vs_host_map_m=dev_t,
-                                       map_size=dm.size()[0])
-    dm.close()
-    ctx.close()
-    if a.oracle:
-        from oracle import loader
-        L = loader.lib()
-        P = params(a.h, a.w, 1, submap=a.submap)
-        s = L.oracle_create(C.byref(P))
-        est, dt = run(oracle_keyframe_fn(L, s), P, poses, odo, scans, a.submap)
-        L.oracle_destroy(s)
-        res["cpu_reference_port"] = dict(drift(poses, est), seconds=dt, keyframes_per_s=a.kf / dt)
-    odo_only = [poses[0]]
-    for d in odo:
-        odo_only.append(_compose(odo_only[-1][0], odo_only[-1][1], *d))
-    res["odometry_only"] = drift(poses, odo_only)
-    line = json.dumps(res)
-    print(line)
-    if a.out:
-        with open(a.out, "w") as f:
-            f.write(line + "\n")
-
-
-if __name__ == "__main__":
-    main()

@@ -1,6 +1,6 @@
 """Converts the reference's own test fixtures into compact arrays.
 
-Reads (from a KumarRobotics/sloam checkout, default /root/reference):
+Reads (from a KumarRobotics/sloam checkout given on the command line):
   sloam/src/tests/aux/{still,moving}_tree_t{0,1}.pcd   organised 64x2048 tree clouds
   sloam/src/tests/aux/{still,moving}_landmarks_t{0,1}  Boost text archives of the
                                                         Trellis output for each cloud
@@ -15,7 +15,7 @@ TreeVertex is `treeId beam prevVertexSize radius isValid coords points` with
 coords = x y z and points a collection of x y z; the first occurrence of every
 class is preceded by a `0 0` class-info pair.
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py <reference_root>
 """
 import os
 import sys
@@ -118,4 +118,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference_root>")
+    main(sys.argv[1])

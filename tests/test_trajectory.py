@@ -75,6 +75,7 @@ def test_scene_scan_on_cpu():
 def test_short_trajectory_gpu_and_oracle():
     import ctypes as C
     from oracle import loader
+    import trajectory_run
     from sloam_gb300.lib import Context
     poses, odo, forest, ter, scans = TJ.scene(seed=0, n_kf=12, H=64, W=1024, n_trees=300,
                                               device="cuda")
@@ -84,7 +85,7 @@ def test_short_trajectory_gpu_and_oracle():
     ctx.close()
     L = loader.lib()
     s = L.oracle_create(C.byref(P))
-    est_o, _ = TJ.run(TJ.oracle_keyframe_fn(L, s), P, poses, odo, scans, 300)
+    est_o, _ = TJ.run(trajectory_run.oracle_keyframe_fn(L, s), P, poses, odo, scans, 300)
     L.oracle_destroy(s)
     dg, do = TJ.drift(poses, est_g), TJ.drift(poses, est_o)
     print(dg, do)
