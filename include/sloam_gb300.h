@@ -120,6 +120,13 @@ typedef struct sloam_params {
                                        lm_max_iters iterations, default
                                        trust-region options)              */
   int32_t lm_max_iters;             /* max_num_iterations (sloam.cpp:92) (50) */
+  /* shape of the point-level cylinder fit's work queue (modes 1 and 2):
+     chosen per GPU and workload by sloam_gb300/autotune.py            */
+  int32_t cyl_chunk_points;         /* points per work item: 256, 512 or
+                                       1024                          (256) */
+  int32_t cyl_hyp_tile;             /* hypotheses staged per pass: 64, 128,
+                                       256, 512 or 1024              (256) */
+  int32_t cyl_queue_blocks;         /* persistent blocks (0: 152)          */
 } sloam_params;
 
 void sloam_params_default(sloam_params* p);
@@ -250,8 +257,9 @@ int sloam_compute_models(sloam_ctx* ctx, const sloam_se3* pose_estimate,
                          sloam_models_out* out);
 
 /* Plane::Plane(points, fmParams) (plane.cpp:3-17, computeModel :96-128):
- * the plane of all n points (float centroid, smallest-eigenvalue normal,
- * sign canonical n_z > 0), valid iff n >= num_ground_features (no gates;
+ * the plane of all n points (float centroid, smallest-eigenvalue normal
+ * with the sign Eigen 3.3's JacobiSVD gives it, as the reference's
+ * plane.cpp:113-115 does), valid iff n >= num_ground_features (no gates;
  * those belong to computeModels).  features [num_ground_features*4]
  * receives the first points (may be NULL).  n <= max_ground. */
 int sloam_fit_plane(sloam_ctx* ctx, const float* xyzi, int32_t n, sloam_plane* out,
@@ -357,6 +365,32 @@ int sloam_pack_points(const void* d_points, int32_t n, int32_t point_step, int32
  * until weights are set. */
 int sloam_set_proposal_weights(sloam_ctx* ctx, const float* weights, int32_t n);
 
+/* Training and evaluation of the proposal network (no reference
+ * counterpart; sloam_gb300/proposal.py drives them).  They run on the
+ * current device with their own temporaries.
+ * sloam_prop_num_params: 75399.
+ * sloam_prop_sample: n synthetic trunk clusters, Philox-keyed by (seed,
+ *   first_id + i): d_points [n*128*3] centred and scale-normalised,
+ *   d_targets [n*8] (axis, centre xy, log(r/s), s, r).
+ * sloam_prop_train: `steps` Adam steps (lr, betas 0.9/0.999, eps 1e-8) of
+ *   `batch` fresh clusters each (samples of seed ^ 0x5a5a5a5a, ids from
+ *   first_id), from `init` (NULL: seeded uniform init); weights_out
+ *   [75399], loss_out [steps] mean losses (may be NULL).
+ * sloam_prop_grad: one step's mean gradient grad_out [75399] (and the n
+ *   per-cluster losses, loss_out may be NULL) of `weights` on device
+ *   samples, without the update.
+ * sloam_prop_infer: network outputs d_out [n*8] for device samples; mode 0
+ *   the tensor-core kernel, 1 the SIMT kernel of the same arithmetic. */
+int sloam_prop_num_params(void);
+int sloam_prop_sample(uint64_t seed, int64_t first_id, int32_t n, float* d_points,
+                      float* d_targets);
+int sloam_prop_train(const float* init, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                     int64_t first_id, float* weights_out, float* loss_out);
+int sloam_prop_grad(const float* weights, const float* d_points, const float* d_targets,
+                    int32_t n, float* grad_out, float* loss_out);
+int sloam_prop_infer(const float* weights, const float* d_points, int32_t n, float* d_out,
+                     int32_t mode);
+
 /* Projection + masking that allocates nothing (no reference counterpart: it
  * exists for callers that cannot call cudaMalloc, such as plugins inside a
  * process whose allocator owns the GPU or real-time loops that forbid
@@ -369,8 +403,10 @@ int sloam_set_proposal_weights(sloam_ctx* ctx, const float* weights, int32_t n);
  * [n], d_n_ground [1], d_tree_cloud [H*W*4] and, optionally (NULL skips),
  * d_pix [n] (py*W + px), d_range_image [H*W], d_mask_out [H*W].  `stream`
  * is a cudaStream_t (NULL = legacy default stream); results are ready when
- * the stream reaches them.  The first call on a device looks up the array's
- * address (make it before any stream capture).  All calls share the one
+ * the stream reaches them.  The first call in each CUDA context (a device's
+ * primary context, or one the caller made current) looks up the array's
+ * address in that context (make it before any stream capture).  All calls
+ * of a context share the one
  * array: calls that overlap on the GPU (other streams, other threads) race.
  * Host code must treat the array only through this entry point. */
 int sloam_project_mask_noalloc(const sloam_params* params, const float* d_xyzi, int32_t n,
@@ -424,6 +460,15 @@ int64_t sloam_last_launch_count(const sloam_ctx* ctx);
 
 /* The CUDA stream the context runs on (as void*). */
 void* sloam_stream(sloam_ctx* ctx);
+
+/* Retry limit of one connected-components union (no reference counterpart:
+ * the union is a compare-and-swap loop that contention can repeat).  When a
+ * union runs out of rounds the kernel records it and returns, and the call
+ * ends with SLOAM_ERR_TIMEOUT and "connected-components union loop hit its
+ * iteration limit"; the context stays usable.  limit < 0 restores the
+ * default (2^20); 0 makes every union that is needed give up at once
+ * (used to test that path).  Drops the captured keyframe graphs. */
+int sloam_set_cc_iter_limit(sloam_ctx* ctx, int32_t limit);
 
 #ifdef __cplusplus
 }

@@ -72,5 +72,6 @@ def lib():
     L.oracle_plane_distance_point.argtypes = [C.POINTER(A.Plane), C.POINTER(C.c_float)]
     L.oracle_plane_project.argtypes = [C.POINTER(A.Plane), C.POINTER(A.SE3)]
     L.oracle_philox.argtypes = [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    L.oracle_eigen_svd_u3.argtypes = [C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_double)]
     _lib = L
     return L

@@ -5,9 +5,11 @@
 // KumarRobotics/sloam repository).  Where the reference delegates to a
 // third-party library that is absent here (PCL 1.10, Eigen 3.3, Ceres
 // @206061a), the published behaviour of that library is restated and the
-// choice is named in the comment.  Where the reference is not deterministic
-// (std::sort ties, PCL's internal RANSAC RNG, Eigen's SVD sign, Ceres LM) the
-// contract of this project is stated instead; the GPU kernels follow the same
+// choice is named in the comment (Eigen's JacobiSVD, down to the sign of the
+// plane normal, is restated step by step).  Where the reference is not
+// deterministic or its library is not restated (std::sort ties, PCL's
+// internal RANSAC RNG, Ceres LM) the contract of this project is stated
+// instead; the GPU kernels follow the same
 // contract and are checked bit-exact on integers against this file.
 //
 // Build: g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared (see build.py);
@@ -558,12 +560,190 @@ struct PlaneObj {  // Plane, plane.h / plane.cpp
   int bin = 0;
 };
 
+// The sign of the normal Plane::computeModel gets from
+// `JacobiSVD<MatrixX>(centeredGf, ComputeThinU | ComputeThinV).matrixU()
+// .col(2)` (plane.cpp:113-115), restated from Eigen 3.3.7 (Ubuntu 20.04's
+// libeigen3-dev, the version ROS Noetic builds against; not in the
+// reference tree): JacobiSVD::compute (scaling by the largest |entry|), the
+// ColPivHouseholderQR preconditioner for more columns than rows (QR of the
+// adjoint with column pivoting and norm downdates; work matrix = R^T; U
+// starts as the column permutation), the two-sided Jacobi sweep
+// (real_2x2_jacobi_svd, JacobiRotation::makeJacobi), the positive-diagonal
+// sign fix of U and the descending sort.  Only the third column of U is
+// returned; its sign decides the plane gate (sloam.cpp:402-406), where a
+// downward normal fails the Euler-angle test.  `a` holds the 3 x n centred
+// coordinates row by row.
+void eigen_jacobi_svd_u3(const std::vector<double>& a_in, int n, double u3[3]) {
+  const double kMin = std::numeric_limits<double>::min();
+  const double kEps = std::numeric_limits<double>::epsilon();
+  double scale = 0.0;
+  for (double v : a_in) scale = std::max(scale, std::fabs(v));
+  if (scale == 0.0) scale = 1.0;
+  // m = (A / scale)^T, n x 3, column-major: m[j * n + i]
+  std::vector<double> m((size_t)3 * n);
+  for (int r = 0; r < 3; ++r)
+    for (int i = 0; i < n; ++i) m[(size_t)r * n + i] = a_in[(size_t)r * n + i] / scale;
+  auto col = [&](int j) { return m.data() + (size_t)j * n; };
+  // ColPivHouseholderQR::computeInPlace
+  double nu[3], nd[3];
+  for (int j = 0; j < 3; ++j) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += col(j)[i] * col(j)[i];
+    nd[j] = nu[j] = std::sqrt(s);
+  }
+  const double downdate_thr = std::sqrt(kEps);
+  int trans[3];
+  const int size = std::min(n, 3);
+  for (int k = 0; k < size; ++k) {
+    int big = k;
+    for (int j = k + 1; j < 3; ++j)
+      if (nu[j] > nu[big]) big = j;  // maxCoeff: first index of the maximum
+    trans[k] = big;
+    if (big != k) {
+      for (int i = 0; i < n; ++i) std::swap(col(k)[i], col(big)[i]);
+      std::swap(nu[k], nu[big]);
+      std::swap(nd[k], nd[big]);
+    }
+    // makeHouseholderInPlace on col(k)[k..n)
+    double* c = col(k);
+    double tail = 0;
+    for (int i = k + 1; i < n; ++i) tail += c[i] * c[i];
+    const double c0 = c[k];
+    double tau, beta;
+    if (tail <= kMin) {
+      tau = 0.0;
+      beta = c0;
+      for (int i = k + 1; i < n; ++i) c[i] = 0.0;
+    } else {
+      beta = std::sqrt(c0 * c0 + tail);
+      if (c0 >= 0.0) beta = -beta;
+      for (int i = k + 1; i < n; ++i) c[i] = c[i] / (c0 - beta);
+      tau = (beta - c0) / beta;
+    }
+    c[k] = beta;
+    // applyHouseholderOnTheLeft to the columns right of k, rows k..n
+    if (tau != 0.0) {
+      for (int j = k + 1; j < 3; ++j) {
+        double* x = col(j);
+        double tmp = 0;
+        for (int i = k + 1; i < n; ++i) tmp += c[i] * x[i];
+        tmp += x[k];
+        x[k] -= tau * tmp;
+        for (int i = k + 1; i < n; ++i) x[i] -= tau * c[i] * tmp;
+      }
+    }
+    for (int j = k + 1; j < 3; ++j) {
+      if (nu[j] != 0.0) {
+        double t = std::fabs(col(j)[k]) / nu[j];
+        t = (1.0 + t) * (1.0 - t);
+        t = t < 0.0 ? 0.0 : t;
+        const double t2 = t * (nu[j] / nd[j]) * (nu[j] / nd[j]);
+        if (t2 <= downdate_thr) {
+          double s = 0;
+          for (int i = k + 1; i < n; ++i) s += col(j)[i] * col(j)[i];
+          nd[j] = nu[j] = std::sqrt(s);
+        } else {
+          nu[j] *= std::sqrt(t);
+        }
+      }
+    }
+  }
+  int idx[3] = {0, 1, 2};
+  for (int k = 0; k < size; ++k) std::swap(idx[k], idx[trans[k]]);
+  // W = R^T (lower triangular), U = the permutation matrix
+  double W[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, U[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j <= i; ++j) W[i][j] = col(i)[j];
+  for (int i = 0; i < 3; ++i) U[idx[i]][i] = 1.0;
+  // rotations: (c, s) applied as x' = c x + s y, y' = -s x + c y
+  auto rows = [&](double M[3][3], int p, int q, double c, double s) {
+    for (int i = 0; i < 3; ++i) {
+      const double x = M[p][i], y = M[q][i];
+      M[p][i] = c * x + s * y;
+      M[q][i] = -s * x + c * y;
+    }
+  };
+  auto cols = [&](double M[3][3], int p, int q, double c, double s) {  // applyOnTheRight(j)
+    for (int i = 0; i < 3; ++i) {
+      const double x = M[i][p], y = M[i][q];
+      M[i][p] = c * x - s * y;
+      M[i][q] = s * x + c * y;
+    }
+  };
+  double maxd = std::max({std::fabs(W[0][0]), std::fabs(W[1][1]), std::fabs(W[2][2])});
+  const double precision = 2.0 * kEps;
+  bool finished = false;
+  for (int sweep = 0; !finished && sweep < 100; ++sweep) {
+    finished = true;
+    for (int p = 1; p < 3; ++p) {
+      for (int q = 0; q < p; ++q) {
+        const double thr = std::max(kMin, precision * maxd);
+        if (!(std::fabs(W[p][q]) > thr || std::fabs(W[q][p]) > thr)) continue;
+        finished = false;
+        // real_2x2_jacobi_svd
+        double mm[2][2] = {{W[p][p], W[p][q]}, {W[q][p], W[q][q]}};
+        const double t = mm[0][0] + mm[1][1], d = mm[1][0] - mm[0][1];
+        double c1, s1;
+        if (std::fabs(d) < kMin) {
+          c1 = 1.0;
+          s1 = 0.0;
+        } else {
+          const double u = t / d, tmp = std::sqrt(1.0 + u * u);
+          s1 = 1.0 / tmp;
+          c1 = u / tmp;
+        }
+        for (int i = 0; i < 2; ++i) {
+          const double x = mm[0][i], y = mm[1][i];
+          mm[0][i] = c1 * x + s1 * y;
+          mm[1][i] = -s1 * x + c1 * y;
+        }
+        // makeJacobi(m(0,0), m(0,1), m(1,1))
+        double cr = 1.0, sr = 0.0;
+        {
+          const double x = mm[0][0], y = mm[0][1], z = mm[1][1];
+          const double deno = 2.0 * std::fabs(y);
+          if (!(deno < kMin)) {
+            const double tau = (x - z) / deno, w = std::sqrt(tau * tau + 1.0);
+            const double tt = tau > 0.0 ? 1.0 / (tau + w) : 1.0 / (tau - w);
+            const double sign_t = tt > 0.0 ? 1.0 : -1.0;
+            const double nn = 1.0 / std::sqrt(tt * tt + 1.0);
+            sr = -sign_t * (y / std::fabs(y)) * std::fabs(tt) * nn;
+            cr = nn;
+          }
+        }
+        // j_left = rot1 * j_right^T, with j_right^T = (cr, -sr)
+        const double lc = c1 * cr - s1 * (-sr), ls = c1 * (-sr) + s1 * cr;
+        rows(W, p, q, lc, ls);
+        cols(U, p, q, lc, -ls);  // U.applyOnTheRight(p, q, j_left^T)
+        cols(W, p, q, cr, sr);
+        maxd = std::max({maxd, std::fabs(W[p][p]), std::fabs(W[q][q])});
+      }
+    }
+  }
+  double sv[3];
+  for (int i = 0; i < 3; ++i) {
+    sv[i] = std::fabs(W[i][i]);
+    if (W[i][i] < 0.0)
+      for (int r = 0; r < 3; ++r) U[r][i] = -U[r][i];
+  }
+  for (int i = 0; i < 3; ++i) {
+    int pos = i;
+    for (int j = i + 1; j < 3; ++j)
+      if (sv[j] > sv[pos]) pos = j;
+    if (sv[pos] == 0.0) break;
+    if (pos != i) {
+      std::swap(sv[i], sv[pos]);
+      for (int r = 0; r < 3; ++r) std::swap(U[r][i], U[r][pos]);
+    }
+  }
+  for (int r = 0; r < 3; ++r) u3[r] = U[r][2];
+}
+
 // Plane::computeModel, plane.cpp:96-128.  Centroid accumulated in float in
 // feature order (utils.h:14-28); the 3xN SVD normal (left singular vector of
 // the smallest singular value) is the eigenvector of the smallest eigenvalue
-// of the FP64 scatter matrix.  Contract: the sign of the normal is chosen so
-// that n_z > 0 (then n_y > 0, then n_x > 0), Eigen's SVD sign being
-// unspecified.
+// of the FP64 scatter matrix, with the sign Eigen's JacobiSVD gives it
+// (eigen_jacobi_svd_u3 above).
 void plane_model(PlaneObj& pl) {
   Pt cen{0, 0, 0, 0};
   for (const Pt& p : pl.features) {
@@ -584,8 +764,18 @@ void plane_model(PlaneObj& pl) {
   double ev[3], V[9];
   jacobi3(S, ev, V);
   V3 nrm{V[0], V[3], V[6]};
-  bool flip = nrm.z < 0 || (nrm.z == 0 && (nrm.y < 0 || (nrm.y == 0 && nrm.x < 0)));
-  if (flip) nrm = -1.0 * nrm;
+  // centeredGf (plane.cpp:102-110): float differences stored as double
+  const int nf = (int)pl.features.size();
+  std::vector<double> a((size_t)3 * nf);
+  for (int i = 0; i < nf; ++i) {
+    const Pt& p = pl.features[i];
+    a[i] = (double)(p.x - cen.x);
+    a[(size_t)nf + i] = (double)(p.y - cen.y);
+    a[(size_t)2 * nf + i] = (double)(p.z - cen.z);
+  }
+  double u3[3];
+  eigen_jacobi_svd_u3(a, nf, u3);
+  if (nrm.x * u3[0] + nrm.y * u3[1] + nrm.z * u3[2] < 0) nrm = -1.0 * nrm;
   double d = -(nrm.x * cen.x + nrm.y * cen.y + nrm.z * cen.z);
   pl.plane[0] = nrm.x; pl.plane[1] = nrm.y; pl.plane[2] = nrm.z; pl.plane[3] = d;
   pl.centroid = {cen.x, cen.y, cen.z};
@@ -1659,6 +1849,10 @@ extern "C" {
 
 void oracle_philox(uint64_t key, const uint32_t ctr[4], uint32_t out[4]) {
   philox(key, ctr, out);
+}
+
+void oracle_eigen_svd_u3(const double* a, int32_t n, double u3[3]) {
+  eigen_jacobi_svd_u3(std::vector<double>(a, a + (size_t)3 * n), n, u3);
 }
 
 int oracle_project_mask(const sloam_params* p, const float* xyzi, int32_t n,

@@ -87,6 +87,10 @@ void   oracle_plane_project(sloam_plane* pl, const sloam_se3* tf);
 /* Philox4x32-10 block, for tests of the RNG contract. */
 void oracle_philox(uint64_t key, const uint32_t ctr[4], uint32_t out[4]);
 
+/* Third column of U of Eigen 3.3.7's JacobiSVD of the 3 x n matrix `a`
+ * (row-major: x row, y row, z row), the plane normal with Eigen's sign. */
+void oracle_eigen_svd_u3(const double* a, int32_t n, double u3[3]);
+
 #ifdef __cplusplus
 }
 #endif

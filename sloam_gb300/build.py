@@ -17,8 +17,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "_build", "libsloam_gb300.so")
 SHIM_SRC = os.path.join(HERE, "shim")
 SHIM_LIB = os.path.join(HERE, "_build", "libsloam_shim.so")
-UNITS = ["project.cu", "trellis.cu", "models.cu", "pose.cu", "context.cu", "noalloc.cu",
-         "proposal.cu", "ingest.cu", "mapmgr.cu"]
+UNITS = ["project.cu", "trellis.cu", "models.cu", "cylqueue.cu", "pose.cu", "context.cu",
+         "noalloc.cu", "proposal.cu", "ingest.cu", "mapmgr.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",

@@ -83,6 +83,9 @@ class Params(C.Structure):
         ("prop_min_inlier_ratio", C.c_float),
         ("pose_solver", C.c_int32),
         ("lm_max_iters", C.c_int32),
+        ("cyl_chunk_points", C.c_int32),
+        ("cyl_hyp_tile", C.c_int32),
+        ("cyl_queue_blocks", C.c_int32),
     ]
 
     def copy(self):
@@ -157,6 +160,9 @@ def default_params(**overrides):
     p.prop_min_inlier_ratio = 0.6
     p.pose_solver = 0
     p.lm_max_iters = 50
+    p.cyl_chunk_points = 256
+    p.cyl_hyp_tile = 256
+    p.cyl_queue_blocks = 0
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)

@@ -77,6 +77,9 @@ extern "C" void sloam_params_default(sloam_params* p) {
   p->prop_min_inlier_ratio = 0.6f;
   p->pose_solver = 0;
   p->lm_max_iters = 50;
+  p->cyl_chunk_points = 256;
+  p->cyl_hyp_tile = 256;
+  p->cyl_queue_blocks = 0;
 }
 
 // sizeof() of every ABI struct, for binding checks.
@@ -239,6 +242,7 @@ struct sloam_ctx {
   int64_t launches = 0;
   int64_t last_launches = 0;
   GraphSet gx;
+  int cc_iter_limit = -1;  // sloam_set_cc_iter_limit override (-1: the default)
   // further keyframe slots of a batch (slot 0 is the fields above)
   struct Slot {
     Dev d{};
@@ -378,6 +382,18 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.lm_uv = c.take<float2>((size_t)d.cap_cluster + d.cap_p);  // cluster | vertex points
   d.hyp = c.take<float4>((size_t)d.cap_lm * std::max(d.K, 1));
   d.hyp_cnt = c.take<int32_t>((size_t)d.cap_lm * std::max(d.K, 1));
+  d.qctl = c.take<QueueCtl>(1);
+  d.q_order = c.take<int32_t>(d.cap_lm);
+  d.q_off = c.take<int32_t>((size_t)d.cap_lm + 1);
+  d.q_soff = c.take<int32_t>((size_t)d.cap_lm + 1);
+  d.q_ready = c.take<int32_t>(d.cap_lm);
+  d.q_done = c.take<int32_t>((size_t)d.cap_lm * kQueuePhases);
+  d.q_st = c.take<double>((size_t)d.cap_lm * 16);
+  d.q_sf = c.take<float>((size_t)d.cap_lm * 16);
+  d.q_hyp = c.take<float4>(d.cap_lm);
+  // 256-point slices, at most one partial slice per tree
+  d.q_cap_chunks = (int)(((size_t)d.cap_cluster + d.cap_p) / 256 + d.cap_lm);
+  d.q_part = c.take<double>((size_t)d.q_cap_chunks * 20);
   const size_t ps = (size_t)std::max(d.prop_cap, 1);
   d.prop_x = c.take<float>(ps * 384);
   d.prop_f = c.take<float4>(ps);
@@ -404,6 +420,11 @@ int check_params(const sloam_params& p) {
   if (p.batch_slots < 0 || p.batch_slots > 64) return 1;
   if (p.cyl_mode < 0 || p.cyl_mode > 2 || p.prop_samples < 1 || p.prop_samples > 8) return 1;
   if (p.pose_solver < 0 || p.pose_solver > 1 || p.lm_max_iters < 1 || p.lm_max_iters > 1000)
+    return 1;
+  if (p.cyl_ls_iters < 0 || p.cyl_ls_iters > kQueuePhases - 1 || p.max_landmarks > 4096)
+    return 1;
+  if (!queue_shape_valid(p.cyl_chunk_points, p.cyl_hyp_tile) || p.cyl_queue_blocks < 0 ||
+      p.cyl_queue_blocks > 65536)
     return 1;
   return 0;
 }
@@ -477,6 +498,7 @@ int setup(sloam_ctx* ctx, const sloam_params& P) {
   free_front(ctx);  // sized by the scan and ground capacities
   ctx->P = P;
   ctx->kp = make_kparams(P);
+  if (ctx->cc_iter_limit >= 0) ctx->kp.cc_iter_limit = ctx->cc_iter_limit;
   int st = init_dev(ctx, P, ctx->d, ctx->arena, ctx->arena_bytes, ctx->st);
   if (st) return st;
   destroy_graphs(ctx->gx);
@@ -515,6 +537,8 @@ int sync_counters(sloam_ctx* ctx) {
     return fail(ctx, SLOAM_ERR_TIMEOUT, "connected-components union loop hit its iteration limit");
   if (ctx->h_cnt->prop_err)
     return fail(ctx, SLOAM_ERR_TIMEOUT, "proposal network: a tensor-core wait gave up");
+  if (ctx->h_cnt->queue_err)
+    return fail(ctx, SLOAM_ERR_TIMEOUT, "cylinder work queue: a wait for a tree's phase gave up");
   return SLOAM_OK;
 }
 
@@ -763,6 +787,19 @@ extern "C" int sloam_set_params(sloam_ctx* ctx, const sloam_params* params) {
   cudaSetDevice(ctx->device);
   CK(cudaStreamSynchronize(ctx->st));
   return setup(ctx, *params);
+}
+
+extern "C" int sloam_set_cc_iter_limit(sloam_ctx* ctx, int32_t limit) {
+  if (!ctx) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->st));
+  for (auto& s : ctx->extra) CK(cudaStreamSynchronize(s.st));
+  ctx->cc_iter_limit = limit < 0 ? -1 : limit;
+  ctx->kp.cc_iter_limit = limit < 0 ? kCCIterLimitDefault : limit;
+  // the captured keyframe graphs hold the old value: capture again
+  destroy_graphs(ctx->gx);
+  for (auto& s : ctx->extra) destroy_graphs(s.gx);
+  return SLOAM_OK;
 }
 
 extern "C" int64_t sloam_last_launch_count(const sloam_ctx* ctx) {

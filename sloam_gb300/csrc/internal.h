@@ -34,8 +34,19 @@ struct Counters {
   int32_t cc_iter_exceeded;
   int32_t n_fallback;    // mode 2: trees that fell back to RANSAC
   int32_t prop_err;      // mode 2: a tensor-core wait gave up
-  int32_t pad[9];
+  int32_t queue_err;     // the cylinder work queue: a wait gave up
+  int32_t pad[8];
 };
+
+// The cylinder work queue (cylqueue.cu): the item counter and the shape of
+// the current keyframe's queue.
+struct QueueCtl {
+  int32_t head;    // next item
+  int32_t tc;      // chunks of all queued trees (items per phase)
+  int32_t nq;      // queued trees
+  int32_t phases;  // 1 + LS iterations
+};
+constexpr int kQueuePhases = 17;  // 1 + at most 16 LS iterations
 
 // Plane and cylinder records used on the device (FP64 models).
 struct PlaneD {
@@ -221,6 +232,18 @@ struct Dev {
   float2* lm_uv;        // [cap_cluster + cap_p] tree points on the prior axis frame
   float4* hyp;          // [cap_lm * K] circle hypotheses (cu, cv, lo2, hi2)
   int32_t* hyp_cnt;     // [cap_lm * K] inlier counts
+  // -- the cylinder work queue (cylqueue.cu)
+  QueueCtl* qctl;
+  int32_t* q_order;     // [cap_lm] queued trees, largest first
+  int32_t* q_off;       // [cap_lm + 1] first chunk of each queued tree
+  int32_t* q_soff;      // [cap_lm + 1] first 256-point slice of each queued tree
+  int32_t* q_ready;     // [cap_lm] phases the tree has finished
+  int32_t* q_done;      // [cap_lm * kQueuePhases] chunks finished per phase
+  double* q_st;         // [cap_lm * 16] LS model state
+  float* q_sf;          // [cap_lm * 16] its float copies
+  float4* q_hyp;        // [cap_lm] the best hypothesis's circle
+  double* q_part;       // [q_cap_chunks * 20] slice sums of an LS iteration
+  int q_cap_chunks;
   // -- learned proposal (cyl_mode 2); capacities 0 in the other modes
   const unsigned char* prop_tc;  // bf16 network weights (the context's, shared by slots)
   float* prop_x;        // [cap_lm * S][128][3] normalised samples
@@ -262,7 +285,13 @@ struct KParams {
   int gn_iters;
   int pose_lm, lm_iters;  // trust-region LM instead of fixed GN iterations
   double huber;
+  int cc_iter_limit;      // retries of one connected-components union
+  int q_chunk, q_tile, q_blocks;  // cylinder work queue shape (tuned)
 };
+
+// Default retry limit of a connected-components union (a CAS loop that
+// contention can repeat; a union normally takes one or two rounds).
+constexpr int kCCIterLimitDefault = 1 << 20;
 
 KParams make_kparams(const sloam_params& p);
 
@@ -278,6 +307,11 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
 int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_state,
                cudaStream_t st);
+// point-level cylinder fit of the trees `only` marks (all eligible: NULL) by
+// the persistent work queue; cylqueue.cu
+int launch_cyl_queue(const Dev& d, const KParams& kp, const int32_t* only, cudaStream_t st);
+bool queue_shape_valid(int chunk_points, int hyp_tile);
+void init_queue_attributes();
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trellis,
                                cudaStream_t st);
 // a6 alone: cylinders of the landmarks against the planes already in d.planes

@@ -6,7 +6,8 @@
 //    fast/slow scheme as the projection), one block per bin selects the
 //    lowest int(n / retainNum) points by (z, index) with a shared-memory
 //    bitonic sort (radix select first when a bin exceeds the staging size),
-//    float centroid in that order, FP64 scatter + Jacobi normal (n_z > 0).
+//    float centroid in that order, FP64 scatter + Jacobi normal (with the
+//    sign Eigen's JacobiSVD gives it: eigen_normal_opposes).
 // a8 landmark -> nearest plane (sloam.cpp:418-431), and
 // a6 Cylinder (cylinder.cpp:3-173): one warp per landmark runs the
 //    vertex-line RANSAC (Philox hypotheses, PCL's sequential stopping rule),
@@ -20,11 +21,13 @@
 #include "internal.h"
 #include "proposal.cuh"
 #include "scan_util.cuh"
+#include "cylinder.cuh"
 
 namespace sg {
 
 KParams make_kparams(const sloam_params& p) {
   KParams k{};
+  k.cc_iter_limit = kCCIterLimitDefault;
   const float fov_up = (float)(p.fov_up_deg / 180.0 * 3.14159265358979323846);
   const float fov_down = (float)(p.fov_down_deg / 180.0 * 3.14159265358979323846);
   k.fov_down_abs = fov_down < 0 ? -fov_down : fov_down;
@@ -71,6 +74,11 @@ KParams make_kparams(const sloam_params& p) {
   k.pose_lm = p.pose_solver == 1 ? 1 : 0;
   k.lm_iters = p.lm_max_iters;
   k.huber = p.huber_delta;
+  k.q_chunk = p.cyl_chunk_points;
+  k.q_tile = p.cyl_hyp_tile;
+  // persistent blocks: the given count, else one wave of the GPU's SMs
+  // (the queue's blocks exit as soon as the items run out)
+  k.q_blocks = p.cyl_queue_blocks > 0 ? p.cyl_queue_blocks : 152;
   return k;
 }
 
@@ -284,12 +292,186 @@ __device__ void bitonic_sort(unsigned long long* a, int n2) {
   }
 }
 
+// The sign Eigen's JacobiSVD gives the plane normal (the third column of U
+// of the 3 x n centred matrix A, plane.cpp:113-115; Eigen 3.3.7): true when
+// it points against `nrm`.  Same steps as Eigen, in a form that needs only
+// the Gram matrix S = A A^T (6 entries, upper triangle row by row) and the
+// first three centred points a[0..2] (rows of A^T):
+//  - the column-pivoted Householder QR of A^T (ColPivHouseholderQR with its
+//    norm downdates), FP64: a reflection's inner products with the columns
+//    follow from S and the rows it leaves in place, S shrinks by the R row
+//    each step produces, and the pivot (c0) of step k is row k of the
+//    reflected column, so only the first three rows are carried;
+//  - the two-sided Jacobi sweep on W = R^T (real_2x2_jacobi_svd, makeJacobi),
+//    the positive-diagonal fix of U and the descending sort, FP32: every
+//    right rotation has a positive cosine, so the sign of u3 = A v3 / s3 does
+//    not depend on where the sweep stops.
+// Only the sign is used; the normal itself comes from the scatter's Jacobi.
+__device__ bool eigen_normal_opposes(const double* S6, const double a[3][3], int n, d3 nrm) {
+  double S[3][3] = {{S6[0], S6[1], S6[2]}, {S6[1], S6[3], S6[4]}, {S6[2], S6[4], S6[5]}};
+  double row[3][3];  // rows 0..2 of the working matrix (the first three points)
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) row[i][j] = a[i][j];
+  double R[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  double nu[3], nd[3];
+  for (int j = 0; j < 3; ++j) nd[j] = nu[j] = sqrt(S[j][j]);
+  int trans[3];
+  const double kMinD = 2.2250738585072014e-308, kEpsD = 2.220446049250313e-16;
+  for (int k = 0; k < 3; ++k) {
+    int big = k;
+    for (int j = k + 1; j < 3; ++j)
+      if (nu[j] > nu[big]) big = j;
+    trans[k] = big;
+    if (big != k) {
+      for (int i = 0; i < 3; ++i) {  // the whole column: S, the rows, R above
+        const double t = S[i][k]; S[i][k] = S[i][big]; S[i][big] = t;
+      }
+      for (int i = 0; i < 3; ++i) {
+        const double t = S[k][i]; S[k][i] = S[big][i]; S[big][i] = t;
+      }
+      for (int i = 0; i < 3; ++i) {
+        const double t = row[i][k]; row[i][k] = row[i][big]; row[i][big] = t;
+      }
+      for (int i = 0; i < k; ++i) {
+        const double t = R[i][k]; R[i][k] = R[i][big]; R[i][big] = t;
+      }
+      double t = nu[k]; nu[k] = nu[big]; nu[big] = t;
+      t = nd[k]; nd[k] = nd[big]; nd[big] = t;
+    }
+    // S now holds the Gram matrix of rows k.. of the working columns
+    const double c0 = row[k][k];
+    const double tail = (k == 2 && n == 3) ? 0.0 : S[k][k] - c0 * c0;
+    double tau = 0.0, beta = c0, den = 1.0;
+    if (tail > kMinD) {
+      beta = sqrt(S[k][k]);
+      if (c0 >= 0.0) beta = -beta;
+      den = c0 - beta;
+      tau = (beta - c0) / beta;
+    }
+    R[k][k] = beta;
+    double rk[3] = {0, 0, 0};
+    for (int j = k + 1; j < 3; ++j) {
+      if (tau != 0.0) {
+        // v^T x over rows k..: x_k + (S_kj - c0 x_k) / (c0 - beta)
+        const double vtx = row[k][j] + (S[k][j] - c0 * row[k][j]) / den;
+        rk[j] = row[k][j] - tau * vtx;
+        for (int i = k + 1; i < 3; ++i) row[i][j] -= tau * (row[i][k] / den) * vtx;
+      } else {
+        rk[j] = row[k][j];
+      }
+      R[k][j] = rk[j];
+    }
+    for (int j = k + 1; j < 3; ++j)
+      for (int l = k + 1; l < 3; ++l) S[j][l] -= rk[j] * rk[l];
+    for (int j = k + 1; j < 3; ++j) {
+      if (nu[j] != 0.0) {
+        double t = fabs(rk[j]) / nu[j];
+        t = (1.0 + t) * (1.0 - t);
+        t = t < 0.0 ? 0.0 : t;
+        const double r = nu[j] / nd[j];
+        if (t * r * r <= sqrt(kEpsD)) {
+          nd[j] = nu[j] = sqrt(S[j][j] > 0.0 ? S[j][j] : 0.0);
+        } else {
+          nu[j] *= sqrt(t);
+        }
+      }
+    }
+  }
+  int idx[3] = {0, 1, 2};
+  for (int k = 0; k < 3; ++k) {
+    const int t = idx[k]; idx[k] = idx[trans[k]]; idx[trans[k]] = t;
+  }
+  // the Jacobi sweep on W = R^T, U from the permutation (FP32)
+  float W[3][3], U[3][3];
+  float scale = 0.f;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) scale = fmaxf(scale, fabsf((float)R[i][j]));
+  if (!(scale > 0.f)) return false;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      W[i][j] = j <= i ? (float)(R[j][i] / (double)scale) : 0.f;
+      U[i][j] = 0.f;
+    }
+  for (int i = 0; i < 3; ++i) U[idx[i]][i] = 1.f;
+  float maxd = fmaxf(fabsf(W[0][0]), fmaxf(fabsf(W[1][1]), fabsf(W[2][2])));
+  bool finished = false;
+  for (int sweep = 0; !finished && sweep < 30; ++sweep) {
+    finished = true;
+    for (int p = 1; p < 3; ++p) {
+      for (int q = 0; q < p; ++q) {
+        const float thr = fmaxf(FLT_MIN, 2.f * FLT_EPSILON * maxd);
+        if (!(fabsf(W[p][q]) > thr || fabsf(W[q][p]) > thr)) continue;
+        finished = false;
+        float m00 = W[p][p], m01 = W[p][q], m10 = W[q][p], m11 = W[q][q];
+        const float t = m00 + m11, dd = m10 - m01;
+        float c1 = 1.f, s1 = 0.f;
+        if (!(fabsf(dd) < FLT_MIN)) {
+          const float u = t / dd, tmp = sqrtf(1.f + u * u);
+          s1 = 1.f / tmp;
+          c1 = u / tmp;
+        }
+        const float x0 = m00, x1 = m01;
+        m00 = c1 * x0 + s1 * m10;
+        m01 = c1 * x1 + s1 * m11;
+        m11 = -s1 * x1 + c1 * m11;
+        float cr = 1.f, sr = 0.f;
+        const float deno = 2.f * fabsf(m01);
+        if (!(deno < FLT_MIN)) {
+          const float tau = (m00 - m11) / deno, w = sqrtf(tau * tau + 1.f);
+          const float tt = tau > 0.f ? 1.f / (tau + w) : 1.f / (tau - w);
+          const float sign_t = tt > 0.f ? 1.f : -1.f;
+          const float nn = 1.f / sqrtf(tt * tt + 1.f);
+          sr = -sign_t * (m01 > 0.f ? 1.f : -1.f) * fabsf(tt) * nn;
+          cr = nn;
+        }
+        const float lc = c1 * cr + s1 * sr, ls = -c1 * sr + s1 * cr;
+        for (int i = 0; i < 3; ++i) {  // W rows p, q by j_left
+          const float x = W[p][i], y = W[q][i];
+          W[p][i] = lc * x + ls * y;
+          W[q][i] = -ls * x + lc * y;
+        }
+        for (int i = 0; i < 3; ++i) {  // U columns p, q by j_left^T
+          const float x = U[i][p], y = U[i][q];
+          U[i][p] = lc * x + ls * y;
+          U[i][q] = -ls * x + lc * y;
+        }
+        for (int i = 0; i < 3; ++i) {  // W columns p, q by j_right
+          const float x = W[i][p], y = W[i][q];
+          W[i][p] = cr * x - sr * y;
+          W[i][q] = sr * x + cr * y;
+        }
+        maxd = fmaxf(maxd, fmaxf(fabsf(W[p][p]), fabsf(W[q][q])));
+      }
+    }
+  }
+  float sv[3];
+  for (int i = 0; i < 3; ++i) {
+    sv[i] = fabsf(W[i][i]);
+    if (W[i][i] < 0.f)
+      for (int r = 0; r < 3; ++r) U[r][i] = -U[r][i];
+  }
+  // the descending sort (first maximum moved forward); its last column
+  int ord[3] = {0, 1, 2};
+  for (int i = 0; i < 3; ++i) {
+    int pos = i;
+    for (int j = i + 1; j < 3; ++j)
+      if (sv[j] > sv[pos]) pos = j;
+    if (pos != i) {
+      const float t = sv[i]; sv[i] = sv[pos]; sv[pos] = t;
+      const int o = ord[i]; ord[i] = ord[pos]; ord[pos] = o;
+    }
+  }
+  const int last = ord[2];
+  const double dot = nrm.x * U[0][last] + nrm.y * U[1][last] + nrm.z * U[2][last];
+  return dot < 0.0;
+}
+
 // Plane::computeModel (plane.cpp:96-128) over points at(0..n-1) by the whole
 // block: float centroid accumulated sequentially in feature order
 // (utils.h:14-28), FP64 scatter about it, normal = eigenvector of the
-// smallest eigenvalue (FP32 Jacobi), sign canonical (n_z > 0, then n_y, n_x),
-// d = -n.c.  `cen` (3 floats) and `red` (6 * 32 doubles) are shared memory;
-// the model lands in `out` of thread 0.
+// smallest eigenvalue (FP32 Jacobi), with the sign Eigen's JacobiSVD gives
+// it (eigen_normal_opposes), d = -n.c.  `cen` (3 floats) and `red` (6 * 32
+// doubles) are shared memory; the model lands in `out` of thread 0.
 template <typename At>
 __device__ void fit_plane_block(At at, int n, float* cen, double* red, PlaneD& out) {
   if (threadIdx.x == 0) {
@@ -341,8 +523,14 @@ __device__ void fit_plane_block(At at, int n, float* cen, double* red, PlaneD& o
     float ev[3], V[9];
     jacobi3f(S, ev, V);
     d3 nrm = mk3(V[0], V[3], V[6]);
-    const bool flip = nrm.z < 0 || (nrm.z == 0 && (nrm.y < 0 || (nrm.y == 0 && nrm.x < 0)));
-    if (flip) nrm = scl3(-1.0, nrm);
+    double a[3][3];
+    for (int i = 0; i < 3; ++i) {
+      const float4 p = at(i);
+      a[i][0] = (double)fsub(p.x, cen[0]);
+      a[i][1] = (double)fsub(p.y, cen[1]);
+      a[i][2] = (double)fsub(p.z, cen[2]);
+    }
+    if (eigen_normal_opposes(S6, a, n, nrm)) nrm = scl3(-1.0, nrm);
     const double dd = -(nrm.x * cen[0] + nrm.y * cen[1] + nrm.z * cen[2]);
     out.plane[0] = nrm.x; out.plane[1] = nrm.y; out.plane[2] = nrm.z; out.plane[3] = dd;
     out.centroid[0] = cen[0]; out.centroid[1] = cen[1]; out.centroid[2] = cen[2];
@@ -939,60 +1127,6 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
 
 // ---------------------------------------------- point-level cylinder fit
 
-struct CylFrame {
-  float ox, oy, oz;
-  float ax, ay, az;
-  float e1x, e1y, e1z, e2x, e2y, e2z;
-};
-
-__device__ __forceinline__ CylFrame make_frame(const Dev& d, const CylD& c) {
-  CylFrame f;
-  const float* vx = d.lm_vxyz + 3 * (size_t)d.lm_vbeg[c.landmark];
-  f.ox = vx[3]; f.oy = vx[4]; f.oz = vx[5];
-  float ax = (float)c.ray[0], ay = (float)c.ray[1], az = (float)c.ray[2];
-  if (az < 0) { ax = -ax; ay = -ay; az = -az; }
-  float tx = 1.0f, ty = 0.0f, tz = 0.0f;
-  if (!(fabsf(ax) < 0.9f)) { tx = 0.0f; ty = 1.0f; }
-  float e1x = fsub(fmul(ay, tz), fmul(az, ty)), e1y = fsub(fmul(az, tx), fmul(ax, tz)),
-        e1z = fsub(fmul(ax, ty), fmul(ay, tx));
-  const float e1n = fsqrt(fadd(fadd(fmul(e1x, e1x), fmul(e1y, e1y)), fmul(e1z, e1z)));
-  e1x = fdiv(e1x, e1n); e1y = fdiv(e1y, e1n); e1z = fdiv(e1z, e1n);
-  f.e2x = fsub(fmul(ay, e1z), fmul(az, e1y));
-  f.e2y = fsub(fmul(az, e1x), fmul(ax, e1z));
-  f.e2z = fsub(fmul(ax, e1y), fmul(ay, e1x));
-  f.ax = ax; f.ay = ay; f.az = az;
-  f.e1x = e1x; f.e1y = e1y; f.e1z = e1z;
-  return f;
-}
-
-__device__ __forceinline__ float2 project_uv(const CylFrame& f, float4 q) {
-  const float dx = fsub(q.x, f.ox), dy = fsub(q.y, f.oy), dz = fsub(q.z, f.oz);
-  const float u = fadd(fadd(fmul(dx, f.e1x), fmul(dy, f.e1y)), fmul(dz, f.e1z));
-  const float v = fadd(fadd(fmul(dx, f.e2x), fmul(dy, f.e2y)), fmul(dz, f.e2z));
-  return make_float2(u, v);
-}
-
-// The tree's points: its CC cluster, or its vertex points when no cluster;
-// *uv = where their projections live in lm_uv.
-__device__ __forceinline__ void tree_points(const Dev& d, int l, const float4** pts, int* n,
-                                            const float2** uv) {
-  const int c0 = d.lm_cbeg[l], c1 = d.lm_cbeg[l + 1];
-  if (c1 > c0) {
-    *pts = d.lm_cpts + c0;
-    *n = c1 - c0;
-    *uv = d.lm_uv + c0;
-  } else {
-    const int vb = d.lm_vbeg[l], ve = d.lm_vbeg[l + 1];
-    *pts = d.lm_pts + d.lm_pbeg[vb];
-    *n = d.lm_pbeg[ve] - d.lm_pbeg[vb];
-    *uv = d.lm_uv + d.cap_cluster + d.lm_pbeg[vb];
-  }
-}
-
-__device__ __forceinline__ bool fit_eligible(const CylD& c) {
-  return c.stage == 1 && c.radius != -1.0;
-}
-
 // Projection of each eligible tree's points on its prior-axis frame.
 __global__ void __launch_bounds__(256) k_cyl_uv(Dev d) {
   const int nl = d.cnt->n_lm;
@@ -1007,39 +1141,6 @@ __global__ void __launch_bounds__(256) k_cyl_uv(Dev d) {
     float2* out = const_cast<float2*>(uv);
     for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = project_uv(f, pts[i]);
   }
-}
-
-struct Hyp {
-  float cu, cv, r, lo2, hi2;
-  bool ok;
-};
-
-template <typename UV>
-__device__ __forceinline__ Hyp make_hyp(const KParams& kp, int h, int tree_id, int n, UV uv) {
-  Hyp H{};
-  H.ok = false;
-  uint32_t u[4], id[3];
-  philox(kp.seed, (uint32_t)h, (uint32_t)tree_id, 1u, 0u, u);
-  draw_distinct(u, (uint32_t)n, 3, id);
-  const float2 p0 = uv(id[0]), p1 = uv(id[1]), p2 = uv(id[2]);
-  const float bx = fsub(p1.x, p0.x), by = fsub(p1.y, p0.y);
-  const float cx = fsub(p2.x, p0.x), cy = fsub(p2.y, p0.y);
-  const float t1 = fmul(bx, cy), t2 = fmul(by, cx);
-  const float den = fmul(2.0f, fsub(t1, t2));
-  if (den == 0.0f) return H;
-  const float b2 = fadd(fmul(bx, bx), fmul(by, by)), c2 = fadd(fmul(cx, cx), fmul(cy, cy));
-  const float ox = fdiv(fsub(fmul(cy, b2), fmul(by, c2)), den);
-  const float oy = fdiv(fsub(fmul(bx, c2), fmul(cx, b2)), den);
-  const float r = fsqrt(fadd(fmul(ox, ox), fmul(oy, oy)));
-  if (!(r <= kp.max_hyp_r)) return H;
-  H.cu = fadd(p0.x, ox);
-  H.cv = fadd(p0.y, oy);
-  H.r = r;
-  const float lo = fsub(r, kp.tau), hi = fadd(r, kp.tau);
-  H.lo2 = lo > 0.0f ? fmul(lo, lo) : -1.0f;
-  H.hi2 = fmul(hi, hi);
-  H.ok = true;
-  return H;
 }
 
 // Hypothesis table: one thread per (tree, hypothesis); clears the counts.
@@ -1245,23 +1346,6 @@ __global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
 // network proposal; the refined model is kept when its inliers
 // (|distance to the refined axis - radius| < tau) are at least prop_ratio
 // of the tree's points, else the tree is flagged for the RANSAC pass.
-// Normal frame of the LS model st (centre st[0..2], unit direction
-// st[3..5], radius st[6]): b1 = dir x t / |dir x t| (t = x unless
-// |dir_x| >= 0.9, then y), b2 = dir x b1, in double into st[8..13], and the
-// float copies every thread uses into sf.
-__device__ __forceinline__ void ls_frame(double* st, float* sf) {
-  const d3 dd = mk3(st[3], st[4], st[5]);
-  const d3 t = fabs(dd.x) < 0.9 ? mk3(1, 0, 0) : mk3(0, 1, 0);
-  d3 b1 = cross3(dd, t);
-  b1 = scl3(1.0 / norm3(b1), b1);
-  const d3 b2 = cross3(dd, b1);
-  st[8] = b1.x; st[9] = b1.y; st[10] = b1.z;
-  st[11] = b2.x; st[12] = b2.y; st[13] = b2.z;
-  for (int j = 0; j < 6; ++j) sf[j] = (float)st[j];
-  sf[6] = (float)b1.x; sf[7] = (float)b1.y; sf[8] = (float)b1.z;
-  sf[9] = (float)b2.x; sf[10] = (float)b2.y; sf[11] = (float)b2.z;
-  sf[12] = (float)st[6];
-}
 constexpr int kLsThreads = 256;
 __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int pass) {
   __shared__ int s_in[kLsThreads / 32];
@@ -1552,10 +1636,7 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream
     only = d.pflag;
   }
   k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp, only);
-  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.hyp, d.hyp_cnt, kp.K, only);
-  k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.hyp_cnt, kp.K, d.cyl_best, only);
-  k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp, 1);
-  return n + 4;
+  return n + 1 + launch_cyl_queue(d, kp, only, st);
 }
 
 int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st) {
@@ -1585,6 +1666,9 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
   return n + launch_cylinders(d, kp, from_trellis, st);
 }
 
-void init_kernel_attributes() { prop::init_attributes(); }
+void init_kernel_attributes() {
+  prop::init_attributes();
+  init_queue_attributes();
+}
 
 }  // namespace sg

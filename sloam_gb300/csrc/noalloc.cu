@@ -38,7 +38,7 @@ constexpr size_t kOffIn = al(kOffRowTab + 4ull * (kNoAllocMaxH + 1));
 constexpr size_t kOffCnt = al(kOffIn + sizeof(sg::InPtrs));
 constexpr size_t kNoAllocBytes = al(kOffCnt + sizeof(sg::Counters));
 
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 
 }  // namespace
 
@@ -49,7 +49,18 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 namespace {
 
 std::mutex g_mu;
-unsigned char* g_base[kMaxDevices] = {};  // device address of the scratch, per device
+// Device address of the scratch per CUDA context: a __device__ symbol has an
+// address in each context that loads the module (the primary context of a
+// device, or a context a plugin host created and made current itself).
+struct ScratchAddr {
+  void* cu_ctx;
+  unsigned char* base;
+};
+ScratchAddr g_base[kMaxContexts] = {};
+int g_nbase = 0;
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn g_ctx_get = nullptr;
+bool g_ctx_get_looked_up = false;
 float g_tab[kNoAllocMaxW + 1];            // host staging of the column table
 float g_row_tab[kNoAllocMaxH + 1];        // host staging of the row table
 
@@ -74,21 +85,41 @@ extern "C" int sloam_project_mask_noalloc(const sloam_params* p, const float* d_
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
     cudaGetLastError();
     return SLOAM_ERR_NO_DEVICE;
   }
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_base[dev]) {
-    // once per device, with that device current: the scratch's device address
+  if (!g_ctx_get_looked_up) {
+    g_ctx_get_looked_up = true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      g_ctx_get = reinterpret_cast<CtxGetCurrentFn>(fn);
+    cudaGetLastError();
+  }
+  // The runtime's current context for this device (its primary context
+  // unless the caller made another one current).  The first call in a
+  // context, made with that context current, looks the scratch's address
+  // up; later calls in it reuse the address.
+  void* cu_ctx = nullptr;
+  if (!g_ctx_get || g_ctx_get(&cu_ctx) != 0 || !cu_ctx) {
+    cudaGetLastError();
+    cu_ctx = nullptr;  // unknown: look the address up on every call
+  }
+  unsigned char* b = nullptr;
+  for (int i = 0; cu_ctx && i < g_nbase; ++i)
+    if (g_base[i].cu_ctx == cu_ctx) b = g_base[i].base;
+  if (!b) {
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
       cudaGetLastError();
       return SLOAM_ERR_CUDA;
     }
-    g_base[dev] = static_cast<unsigned char*>(ptr);
+    b = static_cast<unsigned char*>(ptr);
+    if (cu_ctx && g_nbase < kMaxContexts) g_base[g_nbase++] = ScratchAddr{cu_ctx, b};
   }
-  unsigned char* b = g_base[dev];
   sg::Dev d{};
   d.H = p->img_h;
   d.W = p->img_w;

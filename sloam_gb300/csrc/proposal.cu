@@ -1076,6 +1076,40 @@ extern "C" int sloam_prop_train(const float* init, int32_t steps, int32_t batch,
   return SLOAM_OK;
 }
 
+// One training step's backward pass alone: the per-cluster forward, loss and
+// gradient of k_prop_train over n samples (device arrays of 384 and kTgt
+// floats each), then their mean (k_prop_reduce).  grad_out receives the
+// kNumParams mean gradient, loss_out (may be NULL) the n per-cluster losses.
+extern "C" int sloam_prop_grad(const float* weights, const float* d_points,
+                               const float* d_targets, int32_t n, float* grad_out,
+                               float* loss_out) {
+  if (!weights || !grad_out || n < 1 || !d_points || !d_targets) return SLOAM_ERR_ARG;
+  float *W = nullptr, *G = nullptr, *grad = nullptr, *L = nullptr;
+  cudaError_t e = cudaMalloc(&W, sizeof(float) * kNumParams);
+  if (e == cudaSuccess) e = cudaMalloc(&G, sizeof(float) * kNumParams * (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc(&grad, sizeof(float) * kNumParams);
+  if (e == cudaSuccess) e = cudaMalloc(&L, sizeof(float) * n);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(W, weights, sizeof(float) * kNumParams, cudaMemcpyHostToDevice);
+  const size_t smem = sizeof(float) * kTrainSmemFloats;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_prop_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) {
+    k_prop_train<<<n, kTrainThreads, smem>>>(W, d_points, d_targets, G, L);
+    k_prop_reduce<<<(kNumParams + 255) / 256, 256>>>(G, n, grad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    e = cudaMemcpy(grad_out, grad, sizeof(float) * kNumParams, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && loss_out)
+    e = cudaMemcpy(loss_out, L, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  for (float* p : {W, G, grad, L})
+    if (p) cudaFree(p);
+  if (e != cudaSuccess) return prop_fail("gradient", e);
+  return SLOAM_OK;
+}
+
 extern "C" int sloam_prop_infer(const float* weights, const float* d_points, int32_t n,
                                 float* d_out, int32_t mode) {
   if (!weights || n < 0 || (n > 0 && (!d_points || !d_out)) || mode < 0 || mode > 1)

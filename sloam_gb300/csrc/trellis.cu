@@ -22,8 +22,6 @@ namespace sg {
 
 namespace {
 
-constexpr int kCCIterLimit = 1 << 20;
-
 __device__ __forceinline__ bool cc_close(const float4& a, const float4& b, float thr) {
   const float dx = fsub(a.x, b.x), dy = fsub(a.y, b.y), dz = fsub(a.z, b.z);
   const float dd = fadd(fmul(dx, dx), fadd(fmul(dy, dy), fmul(dz, dz)));
@@ -43,10 +41,10 @@ __device__ __forceinline__ uint32_t cc_find(volatile uint32_t* P, uint32_t x) {
 
 // Union of the components of u and v in parent array P (roots are the
 // minimum index: the larger root is linked under the smaller by CAS).
-// Returns false when the retry limit ran out.
+// Returns false when the retry limit (`limit` rounds) ran out.
 template <typename T, typename Find>
-__device__ __forceinline__ bool cc_union(T* P, T u, T v, Find find) {
-  for (int it = 0; it < kCCIterLimit; ++it) {
+__device__ __forceinline__ bool cc_union(T* P, T u, T v, Find find, int limit) {
+  for (int it = 0; it < limit; ++it) {
     T ru = find(u), rv = find(v);
     if (ru == rv) return true;
     if (ru > rv) { const T t = ru; ru = rv; rv = t; }
@@ -68,7 +66,7 @@ __device__ __forceinline__ bool cc_union(T* P, T u, T v, Find find) {
 // of its tile root to the global parent array.
 constexpr int kCCTile = 32;
 
-__global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr) {
+__global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr, int limit) {
   __shared__ int lp[kCCTile * kCCTile];
   __shared__ float4 pt[kCCTile * kCCTile];
   __shared__ unsigned vbits[kCCTile], hbits[kCCTile];
@@ -119,7 +117,7 @@ __global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr) {
     const unsigned ub = __ballot_sync(0xffffffffu, up);
     const bool joined_left = lane > 0 && ((hbits[row] >> lane) & 1u) &&
                              ((hbits[row - 1] >> lane) & 1u) && ((ub >> (lane - 1)) & 1u);
-    if (up && !joined_left) ok &= cc_union(lp, l, l - kCCTile, find);
+    if (up && !joined_left) ok &= cc_union(lp, l, l - kCCTile, find, limit);
   }
   if (!ok) atomicOr(&d.cnt->cc_iter_exceeded, 1);
   __syncthreads();
@@ -138,7 +136,7 @@ __global__ void __launch_bounds__(256) k_cc_local(Dev d, float thr) {
 // a3, second level: pixel pairs across tile borders (left neighbour across a
 // vertical border, upper neighbour across a horizontal one) join in the
 // global parent array.
-__global__ void __launch_bounds__(256) k_cc_border(Dev d, float thr) {
+__global__ void __launch_bounds__(256) k_cc_border(Dev d, float thr, int limit) {
   const TreeView tree = tree_view(d.in, d.W);
   const int W = d.W, H = d.H;
   const int nv = ((W + kCCTile - 1) / kCCTile - 1) * H;
@@ -159,7 +157,7 @@ __global__ void __launch_bounds__(256) k_cc_border(Dev d, float thr) {
     }
     if (P[p] == kInvalid || P[q] == kInvalid) continue;
     if (!cc_close(tree[p], tree[q], thr)) continue;
-    ok &= cc_union(P, (uint32_t)p, (uint32_t)q, find);
+    ok &= cc_union(P, (uint32_t)p, (uint32_t)q, find, limit);
   }
   if (!ok) atomicOr(&d.cnt->cc_iter_exceeded, 1);
 }
@@ -781,8 +779,9 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   const int N = d.N;
   const int g1k = (N + 1023) / 1024;
   const int tiles = ((d.W + kCCTile - 1) / kCCTile) * ((d.H + kCCTile - 1) / kCCTile);
-  k_cc_local<<<tiles, 256, 0, st>>>(d, kp.cc_thr);
-  k_cc_border<<<(cc_border_pairs(d.W, d.H) + 255) / 256 + 1, 256, 0, st>>>(d, kp.cc_thr);
+  k_cc_local<<<tiles, 256, 0, st>>>(d, kp.cc_thr, kp.cc_iter_limit);
+  k_cc_border<<<(cc_border_pairs(d.W, d.H) + 255) / 256 + 1, 256, 0, st>>>(d, kp.cc_thr,
+                                                                          kp.cc_iter_limit);
   k_cc_flatten<<<g1k, kCCThreads, 0, st>>>(d);
   k_cc_rank<<<g1k, kCCThreads, 0, st>>>(d);
   k_cc_label<<<g1k, kCCThreads, 0, st>>>(d);

@@ -19,7 +19,7 @@ EXPORTS = [
     "sloam_keyframes_device", "sloam_keyframes_host", "sloam_last_launch_count", "sloam_stream",
     "sloam_internal_tables", "sloam_set_proposal_weights", "sloam_pack_points",
     "sloam_mapmgr_create", "sloam_mapmgr_destroy", "sloam_mapmgr_size", "sloam_mapmgr_read",
-    "sloam_mapmgr_load", "sloam_mapmgr_submap", "sloam_keyframe_mapped",
+    "sloam_mapmgr_load", "sloam_mapmgr_submap", "sloam_keyframe_mapped", "sloam_set_cc_iter_limit",
 ]
 
 _lib = None
@@ -73,6 +73,7 @@ def load(path=LIB_PATH):
     L.sloam_project_mask_noalloc.argtypes = [C.POINTER(A.Params), vp, C.c_int32, vp, vp, vp, vp,
                                              vp, vp, vp, vp, vp]
     L.sloam_set_proposal_weights.argtypes = [vp, C.POINTER(C.c_float), C.c_int32]
+    L.sloam_set_cc_iter_limit.argtypes = [vp, C.c_int32]
     L.sloam_pack_points.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_int32, vp, vp]
     L.sloam_mapmgr_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32,

@@ -32,6 +32,8 @@ def _lib():
                                    C.c_int64, C.c_void_p, C.c_void_p]
     L.sloam_prop_sample.argtypes = [C.c_uint64, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]
     L.sloam_prop_infer.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]
+    L.sloam_prop_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                  C.c_void_p]
     return L
 
 
@@ -63,6 +65,45 @@ def train(steps, batch=1024, lr=1e-3, seed=1, first_id=0, init=None):
     if st:
         raise RuntimeError(f"sloam_prop_train failed ({st})")
     return w, loss[:steps]
+
+
+def grad(w, X, T):
+    """The training kernels' mean gradient and per-cluster losses of weights
+    w on device samples X [n,128,3], T [n,8] (no update)."""
+    L = _lib()
+    g = np.zeros(NUM_PARAMS, np.float32)
+    loss = np.zeros(X.shape[0], np.float32)
+    ww = np.ascontiguousarray(w, np.float32)
+    st = L.sloam_prop_grad(ww.ctypes.data, X.data_ptr(), T.data_ptr(), X.shape[0], g.ctypes.data,
+                           loss.ctypes.data)
+    if st:
+        raise RuntimeError(f"sloam_prop_grad failed ({st})")
+    return g, loss
+
+
+def torch_loss(w, X, T):
+    """The training loss in plain PyTorch FP32 (per cluster): squared error
+    on axis, centre xy and log radius, plus 0.1 x the binary cross-entropy
+    of the confidence against exp(-e / 0.01), e the centre and log-radius
+    squared error (the target is a constant of the step).  w is a torch
+    parameter vector."""
+    import torch
+    p, o = {}, 0
+    for name, shape in SHAPES:
+        n = int(np.prod(shape))
+        p[name] = w[o:o + n].reshape(shape)
+        o += n
+    a1 = torch.relu(X @ p["W1"] + p["b1"])
+    a2 = torch.relu(a1 @ p["W2"] + p["b2"])
+    h = torch.relu((a2 @ p["W3"] + p["b3"]).max(dim=1).values)
+    y1 = torch.relu(h @ p["W4"] + p["b4"])
+    out = y1 @ p["W5"] + p["b5"]
+    mse = ((out[:, :6] - T[:, :6]) ** 2).sum(1)
+    ec = ((out[:, 3:6] - T[:, 3:6]) ** 2).sum(1).detach()
+    ct = torch.exp(-ec / 0.01)
+    z = out[:, 6]
+    bce = ct * torch.nn.functional.softplus(-z) + (1 - ct) * torch.nn.functional.softplus(z)
+    return mse + 0.1 * bce
 
 
 def sample(n, seed=7, first_id=10 ** 9):

@@ -312,8 +312,14 @@ def scene(cfg: SceneConfig = C2, seed: int = 0, n_kf: int = 1):
 def preset_params(cfg: SceneConfig, base=None, **kw):
     """Reference parameters adjusted so the reference algorithm can accept the
     synthetic scenes: max_tree_radius above the largest trunk, max_lidar_dist
-    beyond the scan disc, the Trellis minimum vertex count below H, and no
-    Ouster destagger (the synthetic sensor is not staggered)."""
+    beyond the scan disc, the Trellis minimum vertex count below H, no Ouster
+    destagger (the synthetic sensor is not staggered), and at least 16 plane
+    feature matches (more than 3 matched planes) for the pose instead of 37.
+    The keyframes of a synthetic scene stand at scattered places of the
+    forest, so only a few of a keyframe's ground bins lie within the 1 m
+    plane-match distance of the first scan's (sloam.cpp:490), and the plane
+    gate drops every bin whose SVD normal comes out pointing down
+    (sloam.cpp:402-406): about 6 planes of a 64x2048 keyframe match."""
     from .capi import default_params
     p = default_params() if base is None else base.copy()
     p.img_h, p.img_w = cfg.H, cfg.W
@@ -322,6 +328,7 @@ def preset_params(cfg: SceneConfig, base=None, **kw):
     p.max_tree_radius = max(0.3, cfg.r_range[1] + 0.2)
     p.max_lidar_dist = cfg.disc + 5.0
     p.trellis_min_vertices = min(16, max(3, cfg.H // 2 - 1))
+    p.min_ground_models = min(p.min_ground_models, 15.0)
     for k, v in kw.items():
         setattr(p, k, v)
     return p

@@ -197,6 +197,7 @@ def compare_models(mo, mg, ints_only=False, tol_scale=1.0):
         np.testing.assert_array_equal(po[:, 7], pg[:, 7])  # bins
         if not ints_only:
             for a, b in zip(po, pg):
+                assert np.dot(a[:3], b[:3]) > 0  # the same (Eigen's) sign
                 assert angle_between(a[:3], b[:3]) < TOL_AXIS_RAD * tol_scale
                 # offset where the plane is: the oracle centroid's distance to
                 # the GPU plane (d itself grows with the distance of the plane

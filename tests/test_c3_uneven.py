@@ -94,3 +94,45 @@ def test_c3_batch_matches_single():
     torch.cuda.synchronize()
     _check_batch(pose_out.cpu().numpy().reshape(-1, 7), succ.cpu(), ncyl.cpu(), list(range(B)), ref)
     ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("chunk,tile,blocks", [(512, 64, 8), (1024, 1024, 300), (256, 128, 1)])
+def test_c3_queue_shapes_bit_identical(chunk, tile, blocks):
+    """The work queue's shape (points per item, hypotheses staged per pass,
+    persistent blocks: what the autotuner chooses) changes how the work is
+    cut, not the result: every keyframe's cylinders (inlier counts, fits),
+    matches and pose are bit-identical to the default shape's."""
+    from tests.test_gpu_parity import make_ctx
+    forest, kfs, _ = _scene()
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    nm = len(forest.radius)
+    out = {}
+    for shape in ((256, 256, 0), (chunk, tile, blocks)):
+        P = synth.c3_params(forest, two_step_optim=0, cyl_mode=1)
+        P.cyl_chunk_points, P.cyl_hyp_tile, P.cyl_queue_blocks = shape
+        ctx = make_ctx(P)
+        res = []
+        for k in (1, 3, 4):  # 400, 150 and 300 trees
+            kf = kfs[k]
+            rr = []
+            for pose in (A.SE3.from_qt(*kf.pose_gt_qt()), A.SE3.from_qt(*kf.pose_est_qt())):
+                r = A.RunBuffers(P)
+                ctx.check(ctx.L.sloam_keyframe(ctx.h, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                               A.ptr(kf.labels, C.c_uint8), None, C.byref(pose),
+                                               mapc, nm, C.byref(r.s)))
+                r.refresh()
+                n = r.s.models.n_cylinders
+                q, t = r.s.T_Map_Curr.qt()
+                rr.append((r.m.cyl_array()[:n].copy(), r.m.cyl_inliers[:n].copy(),
+                           r.matches[:n].copy(), q, t))
+            ctx.check(ctx.L.sloam_reset(ctx.h))
+            res.append(rr)
+        ctx.close()
+        out[shape] = res
+    a, b = out[(256, 256, 0)], out[(chunk, tile, blocks)]
+    for ra, rb in zip(a, b):
+        for xa, xb in zip(ra, rb):
+            assert len(xa[0]) > 10
+            for u, v in zip(xa, xb):
+                np.testing.assert_array_equal(u, v)

@@ -211,11 +211,14 @@ def gpu_run_pair(ctx):
 
 
 def compare_runs(ro, rg, pose_tol=1.0):
+    """Statuses, checks, match counts and indices exactly; models and pose
+    within the tolerances times pose_tol (the models are returned in the map
+    frame, moved by the estimated pose, so they share its tolerance)."""
     assert ro.s.success == rg.s.success
     assert ro.s.n_tree_matches == rg.s.n_tree_matches
     assert ro.s.n_plane_matches == rg.s.n_plane_matches
     assert ro.s.tree_check == rg.s.tree_check and ro.s.ground_check == rg.s.ground_check
-    H.compare_models(ro.m, rg.m, tol_scale=1.0)
+    H.compare_models(ro.m, rg.m, tol_scale=pose_tol)
     n = ro.s.models.n_cylinders
     np.testing.assert_array_equal(ro.matches[:n], rg.matches[:n])
     qo, to = ro.s.T_Map_Curr.qt()
@@ -224,10 +227,11 @@ def compare_runs(ro, rg, pose_tol=1.0):
     assert H.rot_angle(qo, qg) < H.TOL_ROT_RAD * pose_tol, (qo, qg)
 
 
-@pytest.mark.parametrize("two_step", [0, 1])
-def test_run_reference_pair(two_step):
+@pytest.mark.parametrize("two_step,solver", [(0, 0), (1, 0), (0, 1)])
+def test_run_reference_pair(two_step, solver):
     from tests.test_oracle_reference import oracle_run_pair
     P = core_params(two_step)
+    P.pose_solver = solver
     ctx = make_ctx(P)
     st0, r0, st1, r1 = gpu_run_pair(ctx)
     so0, ro0, so1, ro1 = oracle_run_pair(P)
@@ -237,6 +241,8 @@ def test_run_reference_pair(two_step):
     # core_test.cpp properties on the GPU result
     assert r0.s.models.n_cylinders > 0 and r0.s.models.n_planes > 0
     assert r1.s.success and (r1.matches[:r1.s.models.n_cylinders] != -1).any()
+    # PoseOptimization (core_test.cpp:177), unrelaxed: |T_Delta.t| < 0.1 m
+    assert np.linalg.norm(np.array(r1.s.T_Delta.t[:])) < 0.1
 
 
 def keyframe_pair(P, forest, kf, run):
@@ -282,13 +288,59 @@ def test_keyframe_synthetic_c2(two_step, cyl_mode):
     assert np.linalg.norm(t - kfs[0].t_gt) < 0.1
 
 
+@pytest.mark.parametrize("seed", [0, 2, 3])
+@pytest.mark.parametrize("two_step,cyl_mode", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_keyframe_synthetic_c1(seed, two_step, cyl_mode):
+    """16x1024 keyframes (ground slope U(0, 10 deg), 20 trunks, 64
+    hypotheses per tree), the first scan at the true pose then the keyframe
+    at its estimate, GPU against the oracle in both cylinder modes and both
+    pose modes.  Sixteen beams leave a few trees per scan: seed 0 fits 3
+    cylinders on 3 and 2 planes, seed 2 finds no cylinder (the second
+    keyframe ends in SLOAM_ERR_NO_MODELS, sloam.cpp:481-485), seed 3 none on
+    the first scan and one on the second.  Too few tree features for the
+    pose checks (sloam.cpp:497-499) keep the estimate as it was; the two
+    sides agree on every outcome."""
+    cfg = synth.C1
+    forest, kfs = synth.scene(cfg, seed=seed, n_kf=1)
+    P = synth.preset_params(cfg, two_step_optim=two_step, cyl_mode=cyl_mode, cyl_hypotheses=64)
+    ctx = make_ctx(P)
+    L = H.oracle()
+    os_ = L.oracle_create(C.byref(P))
+
+    def run_o(kf, pose, m, nm, r):
+        return L.oracle_keyframe(os_, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                 A.ptr(kf.labels, C.c_uint8), None, C.byref(pose), m, nm,
+                                 C.byref(r.s))
+
+    def run_g(kf, pose, m, nm, r):
+        return ctx.L.sloam_keyframe(ctx.h, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                    A.ptr(kf.labels, C.c_uint8), None, C.byref(pose), m, nm,
+                                    C.byref(r.s))
+
+    so0, ro0, so1, ro1 = keyframe_pair(P, forest, kfs[0], run_o)
+    sg0, rg0, sg1, rg1 = keyframe_pair(P, forest, kfs[0], run_g)
+    L.oracle_destroy(os_)
+    ctx.close()
+    assert (so0, so1) == (sg0, sg1)
+    compare_runs(ro0, rg0)
+    if so1 == 0:
+        compare_runs(ro1, rg1)
+    else:
+        assert so1 == A.SLOAM_ERR_NO_MODELS
+        assert ro1.s.models.n_cylinders == rg1.s.models.n_cylinders == 0
+
+
 @pytest.mark.parametrize("two_step", [0, 1])
 def test_keyframe_lm_c2(two_step):
     """pose_solver 1 (trust-region Levenberg-Marquardt with the reference's
-    Ceres settings) on the GPU against the oracle's: the same models,
-    matches and poses within the GN tolerance (measured 1e-7 m).  The LM
-    optimum and the 10-iteration GN pose agree within 10x that tolerance
-    (GN stops after a fixed count; measured 2e-5 m on the two-step pose)."""
+    Ceres settings) on the GPU against the oracle's: the same models and
+    matches, poses within 5e-5 m / 5e-6 rad.  The LM stops when a step
+    changes the cost by at most 1e-6 of it (Ceres' function tolerance); the
+    GPU sums FP32 residuals, whose rounding is of that order, so the two
+    sides can stop one step apart near the optimum (measured up to 1.6e-5 m;
+    the GN pose, with a fixed iteration count, keeps 1e-5 m).  The LM optimum
+    and the 10-iteration GN pose agree within 10x the GN tolerance (measured
+    2e-5 m on the two-step pose)."""
     cfg, forest, kfs = H.scene("C2")
     L = H.oracle()
     out = {}
@@ -319,7 +371,7 @@ def test_keyframe_lm_c2(two_step):
     _, t_g = rg1.s.T_Map_Curr.qt()
     _, t_gn = out[0, "o"][3].s.T_Map_Curr.qt()
     print("LM gpu-oracle", np.abs(t_g - t_o).max(), "LM-GN", np.abs(t_o - t_gn).max())
-    compare_runs(ro1, rg1)
+    compare_runs(ro1, rg1, pose_tol=5.0)
     assert np.abs(t_o - t_gn).max() < 10 * H.TOL_TRANS_M
     assert np.linalg.norm(t_g - kfs[0].t_gt) < 0.1
 
@@ -407,4 +459,46 @@ def test_keyframes_batches_match_single(destagger):
     ms, nch, nkf = C.c_float(), C.c_int32(), C.c_int32()
     ctx.check(ctx.L.sloam_frontend_time(ctx.h, C.byref(ms), C.byref(nch), C.byref(nkf)))
     assert nkf.value == B and nch.value >= 2 and ms.value > 0
+    ctx.close()
+
+
+def test_cc_union_limit_runs_out_and_context_recovers():
+    """The bounded union loop of the connected components gives up: with a
+    retry limit of 0 every union that is needed fails at once, the kernels
+    record it and return, the keyframe ends with SLOAM_ERR_TIMEOUT and its
+    message, and the same context then runs the keyframe normally (the
+    oracle's result) once the default limit is back."""
+    cfg, forest, kfs = H.scene("C2")
+    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1)
+    ctx = make_ctx(P)
+    kf = kfs[0]
+    mapc = A.cylinders_from_array(forest.map_cylinders())
+    gt = A.SE3.from_qt(*kf.pose_gt_qt())
+
+    def run():
+        r = A.RunBuffers(P)
+        st = ctx.L.sloam_keyframe(ctx.h, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                                  A.ptr(kf.labels, C.c_uint8), None, C.byref(gt), mapc,
+                                  len(forest.radius), C.byref(r.s))
+        r.refresh()
+        return st, r
+
+    assert ctx.L.sloam_set_cc_iter_limit(ctx.h, 0) == 0
+    st, _ = run()
+    assert st == A.SLOAM_ERR_TIMEOUT
+    assert "iteration limit" in ctx.error()
+    assert ctx.L.sloam_set_cc_iter_limit(ctx.h, -1) == 0
+    assert ctx.L.sloam_reset(ctx.h) == 0
+    st, rg = run()
+    assert st == 0 and rg.s.models.n_cylinders > 10
+    L = H.oracle()
+    os_ = L.oracle_create(C.byref(P))
+    ro = A.RunBuffers(P)
+    so = L.oracle_keyframe(os_, A.ptr(kf.xyzi, C.c_float), len(kf.xyzi),
+                           A.ptr(kf.labels, C.c_uint8), None, C.byref(gt), mapc,
+                           len(forest.radius), C.byref(ro.s))
+    ro.refresh()
+    L.oracle_destroy(os_)
+    assert so == 0
+    compare_runs(ro, rg)
     ctx.close()
