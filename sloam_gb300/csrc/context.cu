@@ -1511,17 +1511,47 @@ extern "C" int sloam_profile_stages(sloam_ctx* ctx, float* ms, int n) {
 
 // which: 0 = projection kernel (k_project), 1 = point-cylinder inlier
 // counting (k_cyl_count), 2 = the proposal network on the tensor cores over
-// the last keyframe's samples (cyl_mode 2).  Average milliseconds per launch
-// over `reps`.
+// the last keyframe's samples (cyl_mode 2), 3 = the whole cylinder stage
+// (vertex-line fits and the point-level fit of the context's cyl_mode),
+// 4 = the Trellis vertex kernel (k_vertex), 5 = the pose solve (k_gn),
+// 6 = the cylinder work queue (its ordering and persistent kernels, plain
+// RANSAC: cyl_mode >= 1).  All over the last keyframe run on the context.
+// Average milliseconds per launch (per stage for 3 and 6) over `reps`.
 extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg_ms) {
-  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 2) return SLOAM_ERR_ARG;
+  if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 6) return SLOAM_ERR_ARG;
   if (which == 2 && (ctx->P.cyl_mode != 2 || !ctx->prop_tc)) return SLOAM_ERR_ARG;
+  if ((which == 3 && ctx->P.cyl_mode == 2 && !ctx->prop_tc) ||
+      (which == 6 && (ctx->P.cyl_mode < 1 || ctx->kp.K < 1)))
+    return SLOAM_ERR_ARG;
   cudaSetDevice(ctx->device);
   Dev& d = ctx->d;
   if (int st = own_views(ctx)) return st;
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
+  if (which >= 3) {
+    // one event pair per repetition; the queue's inputs are rebuilt before
+    // each (it consumes the vertex-line models it refines)
+    float total = 0.0f;
+    for (int r = 0; r < reps; ++r) {
+      if (which == 6) launch_cyl_count_prep(d, ctx->kp, ctx->st);
+      CK(cudaEventRecord(a, ctx->st));
+      if (which == 3) launch_cylinders(d, ctx->kp, true, ctx->st);
+      else if (which == 4) launch_vertex_kernel(d, ctx->kp, ctx->st);
+      else if (which == 5) launch_pose_kernel(d, ctx->kp, ctx->st);
+      else launch_cyl_queue(d, ctx->kp, nullptr, ctx->st);
+      CK(cudaEventRecord(b, ctx->st));
+      CK(cudaEventSynchronize(b));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, a, b));
+      total += ms;
+    }
+    *avg_ms = total / reps;
+    CK(cudaStreamSynchronize(ctx->st));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return SLOAM_OK;
+  }
   // the inlier-counting kernel scores trees still at the vertex-line stage
   if (which == 1) launch_cyl_count_prep(d, ctx->kp, ctx->st);
   CK(cudaEventRecord(a, ctx->st));
@@ -1602,5 +1632,9 @@ extern "C" int sloam_keyframe_stats(const sloam_ctx* ctx, int32_t* out, int n) {
   out[2] = c.n_planes;
   out[3] = c.n_fallback;
   out[4] = c.n_slow_px;
+  if (n > 5) out[5] = c.n_fit;
+  if (n > 6) out[6] = c.n_fit_pts;
+  if (n > 7) out[7] = c.n_bucket;
+  if (n > 8) out[8] = c.n_tm + c.n_pm;
   return SLOAM_OK;
 }

@@ -119,6 +119,9 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
     sbase += stotal;
     const int cnt = __syncthreads_count(nc > 0);
     nq += cnt;
+    // (the last chunk of a tree holds its remainder: points = slices' points)
+    if (nc && !only) atomicAdd(&d.cnt->n_fit_pts,
+                               (int)(0xFFFFFFFFu - (uint32_t)(key[i] >> 32)));
   }
   if (threadIdx.x == 0) {
     d.q_off[nq] = base;
@@ -127,6 +130,7 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
     q->nq = nq;
     q->phases = P;
     q->head = 0;
+    if (!only) d.cnt->n_fit = nq;
   }
 }
 

@@ -35,7 +35,10 @@ struct Counters {
   int32_t n_fallback;    // mode 2: trees that fell back to RANSAC
   int32_t prop_err;      // mode 2: a tensor-core wait gave up
   int32_t queue_err;     // the cylinder work queue: a wait gave up
-  int32_t pad[8];
+  int32_t n_fit;         // trees given to the point-level cylinder fit
+  int32_t n_fit_pts;     // their points (the work queue's trees)
+  int32_t n_bucket;      // tree pixels in the Trellis (component, row) buckets
+  int32_t pad[5];
 };
 
 // The cylinder work queue (cylqueue.cu): the item counter and the shape of
@@ -311,6 +314,8 @@ int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_sta
 // the persistent work queue; cylqueue.cu
 int launch_cyl_queue(const Dev& d, const KParams& kp, const int32_t* only, cudaStream_t st);
 bool queue_shape_valid(int chunk_points, int hyp_tile);
+int launch_vertex_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
+int launch_pose_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 void init_queue_attributes();
 int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trellis,
                                cudaStream_t st);

@@ -1314,7 +1314,10 @@ __global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * S;
        it += gridDim.x * blockDim.x) {
     const int l = it / S;
-    if (it == l * S) d.pflag[l] = 0;
+    if (it == l * S) {
+      d.pflag[l] = 0;
+      if (fit_eligible(d.cyl_all[l])) atomicAdd(&d.cnt->n_fit, 1);
+    }
     d.phyp_cnt[it] = 0;
     float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
     const CylD c = d.cyl_all[l];

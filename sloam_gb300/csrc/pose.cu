@@ -928,6 +928,16 @@ __global__ void __launch_bounds__(kAssocThreads) k_finalize(Dev d, KParams kp, i
 
 }  // namespace
 
+// The pose solve alone over the last keyframe's residual table, for timing
+// (it reads the estimate and writes the result into separate slots).
+int launch_pose_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
+  if (kp.pose_lm)
+    k_gn<true><<<1, kGN, 0, st>>>(d, kp);
+  else
+    k_gn<false><<<1, kGN, 0, st>>>(d, kp);
+  return 1;
+}
+
 int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update, cudaStream_t st) {
   if (first_scan) {
     k_finalize<<<64, kAssocThreads, 0, st>>>(d, kp, 1, update ? 1 : 0);

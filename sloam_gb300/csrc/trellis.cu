@@ -318,7 +318,10 @@ __global__ void __launch_bounds__(1024) k_rowscan(Dev d) {
     if (i < n) d.roff[i] = base + ex;
     base += total;
   }
-  if (threadIdx.x == 0) d.roff[n] = base;
+  if (threadIdx.x == 0) {
+    d.roff[n] = base;
+    d.cnt->n_bucket = base;
+  }
 }
 
 constexpr int kVtxCap = 256;   // points per vertex staged in shared memory
@@ -774,6 +777,12 @@ __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
 }
 
 }  // namespace
+
+// k_vertex alone over the last keyframe's (component, row) buckets, for timing.
+int launch_vertex_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
+  k_vertex<<<2 * 152, kVtxWarps * 32, 0, st>>>(d, kp);
+  return 1;
+}
 
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   const int N = d.N;
