@@ -126,7 +126,7 @@ typedef struct sloam_params {
                                        1024                          (256) */
   int32_t cyl_hyp_tile;             /* hypotheses staged per pass: 64, 128,
                                        256, 512 or 1024              (256) */
-  int32_t cyl_queue_blocks;         /* persistent blocks (0: 152)          */
+  int32_t cyl_queue_blocks;         /* persistent blocks (0: 76)           */
 } sloam_params;
 
 void sloam_params_default(sloam_params* p);

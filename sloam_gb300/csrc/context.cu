@@ -393,7 +393,7 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.q_hyp = c.take<float4>(d.cap_lm);
   // 256-point slices, at most one partial slice per tree
   d.q_cap_chunks = (int)(((size_t)d.cap_cluster + d.cap_p) / 256 + d.cap_lm);
-  d.q_part = c.take<double>((size_t)d.q_cap_chunks * 20);
+  d.q_part = c.take<float>((size_t)d.q_cap_chunks * 20);
   const size_t ps = (size_t)std::max(d.prop_cap, 1);
   d.prop_x = c.take<float>(ps * 384);
   d.prop_f = c.take<float4>(ps);

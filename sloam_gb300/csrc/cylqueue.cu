@@ -4,28 +4,33 @@
 // the least-squares refinement, over trees of very uneven size.
 //
 // The reference fits its trees one after the other (sloam.cpp:418-434, one
-// Cylinder per landmark).  Here a tree of n points is cut into chunks of
-// kC points, and every (phase, tree, chunk) is one work item:
+// Cylinder per landmark).  Here the trees are queued largest first and
+// blocks take work items from one atomic counter.  A tree of at most
+// kSplitChunks chunks (chunk = `cyl_chunk_points` points) is one item: one
+// block counts, selects and refines it with no wait.  A larger tree is cut
+// into chunks, and every (phase, chunk) of it is an item:
 //   phase 0        count the inliers of all K hypotheses on the chunk
 //                  (ballot + popcount per 32 points, integer atomics);
 //   phase 1..L     one LS iteration: the 20 normal-equation sums of each
-//                  256-point slice of the chunk (FP32 per point, warp-shuffle
-//                  sums, FP64 across warps).
-// Items are numbered phase-major, and within a phase the trees come in
-// decreasing size, so that the long chains of the largest trees start first.
-// Blocks take items from one atomic counter.  The block that completes the
-// last chunk of (tree, phase) finishes the phase for the tree: after phase 0
-// the best hypothesis (most inliers, lowest index on ties) and the initial
-// model; after an LS phase the slice sums in slice order (FP64, a fixed
-// order: the results depend neither on which block ran which chunk nor on
-// the chunk size, the hypothesis tile or the block count), the FP64
-// 5x5 solve on one warp and the model update; after the last phase the
-// cylinder record.  An item of phase p > 0 waits until its tree has
-// finished phase p - 1.  Items are claimed in increasing order and a block
-// never waits while it holds an unfinished item, so the lowest unfinished
-// item always belongs to a running block whose dependencies are done: the
-// waits end.  Each wait is still bounded (kQueueWaitPolls); when one runs
-// out the kernel sets the counters' error flag and its blocks stop.
+//                  256-point slice of the chunk.
+// The block that completes the last chunk of (tree, phase) finishes the
+// phase: after phase 0 the best hypothesis (most inliers, lowest index on
+// ties) and the initial model; after an LS phase the slice sums in slice
+// order, the FP64 5x5 solve on one warp and the model update; after the
+// last phase the cylinder record.  Both kinds of tree use the same slice
+// sums (FP32 per point, warp-shuffle sums, the warps in order) added in
+// slice order in FP64, so the result depends neither on the split, nor on
+// which block ran which chunk, the chunk size, the hypothesis tile or the
+// block count.
+//
+// Item order: the split trees' phase-0 chunks, then the whole trees, then
+// the split trees' phases 1..L, so the phase-0 finishers have run by the
+// time their trees' LS items are claimed.  An item of phase p > 0 waits until
+// its tree has finished phase p - 1.  Items are claimed in increasing order
+// and a block never waits while it holds an unfinished item, so the lowest
+// unfinished item always belongs to a running block whose dependencies are
+// done: the waits end.  Each wait is still bounded (kQueueWaitPolls); when
+// one runs out the kernel sets the counters' error flag and its blocks stop.
 #include "cylinder.cuh"
 #include "internal.h"
 #include "scan_util.cuh"
@@ -36,6 +41,8 @@ namespace {
 
 constexpr int kQThreads = 256;
 constexpr int kQWarps = kQThreads / 32;
+constexpr int kSlice = kQThreads;         // points of one LS slice
+constexpr int kSplitChunks = 4;           // larger trees are split over blocks
 constexpr int kQSortCap = 4096;           // trees per keyframe the queue orders
 constexpr long long kQueueWaitPolls = 1ll << 22;  // x ~100 ns: about 0.4 s
 
@@ -45,8 +52,9 @@ __device__ __forceinline__ bool queue_eligible(const Dev& d, const CylD& c, int 
 }
 
 // One block: the eligible trees with points, ordered by decreasing point
-// count (ties by index), their chunk offsets, and the per-tree phase state
-// reset.  chunk = points per work item.
+// count (ties by index); the split trees (more than kSplitChunks chunks)
+// come first, with their chunk and slice offsets, then the whole trees; the
+// per-tree phase state of the split trees is reset.
 __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
                                                          const int32_t* __restrict__ only,
                                                          int chunk) {
@@ -59,6 +67,7 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
       atomicOr(&d.cnt->overflow, 64);
       q->tc = 0;
       q->nq = 0;
+      q->nsplit = 0;
       q->phases = 1;
       q->head = 0;
     }
@@ -95,39 +104,41 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
     }
   }
   const int P = 1 + kp.ls_iters;
-  int base = 0, sbase = 0, nq = 0;
+  int base = 0, sbase = 0, nq = 0, nsplit = 0;
   for (int i0 = 0; i0 < n2; i0 += blockDim.x) {
     const int i = i0 + threadIdx.x;
-    int nc = 0;
-    if (i < n2 && key[i] != ~0ull) {
+    const bool valid = i < n2 && key[i] != ~0ull;
+    const int n = valid ? (int)(0xFFFFFFFFu - (uint32_t)(key[i] >> 32)) : 0;
+    const int nc = valid ? (n + chunk - 1) / chunk : 0;
+    const bool split = nc > kSplitChunks;
+    if (valid) {
       const int l = (int)(uint32_t)key[i];
-      const int n = (int)(0xFFFFFFFFu - (uint32_t)(key[i] >> 32));
-      nc = (n + chunk - 1) / chunk;
       d.q_order[i] = l;
-      d.q_ready[l] = 0;
-      for (int p = 0; p < P; ++p) d.q_done[(size_t)l * kQueuePhases + p] = 0;
+      if (split) {
+        d.q_ready[l] = 0;
+        for (int p = 0; p < P; ++p) d.q_done[(size_t)l * kQueuePhases + p] = 0;
+      }
+      if (!only) atomicAdd(&d.cnt->n_fit_pts, n);
     }
+    // sizes decrease along the order: the split trees are a prefix
     int total, stotal;
-    const int ex = block_excl_scan(nc, sm, &total);
-    const int ns = nc ? (int)((0xFFFFFFFFu - (uint32_t)(key[i] >> 32) + 255u) / 256u) : 0;
-    const int sex = block_excl_scan(ns, sm, &stotal);
-    if (nc) {
+    const int ex = block_excl_scan(split ? nc : 0, sm, &total);
+    const int sex = block_excl_scan(split ? (n + kSlice - 1) / kSlice : 0, sm, &stotal);
+    if (split) {
       d.q_off[i] = base + ex;
       d.q_soff[i] = sbase + sex;
     }
     base += total;
     sbase += stotal;
-    const int cnt = __syncthreads_count(nc > 0);
-    nq += cnt;
-    // (the last chunk of a tree holds its remainder: points = slices' points)
-    if (nc && !only) atomicAdd(&d.cnt->n_fit_pts,
-                               (int)(0xFFFFFFFFu - (uint32_t)(key[i] >> 32)));
+    nq += __syncthreads_count(valid);
+    nsplit += __syncthreads_count(split);
   }
   if (threadIdx.x == 0) {
-    d.q_off[nq] = base;
-    d.q_soff[nq] = sbase;
+    d.q_off[nsplit] = base;
+    d.q_soff[nsplit] = sbase;
     q->tc = base;
     q->nq = nq;
+    q->nsplit = nsplit;
     q->phases = P;
     q->head = 0;
     if (!only) d.cnt->n_fit = nq;
@@ -152,39 +163,264 @@ __device__ void queue_write_cylinder(Dev& d, int l, const double* st, int best_c
   d.cyl_all[l] = c;
 }
 
-// Dynamic shared memory of the worker: the hypothesis tile, the per-warp
-// counts of the tile, then the small state.
+// Dynamic shared memory of the worker: the hypothesis tile and the per-warp
+// counts of the tile.
 template <int kTile>
 struct QueueSmem {
   float4 hyp[kTile];
   int cnt[kQWarps][kTile];
 };
 
+// Small per-block state in static shared memory.
+struct QueueBlock {
+  float red[20][kQWarps];
+  double st[16];  // c(3), dir(3), r, ok, b1(3), b2(3), best count, best h
+  float sf[16];   // float copies of the model and its frame (ls_frame)
+  double ssum[20];
+  double sxls[5];
+  unsigned long long sk[kQWarps];
+  float4 hyp;     // the best hypothesis's circle
+  int idx, last, stop;
+};
+
+// Inlier counts of hypotheses [0, nt) staged in S.hyp over the points
+// [i0, i1) of the tree, 32 points per warp at a time; lane j of each warp
+// adds the count of hypothesis hb * 32 + j to acc[hb].
+template <int kTile>
+__device__ __forceinline__ void count_tile(const QueueSmem<kTile>& S, int nt,
+                                           const float2* __restrict__ uvs, int i0, int i1,
+                                           int* acc) {
+  const int lane = threadIdx.x & 31;
+  for (int b = i0; b < i1; b += kQThreads) {
+    const int i = b + (int)threadIdx.x;
+    const bool mine = i < i1;
+    const float2 pu = mine ? uvs[i] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int hb = 0; hb < kTile / 32; ++hb) {
+      if (hb * 32 >= nt) break;  // block-uniform
+      const int jn = min(32, nt - hb * 32);
+#pragma unroll 4
+      for (int j = 0; j < jn; ++j) {
+        const float4 e = S.hyp[hb * 32 + j];
+        const float du = fsub(pu.x, e.x), dv = fsub(pu.y, e.y);
+        const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+        const unsigned bal = __ballot_sync(0xffffffffu, mine && (d2 > e.z) && (d2 < e.w));
+        if (lane == j) acc[hb] += __popc(bal);
+      }
+    }
+  }
+}
+
+// Inlier counts of all K hypotheses of tree l over points [i0, i1), tile by
+// tile: `whole` keeps the best key (most inliers, lowest index) of the
+// block, otherwise the counts go to hyp_cnt by atomics.
+template <int kTile>
+__device__ unsigned long long count_points(const Dev& d, QueueSmem<kTile>& S, int l, int K,
+                                           const float2* __restrict__ uvs, int i0, int i1,
+                                           bool whole) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  unsigned long long best = 0ull;
+  for (int t0 = 0; t0 < K; t0 += kTile) {
+    const int nt = min(kTile, K - t0);
+    for (int i = tid; i < kTile; i += kQThreads)
+      S.hyp[i] = i < nt ? d.hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
+    __syncthreads();
+    int acc[kTile / 32];
+#pragma unroll
+    for (int hb = 0; hb < kTile / 32; ++hb) acc[hb] = 0;
+    count_tile<kTile>(S, nt, uvs, i0, i1, acc);
+#pragma unroll
+    for (int hb = 0; hb < kTile / 32; ++hb) S.cnt[w][hb * 32 + lane] = acc[hb];
+    __syncthreads();
+    for (int h = tid; h < nt; h += kQThreads) {
+      int s = 0;
+#pragma unroll
+      for (int k = 0; k < kQWarps; ++k) s += S.cnt[k][h];
+      if (!whole) {
+        if (s) atomicAdd(d.hyp_cnt + (size_t)l * K + t0 + h, s);
+      } else if (s > 0) {
+        const unsigned long long kk = ((unsigned long long)s << 32) |
+                                      (unsigned long long)(0xFFFFFFFFu - (uint32_t)(t0 + h));
+        best = kk > best ? kk : best;
+      }
+    }
+    __syncthreads();
+  }
+  return best;
+}
+
+// The 20 LS sums of slice `sl` of the tree (points sl*256 .. +255 that are
+// inliers of the fixed hypothesis B.hyp), for the model in B.sf: FP32 per
+// point, warp-shuffle sums, the warps summed in order; threads 0..19 return
+// sum j = tid, other threads 0.
+__device__ __forceinline__ float slice_sums(QueueBlock& B, const float4* __restrict__ pts,
+                                            const float2* __restrict__ uvs, int n, int sl) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const float* sf = B.sf;
+  const float4 H = B.hyp;
+  const int i = sl * kSlice + tid;
+  float acc[20];
+#pragma unroll
+  for (int j = 0; j < 20; ++j) acc[j] = 0.f;
+  bool use = i < n;
+  float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (use) {
+    const float2 uv = uvs[i];
+    const float du = fsub(uv.x, H.x), dv = fsub(uv.y, H.y);
+    const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+    use = (d2 > H.z) & (d2 < H.w);
+    if (use) qp = pts[i];
+  }
+  const float wx = qp.x - sf[0], wy = qp.y - sf[1], wz = qp.z - sf[2];
+  const float dx = sf[3], dy = sf[4], dz = sf[5];
+  const float wd = wx * dx + wy * dy + wz * dz;
+  const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
+  const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
+  if (use && rho > 0.f) {
+    const float res = rho - sf[12];
+    const float a1 = (px_ * sf[6] + py_ * sf[7] + pz_ * sf[8]) / rho;
+    const float a2 = (px_ * sf[9] + py_ * sf[10] + pz_ * sf[11]) / rho;
+    const float J[5] = {-a1, -a2, -wd * a1, -wd * a2, -1.0f};
+    int m = 0;
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = a; b < 5; ++b) acc[m++] = J[a] * J[b];
+#pragma unroll
+    for (int a = 0; a < 5; ++a) acc[15 + a] = J[a] * res;
+  }
+#pragma unroll
+  for (int j = 0; j < 20; ++j) {
+    const float v = warp_sum(acc[j]);
+    if (lane == 0) B.red[j][w] = v;
+  }
+  __syncthreads();
+  float t = 0.0f;
+  if (tid < 20)
+    for (int q2 = 0; q2 < kQWarps; ++q2) t += B.red[tid][q2];
+  __syncthreads();
+  return t;
+}
+
+// The tree's initial model from its best hypothesis key into B.st, B.sf
+// and B.hyp.  Thread 0.
+__device__ void init_model(Dev& d, const KParams& kp, QueueBlock& B, int l, int n,
+                           const float2* __restrict__ uvs, unsigned long long best) {
+  const int K = kp.K;
+  const int h = (int)(0xFFFFFFFFu - (uint32_t)(best & 0xffffffffull));
+  const CylD cy = d.cyl_all[l];
+  const CylFrame f = make_frame(d, cy);
+  const float4 e = d.hyp[(size_t)l * K + h];
+  double* st = B.st;
+  st[0] = f.ox + (double)e.x * f.e1x + (double)e.y * f.e2x;
+  st[1] = f.oy + (double)e.x * f.e1y + (double)e.y * f.e2y;
+  st[2] = f.oz + (double)e.x * f.e1z + (double)e.y * f.e2z;
+  const double an = sqrt((double)f.ax * f.ax + (double)f.ay * f.ay + (double)f.az * f.az);
+  st[3] = f.ax / an; st[4] = f.ay / an; st[5] = f.az / an;
+  const Hyp Hh = make_hyp(kp, h, cy.id, n, [&](uint32_t i) { return uvs[i]; });
+  st[6] = Hh.r;
+  st[7] = 1.0;
+  st[14] = (double)(int)(best >> 32);
+  st[15] = (double)h;
+  ls_frame(st, B.sf);
+  B.hyp = e;
+}
+
+// The 5x5 normal equations in B.ssum solved on warp 0, the model updated
+// (lane 0); st[7] = 0 when the solve fails.  Called by all of warp 0.
+__device__ __noinline__ void solve_update(QueueBlock& B) {
+  const int lane = threadIdx.x & 31;
+  const bool solved = warp_chol_solve<5>(B.ssum, B.ssum + 15, B.sxls);
+  __syncwarp();
+  if (lane == 0) {
+    double* st = B.st;
+    if (solved) {
+      const double* x = B.sxls;
+      const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
+      const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
+      d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
+      d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
+      d2 = scl3(1.0 / norm3(d2), d2);
+      st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
+      st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
+      st[6] = st[6] + x[4];
+      ls_frame(st, B.sf);
+    } else {
+      st[7] = 0.0;
+    }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ unsigned long long block_max_key(QueueBlock& B, unsigned long long v) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x > v ? x : v;
+  }
+  if (lane == 0) B.sk[w] = v;
+  __syncthreads();
+  unsigned long long m = B.sk[0];
+  for (int k = 1; k < kQWarps; ++k) m = B.sk[k] > m ? B.sk[k] : m;
+  __syncthreads();
+  return m;
+}
+
 template <int kPPT, int kTile>
-__global__ void __launch_bounds__(kQThreads) k_cyl_queue(Dev d, KParams kp) {
+__global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
   extern __shared__ __align__(16) unsigned char q_smem[];
   QueueSmem<kTile>& S = *reinterpret_cast<QueueSmem<kTile>*>(q_smem);
-  __shared__ float red[20][kQWarps];
-  __shared__ double st[16];  // c(3), dir(3), r, ok, b1(3), b2(3), best count, best h
-  __shared__ double ssum[20];
-  __shared__ double sxls[5];
-  __shared__ unsigned long long sk[kQWarps];
-  __shared__ int s_idx, s_last, s_stop;
+  __shared__ QueueBlock B;
   constexpr int kC = kPPT * kQThreads;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   QueueCtl* q = d.qctl;
-  const int TC = q->tc, P = q->phases, nq = q->nq, K = kp.K;
-  const long long total = (long long)TC * P;
+  const int TC = q->tc, P = q->phases, nq = q->nq, nsplit = q->nsplit, K = kp.K;
+  const int nwhole = nq - nsplit;
+  const long long total = (long long)TC * P + nwhole;
   for (;;) {
     if (tid == 0) {
-      s_idx = atomicAdd(&q->head, 1);
-      s_stop = 0;
+      B.idx = atomicAdd(&q->head, 1);
+      B.stop = 0;
     }
     __syncthreads();
-    const int idx = s_idx;
+    const int idx = B.idx;
     if ((long long)idx >= total) break;  // block-uniform
-    const int p = idx / TC, r = idx - p * TC;
-    int lo = 0, hi = nq - 1;  // the tree whose chunks hold r
+    if (idx >= TC && idx < TC + nwhole) {
+      // ---------------- a whole tree: count, best, LS, record
+      const int l = d.q_order[nsplit + (idx - TC)];
+      const float4* pts;
+      const float2* uvs;
+      int n;
+      tree_points(d, l, &pts, &n, &uvs);
+      const unsigned long long best =
+          block_max_key(B, count_points<kTile>(d, S, l, K, uvs, 0, n, true));
+      if (best != 0ull) {
+        if (tid == 0) {
+          d.cyl_best[l] = best;
+          init_model(d, kp, B, l, n, uvs, best);
+        }
+        __syncthreads();
+        const int ns = (n + kSlice - 1) / kSlice;
+        for (int p = 1; p < P; ++p) {
+          if (B.st[7] == 0.0) break;  // block-uniform
+          double t = 0.0;
+          for (int sl = 0; sl < ns; ++sl) t += (double)slice_sums(B, pts, uvs, n, sl);
+          if (tid < 20) B.ssum[tid] = t;
+          __syncthreads();
+          if (w == 0) solve_update(B);
+          __syncthreads();
+        }
+        if (tid == 0) queue_write_cylinder(d, l, B.st, (int)B.st[14]);
+      } else if (tid == 0) {
+        d.cyl_best[l] = 0ull;
+      }
+      __syncthreads();
+      continue;
+    }
+    // ---------------- one chunk of a split tree
+    const int p = idx < TC ? 0 : 1 + (idx - TC - nwhole) / TC;
+    const int r = idx < TC ? idx : (idx - TC - nwhole) % TC;
+    int lo = 0, hi = nsplit - 1;  // the tree whose chunks hold r
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
       if (d.q_off[mid] <= r) lo = mid;
@@ -203,7 +439,7 @@ __global__ void __launch_bounds__(kQThreads) k_cyl_queue(Dev d, KParams kp) {
         while (*reinterpret_cast<volatile int*>(d.q_ready + l) < p) {
           if (++it > kQueueWaitPolls || *reinterpret_cast<volatile int*>(&d.cnt->queue_err)) {
             atomicOr(&d.cnt->queue_err, 1);
-            s_stop = 1;
+            B.stop = 1;
             break;
           }
           __nanosleep(100);
@@ -211,112 +447,25 @@ __global__ void __launch_bounds__(kQThreads) k_cyl_queue(Dev d, KParams kp) {
         __threadfence();
       }
       __syncthreads();
-      if (s_stop) break;
+      if (B.stop) break;
     }
     if (p == 0) {
       // ---- inlier counts of the chunk for every hypothesis of the tree
-      float2 pu[kPPT];
-      bool mine[kPPT];
-#pragma unroll
-      for (int k = 0; k < kPPT; ++k) {
-        const int i = c * kC + k * kQThreads + tid;
-        mine[k] = i < n;
-        pu[k] = mine[k] ? uvs[i] : make_float2(0.f, 0.f);
-      }
-      for (int t0 = 0; t0 < K; t0 += kTile) {
-        const int nt = min(kTile, K - t0);
-        for (int i = tid; i < kTile; i += kQThreads)
-          S.hyp[i] = i < nt ? d.hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
-        __syncthreads();
-        int acc[kTile / 32];
-#pragma unroll
-        for (int hb = 0; hb < kTile / 32; ++hb) acc[hb] = 0;
-#pragma unroll
-        for (int hb = 0; hb < kTile / 32; ++hb) {
-          if (hb * 32 >= nt) break;  // block-uniform
-          const int jn = min(32, nt - hb * 32);
-#pragma unroll 4
-          for (int j = 0; j < jn; ++j) {
-            const float4 e = S.hyp[hb * 32 + j];
-            int votes = 0;
-#pragma unroll
-            for (int k = 0; k < kPPT; ++k) {
-              const float du = fsub(pu[k].x, e.x), dv = fsub(pu[k].y, e.y);
-              const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-              votes += __popc(__ballot_sync(0xffffffffu, mine[k] && (d2 > e.z) && (d2 < e.w)));
-            }
-            if (lane == j) acc[hb] += votes;
-          }
-        }
-#pragma unroll
-        for (int hb = 0; hb < kTile / 32; ++hb) S.cnt[w][hb * 32 + lane] = acc[hb];
-        __syncthreads();
-        for (int h = tid; h < nt; h += kQThreads) {
-          int s = 0;
-#pragma unroll
-          for (int k = 0; k < kQWarps; ++k) s += S.cnt[k][h];
-          if (s) atomicAdd(d.hyp_cnt + (size_t)l * K + t0 + h, s);
-        }
-        __syncthreads();
-      }
+      count_points<kTile>(d, S, l, K, uvs, c * kC, min(n, c * kC + kC), false);
     } else {
-      // ---- one LS iteration's sums over the chunk (the hypothesis's
-      // inliers, fixed over the iterations)
+      // ---- one LS iteration's sums over the chunk's slices (the
+      // hypothesis's inliers, fixed over the iterations)
       const double* gst = d.q_st + (size_t)l * 16;
       const bool live = __ldcg(gst + 15) >= 0.0 && __ldcg(gst + 7) != 0.0;
       if (live) {
-        const float* sf = d.q_sf + (size_t)l * 16;
-        const float cx = __ldcg(sf + 0), cy = __ldcg(sf + 1), cz = __ldcg(sf + 2);
-        const float dx = __ldcg(sf + 3), dy = __ldcg(sf + 4), dz = __ldcg(sf + 5);
-        const float b1x = __ldcg(sf + 6), b1y = __ldcg(sf + 7), b1z = __ldcg(sf + 8);
-        const float b2x = __ldcg(sf + 9), b2y = __ldcg(sf + 10), b2z = __ldcg(sf + 11);
-        const float rf = __ldcg(sf + 12);
-        const float4 H = __ldcg(d.q_hyp + l);
+        if (tid < 13) B.sf[tid] = __ldcg(d.q_sf + (size_t)l * 16 + tid);
+        if (tid == 0) B.hyp = __ldcg(d.q_hyp + l);
+        __syncthreads();
         for (int k = 0; k < kPPT; ++k) {
           const int sl = c * kPPT + k;  // the slice of the tree
           if (sl >= ns) break;          // block-uniform
-          const int i = sl * kQThreads + tid;
-          float acc[20];
-#pragma unroll
-          for (int j = 0; j < 20; ++j) acc[j] = 0.f;
-          bool use = i < n;
-          float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (use) {
-            const float2 uv = uvs[i];
-            const float du = fsub(uv.x, H.x), dv = fsub(uv.y, H.y);
-            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-            use = (d2 > H.z) & (d2 < H.w);
-            if (use) qp = pts[i];
-          }
-          const float wx = qp.x - cx, wy = qp.y - cy, wz = qp.z - cz;
-          const float wd = wx * dx + wy * dy + wz * dz;
-          const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
-          const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
-          if (use && rho > 0.f) {
-            const float res = rho - rf;
-            const float a1 = (px_ * b1x + py_ * b1y + pz_ * b1z) / rho;
-            const float a2 = (px_ * b2x + py_ * b2y + pz_ * b2z) / rho;
-            const float J[5] = {-a1, -a2, -wd * a1, -wd * a2, -1.0f};
-            int m = 0;
-#pragma unroll
-            for (int a = 0; a < 5; ++a)
-#pragma unroll
-              for (int b = a; b < 5; ++b) acc[m++] = J[a] * J[b];
-#pragma unroll
-            for (int a = 0; a < 5; ++a) acc[15 + a] = J[a] * res;
-          }
-#pragma unroll
-          for (int j = 0; j < 20; ++j) {
-            const float v = warp_sum(acc[j]);
-            if (lane == 0) red[j][w] = v;
-          }
-          __syncthreads();
-          if (tid < 20) {
-            double t = 0.0;
-            for (int q2 = 0; q2 < kQWarps; ++q2) t += red[tid][q2];
-            d.q_part[(size_t)(s0 + sl) * 20 + tid] = t;
-          }
-          __syncthreads();
+          const float t = slice_sums(B, pts, uvs, n, sl);
+          if (tid < 20) d.q_part[(size_t)(s0 + sl) * 20 + tid] = t;
         }
       }
     }
@@ -324,13 +473,12 @@ __global__ void __launch_bounds__(kQThreads) k_cyl_queue(Dev d, KParams kp) {
     __syncthreads();
     if (tid == 0) {
       __threadfence();
-      s_last = atomicAdd(d.q_done + (size_t)l * kQueuePhases + p, 1) == nc - 1;
+      B.last = atomicAdd(d.q_done + (size_t)l * kQueuePhases + p, 1) == nc - 1;
     }
     __syncthreads();
-    if (s_last) {
+    if (B.last) {
       __threadfence();
       if (p == 0) {
-        // best hypothesis: most inliers, lowest index on ties
         unsigned long long best = 0ull;
         for (int h = tid; h < K; h += kQThreads) {
           const int cn = __ldcg(d.hyp_cnt + (size_t)l * K + h);
@@ -340,83 +488,42 @@ __global__ void __launch_bounds__(kQThreads) k_cyl_queue(Dev d, KParams kp) {
             best = kk > best ? kk : best;
           }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-          best = x > best ? x : best;
-        }
-        if (lane == 0) sk[w] = best;
-        __syncthreads();
+        best = block_max_key(B, best);
         if (tid == 0) {
-          for (int k = 1; k < kQWarps; ++k) best = sk[k] > best ? sk[k] : best;
           d.cyl_best[l] = best;
           double* gst = d.q_st + (size_t)l * 16;
-          float* gsf = d.q_sf + (size_t)l * 16;
           if (best == 0ull) {
             gst[7] = 0.0;
             gst[15] = -1.0;  // no hypothesis with inliers: the vertex-line model stays
           } else {
-            const int h = (int)(0xFFFFFFFFu - (uint32_t)(best & 0xffffffffull));
-            const CylD cy = d.cyl_all[l];
-            const CylFrame f = make_frame(d, cy);
-            const float4 e = d.hyp[(size_t)l * K + h];
-            st[0] = f.ox + (double)e.x * f.e1x + (double)e.y * f.e2x;
-            st[1] = f.oy + (double)e.x * f.e1y + (double)e.y * f.e2y;
-            st[2] = f.oz + (double)e.x * f.e1z + (double)e.y * f.e2z;
-            const double an =
-                sqrt((double)f.ax * f.ax + (double)f.ay * f.ay + (double)f.az * f.az);
-            st[3] = f.ax / an; st[4] = f.ay / an; st[5] = f.az / an;
-            // the hypothesis radius: sqrt(hi2) - tau reproduces the circle's r
-            const Hyp Hh = make_hyp(kp, h, cy.id, n, [&](uint32_t i) { return uvs[i]; });
-            st[6] = Hh.r;
-            st[7] = 1.0;
-            st[14] = (double)(int)(best >> 32);
-            st[15] = (double)h;
-            float sfl[13];
-            ls_frame(st, sfl);
-            for (int j = 0; j < 16; ++j) gst[j] = st[j];
-            for (int j = 0; j < 13; ++j) gsf[j] = sfl[j];
-            d.q_hyp[l] = e;
-            if (P == 1) queue_write_cylinder(d, l, st, (int)(best >> 32));
+            init_model(d, kp, B, l, n, uvs, best);
+            for (int j = 0; j < 16; ++j) gst[j] = B.st[j];
+            for (int j = 0; j < 13; ++j) d.q_sf[(size_t)l * 16 + j] = B.sf[j];
+            d.q_hyp[l] = B.hyp;
+            if (P == 1) queue_write_cylinder(d, l, B.st, (int)(best >> 32));
           }
         }
       } else {
-        if (tid == 0)
-          for (int j = 0; j < 16; ++j) st[j] = __ldcg(d.q_st + (size_t)l * 16 + j);
+        if (tid < 16) B.st[tid] = __ldcg(d.q_st + (size_t)l * 16 + tid);
         __syncthreads();
-        const bool has_model = st[15] >= 0.0;
-        if (has_model && st[7] != 0.0 && w == 0) {
+        const bool has_model = B.st[15] >= 0.0;
+        if (has_model && B.st[7] != 0.0 && w == 0) {
           if (lane < 20) {
             double t = 0.0;
-            for (int k = 0; k < ns; ++k) t += __ldcg(d.q_part + (size_t)(s0 + k) * 20 + lane);
-            ssum[lane] = t;
+            for (int k = 0; k < ns; ++k)
+              t += (double)__ldcg(d.q_part + (size_t)(s0 + k) * 20 + lane);
+            B.ssum[lane] = t;
           }
           __syncwarp();
-          const bool solved = warp_chol_solve<5>(ssum, ssum + 15, sxls);
-          __syncwarp();
+          solve_update(B);
           if (lane == 0) {
-            if (solved) {
-              const double* x = sxls;
-              const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
-              const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
-              d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
-              d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
-              d2 = scl3(1.0 / norm3(d2), d2);
-              st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
-              st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
-              st[6] = st[6] + x[4];
-              float sfl[13];
-              ls_frame(st, sfl);
-              float* gsf = d.q_sf + (size_t)l * 16;
-              for (int j = 0; j < 13; ++j) gsf[j] = sfl[j];
-            } else {
-              st[7] = 0.0;
-            }
             double* gst = d.q_st + (size_t)l * 16;
-            for (int j = 0; j < 16; ++j) gst[j] = st[j];
+            for (int j = 0; j < 16; ++j) gst[j] = B.st[j];
+            for (int j = 0; j < 13; ++j) d.q_sf[(size_t)l * 16 + j] = B.sf[j];
           }
         }
         __syncthreads();
-        if (tid == 0 && has_model && p == P - 1) queue_write_cylinder(d, l, st, (int)st[14]);
+        if (tid == 0 && has_model && p == P - 1) queue_write_cylinder(d, l, B.st, (int)B.st[14]);
       }
       __syncthreads();
       if (tid == 0) {

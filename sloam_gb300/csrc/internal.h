@@ -45,8 +45,9 @@ struct Counters {
 // the current keyframe's queue.
 struct QueueCtl {
   int32_t head;    // next item
-  int32_t tc;      // chunks of all queued trees (items per phase)
+  int32_t tc;      // chunks of the split trees (items per phase)
   int32_t nq;      // queued trees
+  int32_t nsplit;  // of which split over blocks (the first nsplit)
   int32_t phases;  // 1 + LS iterations
 };
 constexpr int kQueuePhases = 17;  // 1 + at most 16 LS iterations
@@ -245,7 +246,7 @@ struct Dev {
   double* q_st;         // [cap_lm * 16] LS model state
   float* q_sf;          // [cap_lm * 16] its float copies
   float4* q_hyp;        // [cap_lm] the best hypothesis's circle
-  double* q_part;       // [q_cap_chunks * 20] slice sums of an LS iteration
+  float* q_part;        // [q_cap_chunks * 20] slice sums of an LS iteration
   int q_cap_chunks;
   // -- learned proposal (cyl_mode 2); capacities 0 in the other modes
   const unsigned char* prop_tc;  // bf16 network weights (the context's, shared by slots)

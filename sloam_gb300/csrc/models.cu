@@ -76,9 +76,9 @@ KParams make_kparams(const sloam_params& p) {
   k.huber = p.huber_delta;
   k.q_chunk = p.cyl_chunk_points;
   k.q_tile = p.cyl_hyp_tile;
-  // persistent blocks: the given count, else one wave of the GPU's SMs
-  // (the queue's blocks exit as soon as the items run out)
-  k.q_blocks = p.cyl_queue_blocks > 0 ? p.cyl_queue_blocks : 152;
+  // persistent blocks: the given count, else 76 (half the SMs; with 32
+  // keyframes in flight fewer, longer-lived blocks did best)
+  k.q_blocks = p.cyl_queue_blocks > 0 ? p.cyl_queue_blocks : 76;
   return k;
 }
 
