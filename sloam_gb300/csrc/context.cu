@@ -141,15 +141,20 @@ void build_px_table(const sloam_params& p, float* tab) {
   tab[W] = INFINITY;
 }
 
-// Row of a float pitch exactly as inference.cpp:112-126 computes it (float
-// arithmetic, unfused).  The row falls as the pitch grows, so the table holds
-// tab[k] = smallest float pitch whose row is <= H-1-k (k = 1..H-1): the row
-// of p is H-1 minus the number of k with p >= tab[k].
+// Row of a point exactly as inference.cpp:108-126 computes it, as a table on
+// q = z / range itself (the float division the reference computes):
+// pitch = asinf(q) correctly rounded (the projection's contract, the float
+// of the FP64 asin), then the row in float arithmetic, unfused.  The row falls
+// as q grows, so the table holds tab[k] = smallest float q in [-1, 1] whose
+// row is <= H-1-k (k = 1..H-1; +inf when no q reaches it): the row of q is
+// H-1 minus the number of k with q >= tab[k].  A q outside [-1, 1] (or NaN)
+// has a NaN pitch, which the reference's clamps send to row H-1.
 void build_py_table(const sloam_params& p, float* tab) {
   const int H = p.img_h;
   const KParams kp = make_kparams(p);
   const float fd = kp.fov_down_abs, fov = kp.fov;
-  auto g = [H, fd, fov](float pitch) {
+  auto g = [H, fd, fov](float q) {
+    const float pitch = (float)std::asin((double)q);
     float t = (pitch + fd) / fov;
     float y = (1.0f - t) * (float)H;
     y = std::floor(y);
@@ -158,7 +163,8 @@ void build_py_table(const sloam_params& p, float* tab) {
     return H - 1 - (int)y;
   };
   tab[0] = -INFINITY;
-  for (int k = 1; k < H; ++k) tab[k] = first_at_least(g, k, -2.0f, 2.0f);
+  for (int k = 1; k < H; ++k)
+    tab[k] = g(1.0f) >= k ? first_at_least(g, k, -1.0f, 1.0f) : INFINITY;
   tab[H] = INFINITY;
 }
 
@@ -391,8 +397,8 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.q_st = c.take<double>((size_t)d.cap_lm * 16);
   d.q_sf = c.take<float>((size_t)d.cap_lm * 16);
   d.q_hyp = c.take<float4>(d.cap_lm);
-  // 256-point slices, at most one partial slice per tree
-  d.q_cap_chunks = (int)(((size_t)d.cap_cluster + d.cap_p) / 256 + d.cap_lm);
+  // 1024-point LS slices, at most one partial slice per tree
+  d.q_cap_chunks = (int)(((size_t)d.cap_cluster + d.cap_p) / 1024 + d.cap_lm);
   d.q_part = c.take<float>((size_t)d.q_cap_chunks * 20);
   const size_t ps = (size_t)std::max(d.prop_cap, 1);
   d.prop_x = c.take<float>(ps * 384);
@@ -1509,9 +1515,9 @@ extern "C" int sloam_profile_stages(sloam_ctx* ctx, float* ms, int n) {
   return SLOAM_OK;
 }
 
-// which: 0 = projection kernel (k_project), 1 = point-cylinder inlier
-// counting (k_cyl_count), 2 = the proposal network on the tensor cores over
-// the last keyframe's samples (cyl_mode 2), 3 = the whole cylinder stage
+// which: 0 = projection kernel (k_project), 1 = the point-cylinder inlier
+// counting (inside the work queue: the same as 6), 2 = the proposal network
+// on the tensor cores over the last keyframe's samples (cyl_mode 2), 3 = the whole cylinder stage
 // (vertex-line fits and the point-level fit of the context's cyl_mode),
 // 4 = the Trellis vertex kernel (k_vertex), 5 = the pose solve (k_gn),
 // 6 = the cylinder work queue (its ordering and persistent kernels, plain
@@ -1519,6 +1525,7 @@ extern "C" int sloam_profile_stages(sloam_ctx* ctx, float* ms, int n) {
 // Average milliseconds per launch (per stage for 3 and 6) over `reps`.
 extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg_ms) {
   if (!ctx || !avg_ms || reps < 1 || which < 0 || which > 6) return SLOAM_ERR_ARG;
+  if (which == 1) which = 6;  // the inlier counting runs inside the work queue
   if (which == 2 && (ctx->P.cyl_mode != 2 || !ctx->prop_tc)) return SLOAM_ERR_ARG;
   if ((which == 3 && ctx->P.cyl_mode == 2 && !ctx->prop_tc) ||
       (which == 6 && (ctx->P.cyl_mode < 1 || ctx->kp.K < 1)))
@@ -1553,11 +1560,9 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
     return SLOAM_OK;
   }
   // the inlier-counting kernel scores trees still at the vertex-line stage
-  if (which == 1) launch_cyl_count_prep(d, ctx->kp, ctx->st);
   CK(cudaEventRecord(a, ctx->st));
   for (int r = 0; r < reps; ++r) {
     if (which == 0) launch_project_kernel(d, ctx->kp, ctx->st);
-    else if (which == 1) launch_cyl_hyp_kernel(d, ctx->kp, ctx->st);
     else
       prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, ctx->kp.prop_S,
                                     d.prop_cap, d.prop_f, d.prop_out, d.prop_err, ctx->st);

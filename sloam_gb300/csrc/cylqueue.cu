@@ -11,17 +11,17 @@
 // into chunks, and every (phase, chunk) of it is an item:
 //   phase 0        count the inliers of all K hypotheses on the chunk
 //                  (ballot + popcount per 32 points, integer atomics);
-//   phase 1..L     one LS iteration: the 20 normal-equation sums of each
-//                  256-point slice of the chunk.
+//   phase 1..L     one LS iteration: the 20 normal-equation sums of one
+//                  1024-point slice of the tree.
 // The block that completes the last chunk of (tree, phase) finishes the
 // phase: after phase 0 the best hypothesis (most inliers, lowest index on
 // ties) and the initial model; after an LS phase the slice sums in slice
 // order, the FP64 5x5 solve on one warp and the model update; after the
 // last phase the cylinder record.  Both kinds of tree use the same slice
-// sums (FP32 per point, warp-shuffle sums, the warps in order) added in
-// slice order in FP64, so the result depends neither on the split, nor on
-// which block ran which chunk, the chunk size, the hypothesis tile or the
-// block count.
+// sums (each thread's 4 points in FP32 in a fixed order, warp-shuffle sums,
+// the warps in order) added in slice order in FP64, so the result depends
+// neither on the split, nor on which block ran which item, the chunk size,
+// the hypothesis tile or the block count.
 //
 // Item order: the split trees' phase-0 chunks, then the whole trees, then
 // the split trees' phases 1..L, so the phase-0 finishers have run by the
@@ -41,7 +41,8 @@ namespace {
 
 constexpr int kQThreads = 256;
 constexpr int kQWarps = kQThreads / 32;
-constexpr int kSlice = kQThreads;         // points of one LS slice
+constexpr int kSlicePer = 4;              // points per thread of one LS slice
+constexpr int kSlice = kSlicePer * kQThreads;  // points of one LS slice
 constexpr int kSplitChunks = 4;           // larger trees are split over blocks
 constexpr int kQSortCap = 4096;           // trees per keyframe the queue orders
 constexpr long long kQueueWaitPolls = 1ll << 22;  // x ~100 ns: about 0.4 s
@@ -66,6 +67,7 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
     if (threadIdx.x == 0) {
       atomicOr(&d.cnt->overflow, 64);
       q->tc = 0;
+      q->ts = 0;
       q->nq = 0;
       q->nsplit = 0;
       q->phases = 1;
@@ -137,6 +139,7 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
     d.q_off[nsplit] = base;
     d.q_soff[nsplit] = sbase;
     q->tc = base;
+    q->ts = sbase;
     q->nq = nq;
     q->nsplit = nsplit;
     q->phases = P;
@@ -215,15 +218,16 @@ __device__ __forceinline__ void count_tile(const QueueSmem<kTile>& S, int nt,
 // tile: `whole` keeps the best key (most inliers, lowest index) of the
 // block, otherwise the counts go to hyp_cnt by atomics.
 template <int kTile>
-__device__ unsigned long long count_points(const Dev& d, QueueSmem<kTile>& S, int l, int K,
-                                           const float2* __restrict__ uvs, int i0, int i1,
-                                           bool whole) {
+__device__ unsigned long long count_points(const float4* __restrict__ hyp_tab,
+                                           int* __restrict__ cnt_tab, QueueSmem<kTile>& S,
+                                           int l, int K, const float2* __restrict__ uvs, int i0,
+                                           int i1, bool whole) {
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   unsigned long long best = 0ull;
   for (int t0 = 0; t0 < K; t0 += kTile) {
     const int nt = min(kTile, K - t0);
     for (int i = tid; i < kTile; i += kQThreads)
-      S.hyp[i] = i < nt ? d.hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
+      S.hyp[i] = i < nt ? hyp_tab[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
     __syncthreads();
     int acc[kTile / 32];
 #pragma unroll
@@ -237,7 +241,7 @@ __device__ unsigned long long count_points(const Dev& d, QueueSmem<kTile>& S, in
 #pragma unroll
       for (int k = 0; k < kQWarps; ++k) s += S.cnt[k][h];
       if (!whole) {
-        if (s) atomicAdd(d.hyp_cnt + (size_t)l * K + t0 + h, s);
+        if (s) atomicAdd(cnt_tab + (size_t)l * K + t0 + h, s);
       } else if (s > 0) {
         const unsigned long long kk = ((unsigned long long)s << 32) |
                                       (unsigned long long)(0xFFFFFFFFu - (uint32_t)(t0 + h));
@@ -249,45 +253,48 @@ __device__ unsigned long long count_points(const Dev& d, QueueSmem<kTile>& S, in
   return best;
 }
 
-// The 20 LS sums of slice `sl` of the tree (points sl*256 .. +255 that are
+// The 20 LS sums of slice `sl` of the tree (points sl*1024 .. +1023 that are
 // inliers of the fixed hypothesis B.hyp), for the model in B.sf: FP32 per
-// point, warp-shuffle sums, the warps summed in order; threads 0..19 return
-// sum j = tid, other threads 0.
+// point (each thread's 4 points in order), warp-shuffle sums, the warps
+// summed in order; threads 0..19 return sum j = tid, other threads 0.
 __device__ __forceinline__ float slice_sums(QueueBlock& B, const float4* __restrict__ pts,
                                             const float2* __restrict__ uvs, int n, int sl) {
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const float* sf = B.sf;
   const float4 H = B.hyp;
-  const int i = sl * kSlice + tid;
   float acc[20];
 #pragma unroll
   for (int j = 0; j < 20; ++j) acc[j] = 0.f;
-  bool use = i < n;
-  float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (use) {
-    const float2 uv = uvs[i];
-    const float du = fsub(uv.x, H.x), dv = fsub(uv.y, H.y);
-    const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-    use = (d2 > H.z) & (d2 < H.w);
-    if (use) qp = pts[i];
-  }
-  const float wx = qp.x - sf[0], wy = qp.y - sf[1], wz = qp.z - sf[2];
-  const float dx = sf[3], dy = sf[4], dz = sf[5];
-  const float wd = wx * dx + wy * dy + wz * dz;
-  const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
-  const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
-  if (use && rho > 0.f) {
-    const float res = rho - sf[12];
-    const float a1 = (px_ * sf[6] + py_ * sf[7] + pz_ * sf[8]) / rho;
-    const float a2 = (px_ * sf[9] + py_ * sf[10] + pz_ * sf[11]) / rho;
-    const float J[5] = {-a1, -a2, -wd * a1, -wd * a2, -1.0f};
-    int m = 0;
 #pragma unroll
-    for (int a = 0; a < 5; ++a)
+  for (int k = 0; k < kSlicePer; ++k) {
+    const int i = sl * kSlice + k * kQThreads + tid;
+    bool use = i < n;
+    float4 qp = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (use) {
+      const float2 uv = uvs[i];
+      const float du = fsub(uv.x, H.x), dv = fsub(uv.y, H.y);
+      const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+      use = (d2 > H.z) & (d2 < H.w);
+      if (use) qp = pts[i];
+    }
+    const float wx = qp.x - sf[0], wy = qp.y - sf[1], wz = qp.z - sf[2];
+    const float dx = sf[3], dy = sf[4], dz = sf[5];
+    const float wd = wx * dx + wy * dy + wz * dz;
+    const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
+    const float rho = sqrtf(px_ * px_ + py_ * py_ + pz_ * pz_);
+    if (use && rho > 0.f) {
+      const float res = rho - sf[12];
+      const float a1 = (px_ * sf[6] + py_ * sf[7] + pz_ * sf[8]) / rho;
+      const float a2 = (px_ * sf[9] + py_ * sf[10] + pz_ * sf[11]) / rho;
+      const float J[5] = {-a1, -a2, -wd * a1, -wd * a2, -1.0f};
+      int m = 0;
 #pragma unroll
-      for (int b = a; b < 5; ++b) acc[m++] = J[a] * J[b];
+      for (int a = 0; a < 5; ++a)
 #pragma unroll
-    for (int a = 0; a < 5; ++a) acc[15 + a] = J[a] * res;
+        for (int b = a; b < 5; ++b) acc[m++] += J[a] * J[b];
+#pragma unroll
+      for (int a = 0; a < 5; ++a) acc[15 + a] += J[a] * res;
+    }
   }
 #pragma unroll
   for (int j = 0; j < 20; ++j) {
@@ -366,17 +373,20 @@ __device__ __forceinline__ unsigned long long block_max_key(QueueBlock& B, unsig
   return m;
 }
 
-template <int kPPT, int kTile>
+template <int kTile>
 __global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
   extern __shared__ __align__(16) unsigned char q_smem[];
   QueueSmem<kTile>& S = *reinterpret_cast<QueueSmem<kTile>*>(q_smem);
   __shared__ QueueBlock B;
-  constexpr int kC = kPPT * kQThreads;
+  const int kC = kp.q_chunk;  // points per counting item
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   QueueCtl* q = d.qctl;
-  const int TC = q->tc, P = q->phases, nq = q->nq, nsplit = q->nsplit, K = kp.K;
+  const int TC = q->tc, TS = q->ts, P = q->phases, nq = q->nq, nsplit = q->nsplit;
+  const int K = kp.K;
+  const float4* __restrict__ hyp_tab = d.hyp;
+  int* __restrict__ cnt_tab = d.hyp_cnt;
   const int nwhole = nq - nsplit;
-  const long long total = (long long)TC * P + nwhole;
+  const long long total = (long long)TC + nwhole + (long long)TS * (P - 1);
   for (;;) {
     if (tid == 0) {
       B.idx = atomicAdd(&q->head, 1);
@@ -393,12 +403,10 @@ __global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
       int n;
       tree_points(d, l, &pts, &n, &uvs);
       const unsigned long long best =
-          block_max_key(B, count_points<kTile>(d, S, l, K, uvs, 0, n, true));
+          block_max_key(B, count_points<kTile>(hyp_tab, cnt_tab, S, l, K, uvs, 0, n, true));
+      if (tid == 0) d.cyl_best[l] = best;
       if (best != 0ull) {
-        if (tid == 0) {
-          d.cyl_best[l] = best;
-          init_model(d, kp, B, l, n, uvs, best);
-        }
+        if (tid == 0) init_model(d, kp, B, l, n, uvs, best);
         __syncthreads();
         const int ns = (n + kSlice - 1) / kSlice;
         for (int p = 1; p < P; ++p) {
@@ -411,23 +419,25 @@ __global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
           __syncthreads();
         }
         if (tid == 0) queue_write_cylinder(d, l, B.st, (int)B.st[14]);
-      } else if (tid == 0) {
-        d.cyl_best[l] = 0ull;
       }
       __syncthreads();
       continue;
     }
-    // ---------------- one chunk of a split tree
-    const int p = idx < TC ? 0 : 1 + (idx - TC - nwhole) / TC;
-    const int r = idx < TC ? idx : (idx - TC - nwhole) % TC;
-    int lo = 0, hi = nsplit - 1;  // the tree whose chunks hold r
+    // ---------------- one chunk (counting) or slice (LS) of a split tree
+    const int p = idx < TC ? 0 : 1 + (idx - TC - nwhole) / TS;
+    const int r = idx < TC ? idx : (idx - TC - nwhole) % TS;
+    const int32_t* offs = p == 0 ? d.q_off : d.q_soff;
+    int lo = 0, hi = nsplit - 1;  // the tree whose chunks / slices hold r
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (d.q_off[mid] <= r) lo = mid;
+      if (offs[mid] <= r) lo = mid;
       else hi = mid - 1;
     }
-    const int l = d.q_order[lo], c0 = d.q_off[lo], nc = d.q_off[lo + 1] - c0, c = r - c0;
-    const int s0 = d.q_soff[lo], ns = d.q_soff[lo + 1] - s0;  // 256-point slices
+    const int l = d.q_order[lo];
+    const int c0 = d.q_off[lo], nc = d.q_off[lo + 1] - c0;   // counting chunks
+    const int s0 = d.q_soff[lo], ns = d.q_soff[lo + 1] - s0;  // LS slices
+    const int c = r - offs[lo];  // this item's chunk (p == 0) or slice (p > 0)
+    const int n_items = p == 0 ? nc : ns;
     const float4* pts;
     const float2* uvs;
     int n;
@@ -451,29 +461,24 @@ __global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
     }
     if (p == 0) {
       // ---- inlier counts of the chunk for every hypothesis of the tree
-      count_points<kTile>(d, S, l, K, uvs, c * kC, min(n, c * kC + kC), false);
+      count_points<kTile>(hyp_tab, cnt_tab, S, l, K, uvs, c * kC, min(n, c * kC + kC), false);
     } else {
-      // ---- one LS iteration's sums over the chunk's slices (the
-      // hypothesis's inliers, fixed over the iterations)
       const double* gst = d.q_st + (size_t)l * 16;
       const bool live = __ldcg(gst + 15) >= 0.0 && __ldcg(gst + 7) != 0.0;
       if (live) {
         if (tid < 13) B.sf[tid] = __ldcg(d.q_sf + (size_t)l * 16 + tid);
         if (tid == 0) B.hyp = __ldcg(d.q_hyp + l);
         __syncthreads();
-        for (int k = 0; k < kPPT; ++k) {
-          const int sl = c * kPPT + k;  // the slice of the tree
-          if (sl >= ns) break;          // block-uniform
-          const float t = slice_sums(B, pts, uvs, n, sl);
-          if (tid < 20) d.q_part[(size_t)(s0 + sl) * 20 + tid] = t;
-        }
+        // ---- one LS iteration's sums over the slice
+        const float t = slice_sums(B, pts, uvs, n, c);
+        if (tid < 20) d.q_part[(size_t)(s0 + c) * 20 + tid] = t;
       }
     }
     // ---- arrival; the last chunk's block finishes the phase for the tree
     __syncthreads();
     if (tid == 0) {
       __threadfence();
-      B.last = atomicAdd(d.q_done + (size_t)l * kQueuePhases + p, 1) == nc - 1;
+      B.last = atomicAdd(d.q_done + (size_t)l * kQueuePhases + p, 1) == n_items - 1;
     }
     __syncthreads();
     if (B.last) {
@@ -481,7 +486,7 @@ __global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
       if (p == 0) {
         unsigned long long best = 0ull;
         for (int h = tid; h < K; h += kQThreads) {
-          const int cn = __ldcg(d.hyp_cnt + (size_t)l * K + h);
+          const int cn = __ldcg(cnt_tab + (size_t)l * K + h);
           if (cn > 0) {
             const unsigned long long kk =
                 ((unsigned long long)cn << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
@@ -535,44 +540,36 @@ __global__ void __launch_bounds__(kQThreads, 4) k_cyl_queue(Dev d, KParams kp) {
   }
 }
 
-template <int kPPT, int kTile>
+template <int kTile>
 void set_queue_attr() {
-  cudaFuncSetAttribute(k_cyl_queue<kPPT, kTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_cyl_queue<kTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(QueueSmem<kTile>));
 }
 
-template <int kPPT, int kTile>
+template <int kTile>
 void launch_queue_t(const Dev& d, const KParams& kp, int blocks, cudaStream_t st) {
-  k_cyl_queue<kPPT, kTile><<<blocks, kQThreads, sizeof(QueueSmem<kTile>), st>>>(d, kp);
+  k_cyl_queue<kTile><<<blocks, kQThreads, sizeof(QueueSmem<kTile>), st>>>(d, kp);
 }
 
-template <int kPPT>
 bool launch_queue_tile(const Dev& d, const KParams& kp, int tile, int blocks, cudaStream_t st) {
   switch (tile) {
-    case 64: launch_queue_t<kPPT, 64>(d, kp, blocks, st); return true;
-    case 128: launch_queue_t<kPPT, 128>(d, kp, blocks, st); return true;
-    case 256: launch_queue_t<kPPT, 256>(d, kp, blocks, st); return true;
-    case 512: launch_queue_t<kPPT, 512>(d, kp, blocks, st); return true;
-    case 1024: launch_queue_t<kPPT, 1024>(d, kp, blocks, st); return true;
+    case 64: launch_queue_t<64>(d, kp, blocks, st); return true;
+    case 128: launch_queue_t<128>(d, kp, blocks, st); return true;
+    case 256: launch_queue_t<256>(d, kp, blocks, st); return true;
+    case 512: launch_queue_t<512>(d, kp, blocks, st); return true;
+    case 1024: launch_queue_t<1024>(d, kp, blocks, st); return true;
   }
   return false;
-}
-
-template <int kPPT>
-void set_queue_attrs() {
-  set_queue_attr<kPPT, 64>();
-  set_queue_attr<kPPT, 128>();
-  set_queue_attr<kPPT, 256>();
-  set_queue_attr<kPPT, 512>();
-  set_queue_attr<kPPT, 1024>();
 }
 
 }  // namespace
 
 void init_queue_attributes() {
-  set_queue_attrs<1>();
-  set_queue_attrs<2>();
-  set_queue_attrs<4>();
+  set_queue_attr<64>();
+  set_queue_attr<128>();
+  set_queue_attr<256>();
+  set_queue_attr<512>();
+  set_queue_attr<1024>();
 }
 
 bool queue_shape_valid(int chunk_points, int hyp_tile) {
@@ -586,14 +583,8 @@ bool queue_shape_valid(int chunk_points, int hyp_tile) {
 // (every eligible tree when NULL), from the hypothesis table of
 // k_cyl_hypgen.  Two launches: the ordering and the persistent queue.
 int launch_cyl_queue(const Dev& d, const KParams& kp, const int32_t* only, cudaStream_t st) {
-  const int chunk = kp.q_chunk, tile = kp.q_tile;
-  k_cyl_queue_prep<<<1, 1024, 0, st>>>(d, kp, only, chunk);
-  const int blocks = kp.q_blocks;
-  bool ok = false;
-  if (chunk == 256) ok = launch_queue_tile<1>(d, kp, tile, blocks, st);
-  else if (chunk == 512) ok = launch_queue_tile<2>(d, kp, tile, blocks, st);
-  else if (chunk == 1024) ok = launch_queue_tile<4>(d, kp, tile, blocks, st);
-  return ok ? 2 : 1;
+  k_cyl_queue_prep<<<1, 1024, 0, st>>>(d, kp, only, kp.q_chunk);
+  return launch_queue_tile(d, kp, kp.q_tile, kp.q_blocks, st) ? 2 : 1;
 }
 
 }  // namespace sg

@@ -1,11 +1,10 @@
-// fastpoly.cuh — the projection's first-try arctangent and arcsine: odd
-// polynomials in FP32, fitted here by iteratively reweighted least squares
-// on Chebyshev nodes (relative error), evaluated by Horner's rule with fma.
+// fastpoly.cuh — the projection's first-try arctangent: an odd polynomial
+// in FP32, fitted here by iteratively reweighted least squares on Chebyshev
+// nodes (relative error), evaluated by Horner's rule with fma.
 //
-//   atan(a) = a * P(a^2),  0 <= a <= 1,    P of degree 8;
-//   asin(q) = q * Q(q^2),  |q| <= 0.5,     Q of degree 5.
+//   atan(a) = a * P(a^2),  0 <= a <= 1,    P of degree 8.
 //
-// Measured in emulated FP32 over 8 M arguments each: at most 1.6 ulp
+// Measured in emulated FP32 over 8 M arguments: at most 1.6 ulp
 // (1.27e-7 relative) from the exact value.  atan2 is rebuilt from atan on
 // min/max of |x|, |y| with an approximate quotient (2 ulp): 4.9e-7 relative
 // at most from the correctly rounded float.  The projection accepts these
@@ -22,9 +21,6 @@ namespace sg {
   9.999999848e-01f, -3.333307364e-01f, 1.999262348e-01f, -1.420367011e-01f,    \
       1.064101933e-01f, -7.504455481e-02f, 4.269324857e-02f, -1.606961499e-02f, \
       2.850121155e-03f
-#define SG_ASIN_Q                                                              \
-  9.999999956e-01f, 1.666678996e-01f, 7.494438032e-02f, 4.554988467e-02f,      \
-      2.385937596e-02f, 4.263388310e-02f
 
 __device__ __forceinline__ float atan01_poly(float a) {
   constexpr float c[9] = {SG_ATAN_P};
@@ -33,15 +29,6 @@ __device__ __forceinline__ float atan01_poly(float a) {
 #pragma unroll
   for (int k = 7; k >= 0; --k) p = fmaf(p, s, c[k]);
   return a * p;
-}
-
-__device__ __forceinline__ float asin05_poly(float q) {
-  constexpr float c[6] = {SG_ASIN_Q};
-  const float s = q * q;
-  float p = c[5];
-#pragma unroll
-  for (int k = 4; k >= 0; --k) p = fmaf(p, s, c[k]);
-  return q * p;
 }
 
 // atan2(y, x) for finite nonzero x, y with 1e-18 <= min(|x|,|y|) and

@@ -45,7 +45,8 @@ struct Counters {
 // the current keyframe's queue.
 struct QueueCtl {
   int32_t head;    // next item
-  int32_t tc;      // chunks of the split trees (items per phase)
+  int32_t tc;      // counting chunks of the split trees
+  int32_t ts;      // LS slices of the split trees (items per LS phase)
   int32_t nq;      // queued trees
   int32_t nsplit;  // of which split over blocks (the first nsplit)
   int32_t phases;  // 1 + LS iterations
@@ -329,7 +330,6 @@ int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st)
 int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 // the projection stage after k_project (labels, tree cloud, ground list, key re-arm)
 int launch_project_rest(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st);
-int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st);
 

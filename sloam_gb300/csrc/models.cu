@@ -1169,6 +1169,7 @@ __global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp,
   }
 }
 
+// ---- scoring of the learned proposals (cyl_mode 2)
 constexpr int kCountThreads = 256;
 constexpr int kHypTile = 256;  // hypotheses staged per pass (8 per lane)
 
@@ -1179,8 +1180,7 @@ constexpr int kHypTile = 256;  // hypotheses staged per pass (8 per lane)
 // (lane = h % 32); per-block totals go to the (tree, hypothesis) counter.
 // A chunk that straddles trees runs once per tree.
 __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, const float4* __restrict__ hyp,
-                                                              int* __restrict__ hcnt, int K,
-                                                              const int32_t* __restrict__ only) {
+                                                              int* __restrict__ hcnt, int K) {
   __shared__ float4 sh[kHypTile];
   __shared__ int sred[kCountThreads / 32][kHypTile];
   const int nl = d.cnt->n_lm;
@@ -1199,7 +1199,7 @@ __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, const float4
     }
     for (int l = lo; l < nl && seg(l) < q0 + kCountThreads; ++l) {
       const int s0 = max(q0, seg(l)), s1 = min(q0 + kCountThreads, seg(l + 1));
-      if (s1 <= s0 || !fit_eligible(d.cyl_all[l]) || (only && !only[l])) continue;
+      if (s1 <= s0 || !fit_eligible(d.cyl_all[l])) continue;
       const int q = q0 + threadIdx.x;
       const bool mine = q >= s0 && q < s1;
       float2 p = make_float2(0.f, 0.f);
@@ -1241,13 +1241,12 @@ __global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, const float4
 
 // Best hypothesis per tree: most inliers, lowest hypothesis on ties.
 __global__ void __launch_bounds__(256) k_cyl_best(Dev d, const int* __restrict__ hcnt, int K,
-                                                  unsigned long long* __restrict__ best_out,
-                                                  const int32_t* __restrict__ only) {
+                                                  unsigned long long* __restrict__ best_out) {
   __shared__ unsigned long long sk[8];
   const int nl = d.cnt->n_lm;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
     unsigned long long best = 0ull;
-    if (fit_eligible(d.cyl_all[l]) && (!only || only[l])) {
+    if (fit_eligible(d.cyl_all[l])) {
       for (int h = threadIdx.x; h < K; h += blockDim.x) {
         const int c = hcnt[(size_t)l * K + h];
         if (c > 0) {
@@ -1343,14 +1342,17 @@ __global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
   }
 }
 
-// One block per tree: inliers of the best hypothesis, LS refinement.
-// pass 1: from the best RANSAC hypothesis (cyl_mode 1: every eligible tree;
-// cyl_mode 2: the trees pass 0 flagged).  pass 0 (cyl_mode 2): from the best
-// network proposal; the refined model is kept when its inliers
-// (|distance to the refined axis - radius| < tau) are at least prop_ratio
-// of the tree's points, else the tree is flagged for the RANSAC pass.
+// The learned proposals' LS pass (cyl_mode 2), one block per tree: from the
+// best network proposal, LS refinement with the inliers re-selected by the
+// current model; the refined model is kept when its inliers (|distance to
+// the refined axis - radius| < tau) are at least prop_ratio of the tree's
+// points, else the tree is flagged for the RANSAC pass (the cylinder work
+// queue).  The proposals are few (prop_S per tree) and their trees all
+// alike in cost, so the plain per-tree blocks do better here than the
+// queue, whose ordering launch and persistent blocks only pay off on the
+// 256-hypothesis counting.
 constexpr int kLsThreads = 256;
-__global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int pass) {
+__global__ void __launch_bounds__(kLsThreads, 4) k_prop_ls(Dev d, KParams kp) {
   __shared__ int s_in[kLsThreads / 32];
   __shared__ float red[20][kLsThreads / 32];
   __shared__ double st[14];  // c(3), dir(3), r, ok, b1(3), b2(3)
@@ -1361,12 +1363,10 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
     CylD c = d.cyl_all[l];
-    const bool learned = pass == 0;
     if (c.stage != 1 || c.radius == -1.0) continue;
-    if (!learned && kp.cyl_mode == 2 && !d.pflag[l]) continue;
-    const unsigned long long key = learned ? d.pbest[l] : d.cyl_best[l];
+    const unsigned long long key = d.pbest[l];
     if (key == 0ull) {
-      if (learned && threadIdx.x == 0) {
+      if (threadIdx.x == 0) {
         d.pflag[l] = 1;
         atomicAdd(&d.cnt->n_fallback, 1);
       }
@@ -1380,7 +1380,7 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
     tree_points(d, l, &pts, &n, &uvs);
     const CylFrame f = make_frame(d, c);
     Hyp H;
-    if (learned) {
+    {
       const float4 e = d.phyp[(size_t)l * kp.prop_S + h];
       H.cu = e.x;
       H.cv = e.y;
@@ -1388,8 +1388,6 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
       H.hi2 = e.w;
       H.r = fsub(fsqrt(e.w), kp.tau);
       H.ok = true;
-    } else {
-      H = make_hyp(kp, h, c.id, n, [&](uint32_t i) { return uvs[i]; });
     }
     if (threadIdx.x == 0) {
       st[0] = f.ox + (double)H.cu * f.e1x + (double)H.cv * f.e2x;
@@ -1415,13 +1413,6 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
       for (int j = 0; j < 20; ++j) acc[j] = 0.f;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const float4 q = pts[i];
-        if (!learned) {
-          // the inliers of the RANSAC hypothesis, fixed over the iterations
-          const float2 uv = uvs[i];
-          const float du = fsub(uv.x, H.cu), dv = fsub(uv.y, H.cv);
-          const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-          if (!((d2 > H.lo2) & (d2 < H.hi2))) continue;
-        }
         const float wx = q.x - cx, wy = q.y - cy, wz = q.z - cz;
         const float wd = wx * dx + wy * dy + wz * dz;
         const float px_ = wx - wd * dx, py_ = wy - wd * dy, pz_ = wz - wd * dz;
@@ -1429,7 +1420,7 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
         if (!(rho > 0.f)) continue;
         // a proposal starts coarser: its inliers follow the current model,
         // in a band of 2 tau on the first iteration and tau after it
-        if (learned && !(fabsf(rho - rf) < (itn == 0 ? 2.0f : 1.0f) * kp.tau)) continue;
+        if (!(fabsf(rho - rf) < (itn == 0 ? 2.0f : 1.0f) * kp.tau)) continue;
         const float res = rho - rf;
         const float a1 = (px_ * b1x + py_ * b1y + pz_ * b1z) / rho;
         const float a2 = (px_ * b2x + py_ * b2y + pz_ * b2z) / rho;
@@ -1481,7 +1472,7 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_cyl_ls(Dev d, KParams kp, int
       }
       __syncthreads();
     }
-    if (learned) {
+    {
       // inliers of the refined model over all the tree's points
       const float cx = sf[0], cy = sf[1], cz = sf[2];
       const float dx = sf[3], dy = sf[4], dz = sf[5];
@@ -1603,18 +1594,13 @@ int launch_cyl_fit_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
 
 constexpr int kCountBlocks = 304;
 
-// The inlier-counting kernel alone (its inputs prepared by
-// launch_cyl_count_prep); counts accumulate, so a repeated launch is for
-// timing only.
+// The inputs of the cylinder work queue (vertex-line models, projected
+// points, hypothesis table), for timing the queue alone.
 int launch_cyl_count_prep(const Dev& d, const KParams& kp, cudaStream_t st) {
   k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
   k_cyl_uv<<<kCylBlocks, 256, 0, st>>>(d);
   k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp, nullptr);
   return 3;
-}
-int launch_cyl_hyp_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
-  k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.hyp, d.hyp_cnt, kp.K, nullptr);
-  return 1;
 }
 
 // mode 1: K random 3-point circles per tree, LS refinement of the best.
@@ -1632,9 +1618,9 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream
     n += 1 + prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, kp.prop_S,
                                            d.prop_cap, d.prop_f, d.prop_out, d.prop_err, st);
     k_prop_hyp<<<kCylBlocks, 256, 0, st>>>(d, kp);
-    k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.phyp, d.phyp_cnt, kp.prop_S, nullptr);
-    k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.phyp_cnt, kp.prop_S, d.pbest, nullptr);
-    k_cyl_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp, 0);
+    k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.phyp, d.phyp_cnt, kp.prop_S);
+    k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.phyp_cnt, kp.prop_S, d.pbest);
+    k_prop_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
     n += 4;
     only = d.pflag;
   }

@@ -8,13 +8,14 @@
 // correctly rounded float atan2/asin.  Yaw enters the column through a double
 // expression, so the column is read from an exact boundary table built on the
 // host (px_tab[k] = smallest float yaw whose column is >= k).  The first try
-// evaluates yaw and pitch with the FP32 polynomials of fastpoly.cuh (at most
-// 4.9e-7 relative from the correctly rounded angle), reads the table entry
-// the column/row formula estimates, and accepts it when the whole +-1.2e-6
-// relative margin (about 10 ulp) lies inside that entry; otherwise the
-// column takes the FP64 path and the row the library asinf under the same
-// margin, then FP64.  The row likewise comes from an exact boundary table of
-// the pitch.
+// evaluates yaw with the FP32 polynomial of fastpoly.cuh (at most 4.9e-7
+// relative from the correctly rounded angle), reads the table entry the
+// column formula estimates, and accepts it when the whole +-1.2e-6 relative
+// margin (about 10 ulp) lies inside that entry; otherwise the column takes
+// the FP64 path.  The row is monotone in q = z / range (asin and the row
+// formula both are), so its boundary table is on q itself (py_tab[k] =
+// smallest float q whose row is <= H-1-k): q is exact, and the row is exact
+// comparisons, with no angle evaluated.
 // The nearest point wins its pixel: 64-bit atomicMin on
 // range bits (32) : point index (24) : point label (8), ties to the lowest
 // index; the label rides in the key so the winner's label needs no gather.
@@ -51,20 +52,17 @@ __device__ __forceinline__ int table_guess(const float* __restrict__ tab, float 
   const int k = min(n - 1, max(0, __float2int_rz(e)));
   return (__ldg(tab + k) <= v - m && v + m < __ldg(tab + k + 1)) ? k : -1;
 }
-// The index of v when the whole interval [v - m, v + m] has it, else -1.
-__device__ __forceinline__ int table_index_margin(const float* __restrict__ tab, float v,
-                                                  float m, float e, int n) {
-  const int k = table_index(tab, v - m, e, n);
-  return (k == n - 1 || v + m < __ldg(tab + k + 1)) ? k : -1;
-}
 // Column of a yaw: px_tab[k] = smallest yaw of column k (inference.cpp:111-121;
 // NaN: std::min/max keep the bound, W - 1).
 __device__ __forceinline__ float col_estimate(float yaw, int W) {
   return (yaw * 0.318309886f + 1.0f) * 0.5f * (float)W;
 }
-// Row of a pitch: py_tab[k] = smallest pitch of row H-1-k (inference.cpp:
-// 112-126; NaN: row H - 1).
-__device__ __forceinline__ float row_estimate(float pitch, const KParams& kp) {
+// Row of q = z / range: py_tab[k] = smallest q of row H-1-k
+// (inference.cpp:108-126 through the correctly rounded asinf); the estimate
+// takes asin(q) ~ q (1 + q^2 / 6 + 3 q^4 / 40), and the exact table decides.
+__device__ __forceinline__ float row_estimate_q(float q, const KParams& kp) {
+  const float q2 = q * q;
+  const float pitch = q * (1.0f + q2 * (0.16666667f + q2 * 0.075f));
   return (pitch + kp.fov_down_abs) * (1.0f / kp.fov) * (float)kp.img_h;
 }
 
@@ -149,31 +147,15 @@ __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontR
                                  col_estimate(yaw0, W), W)
                    : -1;
       px = nan_xy ? W - 1 : px;  // NaN in, NaN out: column W - 1
+      // ---- the row: exact comparisons of q with its boundary table (a NaN
+      // q, or |q| > 1 after rounding, has a NaN pitch: row H - 1)
       const float q = fdiv(z, range);
-      const float aq = fabsf(q);
-      const float pitch0 = asin05_poly(q);
-      int g = aq <= 0.5f ? table_guess(d.py_tab, pitch0, fmaxf(fabsf(pitch0) * 1.2e-6f, 1e-30f),
-                                       row_estimate(pitch0, kp), H)
-                         : -1;
-      g = isnan(q) ? 0 : g;  // NaN: row H - 1
+      const int g = fabsf(q) <= 1.0f ? table_index(d.py_tab, q, row_estimate_q(q, kp), H) : 0;
       // ---- exact column: correctly rounded yaw from FP64
       if (px < 0) {
         const float yaw = -(float)atan2((double)y, (double)x);
         px = table_index(d.px_tab, yaw, col_estimate(yaw, W), W);
         ++slow;
-      }
-      // ---- exact row: the library asinf under the same margin, else FP64
-      if (g < 0) {
-        if (aq < 1.0f) {
-          const float pitch = asinf(q);
-          g = table_index_margin(d.py_tab, pitch, fmaxf(fabsf(pitch) * 1.2e-6f, 1e-30f),
-                                 row_estimate(pitch, kp), H);
-        }
-        if (g < 0) {
-          const float pitch = (float)asin((double)q);
-          g = table_index(d.py_tab, pitch, row_estimate(pitch, kp), H);
-          ++slow;
-        }
       }
       const int py = H - 1 - g;
       pix = py * W + px;

@@ -88,13 +88,26 @@ def test_boundary_tables_reproduce_oracle_pixels_and_bins(L):
     yaw = -np.arctan2(xyzi[:, 1].astype(np.float64), xyzi[:, 0].astype(np.float64)).astype(np.float32)
     px = np.searchsorted(tab[1:P.img_w], yaw, side="right")
     np.testing.assert_array_equal(px, o["px"])
-    # rows: pitch = float asin of the float z / range, row from the table
+    # rows: from the table on q = the float z / range (the pitch is the
+    # float asin of q; |q| > 1 has a NaN pitch: row H - 1)
     x, y, z = xyzi[:, 0], xyzi[:, 1], xyzi[:, 2]
     rng3 = np.sqrt((x * x + y * y) + z * z)
-    pitch = np.arcsin((z / rng3).astype(np.float64)).astype(np.float32)
+    q = (z / rng3).astype(np.float32)
     assert np.all(np.diff(ptab[1:-1]) >= 0)
-    py = P.img_h - 1 - np.searchsorted(ptab[1:P.img_h], pitch, side="right")
+    py = P.img_h - 1 - np.searchsorted(ptab[1:P.img_h], q, side="right")
+    py = np.where(np.abs(q) <= 1, py, P.img_h - 1)
     np.testing.assert_array_equal(py, o["py"])
+    # boundary q values themselves, and their float neighbours, against the
+    # reference's row formula through the correctly rounded asin
+    qs = np.concatenate([ptab[1:P.img_h][np.isfinite(ptab[1:P.img_h])]])
+    qs = np.concatenate([qs, np.nextafter(qs, -np.inf), np.nextafter(qs, np.inf)]).astype(np.float32)
+    fd = np.float32(np.radians(22.5)); fov = np.float32(fd + fd)
+    pitch = np.arcsin(qs.astype(np.float64)).astype(np.float32)
+    t = ((pitch + fd) / fov).astype(np.float32)
+    yy = np.floor(((np.float32(1) - t) * np.float32(P.img_h)).astype(np.float32))
+    row = np.clip(yy, 0, P.img_h - 1).astype(int)
+    py2 = P.img_h - 1 - np.searchsorted(ptab[1:P.img_h], qs, side="right")
+    np.testing.assert_array_equal(py2, row)
     # ground bins: theta from the float atan2, radius window in double
     x, y = xyzi[:, 0], xyzi[:, 1]
     r = np.sqrt(x * x + y * y).astype(np.float32)
