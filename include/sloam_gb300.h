@@ -341,6 +341,20 @@ int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t n
                          const sloam_cylinder* map, int32_t n_map, double* pose_out,
                          int32_t* success_out, int32_t* ncyl_out);
 
+/* Projection outputs of keyframe k of the last batch call (the outputs of
+ * Segmentation::maskCloud for that scan, inference.cpp:200-273), into host
+ * buffers as sloam_project_mask gives them: range_image, mask_out,
+ * ground_idx (+ n_ground) and tree_cloud (derived from the batch's
+ * per-point tree flags and the scan, which must still be in place for a
+ * device batch).  px and py are not kept for batch keyframes and must be
+ * NULL.  Valid until the next batch call. */
+int sloam_batch_scan_out(sloam_ctx* ctx, int32_t k, sloam_scan_out* out);
+
+/* Device time of the last batch call's projection launches (CUDA events on
+ * the projection stream around each chunk of keyframes, summed), the number
+ * of chunks and of keyframes they covered. */
+int sloam_frontend_time(sloam_ctx* ctx, float* ms, int32_t* n_chunks, int32_t* n_keyframes);
+
 /* Input ingestion (pcl::fromROSMsg at inputNode.cpp:247 and the XYZI
  * packing of inference.cpp:374-379, on the device): n points of a
  * sensor message with point_step bytes per point and little-endian fields

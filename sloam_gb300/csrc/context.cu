@@ -404,9 +404,6 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.prop_x = c.take<float>(ps * 384);
   d.prop_f = c.take<float4>(ps);
   d.prop_out = c.take<float>(ps * 8);
-  d.phyp = c.take<float4>(ps);
-  d.phyp_cnt = c.take<int32_t>(ps);
-  d.pbest = c.take<unsigned long long>(d.cap_lm);
   d.pflag = c.take<int32_t>(d.cap_lm);
   d.pose_io = c.take<double>(32);
   d.cnt = c.take<Counters>(1);
@@ -1152,7 +1149,9 @@ __global__ void k_batch_out(Counters* c, const double* pose_io, double* pose_out
                             int32_t* success_out, int32_t* ncyl_out, int k) {
   if (threadIdx.x < 7) pose_out[7 * k + threadIdx.x] = pose_io[7 + threadIdx.x];
   if (threadIdx.x == 0) {
-    success_out[k] = c->status == SLOAM_OK ? c->success : 0;
+    // a keyframe where a bounded wait gave up is not a success
+    const bool gave_up = c->cc_iter_exceeded || c->prop_err || c->queue_err;
+    success_out[k] = (c->status == SLOAM_OK && !gave_up) ? c->success : 0;
     ncyl_out[k] = c->n_cyl;
   }
 }
@@ -1582,6 +1581,34 @@ extern "C" int sloam_time_kernel(sloam_ctx* ctx, int which, int reps, float* avg
 // Device time of the batch projection launches of the last batch call: the
 // sum over its chunks of the CUDA-event time between the first and the last
 // kernel of the chunk on the projection stream.
+extern "C" int sloam_batch_scan_out(sloam_ctx* ctx, int32_t k, sloam_scan_out* out) {
+  if (!ctx || !out || k < 0 || k >= ctx->fe_nkf || out->px || out->py) return SLOAM_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const int n = ctx->d.N;
+  const FrontRef& f = ctx->h_refs[k];
+  CK(cudaStreamSynchronize(ctx->fe_st));
+  int32_t fe[4] = {0, 0, 0, 0};
+  CK(cudaMemcpy(fe, f.fe, sizeof(fe), cudaMemcpyDeviceToHost));
+  out->n_ground = fe[0];
+  if (out->range_image)
+    CK(cudaMemcpy(out->range_image, f.range_img, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  if (out->mask_out) CK(cudaMemcpy(out->mask_out, f.mask, n, cudaMemcpyDeviceToHost));
+  if (out->ground_idx && fe[0] > 0)
+    CK(cudaMemcpy(out->ground_idx, f.ground_idx, sizeof(int32_t) * fe[0],
+                  cudaMemcpyDeviceToHost));
+  if (out->tree_cloud) {
+    // the context's own tree-cloud buffer as scratch (rewritten by every
+    // keyframe on the context)
+    CK(cudaStreamSynchronize(ctx->st));
+    launch_tree_out(f, ctx->kp, n, ctx->d.tree, ctx->st);
+    CK(cudaMemcpyAsync(out->tree_cloud, ctx->d.tree, sizeof(float4) * n,
+                       cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  if (fe[1]) return fail(ctx, SLOAM_ERR_CAPACITY, "batch projection: ground list over max_ground");
+  return SLOAM_OK;
+}
+
 extern "C" int sloam_frontend_time(sloam_ctx* ctx, float* ms, int32_t* n_chunks,
                                    int32_t* n_keyframes) {
   if (!ctx || !ms) return SLOAM_ERR_ARG;

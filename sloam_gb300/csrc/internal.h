@@ -254,9 +254,6 @@ struct Dev {
   float* prop_x;        // [cap_lm * S][128][3] normalised samples
   float4* prop_f;       // [cap_lm * S] sample mean (xyz), scale (w)
   float* prop_out;      // [cap_lm * S][8] network outputs
-  float4* phyp;         // [cap_lm * S] proposal circles (cu, cv, lo2, hi2)
-  int32_t* phyp_cnt;    // [cap_lm * S] inlier counts
-  unsigned long long* pbest;  // [cap_lm] best proposal (count << 32 | ~index)
   int32_t* pflag;       // [cap_lm] 1: the tree falls back to RANSAC
   int32_t* prop_err;    // &cnt->prop_err
   int prop_cap;         // cap_lm * S (0: mode 0/1)
@@ -307,6 +304,7 @@ int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStrea
 int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, int kf0,
                          int nkf, bool point_labels, cudaStream_t st);
 size_t front_gbits_words(int N);
+int launch_tree_out(const FrontRef& f, const KParams& kp, int N, float4* out, cudaStream_t st);
 int front_blocks(int N);
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);

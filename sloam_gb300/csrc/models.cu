@@ -1169,107 +1169,6 @@ __global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp,
   }
 }
 
-// ---- scoring of the learned proposals (cyl_mode 2)
-constexpr int kCountThreads = 256;
-constexpr int kHypTile = 256;  // hypotheses staged per pass (8 per lane)
-
-// Inlier counting.  The trees' projected points form one flat array (the
-// clusters back to back); blocks take 256-point chunks, one point per lane.
-// For every hypothesis of the point's tree the warp votes (ballot) and the
-// popcount lands in the register of the lane that owns the hypothesis
-// (lane = h % 32); per-block totals go to the (tree, hypothesis) counter.
-// A chunk that straddles trees runs once per tree.
-__global__ void __launch_bounds__(kCountThreads) k_cyl_count(Dev d, const float4* __restrict__ hyp,
-                                                              int* __restrict__ hcnt, int K) {
-  __shared__ float4 sh[kHypTile];
-  __shared__ int sred[kCountThreads / 32][kHypTile];
-  const int nl = d.cnt->n_lm;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const bool clusters = d.cnt->n_cluster > 0;
-  const int total = clusters ? d.cnt->n_cluster : d.cnt->n_p;
-  const float2* uvbase = clusters ? d.lm_uv : d.lm_uv + d.cap_cluster;
-  auto seg = [&](int l) { return clusters ? d.lm_cbeg[l] : d.lm_pbeg[d.lm_vbeg[l]]; };
-  for (int q0 = blockIdx.x * kCountThreads; q0 < total; q0 += gridDim.x * kCountThreads) {
-    // first tree whose segment holds q0
-    int lo = 0, hi = nl - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (seg(mid) <= q0) lo = mid;
-      else hi = mid - 1;
-    }
-    for (int l = lo; l < nl && seg(l) < q0 + kCountThreads; ++l) {
-      const int s0 = max(q0, seg(l)), s1 = min(q0 + kCountThreads, seg(l + 1));
-      if (s1 <= s0 || !fit_eligible(d.cyl_all[l])) continue;
-      const int q = q0 + threadIdx.x;
-      const bool mine = q >= s0 && q < s1;
-      float2 p = make_float2(0.f, 0.f);
-      if (mine) p = uvbase[q];
-      for (int t0 = 0; t0 < K; t0 += kHypTile) {
-        const int nt = min(kHypTile, K - t0);
-        for (int i = threadIdx.x; i < kHypTile; i += blockDim.x)
-          sh[i] = i < nt ? hyp[(size_t)l * K + t0 + i] : make_float4(0.f, 0.f, 0.f, -1.f);
-        __syncthreads();
-        int acc[kHypTile / 32];
-#pragma unroll
-        for (int hb = 0; hb < kHypTile / 32; ++hb) acc[hb] = 0;
-#pragma unroll
-        for (int hb = 0; hb < kHypTile / 32; ++hb) {
-          const int jn = min(32, nt - hb * 32);  // block-uniform
-#pragma unroll 8
-          for (int j = 0; j < jn; ++j) {
-            const float4 e = sh[hb * 32 + j];
-            const float du = fsub(p.x, e.x), dv = fsub(p.y, e.y);
-            const float d2 = fadd(fmul(du, du), fmul(dv, dv));
-            const unsigned b = __ballot_sync(0xffffffffu, mine && (d2 > e.z) && (d2 < e.w));
-            if (lane == j) acc[hb] += __popc(b);
-          }
-        }
-#pragma unroll
-        for (int hb = 0; hb < kHypTile / 32; ++hb) sred[w][hb * 32 + lane] = acc[hb];
-        __syncthreads();
-        for (int h = threadIdx.x; h < nt; h += blockDim.x) {
-          int s = 0;
-#pragma unroll
-          for (int k = 0; k < kCountThreads / 32; ++k) s += sred[k][h];
-          if (s) atomicAdd(hcnt + (size_t)l * K + t0 + h, s);
-        }
-        __syncthreads();
-      }
-    }
-  }
-}
-
-// Best hypothesis per tree: most inliers, lowest hypothesis on ties.
-__global__ void __launch_bounds__(256) k_cyl_best(Dev d, const int* __restrict__ hcnt, int K,
-                                                  unsigned long long* __restrict__ best_out) {
-  __shared__ unsigned long long sk[8];
-  const int nl = d.cnt->n_lm;
-  for (int l = blockIdx.x; l < nl; l += gridDim.x) {
-    unsigned long long best = 0ull;
-    if (fit_eligible(d.cyl_all[l])) {
-      for (int h = threadIdx.x; h < K; h += blockDim.x) {
-        const int c = hcnt[(size_t)l * K + h];
-        if (c > 0) {
-          const unsigned long long key =
-              ((unsigned long long)c << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
-          best = key > best ? key : best;
-        }
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-      best = x > best ? x : best;
-    }
-    if ((threadIdx.x & 31) == 0) sk[threadIdx.x >> 5] = best;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int k = 1; k < (int)(blockDim.x >> 5); ++k) best = sk[k] > best ? sk[k] : best;
-      best_out[l] = best;
-    }
-    __syncthreads();
-  }
-}
-
 // ----------------------------------------- learned proposals (cyl_mode 2)
 // 8 (prop_S) samples of 128 points per eligible tree, drawn with
 // replacement from the tree's points (Philox keyed by tree id, sample and
@@ -1307,81 +1206,117 @@ __global__ void __launch_bounds__(128) k_prop_gather(Dev d, KParams kp) {
 
 // Network output -> circle hypothesis on the tree's prior-axis frame: the
 // proposed axis point nearest the sample mean, projected along the prior
-// axis, and the proposed radius with the inlier band +-tau.
-__global__ void __launch_bounds__(256) k_prop_hyp(Dev d, KParams kp) {
-  const int nl = d.cnt->n_lm, S = kp.prop_S;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * S;
-       it += gridDim.x * blockDim.x) {
-    const int l = it / S;
-    if (it == l * S) {
-      d.pflag[l] = 0;
-      if (fit_eligible(d.cyl_all[l])) atomicAdd(&d.cnt->n_fit, 1);
+// axis, and the proposed radius with the inlier band +-tau; (0, 0, 0, -1)
+// (no inlier) when the output gives no usable circle.
+__device__ __forceinline__ float4 prop_hyp(const Dev& d, const KParams& kp, int it,
+                                           const CylFrame& f) {
+  float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
+  const float* o = d.prop_out + (size_t)it * 8;
+  const float4 fm = d.prop_f[it];
+  float ax = o[0], ay = o[1], az = o[2];
+  const float an = sqrtf(ax * ax + ay * ay + az * az);
+  if (an > 0.f && fabsf(az) > 1e-3f * an) {
+    ax /= an; ay /= an; az /= an;
+    const float cz = -(o[3] * ax + o[4] * ay) / az;
+    const float4 C = make_float4(fm.x + fm.w * o[3], fm.y + fm.w * o[4], fm.z + fm.w * cz, 0.f);
+    const float r = fm.w * expf(o[5]);
+    const float2 cuv = project_uv(f, C);
+    if (r > 0.f && r <= kp.max_hyp_r && isfinite(cuv.x) && isfinite(cuv.y)) {
+      const float lo = fsub(r, kp.tau), hi = fadd(r, kp.tau);
+      e = make_float4(cuv.x, cuv.y, lo > 0.0f ? fmul(lo, lo) : -1.0f, fmul(hi, hi));
     }
-    d.phyp_cnt[it] = 0;
-    float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
-    const CylD c = d.cyl_all[l];
-    if (fit_eligible(c)) {
-      const float* o = d.prop_out + (size_t)it * 8;
-      const float4 fm = d.prop_f[it];
-      float ax = o[0], ay = o[1], az = o[2];
-      const float an = sqrtf(ax * ax + ay * ay + az * az);
-      if (an > 0.f && fabsf(az) > 1e-3f * an) {
-        ax /= an; ay /= an; az /= an;
-        const float cz = -(o[3] * ax + o[4] * ay) / az;
-        const float4 C = make_float4(fm.x + fm.w * o[3], fm.y + fm.w * o[4], fm.z + fm.w * cz, 0.f);
-        const float r = fm.w * expf(o[5]);
-        const CylFrame f = make_frame(d, c);
-        const float2 cuv = project_uv(f, C);
-        if (r > 0.f && r <= kp.max_hyp_r && isfinite(cuv.x) && isfinite(cuv.y)) {
-          const float lo = fsub(r, kp.tau), hi = fadd(r, kp.tau);
-          e = make_float4(cuv.x, cuv.y, lo > 0.0f ? fmul(lo, lo) : -1.0f, fmul(hi, hi));
-        }
-      }
-    }
-    d.phyp[it] = e;
   }
+  return e;
 }
 
-// The learned proposals' LS pass (cyl_mode 2), one block per tree: from the
-// best network proposal, LS refinement with the inliers re-selected by the
-// current model; the refined model is kept when its inliers (|distance to
-// the refined axis - radius| < tau) are at least prop_ratio of the tree's
-// points, else the tree is flagged for the RANSAC pass (the cylinder work
-// queue).  The proposals are few (prop_S per tree) and their trees all
-// alike in cost, so the plain per-tree blocks do better here than the
-// queue, whose ordering launch and persistent blocks only pay off on the
-// 256-hypothesis counting.
-constexpr int kLsThreads = 256;
-__global__ void __launch_bounds__(kLsThreads, 4) k_prop_ls(Dev d, KParams kp) {
+// The learned proposals' pass (cyl_mode 2), one block per tree: the tree's
+// prop_S circle hypotheses from the network outputs, their inlier counts
+// over the tree's projected points (|(u, v) - centre|^2 strictly inside the
+// band), the best (most inliers, the lowest proposal on ties, none without
+// an inlier), then LS refinement from it with the inliers re-selected by
+// the current model; the refined model is kept when its inliers (|distance
+// to the refined axis - radius| < tau) are at least prop_ratio of the
+// tree's points, else the tree is flagged for the RANSAC pass (the cylinder
+// work queue).  The proposals are few and their trees all alike in cost, so
+// one block per tree does the whole pass with no launch in between.
+constexpr int kLsThreads = 256, kMaxProp = 8;
+__global__ void __launch_bounds__(kLsThreads, 4) k_prop_fit(Dev d, KParams kp) {
   __shared__ int s_in[kLsThreads / 32];
   __shared__ float red[20][kLsThreads / 32];
   __shared__ double st[14];  // c(3), dir(3), r, ok, b1(3), b2(3)
   __shared__ double ssum[20];
   __shared__ double sxls[5];
   __shared__ float sf[13];   // c(3), dir(3), b1(3), b2(3), r as float
-  const int nl = d.cnt->n_lm;
+  __shared__ float4 s_hyp[kMaxProp];
+  __shared__ int s_cnt[kLsThreads / 32][kMaxProp];
+  __shared__ unsigned long long s_best;
+  const int nl = d.cnt->n_lm, S = kp.prop_S;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int l = blockIdx.x; l < nl; l += gridDim.x) {
     CylD c = d.cyl_all[l];
-    if (c.stage != 1 || c.radius == -1.0) continue;
-    const unsigned long long key = d.pbest[l];
-    if (key == 0ull) {
-      if (threadIdx.x == 0) {
-        d.pflag[l] = 1;
-        atomicAdd(&d.cnt->n_fallback, 1);
-      }
-      continue;
+    const bool elig = fit_eligible(c);
+    if (threadIdx.x == 0) {
+      d.pflag[l] = 0;
+      if (elig) atomicAdd(&d.cnt->n_fit, 1);
     }
-    const int h = (int)(0xFFFFFFFFu - (uint32_t)(key & 0xffffffffull));
-    const int best_cnt = (int)(key >> 32);
+    if (!elig) continue;
     const float4* pts;
     const float2* uvs;
     int n;
     tree_points(d, l, &pts, &n, &uvs);
     const CylFrame f = make_frame(d, c);
+    if (threadIdx.x < S) s_hyp[threadIdx.x] = prop_hyp(d, kp, l * S + threadIdx.x, f);
+    __syncthreads();
+    {
+      int cnt[kMaxProp];
+#pragma unroll
+      for (int h = 0; h < kMaxProp; ++h) cnt[h] = 0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float2 p = uvs[i];
+#pragma unroll
+        for (int h = 0; h < kMaxProp; ++h) {
+          if (h >= S) break;
+          const float4 e = s_hyp[h];
+          const float du = fsub(p.x, e.x), dv = fsub(p.y, e.y);
+          const float d2 = fadd(fmul(du, du), fmul(dv, dv));
+          cnt[h] += (d2 > e.z) && (d2 < e.w) ? 1 : 0;
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < kMaxProp; ++h) {
+        const int v = warp_sumi(cnt[h]);
+        if (lane == 0) s_cnt[w][h] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long best = 0ull;
+        for (int h = 0; h < S; ++h) {
+          int t = 0;
+          for (int q2 = 0; q2 < kLsThreads / 32; ++q2) t += s_cnt[q2][h];
+          if (t > 0) {
+            const unsigned long long key =
+                ((unsigned long long)t << 32) | (unsigned long long)(0xFFFFFFFFu - (uint32_t)h);
+            best = key > best ? key : best;
+          }
+        }
+        s_best = best;
+      }
+      __syncthreads();
+    }
+    const unsigned long long key = s_best;
+    if (key == 0ull) {
+      if (threadIdx.x == 0) {
+        d.pflag[l] = 1;
+        atomicAdd(&d.cnt->n_fallback, 1);
+      }
+      __syncthreads();
+      continue;
+    }
+    const int h = (int)(0xFFFFFFFFu - (uint32_t)(key & 0xffffffffull));
+    const int best_cnt = (int)(key >> 32);
     Hyp H;
     {
-      const float4 e = d.phyp[(size_t)l * kp.prop_S + h];
+      const float4 e = s_hyp[h];
       H.cu = e.x;
       H.cv = e.y;
       H.lo2 = e.z;
@@ -1617,11 +1552,8 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool, cudaStream
     k_prop_gather<<<kCountBlocks, 128, 0, st>>>(d, kp);
     n += 1 + prop::launch_prop_infer_trees(d.prop_tc, d.prop_x, &d.cnt->n_lm, kp.prop_S,
                                            d.prop_cap, d.prop_f, d.prop_out, d.prop_err, st);
-    k_prop_hyp<<<kCylBlocks, 256, 0, st>>>(d, kp);
-    k_cyl_count<<<kCountBlocks, kCountThreads, 0, st>>>(d, d.phyp, d.phyp_cnt, kp.prop_S);
-    k_cyl_best<<<kCylBlocks, 256, 0, st>>>(d, d.phyp_cnt, kp.prop_S, d.pbest);
-    k_prop_ls<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
-    n += 4;
+    k_prop_fit<<<kCylBlocks, kLsThreads, 0, st>>>(d, kp);
+    n += 1;
     only = d.pflag;
   }
   k_cyl_hypgen<<<kCylBlocks, 256, 0, st>>>(d, kp, only);

@@ -16,7 +16,7 @@
 // formula both are), so its boundary table is on q itself (py_tab[k] =
 // smallest float q whose row is <= H-1-k): q is exact, and the row is exact
 // comparisons, with no angle evaluated.
-// The nearest point wins its pixel: 64-bit atomicMin on
+// The nearest point wins its pixel: 64-bit minimum reduction on
 // range bits (32) : point index (24) : point label (8), ties to the lowest
 // index; the label rides in the key so the winner's label needs no gather.
 //
@@ -66,6 +66,13 @@ __device__ __forceinline__ float row_estimate_q(float q, const KParams& kp) {
   return (pitch + kp.fov_down_abs) * (1.0f / kp.fov) * (float)kp.img_h;
 }
 
+// 64-bit minimum without a returned value (a reduction, not an atomic with
+// a result): nothing waits for it, so a thread's next point does not wait
+// for the previous point's round trip to L2.
+__device__ __forceinline__ void red_min_u64(unsigned long long* a, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.min.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+
 // The buffers of the keyframe this block works on.
 template <bool kBatch>
 __device__ __forceinline__ FrontRef front(const Dev& d, const FrontRef* refs, int kf0) {
@@ -96,7 +103,8 @@ __device__ __forceinline__ int32_t* fe_slot(const Dev& d, const FrontRef& f, int
 }
 
 // In an organised scan the points of a warp fall on distinct pixels, so each
-// point makes its own 64-bit atomicMin.  Pixel (H-1, W-1), where every
+// point makes its own 64-bit minimum reduction (no returned value, so the
+// thread's next point does not wait for it).  Pixel (H-1, W-1), where every
 // no-return (NaN) point lands, is the exception: its keys are reduced over
 // the warp (two full-warp min reductions), kept as a running minimum per
 // warp, and sent by one atomic per block.  The minimum is the same, so the
@@ -131,7 +139,7 @@ __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontR
     const float4 p = p_next;
     const uint32_t lab = lab_next;
     if (i + stride < N) {
-      p_next = f.xyzi[i + stride];  // kept in L2 for k_label
+      p_next = f.xyzi[i + stride];  // kept in L2 for the label pass
       lab_next = point_labels ? f.plabel[i + stride] : 0u;
     }
     if (valid) {
@@ -163,7 +171,7 @@ __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontR
       key = ((unsigned long long)range_key(range) << 32) | ((uint32_t)i << 8) | lab;
     }
     const bool at_hot = valid && pix == hot;
-    if (valid && !at_hot) atomicMin(f.pkey + pix, key);
+    if (valid && !at_hot) red_min_u64(f.pkey + pix, key);
     if (__any_sync(0xffffffffu, at_hot)) {
       const uint32_t hi = at_hot ? (uint32_t)(key >> 32) : 0xffffffffu;
       const uint32_t hmin = __reduce_min_sync(0xffffffffu, hi);
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(256) k_project(Dev d, KParams kp, const FrontR
   if (threadIdx.x == 0) {
     unsigned long long m = hot_w[0];
     for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = hot_w[w] < m ? hot_w[w] : m;
-    if (m != ~0ull) atomicMin(f.pkey + hot, m);
+    if (m != ~0ull) red_min_u64(f.pkey + hot, m);
   }
   slow = warp_sumi(slow);
   if (lane == 0 && slow) atomicAdd(fe_slot<kBatch>(d, f, 2), slow);
@@ -254,7 +262,10 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
       if (!point_labels) m = min_[j];
       f.range_img[o] = r;
       f.mask[o] = m;
-      const uint8_t mo = pixel_label(f, pix[j], point_labels);
+      // a point that won its own pixel (the common case in an organised
+      // scan) has the pixel's label in the key already loaded
+      const uint8_t mo = (point_labels && pix[j] == o) ? (uint8_t)key[j]
+                                                       : pixel_label(f, pix[j], point_labels);
       ground = (mo == 1);
       if (kBatch) {
         // the tree cloud stays a view: this flag + the scan (TreeView)
@@ -319,6 +330,13 @@ __global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const F
   }
 }
 
+// The organised tree cloud of a batch keyframe, written out from its view
+// (the per-point tree flags and the scan), for the caller.
+__global__ void k_tree_out(TreeView v, float4* out, int N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) out[i] = v[i];
+}
+
 // Per-keyframe counter reset.  A keyframe whose projection ran in a batch
 // launch takes the counts of that launch from its fe block.
 __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster) {
@@ -346,8 +364,9 @@ __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_c
 }  // namespace
 
 // Blocks per keyframe of a batch projection launch: the resident blocks of
-// the whole GPU shared among the launch's keyframes (each thread then walks
-// several points), at most one point per thread.
+// the whole GPU shared among the launch's keyframes, rounded down so that the
+// whole grid is resident in one wave (a block left for a second wave would
+// walk its points after all the others), at most one point per thread.
 static int project_blocks_per_kf(int N, int nkf) {
   static int resident = 0;
   if (!resident) {
@@ -358,12 +377,18 @@ static int project_blocks_per_kf(int N, int nkf) {
     resident = std::max(1, sms) * std::max(1, per_sm);
   }
   const int full = (N + 255) / 256;
-  const int share = (resident + nkf - 1) / std::max(1, nkf);
+  const int share = resident / std::max(1, nkf);
   return std::max(1, std::min(full, share));
 }
 
 size_t front_gbits_words(int N) { return (size_t)((N + 1023) / 1024) * 32 + 32; }
 int front_blocks(int N) { return (N + 1023) / 1024; }
+
+int launch_tree_out(const FrontRef& f, const KParams& kp, int N, float4* out, cudaStream_t st) {
+  const TreeView v{nullptr, f.xyzi, f.tflag, kp.img_w, kp.do_destagger ? 1 : 0};
+  k_tree_out<<<(N + 255) / 256, 256, 0, st>>>(v, out, N);
+  return 1;
+}
 
 int launch_begin(const Dev& d, int n_ground, int n_lm, int n_v, int n_p, int n_cluster,
                  cudaStream_t st) {

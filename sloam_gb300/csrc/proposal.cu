@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <vector>
 
+#include "bulk.cuh"
 #include "common.cuh"
 #include "internal.h"
 #include "proposal.cuh"
@@ -459,7 +460,6 @@ __global__ void __launch_bounds__(128) k_prop_infer_ref(const unsigned char* __r
 }
 
 // ------------------------------------------------- tcgen05 primitives
-SLOAM_D uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 // shared-memory matrix descriptor: K-major, no swizzle; LBO = byte stride
 // between core matrices along K, SBO = along M/N; version 1 (bit 46)
 SLOAM_D uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -484,20 +484,6 @@ SLOAM_D void mma_commit(uint64_t* mbar) {
 }
 SLOAM_D void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 SLOAM_D void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-SLOAM_D void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-SLOAM_D void mbar_init(uint64_t* m, uint32_t n) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(m)), "r"(n) : "memory");
-}
-SLOAM_D bool mbar_test(uint64_t* m, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(saddr(m)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
 constexpr int kMbarSpin = 1 << 20;  // bounded wait (the MMAs take microseconds)
 
 #define SG_TMEM_LD32(taddr, v)                                                                 \
@@ -568,20 +554,6 @@ SLOAM_D bool mbar_wait_bounded(uint64_t* m, uint32_t phase, int* err, int* abort
     return false;
   }
   return true;
-}
-SLOAM_D void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(m)),
-               "r"(bytes)
-               : "memory");
-}
-// bulk copy global -> shared (16-byte aligned, size a multiple of 16),
-// completing on the mbarrier's transaction count
-SLOAM_D void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(dst),
-      "l"((uint64_t)__cvta_generic_to_global(src)), "r"(bytes), "r"(saddr(bar))
-      : "memory");
 }
 // ReLU, round to bf16 and pack: lo in the low half, hi in the high half
 SLOAM_D uint32_t relu_bf16x2(float lo, float hi) {
@@ -674,7 +646,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     for (int q = 0; q < kTcWg; ++q) mbar_init(mbar + q, 1);
     mbar_init(lbar, 1);
     *abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init_fence();
     mbar_expect_tx(lbar, kTcB2xBytes + kTcW3Bytes + kTcB1Bytes + kSmallCopy + kTcW5hBytes);
     bulk_load(saddr(smem + kSmB2), tcw + kTcB2xOff, kTcB2xBytes, lbar);
     bulk_load(saddr(smem + kSmB3), tcw + kTcW2Bytes, kTcW3Bytes, lbar);

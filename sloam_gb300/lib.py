@@ -20,6 +20,7 @@ EXPORTS = [
     "sloam_internal_tables", "sloam_set_proposal_weights", "sloam_pack_points",
     "sloam_mapmgr_create", "sloam_mapmgr_destroy", "sloam_mapmgr_size", "sloam_mapmgr_read",
     "sloam_mapmgr_load", "sloam_mapmgr_submap", "sloam_keyframe_mapped", "sloam_set_cc_iter_limit",
+    "sloam_batch_scan_out", "sloam_frontend_time",
 ]
 
 _lib = None
@@ -98,6 +99,7 @@ def load(path=LIB_PATH):
     L.sloam_time_kernel.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.sloam_frontend_time.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32)]
+    L.sloam_batch_scan_out.argtypes = [vp, C.c_int32, C.POINTER(A.ScanOut)]
     L.sloam_keyframe_stats.argtypes = [vp, C.POINTER(C.c_int32), C.c_int]
     _lib = L
     return L

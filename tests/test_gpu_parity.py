@@ -462,6 +462,76 @@ def test_keyframes_batches_match_single(destagger):
     ctx.close()
 
 
+def _scan_out_equal(g, o, n_ground):
+    np.testing.assert_array_equal(g["range_image"].view(np.uint32), o["range_image"].view(np.uint32))
+    np.testing.assert_array_equal(g["mask_out"], o["mask_out"])
+    assert n_ground == o["n_ground"]
+    np.testing.assert_array_equal(g["ground_idx"][:n_ground], o["ground_idx"][:n_ground])
+    np.testing.assert_array_equal(g["tree_cloud"].view(np.uint32), o["tree_cloud"].view(np.uint32))
+
+
+@pytest.mark.parametrize("destagger", [0, 1])
+def test_batch_projection_matches_oracle(destagger):
+    """The batch projection (the resident projection grid, the label pass
+    and the ordered ground compaction, the pixel keys re-armed chunk by
+    chunk): 37 keyframes through the device entry point (chunks of 16, 16
+    and a partial 5) twice, then through the host entry point (chunks of 8),
+    every keyframe's range image, mask, ground list and organised tree cloud
+    bit-identical to the oracle's projection of its scan."""
+    import torch
+    cfg, forest, kfs = H.scene("C2", seed=3, n_kf=3)
+    P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1, do_destagger=destagger)
+    P.batch_slots = 3
+    mapa = forest.map_cylinders()
+    mapc = A.cylinders_from_array(mapa)
+    nm = len(mapa)
+    ref = [H.oracle_project(P, kf.xyzi, labels=kf.labels) for kf in kfs]
+    ctx = make_ctx(P)
+    _first_scan(ctx, P, kfs[0], mapc, nm)
+    B = 37
+    order = [(5 * k) % len(kfs) for k in range(B)]
+    n = len(kfs[0].xyzi)
+    xs = np.stack([kfs[j].xyzi for j in order])
+    ls = np.stack([kfs[j].labels for j in order])
+    poses = (A.SE3 * B)(*[A.SE3.from_qt(*kfs[j].pose_est_qt()) for j in order])
+    dx = torch.from_numpy(xs).cuda()
+    dl = torch.from_numpy(ls).cuda()
+    dm = torch.from_numpy(np.frombuffer(bytes(mapc), np.uint8).copy()).cuda()
+    pose_out = torch.zeros(B * 7, dtype=torch.float64, device="cuda")
+    succ = torch.zeros(B, dtype=torch.int32, device="cuda")
+    ncyl = torch.zeros(B, dtype=torch.int32, device="cuda")
+
+    def check_all():
+        for k, j in enumerate(order):
+            b, s = H.scan_buffers(n, P.img_h, P.img_w)
+            s.px = None
+            s.py = None
+            ctx.check(ctx.L.sloam_batch_scan_out(ctx.h, k, C.byref(s)))
+            _scan_out_equal(b, ref[j], s.n_ground)
+
+    for _ in range(2):
+        ctx.check(ctx.L.sloam_keyframes_device(ctx.h, dx.data_ptr(), n, B, dl.data_ptr(), poses,
+                                               dm.data_ptr(), nm, pose_out.data_ptr(),
+                                               succ.data_ptr(), ncyl.data_ptr()))
+        torch.cuda.synchronize()
+        check_all()
+    h_pose = np.zeros(B * 7, np.float64)
+    h_succ = np.zeros(B, np.int32)
+    h_ncyl = np.zeros(B, np.int32)
+    ctx.check(ctx.L.sloam_keyframes_host(ctx.h, A.ptr(xs, C.c_float), n, B,
+                                         A.ptr(ls, C.c_uint8), poses, mapc, nm,
+                                         h_pose.ctypes.data, h_succ.ctypes.data,
+                                         h_ncyl.ctypes.data))
+    check_all()
+    # px / py are not kept for batch keyframes; a keyframe past the batch
+    b, s = H.scan_buffers(n, P.img_h, P.img_w)
+    assert ctx.L.sloam_batch_scan_out(ctx.h, 0, C.byref(s)) == A.SLOAM_ERR_ARG
+    s.px = None
+    s.py = None
+    assert ctx.L.sloam_batch_scan_out(ctx.h, B, C.byref(s)) == A.SLOAM_ERR_ARG
+    ctx.close()
+
+
 def test_cc_union_limit_runs_out_and_context_recovers():
     """The bounded union loop of the connected components gives up: with a
     retry limit of 0 every union that is needed fails at once, the kernels
