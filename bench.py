@@ -14,9 +14,9 @@ these; `e2e` runs the learned path through the host C ABI
 (sloam_keyframes_host) from pinned host buffers.  L2 is flushed (256 MB
 write) before every timed step.
 
-`roofline` is the batch projection stage (k_project, k_label,
-k_ground_compact over 16 keyframes per launch), timed with CUDA events on its
-stream inside the timed steps: 26 algorithmic bytes per point (16 B XYZI +
+`roofline` is the batch projection stage (k_project, k_label_batch,
+k_compact_batch over the step's 64 keyframes per launch group), timed with
+CUDA events on its streams inside the timed steps: 26 algorithmic bytes per point (16 B XYZI +
 1 B label read, 4 B pixel index + 4 B range + 1 B mask written).  `kernels`
 holds the kernels that decide keyframes/s, each timed alone with CUDA events
 against the roof that binds it.
@@ -548,7 +548,7 @@ def main():
     e2e_ok = int(h_succ.sum())
 
     # ---- roofline: the batch projection stage (HBM-bound), per launch group
-    # (16 keyframes per launch with the inputs in device memory);
+    # (64 keyframes per launch with the inputs in device memory);
     # algorithmic bytes = 26 B per point.
     peaks, peak_src = {}, "fallback"
     try:
@@ -566,7 +566,7 @@ def main():
         "traffic": (FRONT_TRAFFIC_PER_KF * fe_kf / fe_launches
                     if fe_launches and FRONT_TRAFFIC_PER_KF else None),
         "peak_source": peak_src,
-        "kernel": "batch projection stage: k_project + k_label + k_ground_compact, "
+        "kernel": "batch projection stage: k_project + k_label_batch + k_compact_batch, "
                   f"{fe_kf / max(fe_launches, 1):.0f} keyframes per launch",
         "algorithmic_bytes_per_launch": fe_bytes / fe_launches if fe_launches else None,
         "ms_per_launch": fe_ms / fe_launches if fe_launches else None,

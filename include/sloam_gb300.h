@@ -350,9 +350,10 @@ int sloam_keyframes_host(sloam_ctx* ctx, const float* xyzi, int32_t n, int32_t n
  * NULL.  Valid until the next batch call. */
 int sloam_batch_scan_out(sloam_ctx* ctx, int32_t k, sloam_scan_out* out);
 
-/* Device time of the last batch call's projection launches (CUDA events on
- * the projection stream around each chunk of keyframes, summed), the number
- * of chunks and of keyframes they covered. */
+/* Device time of the last batch call's projection (CUDA events from the
+ * first chunk's projection kernel to the last chunk's ground compaction; a
+ * chunk's label kernels overlap the next chunk's projection), the number of
+ * chunks and of keyframes they covered. */
 int sloam_frontend_time(sloam_ctx* ctx, float* ms, int32_t* n_chunks, int32_t* n_keyframes);
 
 /* Input ingestion (pcl::fromROSMsg at inputNode.cpp:247 and the XYZI

@@ -301,8 +301,12 @@ KParams make_kparams(const sloam_params& p);
 // Every launcher enqueues on `st` and returns the number of kernels launched.
 int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st);
 // a1-a2 for keyframes [kf0, kf0 + nkf) of refs (device array), one launch per kernel
-int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, int kf0,
-                         int nkf, bool point_labels, cudaStream_t st);
+// A chunk of batch keyframes: the projection kernel, then (on another
+// stream, after it) the label and compaction kernels.
+int launch_project_batch_points(const Dev& d, const KParams& kp, const FrontRef* refs,
+                                int kf0, int nkf, bool point_labels, cudaStream_t st);
+int launch_project_batch_labels(const Dev& d, const FrontRef* refs, int kf0, int nkf,
+                                bool point_labels, cudaStream_t st);
 size_t front_gbits_words(int N);
 int launch_tree_out(const FrontRef& f, const KParams& kp, int N, float4* out, cudaStream_t st);
 int front_blocks(int N);

@@ -20,10 +20,11 @@
 // range bits (32) : point index (24) : point label (8), ties to the lowest
 // index; the label rides in the key so the winner's label needs no gather.
 //
-// Every kernel runs in two forms: one keyframe on the context's own buffers
-// (inputs read through the context's input block, so a captured graph can be
-// replayed on new inputs), or a batch of keyframes, blockIdx.y selecting the
-// keyframe's FrontRef.
+// Two forms: one keyframe on the context's own buffers (inputs read through
+// the context's input block, so a captured graph can be replayed on new
+// inputs): k_project, k_label, k_ground_compact; or a chunk of batch
+// keyframes, blockIdx.y selecting the keyframe's FrontRef: k_project,
+// k_label_batch, k_compact_batch (warp by warp, no block barrier).
 #include <algorithm>
 
 #include "internal.h"
@@ -203,21 +204,17 @@ __device__ __forceinline__ uint8_t pixel_label(const FrontRef& f, int pix, int p
 // The label stage works in blocks of 1024 pixels / points (the ground
 // bits, 32 per word, and the per-block ground counts); 256 threads take 4
 // each, at a stride of 256, all loads issued before use.
-constexpr int kLabelThreads = 256, kLabelPer = 4;
+constexpr int kLabelThreads = 256, kLabelPer = 4, kLabelWarps = kLabelThreads / 32;
 static_assert(kLabelThreads * kLabelPer == 1024, "label block");
 
-// Index o is pixel o and point o.  Pixel: range image and mask from the
-// winner.  Point: maskCloud -- the ground bit and the organised tree cloud,
-// both from the label of the point's pixel.  One keyframe on the context
-// materialises the tree cloud (with the Ouster destagger as a gather: even
-// rows take x,y,z from column c-32 for c >= 32 and keep their own
-// intensity; inference.cpp:200-228); a batch keyframe writes a tree flag per
-// point, from which TreeView derives the same values.
-template <bool kBatch>
-__global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, const FrontRef* refs,
-                                                         int kf0, int point_labels) {
+// One keyframe on the context.  Index o is pixel o and point o.  Pixel:
+// range image and mask from the winner.  Point: maskCloud -- the ground bit
+// and the organised tree cloud, both from the label of the point's pixel,
+// with the Ouster destagger as a gather: even rows take x,y,z from column
+// c-32 for c >= 32 and keep their own intensity (inference.cpp:200-228).
+__global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, int point_labels) {
   __shared__ int sm[33];
-  const FrontRef f = front<kBatch>(d, refs, kf0);
+  const FrontRef f = front<false>(d, nullptr, 0);
   const int N = d.N, W = kp.img_w;
   const int o0 = blockIdx.x * 1024 + threadIdx.x;
   const float nan = __int_as_float(0x7fc00000);
@@ -236,14 +233,12 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
       key[j] = f.pkey[o];
       pix[j] = f.pix[o];
       min_[j] = point_labels ? 0 : f.mask_in[o];
-      if (!kBatch) {  // the materialised tree cloud needs the points
-        src[j] = f.xyzi[o];
-        const int row = o / W, c = o - row * W;
-        stag[j] = kp.do_destagger && (row & 1) == 0 && c >= 32;
-        if (stag[j]) {
-          spix[j] = f.pix[o - 32];
-          sq[j] = f.xyzi[o - 32];
-        }
+      src[j] = f.xyzi[o];
+      const int row = o / W, c = o - row * W;
+      stag[j] = kp.do_destagger && (row & 1) == 0 && c >= 32;
+      if (stag[j]) {
+        spix[j] = f.pix[o - 32];
+        sq[j] = f.xyzi[o - 32];
       }
     }
   }
@@ -262,24 +257,16 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
       if (!point_labels) m = min_[j];
       f.range_img[o] = r;
       f.mask[o] = m;
-      // a point that won its own pixel (the common case in an organised
-      // scan) has the pixel's label in the key already loaded
-      const uint8_t mo = (point_labels && pix[j] == o) ? (uint8_t)key[j]
-                                                       : pixel_label(f, pix[j], point_labels);
+      const uint8_t mo = pixel_label(f, pix[j], point_labels);
       ground = (mo == 1);
-      if (kBatch) {
-        // the tree cloud stays a view: this flag + the scan (TreeView)
-        f.tflag[o] = mo == 255 ? 1 : 0;
-      } else {
-        float4 t = (mo == 255) ? src[j] : make_float4(nan, nan, nan, 0.0f);
-        if (stag[j]) {
-          const uint8_t ms = pixel_label(f, spix[j], point_labels);
-          t.x = (ms == 255) ? sq[j].x : nan;
-          t.y = (ms == 255) ? sq[j].y : nan;
-          t.z = (ms == 255) ? sq[j].z : nan;
-        }
-        f.tree[o] = t;
+      float4 t = (mo == 255) ? src[j] : make_float4(nan, nan, nan, 0.0f);
+      if (stag[j]) {
+        const uint8_t ms = pixel_label(f, spix[j], point_labels);
+        t.x = (ms == 255) ? sq[j].x : nan;
+        t.y = (ms == 255) ? sq[j].y : nan;
+        t.z = (ms == 255) ? sq[j].z : nan;
       }
+      f.tree[o] = t;
     }
     const unsigned b = __ballot_sync(0xffffffffu, ground);
     if ((threadIdx.x & 31) == 0 && o < N + 31) f.gbits[o >> 5] = b;
@@ -290,14 +277,12 @@ __global__ void __launch_bounds__(kLabelThreads) k_label(Dev d, KParams kp, cons
   if (threadIdx.x == 0) f.blk[blockIdx.x] = total;
 }
 
-// Ordered compaction of the ground points (point order: the 4 slices of a
-// block in turn): their indices, and for one keyframe on the context their
-// points too; re-arms the pixel keys for the next scan.
-template <bool kBatch>
-__global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const FrontRef* refs,
-                                                                  int kf0) {
+// One keyframe on the context: ordered compaction of the ground points
+// (point order: the 4 slices of a block in turn), their indices and points;
+// re-arms the pixel keys for the next scan.
+__global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d) {
   __shared__ int sm[33];
-  const FrontRef f = front<kBatch>(d, refs, kf0);
+  const FrontRef f = front<false>(d, nullptr, 0);
   const int N = d.N;
   const int o0 = blockIdx.x * 1024 + threadIdx.x;
   bool g[kLabelPer];
@@ -308,7 +293,7 @@ __global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const F
     const unsigned b = (o < N + 31) ? f.gbits[o >> 5] : 0u;
     g[j] = o < N && ((b >> (threadIdx.x & 31)) & 1u);
     v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!kBatch && g[j]) v[j] = f.xyzi[o];  // issued before the prefix sums
+    if (g[j]) v[j] = f.xyzi[o];  // issued before the prefix sums
     if (o < N) f.pkey[o] = ~0ull;
   }
   int run = block_sum_prefix(f.blk, blockIdx.x, sm);
@@ -319,14 +304,130 @@ __global__ void __launch_bounds__(kLabelThreads) k_ground_compact(Dev d, const F
     const int pos = run + block_excl_scan(g[j] ? 1 : 0, sm, &total);
     if (g[j]) {
       f.ground_idx[pos] = o;
-      // batch keyframes keep the ground list as indices (GroundView)
-      if (!kBatch && pos < d.cap_ground) f.ground[pos] = v[j];
+      if (pos < d.cap_ground) f.ground[pos] = v[j];
     }
     run += total;
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-    *fe_slot<kBatch>(d, f, 0) = run < d.cap_ground ? run : d.cap_ground;
-    if (run > d.cap_ground) atomicOr(fe_slot<kBatch>(d, f, 1), 1);
+    d.cnt->n_ground = run < d.cap_ground ? run : d.cap_ground;
+    if (run > d.cap_ground) atomicOr(&d.cnt->overflow, 1);
+  }
+}
+
+// Batch keyframes.  The label pass: block c covers points [1024 c,
+// 1024 c + 1024), 4 per thread at a stride of 256; it writes the range image,
+// mask and tree flag, the ground bits (one ballot word per 32 points) and
+// the chunk's ground count (the warps' ballot counts added once), so the
+// compaction's prefix needs no block scan.
+__global__ void __launch_bounds__(kLabelThreads) k_label_batch(Dev d, const FrontRef* refs,
+                                                               int kf0, int point_labels) {
+  const FrontRef f = refs[kf0 + blockIdx.y];
+  const int N = d.N;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int o0 = blockIdx.x * 1024 + threadIdx.x;
+  unsigned long long key[kLabelPer];
+  int pix[kLabelPer];
+#pragma unroll
+  for (int j = 0; j < kLabelPer; ++j) {
+    const int o = o0 + j * kLabelThreads;
+    key[j] = o < N ? f.pkey[o] : ~0ull;
+    pix[j] = o < N ? f.pix[o] : 0;
+  }
+  int cnt = 0;
+#pragma unroll
+  for (int j = 0; j < kLabelPer; ++j) {
+    const int o = o0 + j * kLabelThreads;
+    bool ground = false;
+    if (o < N) {
+      float r = 0.0f;
+      uint8_t m = point_labels ? 0 : f.mask_in[o];
+      if (key[j] != ~0ull) {
+        r = __uint_as_float((uint32_t)(key[j] >> 32));
+        if (point_labels) m = (uint8_t)key[j];
+      }
+      f.range_img[o] = r;
+      f.mask[o] = m;
+      // a point that won its own pixel (the common case in an organised
+      // scan) has the pixel's label in the key already loaded
+      const uint8_t mo = (point_labels && pix[j] == o) ? (uint8_t)key[j]
+                                                       : pixel_label(f, pix[j], point_labels);
+      f.tflag[o] = mo == 255 ? 1 : 0;
+      ground = (mo == 1);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, ground);
+    if (lane == 0 && o < N + 31) f.gbits[o >> 5] = b;
+    cnt += __popc(b);
+  }
+  __shared__ int wc[kLabelWarps];
+  if (lane == 0) wc[w] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+#pragma unroll
+    for (int q = 0; q < kLabelWarps; ++q) t += wc[q];
+    f.blk[blockIdx.x] = t;
+  }
+}
+
+// Batch keyframes: the ordered ground compaction, one warp per 1024-point
+// chunk.  Its first position is the sum of the counts of the chunks before
+// it; inside the chunk, a warp scan of the 32 ground words' bit
+// counts places each word's points, written word by word (coalesced); the
+// warp then re-arms the chunk's pixel keys, and the last chunk's warp
+// writes the keyframe's ground count.
+__global__ void __launch_bounds__(kLabelThreads) k_compact_batch(Dev d, const FrontRef* refs,
+                                                                 int kf0) {
+  const FrontRef f = refs[kf0 + blockIdx.y];
+  const int N = d.N, nch = (N + 1023) >> 10;
+  const int lane = threadIdx.x & 31;
+  const int c = blockIdx.x * kLabelWarps + (threadIdx.x >> 5);
+  if (c >= nch) return;  // the whole warp
+  const int wi = c * 32 + lane;  // this lane's ground word: points 32 wi .. 32 wi + 31
+  const unsigned word = (wi << 5) < N ? f.gbits[wi] : 0u;
+  // the counts of the chunks before this one, eight independent loads per
+  // lane at a time
+  int s = 0;
+  const int lim = c;
+  for (int base = 0; base < lim; base += 256) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int k = base + r * 32 + lane;
+      s += k < lim ? f.blk[k] : 0;
+    }
+  }
+  const int run = warp_sumi(s);
+  const int pc = __popc(word);
+  int incl = pc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  // word by word in point order, so each word's ground points go out as
+  // one coalesced store: lane l writes point 32 i + l of word i
+  const int excl = run + incl - pc;
+  for (int i = 0; i < 32; ++i) {
+    const unsigned wd = __shfl_sync(0xffffffffu, word, i);
+    const int e = __shfl_sync(0xffffffffu, excl, i);
+    if ((wd >> lane) & 1u)
+      f.ground_idx[e + __popc(wd & ((1u << lane) - 1u))] = ((c * 32 + i) << 5) + lane;
+  }
+  // re-arm the chunk's keys for the next scan in this slot
+  const int p0 = c << 10, p1 = min(p0 + 1024, N);
+  if (p1 - p0 == 1024 && ((reinterpret_cast<uintptr_t>(f.pkey + p0) & 15) == 0)) {
+    ulonglong2* k2 = reinterpret_cast<ulonglong2*>(f.pkey + p0);
+    const ulonglong2 ones = make_ulonglong2(~0ull, ~0ull);
+#pragma unroll 4
+    for (int q = lane; q < 512; q += 32) k2[q] = ones;
+  } else {
+    for (int q = p0 + lane; q < p1; q += 32) f.pkey[q] = ~0ull;
+  }
+  if (c == nch - 1) {
+    const int total = __shfl_sync(0xffffffffu, run + incl, 31);
+    if (lane == 0) {
+      f.fe[0] = total < d.cap_ground ? total : d.cap_ground;
+      if (total > d.cap_ground) atomicOr(f.fe + 1, 1);
+    }
   }
 }
 
@@ -367,6 +468,7 @@ __global__ void k_begin(Dev d, int n_ground, int n_lm, int n_v, int n_p, int n_c
 // the whole GPU shared among the launch's keyframes, rounded down so that the
 // whole grid is resident in one wave (a block left for a second wave would
 // walk its points after all the others), at most one point per thread.
+constexpr int kProjBlocksPerSm = 6;
 static int project_blocks_per_kf(int N, int nkf) {
   static int resident = 0;
   if (!resident) {
@@ -374,7 +476,9 @@ static int project_blocks_per_kf(int N, int nkf) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project<true>, 256, 0);
-    resident = std::max(1, sms) * std::max(1, per_sm);
+    // at most kProjBlocksPerSm per SM, the rest of each SM left to the
+    // previous chunk's label kernels, which run alongside
+    resident = std::max(1, sms) * std::max(1, std::min(per_sm, kProjBlocksPerSm));
   }
   const int full = (N + 255) / 256;
   const int share = resident / std::max(1, nkf);
@@ -402,8 +506,8 @@ int launch_project_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
 }
 int launch_project_rest(const Dev& d, const KParams& kp, bool point_labels, cudaStream_t st) {
   const int g1k = front_blocks(d.N);
-  k_label<false><<<g1k, kLabelThreads, 0, st>>>(d, kp, nullptr, 0, point_labels ? 1 : 0);
-  k_ground_compact<false><<<g1k, kLabelThreads, 0, st>>>(d, nullptr, 0);
+  k_label<<<g1k, kLabelThreads, 0, st>>>(d, kp, point_labels ? 1 : 0);
+  k_ground_compact<<<g1k, kLabelThreads, 0, st>>>(d);
   return 2;
 }
 
@@ -412,14 +516,21 @@ int launch_project(const Dev& d, const KParams& kp, bool point_labels, cudaStrea
   return 1 + launch_project_rest(d, kp, point_labels, st);
 }
 
-int launch_project_batch(const Dev& d, const KParams& kp, const FrontRef* refs, int kf0,
-                         int nkf, bool point_labels, cudaStream_t st) {
+int launch_project_batch_points(const Dev& d, const KParams& kp, const FrontRef* refs,
+                                int kf0, int nkf, bool point_labels, cudaStream_t st) {
   if (nkf <= 0) return 0;
-  const dim3 g256(project_blocks_per_kf(d.N, nkf), nkf), g1k(front_blocks(d.N), nkf);
+  const dim3 g256(project_blocks_per_kf(d.N, nkf), nkf);
   k_project<true><<<g256, 256, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
-  k_label<true><<<g1k, kLabelThreads, 0, st>>>(d, kp, refs, kf0, point_labels ? 1 : 0);
-  k_ground_compact<true><<<g1k, kLabelThreads, 0, st>>>(d, refs, kf0);
-  return 3;
+  return 1;
+}
+int launch_project_batch_labels(const Dev& d, const FrontRef* refs, int kf0, int nkf,
+                                bool point_labels, cudaStream_t st) {
+  if (nkf <= 0) return 0;
+  const dim3 g1k(front_blocks(d.N), nkf);
+  k_label_batch<<<g1k, kLabelThreads, 0, st>>>(d, refs, kf0, point_labels ? 1 : 0);
+  const dim3 gw((front_blocks(d.N) + kLabelWarps - 1) / kLabelWarps, nkf);
+  k_compact_batch<<<gw, kLabelThreads, 0, st>>>(d, refs, kf0);
+  return 2;
 }
 
 }  // namespace sg

@@ -748,31 +748,28 @@ __global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
 }
 
 // Point copies of the landmarks, spread over the whole grid: one warp per
-// vertex for the kept points, one thread per bucket slot for the cluster
-// points (raster order; the candidate of a slot found by binary search).
+// vertex for the kept points, one warp per (candidate, row) bucket for the
+// cluster points (raster order; the bucket's candidate is its index / H, so
+// no search).
 __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
   const TreeView tree = tree_view(d.in, d.W);
   const int H = d.H;
   const int lane = threadIdx.x & 31;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
   const int nv = d.cnt->n_v;
-  for (int v = gt >> 5; v < nv; v += nt >> 5) {
+  for (int v = gw; v < nv; v += nw) {
     const int src = d.lm_vsrc[v], dst = d.lm_pbeg[v], cnt = d.lm_pbeg[v + 1] - dst;
     for (int q = lane; q < cnt; q += 32) d.lm_pts[dst + q] = d.kept[src + q];
   }
-  const int nc = d.cnt->n_cand;
-  const int total = d.roff[nc * H];
-  for (int q = gt; q < total; q += nt) {
-    int lo = 0, hi = nc - 1;  // last candidate whose first slot <= q
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (d.roff[mid * H] <= q) lo = mid;
-      else hi = mid - 1;
-    }
-    const int l = d.cand_lm[lo];
-    if (l < 0) continue;
-    d.lm_cpts[d.lm_cbeg[l] + (q - d.roff[lo * H])] = tree[d.bucket[q]];
+  const int items = d.cnt->n_cand * H;
+  for (int it = gw; it < items; it += nw) {
+    const int cand = it / H;
+    const int l = d.cand_lm[cand];
+    const int q0 = d.roff[it], q1 = d.roff[it + 1];
+    if (l < 0 || q1 <= q0) continue;
+    const int dst = d.lm_cbeg[l] - d.roff[cand * H];  // slot q -> dst + q
+    for (int q = q0 + lane; q < q1; q += 32) d.lm_cpts[dst + q] = tree[d.bucket[q]];
   }
 }
 

@@ -474,10 +474,12 @@ def _scan_out_equal(g, o, n_ground):
 def test_batch_projection_matches_oracle(destagger):
     """The batch projection (the resident projection grid, the label pass
     and the ordered ground compaction, the pixel keys re-armed chunk by
-    chunk): 37 keyframes through the device entry point (chunks of 16, 16
-    and a partial 5) twice, then through the host entry point (chunks of 8),
-    every keyframe's range image, mask, ground list and organised tree cloud
-    bit-identical to the oracle's projection of its scan."""
+    chunk): 37 keyframes through the device entry point (one launch group)
+    twice, then through the host entry point (chunks of 8 on two
+    alternating scratch sets, a chunk's labels overlapping the next chunk's
+    projection), every keyframe's range image, mask, ground list and
+    organised tree cloud bit-identical to the oracle's projection of its
+    scan."""
     import torch
     cfg, forest, kfs = H.scene("C2", seed=3, n_kf=3)
     P = synth.preset_params(cfg, two_step_optim=0, cyl_mode=1, do_destagger=destagger)
