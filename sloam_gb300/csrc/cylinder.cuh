@@ -113,4 +113,58 @@ __device__ __forceinline__ void ls_frame(double* st, float* sf) {
   sf[9] = (float)b2.x; sf[10] = (float)b2.y; sf[11] = (float)b2.z;
   sf[12] = (float)st[6];
 }
+// ls_frame on a whole warp: lane i < 3 computes component i of b1 and b2
+// (the same expressions, component by component; lanes 3..31 repeat lane
+// 0's), so each FP64 instruction serves three components: the FP64 pipe
+// takes about as long for one active lane as for 32.
+__device__ __forceinline__ void warp_ls_frame(double* st, float* sf) {
+  const int lane = threadIdx.x & 31;
+  const int i = lane < 3 ? lane : 0;
+  const d3 dd = mk3(st[3], st[4], st[5]);
+  const d3 t = fabs(dd.x) < 0.9 ? mk3(1, 0, 0) : mk3(0, 1, 0);
+  const int i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;  // the cross product's indices
+  const double da[3] = {dd.x, dd.y, dd.z}, ta[3] = {t.x, t.y, t.z};
+  double b1 = da[i1] * ta[i2] - da[i2] * ta[i1];
+  const double b1x = __shfl_sync(0xffffffffu, b1, 0), b1y = __shfl_sync(0xffffffffu, b1, 1),
+               b1z = __shfl_sync(0xffffffffu, b1, 2);
+  b1 = (1.0 / norm3(mk3(b1x, b1y, b1z))) * b1;
+  const double n0 = __shfl_sync(0xffffffffu, b1, 0), n1 = __shfl_sync(0xffffffffu, b1, 1),
+               n2 = __shfl_sync(0xffffffffu, b1, 2);
+  const double ba[3] = {n0, n1, n2};
+  const double b2 = da[i1] * ba[i2] - da[i2] * ba[i1];
+  __syncwarp();
+  if (lane < 3) {
+    st[8 + i] = b1;
+    st[11 + i] = b2;
+    sf[6 + i] = (float)b1;
+    sf[9 + i] = (float)b2;
+  }
+  if (lane < 6) sf[lane] = (float)st[lane];
+  if (lane == 0) sf[12] = (float)st[6];
+  __syncwarp();
+}
+
+// The LS model update on a whole warp (st in shared memory, x the 5x5
+// solution): centre += x0 b1 + x1 b2, direction += x2 b1 + x3 b2 then
+// normalised, radius += x4, then the new frame -- the expressions of the
+// one-thread update, component by component on lanes 0..2.
+__device__ __forceinline__ void warp_model_update(double* st, const double* x, float* sf) {
+  const int lane = threadIdx.x & 31;
+  const int i = lane < 3 ? lane : 0;
+  const double b1 = st[8 + i], b2 = st[11 + i];
+  const double c2 = (st[i] + x[0] * b1) + x[1] * b2;
+  double d2 = (st[3 + i] + x[2] * b1) + x[3] * b2;
+  const double dx = __shfl_sync(0xffffffffu, d2, 0), dy = __shfl_sync(0xffffffffu, d2, 1),
+               dz = __shfl_sync(0xffffffffu, d2, 2);
+  d2 = (1.0 / norm3(mk3(dx, dy, dz))) * d2;
+  const double r = st[6] + x[4];
+  __syncwarp();
+  if (lane < 3) {
+    st[i] = c2;
+    st[3 + i] = d2;
+  }
+  if (lane == 0) st[6] = r;
+  __syncwarp();
+  warp_ls_frame(st, sf);
+}
 }  // namespace sg

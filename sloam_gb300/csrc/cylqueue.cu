@@ -63,6 +63,19 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
   __shared__ int sm[33];
   const int nl = d.cnt->n_lm;
   QueueCtl* q = d.qctl;
+  if (only && d.cnt->n_fallback == 0) {  // the learned pass kept every tree
+    if (threadIdx.x == 0) {
+      d.q_off[0] = 0;
+      d.q_soff[0] = 0;
+      q->tc = 0;
+      q->ts = 0;
+      q->nq = 0;
+      q->nsplit = 0;
+      q->phases = 1 + kp.ls_iters;
+      q->head = 0;
+    }
+    return;
+  }
   if (nl > kQSortCap) {
     if (threadIdx.x == 0) {
       atomicOr(&d.cnt->overflow, 64);
@@ -334,29 +347,18 @@ __device__ void init_model(Dev& d, const KParams& kp, QueueBlock& B, int l, int 
 }
 
 // The 5x5 normal equations in B.ssum solved on warp 0, the model updated
-// (lane 0); st[7] = 0 when the solve fails.  Called by all of warp 0.
+// on the same warp (three components at a time); st[7] = 0 when the solve
+// fails.  Called by all of warp 0.
 __device__ __noinline__ void solve_update(QueueBlock& B) {
   const int lane = threadIdx.x & 31;
   const bool solved = warp_chol_solve<5>(B.ssum, B.ssum + 15, B.sxls);
   __syncwarp();
-  if (lane == 0) {
-    double* st = B.st;
-    if (solved) {
-      const double* x = B.sxls;
-      const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
-      const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
-      d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
-      d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
-      d2 = scl3(1.0 / norm3(d2), d2);
-      st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
-      st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
-      st[6] = st[6] + x[4];
-      ls_frame(st, B.sf);
-    } else {
-      st[7] = 0.0;
-    }
+  if (solved) {
+    warp_model_update(B.st, B.sxls, B.sf);
+  } else {
+    if (lane == 0) B.st[7] = 0.0;
+    __syncwarp();
   }
-  __syncwarp();
 }
 
 __device__ __forceinline__ unsigned long long block_max_key(QueueBlock& B, unsigned long long v) {

@@ -1145,13 +1145,16 @@ __global__ void __launch_bounds__(256) k_cyl_uv(Dev d) {
 
 // Hypothesis table: one thread per (tree, hypothesis); clears the counts.
 // An invalid hypothesis gets hi2 = -1 (no point can be an inlier).  With a
-// mask (`only`), trees whose entry is 0 get no hypotheses.
+// mask (`only`), only the masked trees' rows are written (the queue reads no
+// other), and nothing at all when the learned pass kept every tree.
 __global__ void __launch_bounds__(256) k_cyl_hypgen(Dev d, KParams kp,
                                                     const int32_t* __restrict__ only) {
   const int nl = d.cnt->n_lm, K = kp.K;
+  if (only && d.cnt->n_fallback == 0) return;  // no tree for the RANSAC pass
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nl * K;
        it += gridDim.x * blockDim.x) {
     const int l = it / K, h = it - l * K;
+    if (only && !only[l]) continue;  // only the queued trees' rows are read
     d.hyp_cnt[it] = 0;
     float4 e = make_float4(0.f, 0.f, 0.f, -1.f);
     const CylD c = d.cyl_all[l];
@@ -1383,26 +1386,14 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_prop_fit(Dev d, KParams kp) {
           ssum[lane] = t2;
         }
         __syncwarp();
-        // the 5x5 normal equations (ssum: upper triangle, then J^T r) on
-        // the warp; the model update on lane 0
+        // the 5x5 normal equations (ssum: upper triangle, then J^T r) and
+        // the model update on the warp
         const bool solved = warp_chol_solve<5>(ssum, ssum + 15, sxls);
         __syncwarp();
-        if (lane == 0) {
-          if (solved) {
-            const double* x = sxls;
-            const d3 cc = mk3(st[0], st[1], st[2]), dd = mk3(st[3], st[4], st[5]);
-            const d3 b1 = mk3(st[8], st[9], st[10]), b2 = mk3(st[11], st[12], st[13]);
-            const double r = st[6];
-            d3 c2 = add3(add3(cc, scl3(x[0], b1)), scl3(x[1], b2));
-            d3 d2 = add3(add3(dd, scl3(x[2], b1)), scl3(x[3], b2));
-            d2 = scl3(1.0 / norm3(d2), d2);
-            st[0] = c2.x; st[1] = c2.y; st[2] = c2.z;
-            st[3] = d2.x; st[4] = d2.y; st[5] = d2.z;
-            st[6] = r + x[4];
-            ls_frame(st, sf);
-          } else {
-            st[7] = 0.0;
-          }
+        if (solved) {
+          warp_model_update(st, sxls, sf);
+        } else if (lane == 0) {
+          st[7] = 0.0;
         }
       }
       __syncthreads();
