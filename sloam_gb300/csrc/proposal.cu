@@ -911,7 +911,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
 }
 
 int g_tc_attr = 0;
-constexpr int kTreeCtas = 48;
+// Persistent CTAs of the per-keyframe launch.  Each needs an empty SM (its
+// shared memory and registers fill one), so in a batch every CTA waits for
+// an SM to drain: 24 CTAs, two trees each for a 64x2048 scene's ~40 trees,
+// ran the 32-slot batch 1 % faster than 48 (which left CTAs without a tree).
+constexpr int kTreeCtas = 24;
 
 }  // namespace
 
@@ -936,8 +940,8 @@ int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const 
                             int* d_err, cudaStream_t st) {
   init_attributes();
   // persistent CTAs over the trees: at most kTreeCtas, each of which needs
-  // a whole SM's shared memory, so that the many CTAs of a large capacity
-  // do not each wait for an empty SM only to exit
+  // a whole SM, so that the many CTAs of a large capacity do not each wait
+  // for an empty SM only to exit
   const int groups = (cap + per_tree - 1) / per_tree;
   const int lim = sm_count() < kTreeCtas ? sm_count() : kTreeCtas;
   const int grid = groups < lim ? (groups > 0 ? groups : 1) : lim;
