@@ -224,6 +224,28 @@ extern "C" int sloam_internal_tables(const sloam_params* p, float* px_tab, float
 constexpr int kFrontChunkHost = 8, kFrontChunkDevice = 64;
 constexpr int kFrontChunkMax = kFrontChunkDevice;
 
+// A slot's second stream and the two events of the fork and join inside
+// its keyframe graph.
+struct Fork {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+bool create_fork(Fork& f) {
+  if (!f.aux && cudaStreamCreateWithFlags(&f.aux, cudaStreamNonBlocking) != cudaSuccess) return false;
+  if (!f.fork && cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming) != cudaSuccess) return false;
+  if (!f.join && cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming) != cudaSuccess) return false;
+  return true;
+}
+void destroy_fork(Fork& f) {
+  if (f.aux) {
+    cudaStreamSynchronize(f.aux);
+    cudaStreamDestroy(f.aux);
+  }
+  if (f.fork) cudaEventDestroy(f.fork);
+  if (f.join) cudaEventDestroy(f.join);
+  f = Fork{};
+}
+
 // Captured keyframe graphs of one slot, keyed
 // [first scan][point labels][state update][projection done by a batch launch].
 struct GraphSet {
@@ -259,9 +281,11 @@ struct sloam_ctx {
     cudaStream_t st = nullptr;
     GraphSet gx;
     cudaEvent_t ev = nullptr;
+    Fork fk;
   };
   std::vector<Slot> extra;
   cudaEvent_t ev_main = nullptr;
+  Fork fk;  // the context's own keyframe graph
   // batch projection: a1-a2 of a whole batch on its own stream, one launch
   // per kernel and chunk of keyframes, into per-keyframe buffers
   // fe_st: uploads and the projection kernel of each chunk; fe_st2: the
@@ -520,12 +544,15 @@ int setup(sloam_ctx* ctx, const sloam_params& P) {
     if (s.arena) cudaFree(s.arena);
     if (s.ev) cudaEventDestroy(s.ev);
     if (s.st) cudaStreamDestroy(s.st);
+    destroy_fork(s.fk);
     ctx->extra.pop_back();
   }
   ctx->extra.resize(ns);
+  if (!create_fork(ctx->fk)) return fail(ctx, SLOAM_ERR_CUDA, "aux stream of the context");
   for (auto& s : ctx->extra) {
     if (!s.st) CK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
     if (!s.ev) CK(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
+    if (!create_fork(s.fk)) return fail(ctx, SLOAM_ERR_CUDA, "aux stream of a slot");
     destroy_graphs(s.gx);
     if ((st = init_dev(ctx, P, s.d, s.arena, s.arena_bytes, s.st))) return st;
   }
@@ -761,7 +788,9 @@ extern "C" void sloam_destroy(sloam_ctx* ctx) {
     if (s.arena) cudaFree(s.arena);
     if (s.ev) cudaEventDestroy(s.ev);
     if (s.st) cudaStreamDestroy(s.st);
+    destroy_fork(s.fk);
   }
+  destroy_fork(ctx->fk);
   if (ctx->ev_main) cudaEventDestroy(ctx->ev_main);
   if (ctx->prop_tc) cudaFree(ctx->prop_tc);
   free_front(ctx);
@@ -1024,28 +1053,45 @@ extern "C" int sloam_run(sloam_ctx* ctx, const sloam_se3* pose, const float* gro
 
 // ----------------------------------------------------------- keyframe
 namespace {
-int enqueue_keyframe(sloam_ctx* ctx, const Dev& d, cudaStream_t st, bool first,
+// The ground planes need only the ground list, the submap prep only the map
+// input, the Trellis and the cylinder fits only the tree cloud: the planes
+// and the submap prep run on the slot's aux stream beside them (a fork and
+// a join in the captured graph), and the plane gates, the cylinder list and
+// the pose follow once both are done.  -1: a fork call failed.
+int enqueue_keyframe(sloam_ctx* ctx, const Dev& d, cudaStream_t st, const Fork& fk, bool first,
                      bool point_labels, bool update, bool pre) {
   int k = launch_begin(d, -1, -1, -1, -1, -1, st);
   if (!pre) k += launch_project(d, ctx->kp, point_labels, st);
+  if (cudaEventRecord(fk.fork, st) != cudaSuccess ||
+      cudaStreamWaitEvent(fk.aux, fk.fork, 0) != cudaSuccess)
+    return -1;
+  k += launch_planes(d, ctx->kp, fk.aux);
+  if (!first) k += launch_map_prep(d, fk.aux);  // the submap needs the map input only
+  if (cudaEventRecord(fk.join, fk.aux) != cudaSuccess) return -1;
   k += launch_trellis(d, ctx->kp, st);
-  k += launch_models(d, ctx->kp, true, st);
-  k += launch_run(d, ctx->kp, first, update, st);
+  k += launch_cylinder_fits(d, ctx->kp, true, st);
+  if (cudaStreamWaitEvent(st, fk.join, 0) != cudaSuccess) return -1;
+  k += launch_cylinder_close(d, ctx->kp, st);
+  k += launch_run(d, ctx->kp, first, update, st, true);
   return k;
 }
 
 // The whole keyframe (a1-a11, or a3-a11 when a batch launch did the
 // projection) of one slot as one CUDA graph, captured on first use; returns
 // the number of kernels it launches in *nk.
-int run_graph(sloam_ctx* ctx, const Dev& d, cudaStream_t st, GraphSet& gs, bool first,
-              bool point_labels, bool update, bool pre, int* nk) {
+int run_graph(sloam_ctx* ctx, const Dev& d, cudaStream_t st, const Fork& fk, GraphSet& gs,
+              bool first, bool point_labels, bool update, bool pre, int* nk) {
   const int a = first ? 1 : 0, b = point_labels ? 1 : 0, u = update ? 1 : 0, q = pre ? 1 : 0;
   cudaGraphExec_t& gx = gs.g[a][b][u][q];
   if (!gx) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const int k = enqueue_keyframe(ctx, d, st, first, point_labels, update, pre);
+    const int k = enqueue_keyframe(ctx, d, st, fk, first, point_labels, update, pre);
     CK(cudaStreamEndCapture(st, &g));
+    if (k < 0) {
+      cudaGraphDestroy(g);
+      return fail(ctx, SLOAM_ERR_CUDA, "keyframe graph: fork or join of the aux stream");
+    }
     cudaError_t e = cudaGraphInstantiate(&gx, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(ctx, SLOAM_ERR_CUDA, "cudaGraphInstantiate", e);
@@ -1058,7 +1104,8 @@ int run_graph(sloam_ctx* ctx, const Dev& d, cudaStream_t st, GraphSet& gs, bool 
 
 int run_keyframe_graph(sloam_ctx* ctx, bool first, bool point_labels, bool update) {
   int nk = 0;
-  const int s = run_graph(ctx, ctx->d, ctx->st, ctx->gx, first, point_labels, update, false, &nk);
+  const int s =
+      run_graph(ctx, ctx->d, ctx->st, ctx->fk, ctx->gx, first, point_labels, update, false, &nk);
   ctx->last_launches = nk;
   return s;
 }
@@ -1173,11 +1220,12 @@ struct SlotView {
   cudaStream_t st;
   GraphSet* gx;
   cudaEvent_t ev;
+  const Fork* fk;
 };
 SlotView slot(sloam_ctx* ctx, int s) {
-  if (s == 0) return {&ctx->d, ctx->st, &ctx->gx, nullptr};
+  if (s == 0) return {&ctx->d, ctx->st, &ctx->gx, nullptr, &ctx->fk};
   auto& x = ctx->extra[s - 1];
-  return {&x.d, x.st, &x.gx, x.ev};
+  return {&x.d, x.st, &x.gx, x.ev, &x.fk};
 }
 
 int grow_batch(sloam_ctx* ctx, int nkf) {
@@ -1303,7 +1351,7 @@ int batch_one(sloam_ctx* ctx, int k, double* pose_out, int32_t* success_out, int
   CK(cudaMemcpyAsync(v.d->pose_io, ctx->h_poses + 8 * k, sizeof(double) * 7,
                      cudaMemcpyHostToDevice, v.st));
   int nk = 0;
-  int st = run_graph(ctx, *v.d, v.st, *v.gx, false, true, false, true, &nk);
+  int st = run_graph(ctx, *v.d, v.st, *v.fk, *v.gx, false, true, false, true, &nk);
   if (st) return st;
   k_batch_out<<<1, 32, 0, v.st>>>(v.d->cnt, v.d->pose_io, pose_out, success_out, ncyl_out, k);
   *launches += nk + 1;

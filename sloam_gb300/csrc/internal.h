@@ -313,7 +313,9 @@ int front_blocks(int N);
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st);
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
 int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_state,
-               cudaStream_t st);
+               cudaStream_t st, bool map_prepped = false);
+// k_map_prep alone (a keyframe graph runs it beside the models)
+int launch_map_prep(const Dev& d, cudaStream_t st);
 // point-level cylinder fit of the trees `only` marks (all eligible: NULL) by
 // the persistent work queue; cylqueue.cu
 int launch_cyl_queue(const Dev& d, const KParams& kp, const int32_t* only, cudaStream_t st);
@@ -325,6 +327,12 @@ int launch_fit_cylinder_points(const Dev& d, const KParams& kp, bool from_trelli
                                cudaStream_t st);
 // a6 alone: cylinders of the landmarks against the planes already in d.planes
 int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
+// The two halves of the model stage a keyframe graph runs side by side: the
+// ground planes (needs the ground list) and the cylinder fits (needs the
+// landmarks), then the plane gates and the cylinder list (needs both).
+int launch_planes(const Dev& d, const KParams& kp, cudaStream_t st);
+int launch_cylinder_fits(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
+int launch_cylinder_close(const Dev& d, const KParams& kp, cudaStream_t st);
 // Plane(points) of the n points of the ground view into plane_all[0]
 int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st);
 

@@ -903,8 +903,12 @@ __device__ __forceinline__ int line_count(const float* vx, int V, float ax, floa
   return cnt;
 }
 
-// One warp per landmark: nearest plane, vertex-line RANSAC model, radius,
-// features.  Writes cyl_all[l] with stage 1 when a model exists.
+// One warp per landmark: vertex-line RANSAC model, radius, features.
+// Writes cyl_all[l] with stage 1 when a model exists.  The plane gates of
+// the same reference code (a model needs a ground plane, and the nearest
+// plane's centroid within max_lidar_dist) are applied by k_cyl_gate once
+// the planes exist: nothing here reads a plane, so the ground planes are
+// fitted beside the Trellis and this fit.
 constexpr int kCylWarps = 4;
 constexpr int kMaxLineHyp = 256;
 
@@ -913,7 +917,7 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int nl = d.cnt->n_lm, np = d.cnt->n_planes;
+  const int nl = d.cnt->n_lm;
   for (int l = wg; l < nl; l += nw) {
     CylD c{};
     c.landmark = l;
@@ -937,28 +941,7 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
         d.cyl_feat_all[(size_t)l * kp.F + f] = q;
       }
     }
-    if (V < 3 || np == 0) {
-      if (lane == 0) d.cyl_all[l] = c;
-      continue;
-    }
-    // ---- nearest plane to vertex[1] (sloam.cpp:420-431)
-    const d3 v1 = mk3(vx[3], vx[4], vx[5]);
-    double bd = 100000.0;
-    int bi = 0;
-    for (int k = lane; k < np; k += 32) {
-      const PlaneD& P = d.planes[k];
-      const double dist = fabs(P.plane[0] * v1.x + P.plane[1] * v1.y + P.plane[2] * v1.z + P.plane[3]) /
-                          norm3(mk3(P.plane[0], P.plane[1], P.plane[2]));
-      if (dist < bd) { bd = dist; bi = k; }
-    }
-    warp_argmin(bd, bi);
-    if (!(bd < 100000.0)) bi = 0;
-    c.plane = bi;
-    const PlaneD P = d.planes[bi];
-    // ---- within maxLidarDist (cylinder.cpp:11-13)
-    const float cxf = (float)P.centroid[0], cyf = (float)P.centroid[1];
-    const bool within = (double)euclid2d_f(vx[3], vx[4], cxf, cyf) < kp.max_lidar_dist;
-    if (!within) {
+    if (V < 3) {
       if (lane == 0) d.cyl_all[l] = c;
       continue;
     }
@@ -1122,6 +1105,61 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
     c.radius = radius;
     c.stage = 1;
     if (lane == 0) d.cyl_all[l] = c;
+  }
+}
+
+// The plane gates of the cylinder model (sloam.cpp:420-431 nearest plane to
+// vertex[1]; cylinder.cpp:11-13 within maxLidarDist of its centroid), one
+// warp per landmark, after the planes and the cylinder fits: a landmark
+// without a plane, or too far from its plane, gets the record the model
+// code gives it at that point (no model, radius -1, the plane index);
+// otherwise the record keeps its fit and gets the plane.
+__device__ __forceinline__ CylD no_model(int l, int id, int plane) {
+  CylD c{};
+  c.landmark = l;
+  c.plane = plane;
+  c.stage = 0;
+  c.valid = 0;
+  c.radius = -1;
+  c.id = id;
+  return c;
+}
+__global__ void __launch_bounds__(kCylWarps * 32) k_cyl_gate(Dev d, KParams kp) {
+  const int lane = threadIdx.x & 31;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int nl = d.cnt->n_lm, np = d.cnt->n_planes;
+  for (int l = wg; l < nl; l += nw) {
+    const int vb = d.lm_vbeg[l], V = d.lm_vbeg[l + 1] - vb;
+    if (V < 3) continue;  // no model and no plane either way
+    CylD c = d.cyl_all[l];
+    if (np == 0) {
+      if (lane == 0) d.cyl_all[l] = no_model(l, c.id, -1);
+      continue;
+    }
+    const float* vx = d.lm_vxyz + 3 * (size_t)vb;
+    const d3 v1 = mk3(vx[3], vx[4], vx[5]);
+    double bd = 100000.0;
+    int bi = 0;
+    for (int k = lane; k < np; k += 32) {
+      const PlaneD& P = d.planes[k];
+      const double dist = fabs(P.plane[0] * v1.x + P.plane[1] * v1.y + P.plane[2] * v1.z + P.plane[3]) /
+                          norm3(mk3(P.plane[0], P.plane[1], P.plane[2]));
+      if (dist < bd) { bd = dist; bi = k; }
+    }
+    warp_argmin(bd, bi);
+    if (!(bd < 100000.0)) bi = 0;
+    const PlaneD P = d.planes[bi];
+    const float cxf = (float)P.centroid[0], cyf = (float)P.centroid[1];
+    const bool within = (double)euclid2d_f(vx[3], vx[4], cxf, cyf) < kp.max_lidar_dist;
+    if (lane == 0) {
+      if (within) {
+        c.plane = bi;
+        d.cyl_all[l] = c;
+      } else {
+        d.cyl_all[l] = no_model(l, c.id, bi);
+      }
+    }
   }
 }
 
@@ -1556,17 +1594,31 @@ int launch_plane_points(const Dev& d, const KParams& kp, int n, cudaStream_t st)
   return 1;
 }
 
-int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
+// The cylinder models before the plane gates: the vertex-line fit and, in
+// modes 1 and 2, the point-level fit.  Needs the landmarks only.
+int launch_cylinder_fits(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
   int n = 1;
   k_cyl_fit<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
   if (kp.cyl_mode >= 1) n += launch_fit_cylinder_points(d, kp, from_trellis, st);
+  return n;
+}
+// The plane gates, the ground-based roots and the valid-cylinder list:
+// needs the fits and the planes.
+int launch_cylinder_close(const Dev& d, const KParams& kp, cudaStream_t st) {
+  k_cyl_gate<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
   k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
   k_cyl_compact<<<1, 1024, 0, st>>>(d, kp);
-  return n + 2;
+  return 3;
 }
 
-int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
-  int n = 0;
+int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
+  const int n = launch_cylinder_fits(d, kp, from_trellis, st);
+  return n + launch_cylinder_close(d, kp, st);
+}
+
+// The ground planes (a7): ground bins, plane fits and gates.  Needs the
+// ground list only.
+int launch_planes(const Dev& d, const KParams& kp, cudaStream_t st) {
   k_zero_bins<<<1, 256, 0, st>>>(d);
   const int gg = (d.cap_ground + kGbinSpan - 1) / kGbinSpan;
   k_gbin<<<gg < 1 ? 1 : gg, 256, 0, st>>>(d, kp);
@@ -1574,7 +1626,11 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
   k_gbin_scatter<<<gg < 1 ? 1 : gg, 256, 0, st>>>(d);
   k_plane<<<d.n_bins, kPlaneThreads, 0, st>>>(d, kp);
   k_plane_compact<<<1, 1024, 0, st>>>(d, kp);
-  n += 6;
+  return 6;
+}
+
+int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {
+  const int n = launch_planes(d, kp, st);
   return n + launch_cylinders(d, kp, from_trellis, st);
 }
 

@@ -938,19 +938,30 @@ int launch_pose_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
   return 1;
 }
 
-int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update, cudaStream_t st) {
+// The submap's per-cylinder prep (needs the map input only).
+int launch_map_prep(const Dev& d, cudaStream_t st) {
+  k_map_prep<<<16, 256, 0, st>>>(d);
+  return 1;
+}
+
+int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update, cudaStream_t st,
+               bool map_prepped) {
   if (first_scan) {
     k_finalize<<<64, kAssocThreads, 0, st>>>(d, kp, 1, update ? 1 : 0);
     return 1;
   }
-  k_map_prep<<<16, 256, 0, st>>>(d);
+  int n = 3;
+  if (!map_prepped) {
+    k_map_prep<<<16, 256, 0, st>>>(d);
+    ++n;
+  }
   k_assoc<<<96, kAssocThreads, 0, st>>>(d, kp);
   if (kp.pose_lm)
     k_gn<true><<<1, kGN, 0, st>>>(d, kp);
   else
     k_gn<false><<<1, kGN, 0, st>>>(d, kp);
   k_finalize<<<64, kAssocThreads, 0, st>>>(d, kp, 0, update ? 1 : 0);
-  return 4;
+  return n;
 }
 
 }  // namespace sg
