@@ -55,9 +55,9 @@ WORKLOAD = ("C2: 64x2048 keyframes, 150 trees, 400-landmark submap, 10 GN iterat
             "inlier ratio) + 3 LS; plain: 256 RANSAC hypotheses per tree + 3 LS")
 # DRAM bytes (read + write) per keyframe of the batch projection stage, summed
 # over its three kernels in one ncu capture with the caches left as they are
-# (dram__bytes_read.sum + dram__bytes_write.sum of two 16-keyframe chunk
-# launches: 4.15 and 6.43 MB per keyframe).
-FRONT_TRAFFIC_PER_KF = 5.29e6
+# (dram__bytes_read.sum + dram__bytes_write.sum of one 64-keyframe launch
+# group: 478 MB).
+FRONT_TRAFFIC_PER_KF = 7.47e6
 
 
 def max_over_ranks(x, device=None):

@@ -420,10 +420,12 @@ int sloam_prop_infer(const float* weights, const float* d_points, int32_t n, flo
  * is a cudaStream_t (NULL = legacy default stream); results are ready when
  * the stream reaches them.  The first call in each CUDA context (a device's
  * primary context, or one the caller made current) looks up the array's
- * address in that context (make it before any stream capture).  All calls
- * of a context share the one
- * array: calls that overlap on the GPU (other streams, other threads) race.
- * Host code must treat the array only through this entry point. */
+ * address in that context.  Every call copies its boundary tables and input
+ * pointers from host memory, so the call cannot be captured into a CUDA
+ * graph (issue it on a stream that is not capturing).  All calls of a
+ * context share the one array: calls that overlap on the GPU (other
+ * streams, other threads) race.  Host code must treat the array only
+ * through this entry point. */
 int sloam_project_mask_noalloc(const sloam_params* params, const float* d_xyzi, int32_t n,
                                const uint8_t* d_point_labels, const uint8_t* d_mask_image,
                                int32_t* d_pix, float* d_range_image, uint8_t* d_mask_out,

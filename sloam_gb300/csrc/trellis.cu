@@ -352,8 +352,11 @@ __device__ __forceinline__ uint32_t fkey(float v) {
 // rounds), then the k'-th element, in index order, among those with the
 // selected key -- the element the rank count (b < a, or b == a and k < j)
 // puts at position k.
-constexpr int kVtxSlots = 4;          // the sort path takes buckets of <= 128 points
-constexpr int kVtxSortMax = 32 * kVtxSlots;
+// kSlots = 4 for buckets of at most 128 points, 8 for at most 256 (the
+// wider form costs registers and instructions on every call, so the common
+// narrow buckets keep the narrow one).
+constexpr int kVtxSortMax = 256;
+template <int kVtxSlots>
 __device__ __forceinline__ float warp_select(const float4* P, int axis, int n, int k, int lane) {
   const int ns = (n + 31) >> 5;
   uint32_t key[kVtxSlots];
@@ -491,9 +494,16 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
       // medians by quickselect; kept points in (z, y, x, column) order
       // by a bitonic sort -- the same elements and order as the rank counts
       // below, in O(n log^2 n) instead of O(n^2)
-      const float mx = warp_select(P, 0, n, mid, lane);
-      const float my = warp_select(P, 1, n, mid, lane);
-      const float mz = warp_select(P, 2, n, mid, lane);
+      float mx, my, mz;
+      if (n <= 128) {
+        mx = warp_select<4>(P, 0, n, mid, lane);
+        my = warp_select<4>(P, 1, n, mid, lane);
+        mz = warp_select<4>(P, 2, n, mid, lane);
+      } else {
+        mx = warp_select<8>(P, 0, n, mid, lane);
+        my = warp_select<8>(P, 1, n, mid, lane);
+        mz = warp_select<8>(P, 2, n, mid, lane);
+      }
       int m = 32;
       while (m < n) m <<= 1;
       int* idx = srank[w];
@@ -748,28 +758,34 @@ __global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
 }
 
 // Point copies of the landmarks, spread over the whole grid: one warp per
-// vertex for the kept points, one warp per (candidate, row) bucket for the
-// cluster points (raster order; the bucket's candidate is its index / H, so
-// no search).
+// vertex for the kept points, one thread per bucket slot for the cluster
+// points (raster order; the candidate of a slot found by binary search).
+// One warp per (candidate, row) bucket instead, which needs no search, was
+// measured slower (11.6 against 8.7 us per launch): the wide buckets of near
+// trees leave most warps idle while a few walk long rows.
 __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
   const TreeView tree = tree_view(d.in, d.W);
   const int H = d.H;
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
   const int nv = d.cnt->n_v;
-  for (int v = gw; v < nv; v += nw) {
+  for (int v = gt >> 5; v < nv; v += nt >> 5) {
     const int src = d.lm_vsrc[v], dst = d.lm_pbeg[v], cnt = d.lm_pbeg[v + 1] - dst;
     for (int q = lane; q < cnt; q += 32) d.lm_pts[dst + q] = d.kept[src + q];
   }
-  const int items = d.cnt->n_cand * H;
-  for (int it = gw; it < items; it += nw) {
-    const int cand = it / H;
-    const int l = d.cand_lm[cand];
-    const int q0 = d.roff[it], q1 = d.roff[it + 1];
-    if (l < 0 || q1 <= q0) continue;
-    const int dst = d.lm_cbeg[l] - d.roff[cand * H];  // slot q -> dst + q
-    for (int q = q0 + lane; q < q1; q += 32) d.lm_cpts[dst + q] = tree[d.bucket[q]];
+  const int nc = d.cnt->n_cand;
+  const int total = d.roff[nc * H];
+  for (int q = gt; q < total; q += nt) {
+    int lo = 0, hi = nc - 1;  // last candidate whose first slot <= q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (d.roff[mid * H] <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    const int l = d.cand_lm[lo];
+    if (l < 0) continue;
+    d.lm_cpts[d.lm_cbeg[l] + (q - d.roff[lo * H])] = tree[d.bucket[q]];
   }
 }
 

@@ -75,7 +75,12 @@ def quat_from_R(R):
 
 
 def R_from_quat(q):
-    x, y, z, w = q / np.linalg.norm(q)
+    """Rotation of a quaternion (x, y, z, w); the identity for the all-zero
+    pose a failed keyframe reports."""
+    nq = np.linalg.norm(q)
+    if not nq > 0:
+        return np.eye(3)
+    x, y, z, w = q / nq
     return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
