@@ -6,8 +6,10 @@
 // The reference fits its trees one after the other (sloam.cpp:418-434, one
 // Cylinder per landmark).  Here the trees are queued largest first and
 // blocks take work items from one atomic counter.  A tree of at most
-// kSplitChunks chunks (chunk = `cyl_chunk_points` points) is one item: one
-// block counts, selects and refines it with no wait.  A larger tree is cut
+// kSplitChunks chunks (chunk = `cyl_chunk_points` points; one chunk in the
+// fallback pass, whose one or two trees would otherwise leave most blocks
+// idle) is one item: one block counts, selects and refines it with no wait.
+// A larger tree is cut
 // into chunks, and every (phase, chunk) of it is an item:
 //   phase 0        count the inliers of all K hypotheses on the chunk
 //                  (ballot + popcount per 32 points, integer atomics);
@@ -125,7 +127,10 @@ __global__ void __launch_bounds__(1024) k_cyl_queue_prep(Dev d, KParams kp,
     const bool valid = i < n2 && key[i] != ~0ull;
     const int n = valid ? (int)(0xFFFFFFFFu - (uint32_t)(key[i] >> 32)) : 0;
     const int nc = valid ? (n + chunk - 1) / chunk : 0;
-    const bool split = nc > kSplitChunks;
+    // the RANSAC pass after the learned proposals has a tree or two on 76
+    // blocks: split every tree of more than one chunk, so that its counting
+    // spreads over blocks (the results are the same either way)
+    const bool split = nc > (only ? 1 : kSplitChunks);
     if (valid) {
       const int l = (int)(uint32_t)key[i];
       d.q_order[i] = l;
