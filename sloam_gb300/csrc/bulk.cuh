@@ -1,5 +1,6 @@
 // bulk.cuh — shared-memory mbarriers and the untiled bulk copy
-// (cp.async.bulk, the TMA unit's 1-D form) used by the streaming kernels.
+// (cp.async.bulk, the TMA unit's 1-D form), used by the tensor-core proposal
+// kernel to stage its weights.
 //
 // A bulk copy moves a contiguous range global -> shared and completes on an
 // mbarrier's transaction count.  Both addresses must be 16-byte aligned and
