@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -149,6 +150,22 @@ void build_px_table(const sloam_params& p, float* tab) {
 // row is <= H-1-k (k = 1..H-1; +inf when no q reaches it): the row of q is
 // H-1 minus the number of k with q >= tab[k].  A q outside [-1, 1] (or NaN)
 // has a NaN pitch, which the reference's clamps send to row H-1.
+void build_line_k_table(const sloam_params& p, double* tab) {
+  const double log_p = std::log(1.0 - p.line_ransac_probability);
+  const double eps = std::numeric_limits<double>::epsilon();
+  for (int V = 0; V <= kLineKMax; ++V)
+    for (int c = 0; c <= kLineKMax; ++c) {
+      double k = 1.0;
+      if (V > 0 && c > 0 && c <= V) {
+        const double w = (double)c / V;
+        double p_no = 1.0 - w * w;
+        p_no = std::max(eps, std::min(1.0 - eps, p_no));
+        k = log_p / std::log(p_no);
+      }
+      tab[V * (kLineKMax + 1) + c] = k;
+    }
+}
+
 void build_py_table(const sloam_params& p, float* tab) {
   const int H = p.img_h;
   const KParams kp = make_kparams(p);
@@ -364,6 +381,7 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.ground_idx = c.take<int32_t>(N);
   d.ground = c.take<float4>(d.cap_ground);
   d.px_tab = c.take<float>(d.W + 1);
+  d.line_k = c.take<double>((size_t)(kLineKMax + 1) * (kLineKMax + 1));
   d.py_tab = c.take<float>(d.H + 1);
   d.tb_tab = c.take<float>(4096);
   d.rb_tab = c.take<float>(4096);
@@ -512,6 +530,9 @@ int init_dev(sloam_ctx* ctx, const sloam_params& P, Dev& d, void*& arena, size_t
   build_px_table(P, tab.data());
   build_py_table(P, ptab.data());
   build_ground_tables(P, tb.data(), rb.data(), &d.r_lo, &d.r_hi);
+  std::vector<double> lk((size_t)(kLineKMax + 1) * (kLineKMax + 1));
+  build_line_k_table(P, lk.data());
+  CK(cudaMemcpyAsync(d.line_k, lk.data(), sizeof(double) * lk.size(), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.px_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.py_tab, ptab.data(), sizeof(float) * ptab.size(), cudaMemcpyHostToDevice,
                      st));

@@ -156,6 +156,13 @@ struct FrontRef {
   int32_t* fe;  // {n_ground, overflow, n_slow_px, pad}
 };
 
+// The vertex-line RANSAC's adaptive iteration bound log(1 - p) /
+// log(1 - (c / V)^2) (clamped as PCL clamps it) for every vertex count
+// V <= kLineKMax and inlier count c <= V, computed on the host with the
+// reference's double expression; larger V evaluate it on the device.
+constexpr int kLineKMax = 64;
+void build_line_k_table(const sloam_params& p, double* tab);
+
 struct Dev {
   InPtrs* in;          // device copy of the current inputs
   int H, W, N;
@@ -175,6 +182,7 @@ struct Dev {
   int32_t* ground_idx;
   float4* ground;
   float* px_tab;       // [W+1]
+  double* line_k;      // [(kLineKMax+1)^2] vertex-line RANSAC iteration bound by (V, inliers)
   float* py_tab;       // [H+1]
   float* tb_tab;       // [Tb+1]
   float* rb_tab;       // [Rb+1]

@@ -1008,7 +1008,6 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
     if (lane == 0) {
       double k = 1.0;
       int itn = 0;
-      const double log_p = log(1.0 - kp.line_prob);
       const double eps = DBL_EPSILON;
       for (int h = 0; h < K; ++h) {
         if (!(itn < k)) break;
@@ -1017,10 +1016,14 @@ __global__ void __launch_bounds__(kCylWarps * 32) k_cyl_fit(Dev d, KParams kp) {
         if (cnt > best_count) {
           best_count = cnt;
           best = h;
-          const double wgt = (double)best_count / V;
-          double p_no = 1.0 - wgt * wgt;
-          p_no = fmax(eps, fmin(1.0 - eps, p_no));
-          k = log_p / log(p_no);
+          if (V <= kLineKMax) {  // the host's value of the reference's expression
+            k = d.line_k[V * (kLineKMax + 1) + best_count];
+          } else {
+            const double wgt = (double)best_count / V;
+            double p_no = 1.0 - wgt * wgt;
+            p_no = fmax(eps, fmin(1.0 - eps, p_no));
+            k = log(1.0 - kp.line_prob) / log(p_no);
+          }
         }
         ++itn;
       }

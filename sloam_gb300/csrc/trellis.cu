@@ -641,43 +641,34 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
   }
 }
 
-// Per candidate: vertex count of the landmark (0 = rejected), its kept-point
-// count and its cluster size.  Rows are walked bottom (H-1) to top.
-__global__ void __launch_bounds__(256) k_lm_count(Dev d, KParams kp, int32_t* cand_np,
-                                                  int32_t* cand_ncl) {
-  const int H = d.H;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < d.cnt->n_cand;
-       c += gridDim.x * blockDim.x) {
-    int nv = 0, np = 0, ncl = 0;
-    for (int row = H - 1; row >= 0; --row) {
-      const int it = c * H + row;
-      ncl += d.rc[it];
-      const int k = d.vkept[it];
-      if (k > 0) {
-        if (nv < kp.max_vertices) np += k;
-        ++nv;
-      }
-    }
-    if (nv <= kp.min_vertices) { nv = 0; np = 0; }
-    if (nv > kp.max_vertices) nv = kp.max_vertices;
-    d.cand_nv[c] = nv;
-    cand_np[c] = np;
-    cand_ncl[c] = nv > 0 ? ncl : 0;
-  }
-}
-
-// Landmark numbering and offsets, single block, candidate (= label) order.
-__global__ void __launch_bounds__(1024) k_lm_scan(Dev d, const int32_t* cand_np,
-                                                  const int32_t* cand_ncl, int32_t* cand_vb,
+// Per candidate (thread c): vertex count of the landmark (0 = rejected),
+// its kept-point count and its cluster size, rows walked bottom (H-1) to
+// top; then the landmark numbering and offsets in candidate (= label)
+// order.  Single block: the counts feed the scans with no launch between.
+__global__ void __launch_bounds__(1024) k_lm_scan(Dev d, KParams kp, int32_t* cand_vb,
                                                   int32_t* cand_pb) {
   __shared__ int sm[33];
   const int nc = d.cnt->n_cand;
+  const int H = d.H;
   int bl = 0, bv = 0, bp = 0, bc = 0;
   for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
     const int c = c0 + threadIdx.x;
-    const int nv = c < nc ? d.cand_nv[c] : 0;
-    const int np = c < nc ? cand_np[c] : 0;
-    const int ncl = c < nc ? cand_ncl[c] : 0;
+    int nv = 0, np = 0, ncl = 0;
+    if (c < nc) {
+      for (int row = H - 1; row >= 0; --row) {
+        const int it = c * H + row;
+        ncl += d.rc[it];
+        const int k = d.vkept[it];
+        if (k > 0) {
+          if (nv < kp.max_vertices) np += k;
+          ++nv;
+        }
+      }
+      if (nv <= kp.min_vertices) { nv = 0; np = 0; }
+      if (nv > kp.max_vertices) nv = kp.max_vertices;
+      if (nv == 0) ncl = 0;
+      d.cand_nv[c] = nv;
+    }
     int tl, tv, tp, tc;
     const int el = block_excl_scan(nv > 0 ? 1 : 0, sm, &tl);
     const int ev = block_excl_scan(nv, sm, &tv);
@@ -712,68 +703,74 @@ __global__ void __launch_bounds__(1024) k_lm_scan(Dev d, const int32_t* cand_np,
   }
 }
 
-// One warp per landmark candidate: vertex records, kept points and the
-// cluster points (raster order) into the compact landmark arrays.
-__global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
-                                                  const int32_t* cand_pb) {
-  const int H = d.H;
-  const int lane = threadIdx.x & 31;
-  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int c = wg; c < d.cnt->n_cand; c += nw) {
-    const int l = d.cand_lm[c];
-    if (l < 0) continue;
-    const int nv = d.cand_nv[c];
-    int vbase = cand_vb[c], pbase = cand_pb[c];
-    int vi = 0;
-    for (int r0 = H - 1; r0 >= 0 && vi < nv; r0 -= 32) {
-      const int row = r0 - lane;
-      const int it = c * H + row;
-      const int k = row >= 0 ? d.vkept[it] : 0;
-      const bool v = k > 0;
-      const unsigned b = __ballot_sync(0xffffffffu, v);
-      const int my = vi + __popc(b & ((1u << lane) - 1u));
-      // kept-point prefix inside this chunk
-      int kp = v && my < nv ? k : 0, incl = kp;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      const int pstart = pbase + incl - kp;
-      if (v && my < nv) {
-        const int vv = vbase + my;
-        const float4 m = d.vmed[it];
-        d.lm_vxyz[3 * vv] = m.x;
-        d.lm_vxyz[3 * vv + 1] = m.y;
-        d.lm_vxyz[3 * vv + 2] = m.z;
-        d.lm_vrad[vv] = d.vrad[it];
-        d.lm_vrow[vv] = row;
-        d.lm_pbeg[vv] = pstart;
-        d.lm_vsrc[vv] = d.roff[it];
-      }
-      pbase += __shfl_sync(0xffffffffu, incl, 31);
-      vi += __popc(b);
-    }
-  }
-}
-
-// Point copies of the landmarks, spread over the whole grid: one warp per
-// vertex for the kept points, one thread per bucket slot for the cluster
-// points (raster order; the candidate of a slot found by binary search).
-// One warp per (candidate, row) bucket instead, which needs no search, was
+// The landmark records and point copies in one launch.  Blocks below
+// kLmWriteBlocks: one warp per landmark candidate writes its vertex records
+// and then copies each vertex's kept points (the warp's lanes together, one
+// vertex after the other).  The other blocks copy the cluster points, one
+// thread per bucket slot (raster order; the candidate of a slot found by
+// binary search), which needs only the offsets of k_lm_scan.  One warp per
+// (candidate, row) bucket for the cluster copy, which needs no search, was
 // measured slower (11.6 against 8.7 us per launch): the wide buckets of near
 // trees leave most warps idle while a few walk long rows.
-__global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
-  const TreeView tree = tree_view(d.in, d.W);
+constexpr int kLmWriteBlocks = 32;
+__global__ void __launch_bounds__(256) k_lm_emit(Dev d, const int32_t* cand_vb,
+                                                 const int32_t* cand_pb) {
   const int H = d.H;
   const int lane = threadIdx.x & 31;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
-  const int nv = d.cnt->n_v;
-  for (int v = gt >> 5; v < nv; v += nt >> 5) {
-    const int src = d.lm_vsrc[v], dst = d.lm_pbeg[v], cnt = d.lm_pbeg[v + 1] - dst;
-    for (int q = lane; q < cnt; q += 32) d.lm_pts[dst + q] = d.kept[src + q];
+  if (blockIdx.x < kLmWriteBlocks) {
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (kLmWriteBlocks * blockDim.x) >> 5;
+    for (int c = wg; c < d.cnt->n_cand; c += nw) {
+      const int l = d.cand_lm[c];
+      if (l < 0) continue;
+      const int nv = d.cand_nv[c];
+      int vbase = cand_vb[c], pbase = cand_pb[c];
+      int vi = 0;
+      for (int r0 = H - 1; r0 >= 0 && vi < nv; r0 -= 32) {
+        const int row = r0 - lane;
+        const int it = c * H + row;
+        const int k = row >= 0 ? d.vkept[it] : 0;
+        const bool v = k > 0;
+        const unsigned b = __ballot_sync(0xffffffffu, v);
+        const int my = vi + __popc(b & ((1u << lane) - 1u));
+        // kept-point prefix inside this chunk
+        int kp = v && my < nv ? k : 0, incl = kp;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int pstart = pbase + incl - kp;
+        const int src = v && my < nv ? d.roff[it] : 0;
+        if (v && my < nv) {
+          const int vv = vbase + my;
+          const float4 m = d.vmed[it];
+          d.lm_vxyz[3 * vv] = m.x;
+          d.lm_vxyz[3 * vv + 1] = m.y;
+          d.lm_vxyz[3 * vv + 2] = m.z;
+          d.lm_vrad[vv] = d.vrad[it];
+          d.lm_vrow[vv] = row;
+          d.lm_pbeg[vv] = pstart;
+          d.lm_vsrc[vv] = src;
+        }
+        // this chunk's vertices' kept points, the warp on one vertex at a time
+        unsigned todo = __ballot_sync(0xffffffffu, kp > 0);
+        while (todo) {
+          const int q = __ffs(todo) - 1;
+          todo &= todo - 1u;
+          const int n = __shfl_sync(0xffffffffu, kp, q);
+          const int s0 = __shfl_sync(0xffffffffu, src, q);
+          const int p0 = __shfl_sync(0xffffffffu, pstart, q);
+          for (int t = lane; t < n; t += 32) d.lm_pts[p0 + t] = d.kept[s0 + t];
+        }
+        pbase += __shfl_sync(0xffffffffu, incl, 31);
+        vi += __popc(b);
+      }
+    }
+    return;
   }
+  const TreeView tree = tree_view(d.in, d.W);
+  const int gt = (blockIdx.x - kLmWriteBlocks) * blockDim.x + threadIdx.x;
+  const int nt = (gridDim.x - kLmWriteBlocks) * blockDim.x;
   const int nc = d.cnt->n_cand;
   const int total = d.roff[nc * H];
   for (int q = gt; q < total; q += nt) {
@@ -819,15 +816,11 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   // 1.5 % more keyframes/s in the batch than 2 * 152 blocks)
   k_vertex<<<4 * gw, kVtxWarps * 32, 0, st>>>(d, kp);
   // scratch for the landmark offsets lives in the (now unused) rank array
-  int32_t* cand_np = reinterpret_cast<int32_t*>(d.rank);
-  int32_t* cand_ncl = cand_np + d.cap_cand;
-  int32_t* cand_vb = cand_ncl + d.cap_cand;
+  int32_t* cand_vb = reinterpret_cast<int32_t*>(d.rank);
   int32_t* cand_pb = cand_vb + d.cap_cand;
-  k_lm_count<<<(d.cap_cand + 255) / 256, 256, 0, st>>>(d, kp, cand_np, cand_ncl);
-  k_lm_scan<<<1, 1024, 0, st>>>(d, cand_np, cand_ncl, cand_vb, cand_pb);
-  k_lm_write<<<32, 256, 0, st>>>(d, cand_vb, cand_pb);
-  k_lm_copy<<<gw, 256, 0, st>>>(d);
-  return 14;
+  k_lm_scan<<<1, 1024, 0, st>>>(d, kp, cand_vb, cand_pb);
+  k_lm_emit<<<kLmWriteBlocks + gw, 256, 0, st>>>(d, cand_vb, cand_pb);
+  return 12;
 }
 
 }  // namespace sg
