@@ -1127,41 +1127,37 @@ __device__ __forceinline__ CylD no_model(int l, int id, int plane) {
   c.id = id;
   return c;
 }
-__global__ void __launch_bounds__(kCylWarps * 32) k_cyl_gate(Dev d, KParams kp) {
-  const int lane = threadIdx.x & 31;
-  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int nl = d.cnt->n_lm, np = d.cnt->n_planes;
-  for (int l = wg; l < nl; l += nw) {
-    const int vb = d.lm_vbeg[l], V = d.lm_vbeg[l + 1] - vb;
-    if (V < 3) continue;  // no model and no plane either way
-    CylD c = d.cyl_all[l];
-    if (np == 0) {
-      if (lane == 0) d.cyl_all[l] = no_model(l, c.id, -1);
-      continue;
-    }
-    const float* vx = d.lm_vxyz + 3 * (size_t)vb;
-    const d3 v1 = mk3(vx[3], vx[4], vx[5]);
-    double bd = 100000.0;
-    int bi = 0;
-    for (int k = lane; k < np; k += 32) {
-      const PlaneD& P = d.planes[k];
-      const double dist = fabs(P.plane[0] * v1.x + P.plane[1] * v1.y + P.plane[2] * v1.z + P.plane[3]) /
-                          norm3(mk3(P.plane[0], P.plane[1], P.plane[2]));
-      if (dist < bd) { bd = dist; bi = k; }
-    }
-    warp_argmin(bd, bi);
-    if (!(bd < 100000.0)) bi = 0;
-    const PlaneD P = d.planes[bi];
-    const float cxf = (float)P.centroid[0], cyf = (float)P.centroid[1];
-    const bool within = (double)euclid2d_f(vx[3], vx[4], cxf, cyf) < kp.max_lidar_dist;
-    if (lane == 0) {
-      if (within) {
-        c.plane = bi;
-        d.cyl_all[l] = c;
-      } else {
-        d.cyl_all[l] = no_model(l, c.id, bi);
-      }
+// One landmark's gates, by a whole warp (the nearest plane by a warp argmin).
+__device__ __forceinline__ void cyl_gate_one(const Dev& d, const KParams& kp, int l, int np,
+                                             int lane) {
+  const int vb = d.lm_vbeg[l], V = d.lm_vbeg[l + 1] - vb;
+  if (V < 3) return;  // no model and no plane either way
+  CylD c = d.cyl_all[l];
+  if (np == 0) {
+    if (lane == 0) d.cyl_all[l] = no_model(l, c.id, -1);
+    return;
+  }
+  const float* vx = d.lm_vxyz + 3 * (size_t)vb;
+  const d3 v1 = mk3(vx[3], vx[4], vx[5]);
+  double bd = 100000.0;
+  int bi = 0;
+  for (int k = lane; k < np; k += 32) {
+    const PlaneD& P = d.planes[k];
+    const double dist = fabs(P.plane[0] * v1.x + P.plane[1] * v1.y + P.plane[2] * v1.z + P.plane[3]) /
+                        norm3(mk3(P.plane[0], P.plane[1], P.plane[2]));
+    if (dist < bd) { bd = dist; bi = k; }
+  }
+  warp_argmin(bd, bi);
+  if (!(bd < 100000.0)) bi = 0;
+  const PlaneD P = d.planes[bi];
+  const float cxf = (float)P.centroid[0], cyf = (float)P.centroid[1];
+  const bool within = (double)euclid2d_f(vx[3], vx[4], cxf, cyf) < kp.max_lidar_dist;
+  if (lane == 0) {
+    if (within) {
+      c.plane = bi;
+      d.cyl_all[l] = c;
+    } else {
+      d.cyl_all[l] = no_model(l, c.id, bi);
     }
   }
 }
@@ -1485,47 +1481,61 @@ __global__ void __launch_bounds__(kLsThreads, 4) k_prop_fit(Dev d, KParams kp) {
   }
 }
 
+// One landmark's ground-based root and validity, by one thread:
 // groundBasedRoot (cylinder.cpp:41-55), validNorm, filter (cylinder.cpp:57-73).
-__global__ void __launch_bounds__(256) k_cyl_finalize(Dev d, KParams kp) {
-  const int nl = d.cnt->n_lm;
-  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
-    CylD c = d.cyl_all[l];
-    if (c.stage == 0) {
-      c.valid = 0;
-      d.cyl_all[l] = c;
-      continue;
-    }
-    const PlaneD P = d.planes[c.plane];
-    const d3 n = mk3(P.plane[0], P.plane[1], P.plane[2]);
-    d3 root = mk3(c.root[0], c.root[1], c.root[2]);
-    const d3 ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
-    const float dist = (float)(fabs(P.plane[0] * root.x + P.plane[1] * root.y +
-                                    P.plane[2] * root.z + P.plane[3]) / norm3(n));
-    bool validZ = false;
-    if (dist < kp.root_plane_max_dist) {
-      // rayPlaneIntersection, utils.h:41-51
-      const float denom = (float)dot3(n, ray);
-      if (fabsf(denom) > 0.001f) {
-        const float t = (float)(dot3(sub3(mk3(P.centroid[0], P.centroid[1], P.centroid[2]), root), n) /
-                                (double)denom);
-        if (t >= 0.001f) root = add3(root, scl3((double)t, ray));
-      }
-      validZ = true;
-    }
-    c.root[0] = root.x; c.root[1] = root.y; c.root[2] = root.z;
-    const bool validNorm = norm3(root) > 0.01;
-    const bool validRadius = c.radius > 0.0;
-    bool validTree = false;
-    if (c.radius != -1.0) {
-      const double theta = (180.0 / kPIDEF) * acos(dot3(ray, n) / (norm3(ray) * norm3(n)));
-      validTree = (c.radius < kp.max_tree_radius) &&
-                  ((theta <= kp.max_axis_theta) || (theta >= 180.0 - kp.max_axis_theta));
-    }
-    c.valid = validZ && validRadius && validTree && validNorm;
+__device__ __forceinline__ void cyl_finalize_one(const Dev& d, const KParams& kp, int l) {
+  CylD c = d.cyl_all[l];
+  if (c.stage == 0) {
+    c.valid = 0;
     d.cyl_all[l] = c;
+    return;
+  }
+  const PlaneD P = d.planes[c.plane];
+  const d3 n = mk3(P.plane[0], P.plane[1], P.plane[2]);
+  d3 root = mk3(c.root[0], c.root[1], c.root[2]);
+  const d3 ray = mk3(c.ray[0], c.ray[1], c.ray[2]);
+  const float dist = (float)(fabs(P.plane[0] * root.x + P.plane[1] * root.y +
+                                  P.plane[2] * root.z + P.plane[3]) / norm3(n));
+  bool validZ = false;
+  if (dist < kp.root_plane_max_dist) {
+    // rayPlaneIntersection, utils.h:41-51
+    const float denom = (float)dot3(n, ray);
+    if (fabsf(denom) > 0.001f) {
+      const float t = (float)(dot3(sub3(mk3(P.centroid[0], P.centroid[1], P.centroid[2]), root), n) /
+                              (double)denom);
+      if (t >= 0.001f) root = add3(root, scl3((double)t, ray));
+    }
+    validZ = true;
+  }
+  c.root[0] = root.x; c.root[1] = root.y; c.root[2] = root.z;
+  const bool validNorm = norm3(root) > 0.01;
+  const bool validRadius = c.radius > 0.0;
+  bool validTree = false;
+  if (c.radius != -1.0) {
+    const double theta = (180.0 / kPIDEF) * acos(dot3(ray, n) / (norm3(ray) * norm3(n)));
+    validTree = (c.radius < kp.max_tree_radius) &&
+                ((theta <= kp.max_axis_theta) || (theta >= 180.0 - kp.max_axis_theta));
+  }
+  c.valid = validZ && validRadius && validTree && validNorm;
+  d.cyl_all[l] = c;
+}
+
+// The plane gates and then the ground-based root and validity of each
+// landmark, one warp per landmark over the grid (the FP64 of both spread
+// over the SMs: one block of 1024 threads doing all of it, fused with the
+// compaction below, ran the cylinder stage 7 us longer).
+__global__ void __launch_bounds__(kCylWarps * 32) k_cyl_gate(Dev d, KParams kp) {
+  const int lane = threadIdx.x & 31;
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int nl = d.cnt->n_lm, np = d.cnt->n_planes;
+  for (int l = wg; l < nl; l += nw) {
+    cyl_gate_one(d, kp, l, np, lane);
+    if (lane == 0) cyl_finalize_one(d, kp, l);  // reads the record lane 0 wrote
   }
 }
 
+// The ordered list of the valid cylinders, one block.
 __global__ void __launch_bounds__(1024) k_cyl_compact(Dev d, KParams kp) {
   __shared__ int sm[33];
   const int nl = d.cnt->n_lm;
@@ -1609,9 +1619,8 @@ int launch_cylinder_fits(const Dev& d, const KParams& kp, bool from_trellis, cud
 // needs the fits and the planes.
 int launch_cylinder_close(const Dev& d, const KParams& kp, cudaStream_t st) {
   k_cyl_gate<<<kCylBlocks, kCylWarps * 32, 0, st>>>(d, kp);
-  k_cyl_finalize<<<(d.cap_lm + 255) / 256, 256, 0, st>>>(d, kp);
   k_cyl_compact<<<1, 1024, 0, st>>>(d, kp);
-  return 3;
+  return 2;
 }
 
 int launch_cylinders(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st) {

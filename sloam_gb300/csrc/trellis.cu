@@ -703,74 +703,68 @@ __global__ void __launch_bounds__(1024) k_lm_scan(Dev d, KParams kp, int32_t* ca
   }
 }
 
-// The landmark records and point copies in one launch.  Blocks below
-// kLmWriteBlocks: one warp per landmark candidate writes its vertex records
-// and then copies each vertex's kept points (the warp's lanes together, one
-// vertex after the other).  The other blocks copy the cluster points, one
-// thread per bucket slot (raster order; the candidate of a slot found by
-// binary search), which needs only the offsets of k_lm_scan.  One warp per
-// (candidate, row) bucket for the cluster copy, which needs no search, was
-// measured slower (11.6 against 8.7 us per launch): the wide buckets of near
-// trees leave most warps idle while a few walk long rows.
-constexpr int kLmWriteBlocks = 32;
-__global__ void __launch_bounds__(256) k_lm_emit(Dev d, const int32_t* cand_vb,
-                                                 const int32_t* cand_pb) {
+// One warp per landmark candidate: vertex records, kept points and the
+// cluster points (raster order) into the compact landmark arrays.
+__global__ void __launch_bounds__(256) k_lm_write(Dev d, const int32_t* cand_vb,
+                                                  const int32_t* cand_pb) {
   const int H = d.H;
   const int lane = threadIdx.x & 31;
-  if (blockIdx.x < kLmWriteBlocks) {
-    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (kLmWriteBlocks * blockDim.x) >> 5;
-    for (int c = wg; c < d.cnt->n_cand; c += nw) {
-      const int l = d.cand_lm[c];
-      if (l < 0) continue;
-      const int nv = d.cand_nv[c];
-      int vbase = cand_vb[c], pbase = cand_pb[c];
-      int vi = 0;
-      for (int r0 = H - 1; r0 >= 0 && vi < nv; r0 -= 32) {
-        const int row = r0 - lane;
-        const int it = c * H + row;
-        const int k = row >= 0 ? d.vkept[it] : 0;
-        const bool v = k > 0;
-        const unsigned b = __ballot_sync(0xffffffffu, v);
-        const int my = vi + __popc(b & ((1u << lane) - 1u));
-        // kept-point prefix inside this chunk
-        int kp = v && my < nv ? k : 0, incl = kp;
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        const int pstart = pbase + incl - kp;
-        const int src = v && my < nv ? d.roff[it] : 0;
-        if (v && my < nv) {
-          const int vv = vbase + my;
-          const float4 m = d.vmed[it];
-          d.lm_vxyz[3 * vv] = m.x;
-          d.lm_vxyz[3 * vv + 1] = m.y;
-          d.lm_vxyz[3 * vv + 2] = m.z;
-          d.lm_vrad[vv] = d.vrad[it];
-          d.lm_vrow[vv] = row;
-          d.lm_pbeg[vv] = pstart;
-          d.lm_vsrc[vv] = src;
-        }
-        // this chunk's vertices' kept points, the warp on one vertex at a time
-        unsigned todo = __ballot_sync(0xffffffffu, kp > 0);
-        while (todo) {
-          const int q = __ffs(todo) - 1;
-          todo &= todo - 1u;
-          const int n = __shfl_sync(0xffffffffu, kp, q);
-          const int s0 = __shfl_sync(0xffffffffu, src, q);
-          const int p0 = __shfl_sync(0xffffffffu, pstart, q);
-          for (int t = lane; t < n; t += 32) d.lm_pts[p0 + t] = d.kept[s0 + t];
-        }
-        pbase += __shfl_sync(0xffffffffu, incl, 31);
-        vi += __popc(b);
+  const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int c = wg; c < d.cnt->n_cand; c += nw) {
+    const int l = d.cand_lm[c];
+    if (l < 0) continue;
+    const int nv = d.cand_nv[c];
+    int vbase = cand_vb[c], pbase = cand_pb[c];
+    int vi = 0;
+    for (int r0 = H - 1; r0 >= 0 && vi < nv; r0 -= 32) {
+      const int row = r0 - lane;
+      const int it = c * H + row;
+      const int k = row >= 0 ? d.vkept[it] : 0;
+      const bool v = k > 0;
+      const unsigned b = __ballot_sync(0xffffffffu, v);
+      const int my = vi + __popc(b & ((1u << lane) - 1u));
+      // kept-point prefix inside this chunk
+      int kp = v && my < nv ? k : 0, incl = kp;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
       }
+      const int pstart = pbase + incl - kp;
+      if (v && my < nv) {
+        const int vv = vbase + my;
+        const float4 m = d.vmed[it];
+        d.lm_vxyz[3 * vv] = m.x;
+        d.lm_vxyz[3 * vv + 1] = m.y;
+        d.lm_vxyz[3 * vv + 2] = m.z;
+        d.lm_vrad[vv] = d.vrad[it];
+        d.lm_vrow[vv] = row;
+        d.lm_pbeg[vv] = pstart;
+        d.lm_vsrc[vv] = d.roff[it];
+      }
+      pbase += __shfl_sync(0xffffffffu, incl, 31);
+      vi += __popc(b);
     }
-    return;
   }
+}
+
+// Point copies of the landmarks, spread over the whole grid: one warp per
+// vertex for the kept points, one thread per bucket slot for the cluster
+// points (raster order; the candidate of a slot found by binary search).
+// One warp per (candidate, row) bucket instead, which needs no search, was
+// measured slower (11.6 against 8.7 us per launch): the wide buckets of near
+// trees leave most warps idle while a few walk long rows.
+__global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
   const TreeView tree = tree_view(d.in, d.W);
-  const int gt = (blockIdx.x - kLmWriteBlocks) * blockDim.x + threadIdx.x;
-  const int nt = (gridDim.x - kLmWriteBlocks) * blockDim.x;
+  const int H = d.H;
+  const int lane = threadIdx.x & 31;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  const int nv = d.cnt->n_v;
+  for (int v = gt >> 5; v < nv; v += nt >> 5) {
+    const int src = d.lm_vsrc[v], dst = d.lm_pbeg[v], cnt = d.lm_pbeg[v + 1] - dst;
+    for (int q = lane; q < cnt; q += 32) d.lm_pts[dst + q] = d.kept[src + q];
+  }
   const int nc = d.cnt->n_cand;
   const int total = d.roff[nc * H];
   for (int q = gt; q < total; q += nt) {
@@ -819,8 +813,12 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   int32_t* cand_vb = reinterpret_cast<int32_t*>(d.rank);
   int32_t* cand_pb = cand_vb + d.cap_cand;
   k_lm_scan<<<1, 1024, 0, st>>>(d, kp, cand_vb, cand_pb);
-  k_lm_emit<<<kLmWriteBlocks + gw, 256, 0, st>>>(d, cand_vb, cand_pb);
-  return 12;
+  // the kept-point copies spread over the grid (k_lm_copy) rather than in
+  // the record-writing warps: the merged kernel walked each candidate's
+  // vertices one after the other and ran the Trellis 23 us longer
+  k_lm_write<<<32, 256, 0, st>>>(d, cand_vb, cand_pb);
+  k_lm_copy<<<gw, 256, 0, st>>>(d);
+  return 13;
 }
 
 }  // namespace sg
