@@ -396,6 +396,7 @@ void carve(Dev& d, Carver& c, int n_blk) {
   d.rc = c.take<int32_t>((size_t)d.cap_cand * d.H);
   d.roff = c.take<int32_t>((size_t)d.cap_cand * d.H + 1);
   d.bucket = c.take<int32_t>(N);
+  d.wide_list = c.take<int32_t>((size_t)d.cap_cand * d.H);
   d.kept = c.take<float4>(N);
   d.vmed = c.take<float4>((size_t)d.cap_cand * d.H);
   d.vrad = c.take<double>((size_t)d.cap_cand * d.H);

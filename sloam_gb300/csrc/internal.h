@@ -38,7 +38,8 @@ struct Counters {
   int32_t n_fit;         // trees given to the point-level cylinder fit
   int32_t n_fit_pts;     // their points (the work queue's trees)
   int32_t n_bucket;      // tree pixels in the Trellis (component, row) buckets
-  int32_t pad[5];
+  int32_t n_wide;        // (component, row) buckets wider than a warp's shared memory
+  int32_t pad[4];
 };
 
 // The cylinder work queue (cylqueue.cu): the item counter and the shape of
@@ -200,6 +201,7 @@ struct Dev {
   int32_t* rc;         // [cap_cand*H]
   int32_t* roff;       // [cap_cand*H+1]
   int32_t* bucket;     // [N] pixel index per (cand,row) slot, column order
+  int32_t* wide_list;  // [cap_cand*H] the wide (cand,row) items of the keyframe
   float4* kept;        // [N] kept vertex points (z order), same offsets
   float4* vmed;        // [cap_cand*H] median (w unused)
   double* vrad;        // [cap_cand*H]
@@ -319,6 +321,7 @@ size_t front_gbits_words(int N);
 int launch_tree_out(const FrontRef& f, const KParams& kp, int N, float4* out, cudaStream_t st);
 int front_blocks(int N);
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st);
+void init_trellis_attributes();
 int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream_t st);
 int launch_run(const Dev& d, const KParams& kp, bool first_scan, bool update_state,
                cudaStream_t st, bool map_prepped = false);

@@ -1649,6 +1649,7 @@ int launch_models(const Dev& d, const KParams& kp, bool from_trellis, cudaStream
 void init_kernel_attributes() {
   prop::init_attributes();
   init_queue_attributes();
+  init_trellis_attributes();
 }
 
 }  // namespace sg

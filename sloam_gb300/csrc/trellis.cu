@@ -325,6 +325,7 @@ __global__ void __launch_bounds__(1024) k_rowscan(Dev d) {
 }
 
 constexpr int kVtxCap = 256;   // points per vertex staged in shared memory
+constexpr int kWideCap = 2048; // wider rows (up to this) run one block each in k_vertex_wide
 constexpr int kVtxWarps = 4;
 
 __device__ __forceinline__ bool zless(float4 a, int ia, float4 b, int ib) {
@@ -483,6 +484,13 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
     }
     // stage: shared memory when it fits, else the global scratch `kept`
     // region is read directly (rank pass) - bucket points from the cloud
+    if (n > kVtxCap && n <= kWideCap) {  // listed for k_vertex_wide
+      if (lane == 0) {
+        const int q = atomicAdd(&d.cnt->n_wide, 1);
+        if (q < d.cap_cand * H) d.wide_list[q] = it;
+      }
+      continue;
+    }
     const bool inshm = n <= kVtxCap;
     float4* P = spts[w];
     if (inshm)
@@ -577,7 +585,8 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
     __syncwarp();
     const bool valid = nkept > 1;
     if (!inshm) {
-      // very wide bucket: serial fallback by lane 0 (rare: > kVtxCap points)
+      // a row wider than k_vertex_wide takes (images wider than kWideCap):
+      // serial fallback by lane 0
       if (lane == 0) {
         int first = -1, last = -1, wr = 0;
         // emit kept points in (z,y,x,col) order by repeated minimum search
@@ -639,6 +648,125 @@ __global__ void __launch_bounds__(kVtxWarps * 32) k_vertex(Dev d, KParams kp) {
     }
     __syncwarp();
   }
+}
+
+// Rows of kVtxCap < n <= kWideCap points (the near trees of wide clusters),
+// which k_vertex lists: one block of 256 threads per row at a time, the
+// listed rows spread over the blocks, everything in shared memory.  Each
+// axis median is element `mid` of the order by (value, index) -- the
+// element the rank count selects -- by a block bitonic sort of 64-bit
+// (order-preserving value key, index) words; the kept points' (z, y, x,
+// column) order by a block bitonic sort of their indices with the same
+// comparison as the narrow path.
+constexpr int kWideThreads = 256;
+__device__ __forceinline__ void block_bitonic_u64(unsigned long long* a, int m) {
+  for (int k = 2; k <= m; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < (m >> 1); t += blockDim.x) {
+        const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i | j;
+        const unsigned long long x = a[i], y = a[l];
+        const bool up = (i & k) == 0;
+        if (up ? (y < x) : (x < y)) {
+          a[i] = y;
+          a[l] = x;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+constexpr size_t kWideSmem = (size_t)kWideCap * (sizeof(float4) + sizeof(unsigned long long));
+__global__ void __launch_bounds__(kWideThreads) k_vertex_wide(Dev d, KParams kp) {
+  extern __shared__ __align__(16) unsigned char wsm[];  // P [kWideCap], key [kWideCap]
+  float4* P = reinterpret_cast<float4*>(wsm);
+  unsigned long long* key =
+      reinterpret_cast<unsigned long long*>(wsm + (size_t)kWideCap * sizeof(float4));
+  __shared__ float med[3];
+  __shared__ int s_kept[kWideThreads / 32];
+  const TreeView tree = tree_view(d.in, d.W);
+  // the wide items k_vertex listed, one per block at a time (the list's
+  // order does not matter: each item writes only its own outputs)
+  const int nwide = min(d.cnt->n_wide, d.cap_cand * d.H);
+  {
+    for (int q = blockIdx.x; q < nwide; q += gridDim.x) {
+      const int it = d.wide_list[q];
+      const int n = d.rc[it];
+      const int off = d.roff[it];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) P[j] = tree[d.bucket[off + j]];
+      int m = 1;
+      while (m < n) m <<= 1;
+      __syncthreads();
+      const int mid = n / 2;
+      for (int axis = 0; axis < 3; ++axis) {
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+          unsigned long long k = ~0ull;
+          if (j < n) {
+            const float4 a = P[j];
+            k = ((unsigned long long)fkey(axis == 0 ? a.x : axis == 1 ? a.y : a.z) << 32) |
+                (uint32_t)j;
+          }
+          key[j] = k;
+        }
+        __syncthreads();
+        block_bitonic_u64(key, m);
+        if (threadIdx.x == 0) {
+          const float4 a = P[(int)(uint32_t)key[mid]];
+          med[axis] = axis == 0 ? a.x : axis == 1 ? a.y : a.z;
+        }
+        __syncthreads();
+      }
+      const float mx = med[0], my = med[1], mz = med[2];
+      // kept flags, then the kept indices by (z, y, x, column); key holds the
+      // indices (the kept ones first, n for the others) as 64-bit words
+      int nk = 0;
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        bool keep = false;
+        if (j < n) {
+          const float4 a = P[j];
+          keep = pcl_euclid(a.x, a.y, a.z, mx, my, mz) < kp.max_d_centroid;
+        }
+        key[j] = keep ? (unsigned long long)j : (unsigned long long)n;
+        nk += keep ? 1 : 0;
+      }
+      nk = warp_sumi(nk);
+      if ((threadIdx.x & 31) == 0) s_kept[threadIdx.x >> 5] = nk;
+      __syncthreads();
+      int nkept = 0;
+      for (int w = 0; w < kWideThreads / 32; ++w) nkept += s_kept[w];
+      auto lt = [&](int x, int y) { return x < n && (y >= n || zless(P[x], x, P[y], y)); };
+      for (int k = 2; k <= m; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int t = threadIdx.x; t < (m >> 1); t += blockDim.x) {
+            const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i | j;
+            const int x = (int)key[i], y = (int)key[l];
+            const bool up = (i & k) == 0;
+            if (up ? lt(y, x) : lt(x, y)) {
+              key[i] = (unsigned long long)y;
+              key[l] = (unsigned long long)x;
+            }
+          }
+          __syncthreads();
+        }
+      }
+      for (int r = threadIdx.x; r < nkept; r += blockDim.x) d.kept[off + r] = P[(int)key[r]];
+      if (threadIdx.x == 0) {
+        const bool valid = nkept > 1;
+        double rad = 0.0;
+        if (valid) {
+          const float4 a = P[(int)key[0]], b = P[(int)key[nkept - 1]];
+          rad = (double)pcl_euclid(a.x, a.y, a.z, b.x, b.y, b.z);
+        }
+        d.vmed[it] = make_float4(mx, my, mz, 0.0f);
+        d.vrad[it] = rad;
+        d.vkept[it] = valid ? nkept : 0;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void k_clear_wide(Dev d) {
+  if (threadIdx.x == 0) d.cnt->n_wide = 0;
 }
 
 // Per candidate (thread c): vertex count of the landmark (0 = rejected),
@@ -784,8 +912,20 @@ __global__ void __launch_bounds__(256) k_lm_copy(Dev d) {
 
 // k_vertex alone over the last keyframe's (component, row) buckets, for timing.
 int launch_vertex_kernel(const Dev& d, const KParams& kp, cudaStream_t st) {
+  k_clear_wide<<<1, 32, 0, st>>>(d);  // repeated timing runs: the list starts empty each time
   k_vertex<<<4 * 152, kVtxWarps * 32, 0, st>>>(d, kp);
-  return 1;
+  k_vertex_wide<<<152, kWideThreads, kWideSmem, st>>>(d, kp);
+  return 3;
+}
+
+// The wide-row kernel's 48 KB of dynamic shared memory plus its static
+// words exceed the default per-block limit: opt in once per process.
+void init_trellis_attributes() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_vertex_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)kWideSmem);
+  done = true;
 }
 
 int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
@@ -808,7 +948,9 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   // k_vertex on twice that many warps: a (component, row) item is a long
   // dependent chain, and fewer items per warp shorten the keyframe (measured
   // 1.5 % more keyframes/s in the batch than 2 * 152 blocks)
+  // (the wide list starts empty: k_begin cleared the counters)
   k_vertex<<<4 * gw, kVtxWarps * 32, 0, st>>>(d, kp);
+  k_vertex_wide<<<gw, kWideThreads, kWideSmem, st>>>(d, kp);
   // scratch for the landmark offsets lives in the (now unused) rank array
   int32_t* cand_vb = reinterpret_cast<int32_t*>(d.rank);
   int32_t* cand_pb = cand_vb + d.cap_cand;
@@ -818,7 +960,7 @@ int launch_trellis(const Dev& d, const KParams& kp, cudaStream_t st) {
   // vertices one after the other and ran the Trellis 23 us longer
   k_lm_write<<<32, 256, 0, st>>>(d, cand_vb, cand_pb);
   k_lm_copy<<<gw, 256, 0, st>>>(d);
-  return 13;
+  return 14;
 }
 
 }  // namespace sg

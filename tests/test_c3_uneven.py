@@ -136,3 +136,32 @@ def test_c3_queue_shapes_bit_identical(chunk, tile, blocks):
             assert len(xa[0]) > 10
             for u, v in zip(xa, xb):
                 np.testing.assert_array_equal(u, v)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", [0, 4])
+def test_c3_trellis_wide_rows_match_oracle(k):
+    """Trellis of the uneven scenes whose near trunks give component rows of
+    more than 256 points (284 and 294) (the block-per-row vertex
+    kernel): component labels and landmarks (vertex medians, radii, kept
+    points in order) bit-identical to the oracle's."""
+    from tests.test_gpu_parity import make_ctx
+    forest, kfs, _ = _scene()
+    P = synth.c3_params(forest, two_step_optim=0, cyl_mode=1)
+    kf = kfs[k]
+    o = H.oracle_project(P, kf.xyzi, labels=kf.labels)
+    cloud = o["tree_cloud"]
+    lo, labo, nco = H.oracle_trellis(P, cloud, P.img_h, P.img_w)
+    # some (component, row) holds more than 256 points
+    lab = labo.reshape(P.img_h, P.img_w)
+    widest = 0
+    for r in range(P.img_h):
+        row = lab[r][lab[r] != 0xFFFFFFFF]
+        if len(row):
+            widest = max(widest, np.unique(row, return_counts=True)[1].max())
+    assert widest > 256
+    ctx = make_ctx(P)
+    lg, labg, ncg = H.gpu_trellis(ctx, cloud, P.img_h, P.img_w)
+    assert nco == ncg
+    np.testing.assert_array_equal(labo, labg)
+    H.landmarks_equal_exact(lo, lg)
