@@ -499,38 +499,44 @@ constexpr int kMbarSpin = 1 << 20;  // bounded wait (the MMAs take microseconds)
       : "r"(taddr))
 SLOAM_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Shared-memory layout of the tensor-core inference kernel below.
-constexpr int kTcWg = 4;                // warpgroups, one sample each at a time
-constexpr int kTcThreads = 128 * kTcWg;
+// Shared-memory layout of the tensor-core inference kernel below, which runs
+// with WG warpgroups (one sample each at a time): four for large standalone
+// launches (one CTA per SM, the SM to itself), two inside the keyframe
+// pipeline (the CTA leaves registers and shared memory for other kernels).
 constexpr int kMaxGroup = 8;     // samples per group (one tree's proposals)
 // Per warpgroup one 32 KB operand buffer: A1 [128 x 80] (the ones column
 // at 64 carries b2) at its start and A0 [128 x 16] (layer-1 input) after
 // it while layers 1 and 2 run, then A2 [128 x 128] (written once the
 // layer-2 MMAs, which read A1, have completed).  Between groups the
-// operand buffers hold the head's W4^T (64 KB, bulk copy) and outputs.
+// operand buffers hold the head's W4^T (64 KB, bulk copy), and the head's
+// outputs go to Ht once the head MMA, which reads Ht, has completed.
 // W2^T | b2, W3^T, B1, the biases and W5 arrive by bulk copy from the
 // packed device layout.  Ht [16 x 256] is the head's B operand: the
 // max-pooled features of sample k split exactly into bf16 hi (row k) and
 // lo (row 8 + k) terms.
 constexpr uint32_t kSmB2 = 0, kSmB3 = kSmB2 + kTcB2xBytes,
                    kSmA2 = kSmB3 + kTcW3Bytes,                    // [wg][32 KB]
-                   kSmB1 = kSmA2 + kTcWg * kPts * kD2 * 2,        // [64 x 16] bf16
-                   kSmHt = kSmB1 + kTcB1Bytes,                    // [16 x 256] bf16
-                   kSmSmall = kSmHt + 2 * kMaxGroup * kD3 * 2,    // b3, b4, b5
-                   kSmallCopy = 4 * (kSfW5 - kSfB3),
-                   kSmW5h = kSmSmall + kSmallCopy,                // W5 [128][7] bf16
-                   kSmMisc = kSmW5h + kTcW5hBytes,
-                   kTcSmem = kSmMisc + 64;
+                   kSmallCopy = 4 * (kSfW5 - kSfB3);
 constexpr uint32_t kOpA0 = kPts * kK2x * 2;                       // A0 inside the buffer
-constexpr uint32_t kOpY1 = kTcW4Bytes;                            // head outputs, after W4^T
-static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0 && kSmB1 % 128 == 0 && kSmHt % 128 == 0,
-              "operand alignment");
-static_assert(kSmSmall % 16 == 0 && kSmW5h % 16 == 0 && kSmMisc % 16 == 0 && kOpA0 % 128 == 0,
-              "16-byte alignment");
-static_assert(kTcSmem <= 227 * 1024, "shared memory");
+template <int WG>
+struct TcLayout {
+  static constexpr int kThreads = 128 * WG;
+  static constexpr uint32_t kB1 = kSmA2 + WG * kPts * kD2 * 2,   // [64 x 16] bf16
+      kHt = kB1 + kTcB1Bytes,                                     // [16 x 256] bf16
+      kSmall = kHt + 2 * kMaxGroup * kD3 * 2,                     // b3, b4, b5
+      kW5h = kSmall + kSmallCopy,                                 // W5 [128][7] bf16
+      kMisc = kW5h + kTcW5hBytes,
+      kSmem = kMisc + 64;
+  static constexpr uint32_t kTmemCols = 128 * WG;                 // 128 columns per warpgroup
+  static_assert(WG == 2 || WG == 4, "TMEM allocation: a power of two");
+  static_assert(kB1 % 128 == 0 && kHt % 128 == 0, "operand alignment");
+  static_assert(kSmall % 16 == 0 && kW5h % 16 == 0 && kMisc % 16 == 0, "16-byte alignment");
+  static_assert(kSmem <= 227 * 1024, "shared memory");
+  static_assert(kTcW4Bytes <= WG * kPts * kD2 * 2, "W4^T inside the operand buffers");
+};
+static_assert(kSmA2 % 128 == 0 && kSmB3 % 128 == 0 && kOpA0 % 128 == 0, "operand alignment");
 static_assert(kOpA0 + kPts * kK1 * 2 <= kPts * kD2 * 2, "A1 and A0 inside the A2 buffer");
-static_assert(kOpY1 + kMaxGroup * kD4 * 4 <= kTcWg * kPts * kD2 * 2,
-              "W4^T and the head outputs inside the operand buffers");
+static_assert(kMaxGroup * kD4 * 4 <= 2 * kMaxGroup * kD3 * 2, "head outputs inside Ht");
 static_assert(2 * kMaxGroup == 16, "head MMA: N = 16 (hi and lo rows of 8 samples)");
 // the descriptors address at most: A0 [128 x 16], A1 [128 x 80], A2
 // [128 x 128], B1 [64 x 16], W2^T | b2 [128 x 80], W3^T [256 x 128], W4^T
@@ -584,8 +590,8 @@ SLOAM_D bool wg_any(int wg, bool p) {
 // Tensor-core inference.  Persistent CTAs (one per SM at most: the shared
 // memory allows no second) over groups of `group` samples -- in the
 // pipeline one tree's proposals; groups whose frame scale is 0 (trees not
-// fitted) are skipped.  512 threads: warpgroup g (0..3) takes samples
-// g, g + 4 of the group with its own operand buffer, TMEM columns
+// fitted) are skipped.  kTcWg warpgroups: warpgroup g takes samples
+// g, g + kTcWg, ... of the group with its own operand buffer, TMEM columns
 // [128 g, 128 g + 128), mbarrier and barrier, so that one warpgroup's MMAs
 // overlap the others' CUDA-core work; its next sample's points are loaded
 // while it works on the current one.  Per sample (thread r = point r):
@@ -601,17 +607,22 @@ SLOAM_D bool wg_any(int wg, bool p) {
 // N=16 (hi and lo of 8 samples), K=256, A = W4^T; then bias and ReLU, and
 // one warp per (sample, output) for the last layer.  bf16 operands in
 // shared memory, fp32 accumulators in TMEM.
-__global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
+template <int kTcWg>
+__global__ void __launch_bounds__(128 * kTcWg, 4 / kTcWg) k_prop_infer_tc(
     const unsigned char* __restrict__ tcw, const float* __restrict__ X, int S,
     const int* __restrict__ n_groups_dev, int group, const float4* __restrict__ frames,
     float* __restrict__ out, int* __restrict__ err) {
+  using L = TcLayout<kTcWg>;
+  constexpr int kTcThreads = L::kThreads;
+  constexpr uint32_t kSmB1 = L::kB1, kSmHt = L::kHt, kSmSmall = L::kSmall, kSmW5h = L::kW5h,
+                     kSmMisc = L::kMisc, kTmemCols = L::kTmemCols;
   extern __shared__ __align__(128) unsigned char smem[];
   const float* sb3 = reinterpret_cast<const float*>(smem + kSmSmall);  // b3, b4, b5
   const float* sb4 = sb3 + (kSfB4 - kSfB3);
   const float* sb5 = sb3 + (kSfB5 - kSfB3);
   const __nv_bfloat16* sw5 = reinterpret_cast<const __nv_bfloat16*>(smem + kSmW5h);
   unsigned char* htb = smem + kSmHt;
-  float* y1 = reinterpret_cast<float*>(smem + kSmA2 + kOpY1);  // [group][128], head only
+  float* y1 = reinterpret_cast<float*>(htb);  // [group][128], after the head MMA
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmMisc);  // [kTcWg]
   uint64_t* lbar = mbar + kTcWg;  // bulk copies and the head MMA
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kSmMisc + 8 * kTcWg + 8);
@@ -655,8 +666,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
     bulk_load(saddr(smem + kSmW5h), tcw + kTcW5hOff, kTcW5hBytes, lbar);
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
-                     saddr(tslot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(tslot)), "n"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -907,22 +918,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_prop_infer_tc(
   __syncthreads();
   fence_after();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(*tslot) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot),
+                 "n"(kTmemCols)
+                 : "memory");
 }
 
 int g_tc_attr = 0;
-// Persistent CTAs of the per-keyframe launch.  Each needs an empty SM (its
-// shared memory and registers fill one), so in a batch every CTA waits for
-// an SM to drain: 24 CTAs, two trees each for a 64x2048 scene's ~40 trees,
-// ran the 32-slot batch 1 % faster than 48 (which left CTAs without a tree).
+// Persistent CTAs of the per-keyframe launch, two warpgroups each (160 KB of
+// shared memory and 256 threads: the rest of the SM stays open to the
+// batch's other kernels, where four warpgroups filled it and every CTA
+// waited for an SM to drain).  On the 32-slot 64x2048 batch two warpgroups
+// ran the learned path 1.3-1.7 % faster than four; 24 CTAs, two trees each for
+// the scene's ~40 trees, beat 16, 20, 30, 36 and 48.
+constexpr int kTreeWg = 2;
 constexpr int kTreeCtas = 24;
+// standalone launches (many groups): four warpgroups, one CTA per SM
+constexpr int kBulkWg = 4;
 
 }  // namespace
 
 void init_attributes() {
   if (g_tc_attr) return;
-  cudaFuncSetAttribute(k_prop_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)kTcSmem);
+  cudaFuncSetAttribute(k_prop_infer_tc<kTreeWg>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)TcLayout<kTreeWg>::kSmem);
+  cudaFuncSetAttribute(k_prop_infer_tc<kBulkWg>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)TcLayout<kBulkWg>::kSmem);
   cudaFuncSetAttribute(k_prop_infer_ref, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)kRefSmem);
   g_tc_attr = 1;
@@ -945,8 +965,8 @@ int launch_prop_infer_trees(const unsigned char* d_tcw, const float* d_x, const 
   const int groups = (cap + per_tree - 1) / per_tree;
   const int lim = sm_count() < kTreeCtas ? sm_count() : kTreeCtas;
   const int grid = groups < lim ? (groups > 0 ? groups : 1) : lim;
-  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, cap, d_n_trees, per_tree,
-                                                     d_frames, d_out, d_err);
+  k_prop_infer_tc<kTreeWg><<<grid, TcLayout<kTreeWg>::kThreads, TcLayout<kTreeWg>::kSmem, st>>>(
+      d_tcw, d_x, cap, d_n_trees, per_tree, d_frames, d_out, d_err);
   return 1;
 }
 
@@ -965,8 +985,8 @@ int launch_prop_infer(const unsigned char* d_tcw, const float* d_x, int n, float
   }
   const int groups = (n + kMaxGroup - 1) / kMaxGroup;
   const int grid = groups < sm_count() ? groups : sm_count();
-  k_prop_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(d_tcw, d_x, n, nullptr, kMaxGroup, nullptr,
-                                                     d_out, d_err);
+  k_prop_infer_tc<kBulkWg><<<grid, TcLayout<kBulkWg>::kThreads, TcLayout<kBulkWg>::kSmem, st>>>(
+      d_tcw, d_x, n, nullptr, kMaxGroup, nullptr, d_out, d_err);
   return 1;
 }
 
