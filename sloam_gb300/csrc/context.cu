@@ -284,6 +284,12 @@ struct sloam_ctx {
   InPtrs* h_in = nullptr;       // per-keyframe input pointer blocks (batch)
   double* h_poses = nullptr;    // per-keyframe estimates (batch)
   int h_batch_cap = 0;
+  // their device copies, one upload per batch (each slot takes its
+  // keyframe's block with a kernel, not a host copy: a small copy would
+  // queue behind the batch's scan uploads on the copy engine)
+  InPtrs* d_in_all = nullptr;
+  double* d_poses_all = nullptr;
+  int d_batch_cap = 0;
   bool first_scan = true;
   std::string err;
   int64_t launches = 0;
@@ -305,10 +311,12 @@ struct sloam_ctx {
   Fork fk;  // the context's own keyframe graph
   // batch projection: a1-a2 of a whole batch on its own stream, one launch
   // per kernel and chunk of keyframes, into per-keyframe buffers
-  // fe_st: uploads and the projection kernel of each chunk; fe_st2: the
-  // chunk's label and compaction kernels, so the next chunk's projection
-  // overlaps them (the chunk scratch alternates between two sets)
-  cudaStream_t fe_st = nullptr, fe_st2 = nullptr;
+  // fe_st: the projection kernel of each chunk; fe_st2: the chunk's label
+  // and compaction kernels, so the next chunk's projection overlaps them
+  // (the chunk scratch alternates between two sets); fe_cp: the scan uploads
+  // of the host entry point, back to back, each chunk's projection waiting
+  // for its own chunk's copies only
+  cudaStream_t fe_st = nullptr, fe_st2 = nullptr, fe_cp = nullptr;
   void* fb = nullptr;            // [fb_cap] per-keyframe projection buffers
   size_t fb_stride = 0;          // bytes per keyframe
   int32_t* fb_pix = nullptr;     // [2][kFrontChunkMax * N] point pixels of the chunks in flight
@@ -322,6 +330,7 @@ struct sloam_ctx {
   // chunk c: [3c] before its projection, [3c+1] after it, [3c+2] after
   // its label and compaction kernels
   std::vector<cudaEvent_t> ev_fe;
+  std::vector<cudaEvent_t> ev_cp;  // [chunk] the chunk's uploads done
   int fe_chunks = 0, fe_nkf = 0;
   // learned proposal: bf16 network weights in the tensor-core layout
   unsigned char* prop_tc = nullptr;
@@ -784,7 +793,8 @@ extern "C" sloam_ctx* sloam_create(const sloam_params* params, int device, int* 
   if (cudaSetDevice(device) != cudaSuccess) return bail(SLOAM_ERR_NO_DEVICE);
   if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->fe_st, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&ctx->fe_st2, cudaStreamNonBlocking) != cudaSuccess)
+      cudaStreamCreateWithFlags(&ctx->fe_st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->fe_cp, cudaStreamNonBlocking) != cudaSuccess)
     return bail(SLOAM_ERR_CUDA);
   if (cudaMallocHost((void**)&ctx->h_cnt, sizeof(Counters)) != cudaSuccess ||
       cudaMallocHost((void**)&ctx->h_pose, sizeof(double) * 32) != cudaSuccess ||
@@ -817,8 +827,10 @@ extern "C" void sloam_destroy(sloam_ctx* ctx) {
   if (ctx->prop_tc) cudaFree(ctx->prop_tc);
   free_front(ctx);
   for (auto e : ctx->ev_fe) cudaEventDestroy(e);
+  for (auto e : ctx->ev_cp) cudaEventDestroy(e);
   if (ctx->fe_st) cudaStreamDestroy(ctx->fe_st);
   if (ctx->fe_st2) cudaStreamDestroy(ctx->fe_st2);
+  if (ctx->fe_cp) cudaStreamDestroy(ctx->fe_cp);
   if (ctx->d_out_i) cudaFree(ctx->d_out_i);
   if (ctx->d_out_pose) cudaFree(ctx->d_out_pose);
   if (ctx->arena) cudaFree(ctx->arena);
@@ -826,6 +838,8 @@ extern "C" void sloam_destroy(sloam_ctx* ctx) {
   if (ctx->h_pose) cudaFreeHost(ctx->h_pose);
   if (ctx->h_in) cudaFreeHost(ctx->h_in);
   if (ctx->h_poses) cudaFreeHost(ctx->h_poses);
+  if (ctx->d_in_all) cudaFree(ctx->d_in_all);
+  if (ctx->d_poses_all) cudaFree(ctx->d_poses_all);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -1222,6 +1236,16 @@ extern "C" int sloam_keyframe_mapped(sloam_ctx* ctx, sloam_mapmgr* mm, const flo
 }
 
 namespace sg {
+// keyframe k's input block and pose estimate, from the batch's device copies
+// into its slot
+static_assert(sizeof(InPtrs) % 8 == 0, "InPtrs copied as 8-byte words");
+__global__ void k_batch_in(const InPtrs* __restrict__ all_in, const double* __restrict__ all_pose,
+                           int k, InPtrs* in, double* pose_io) {
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(all_in + k);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(in);
+  for (int i = threadIdx.x; i < (int)(sizeof(InPtrs) / 8); i += blockDim.x) dst[i] = src[i];
+  if (threadIdx.x < 7) pose_io[threadIdx.x] = all_pose[8 * k + threadIdx.x];
+}
 // per-keyframe outputs of a device batch
 __global__ void k_batch_out(Counters* c, const double* pose_io, double* pose_out,
                             int32_t* success_out, int32_t* ncyl_out, int k) {
@@ -1251,14 +1275,24 @@ SlotView slot(sloam_ctx* ctx, int s) {
 }
 
 int grow_batch(sloam_ctx* ctx, int nkf) {
-  if (nkf <= ctx->h_batch_cap) return SLOAM_OK;
-  cudaFreeHost(ctx->h_in);
-  cudaFreeHost(ctx->h_poses);
-  ctx->h_in = nullptr;
-  ctx->h_poses = nullptr;
-  CK(cudaMallocHost((void**)&ctx->h_in, sizeof(InPtrs) * nkf));
-  CK(cudaMallocHost((void**)&ctx->h_poses, sizeof(double) * 8 * nkf));
-  ctx->h_batch_cap = nkf;
+  if (nkf > ctx->h_batch_cap) {
+    cudaFreeHost(ctx->h_in);
+    cudaFreeHost(ctx->h_poses);
+    ctx->h_in = nullptr;
+    ctx->h_poses = nullptr;
+    CK(cudaMallocHost((void**)&ctx->h_in, sizeof(InPtrs) * nkf));
+    CK(cudaMallocHost((void**)&ctx->h_poses, sizeof(double) * 8 * nkf));
+    ctx->h_batch_cap = nkf;
+  }
+  if (ctx->d_batch_cap < ctx->h_batch_cap) {
+    if (ctx->d_in_all) cudaFree(ctx->d_in_all);
+    if (ctx->d_poses_all) cudaFree(ctx->d_poses_all);
+    ctx->d_in_all = nullptr;
+    ctx->d_poses_all = nullptr;
+    CK(cudaMalloc((void**)&ctx->d_in_all, sizeof(InPtrs) * ctx->h_batch_cap));
+    CK(cudaMalloc((void**)&ctx->d_poses_all, sizeof(double) * 8 * ctx->h_batch_cap));
+    ctx->d_batch_cap = ctx->h_batch_cap;
+  }
   return SLOAM_OK;
 }
 
@@ -1294,6 +1328,7 @@ FrontSlice front_slice(const Dev& d, char* base, bool upload, size_t* bytes) {
 }
 
 void free_front(sloam_ctx* ctx) {
+  if (ctx->fe_cp) cudaStreamSynchronize(ctx->fe_cp);
   if (ctx->fe_st) cudaStreamSynchronize(ctx->fe_st);
   if (ctx->fe_st2) cudaStreamSynchronize(ctx->fe_st2);
   if (ctx->fb) cudaFree(ctx->fb);
@@ -1369,14 +1404,12 @@ int batch_one(sloam_ctx* ctx, int k, double* pose_out, int32_t* success_out, int
               int64_t* launches) {
   const int S = 1 + (int)ctx->extra.size();
   SlotView v = slot(ctx, k % S);
-  CK(cudaMemcpyAsync(v.d->in, ctx->h_in + k, sizeof(InPtrs), cudaMemcpyHostToDevice, v.st));
-  CK(cudaMemcpyAsync(v.d->pose_io, ctx->h_poses + 8 * k, sizeof(double) * 7,
-                     cudaMemcpyHostToDevice, v.st));
+  k_batch_in<<<1, 32, 0, v.st>>>(ctx->d_in_all, ctx->d_poses_all, k, v.d->in, v.d->pose_io);
   int nk = 0;
   int st = run_graph(ctx, *v.d, v.st, *v.fk, *v.gx, false, true, false, true, &nk);
   if (st) return st;
   k_batch_out<<<1, 32, 0, v.st>>>(v.d->cnt, v.d->pose_io, pose_out, success_out, ncyl_out, k);
-  *launches += nk + 1;
+  *launches += nk + 2;
   return SLOAM_OK;
 }
 
@@ -1437,6 +1470,20 @@ int batch_run(sloam_ctx* ctx, int nkf, const float* h_xyzi, const uint8_t* h_lab
     CK(cudaEventCreate(&e));
     ctx->ev_fe.push_back(e);
   }
+  while (h_xyzi && (int)ctx->ev_cp.size() < nch) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->ev_cp.push_back(e);
+  }
+  // the uploads start once the batch has forked from the context stream;
+  // first the keyframes' input blocks and pose estimates (each slot waits
+  // for its keyframe's chunk, whose projection comes after them on either
+  // path)
+  cudaStream_t up = h_xyzi ? ctx->fe_cp : ctx->fe_st;
+  if (h_xyzi) CK(cudaStreamWaitEvent(ctx->fe_cp, ctx->ev_main, 0));
+  CK(cudaMemcpyAsync(ctx->d_in_all, ctx->h_in, sizeof(InPtrs) * nkf, cudaMemcpyHostToDevice, up));
+  CK(cudaMemcpyAsync(ctx->d_poses_all, ctx->h_poses, sizeof(double) * 8 * nkf,
+                     cudaMemcpyHostToDevice, up));
   CK(cudaMemcpyAsync(ctx->d_refs, ctx->h_refs, sizeof(FrontRef) * nkf, cudaMemcpyHostToDevice,
                      ctx->fe_st));
   CK(cudaMemsetAsync(ctx->fb_fe, 0, sizeof(int32_t) * 4 * nkf, ctx->fe_st));
@@ -1447,10 +1494,12 @@ int batch_run(sloam_ctx* ctx, int nkf, const float* h_xyzi, const uint8_t* h_lab
       for (int k = kf0; k < kf0 + nc; ++k) {
         FrontRef& f = ctx->h_refs[k];
         CK(cudaMemcpyAsync(const_cast<float4*>(f.xyzi), h_xyzi + (size_t)k * n * 4,
-                           16 * (size_t)n, cudaMemcpyHostToDevice, ctx->fe_st));
+                           16 * (size_t)n, cudaMemcpyHostToDevice, ctx->fe_cp));
         CK(cudaMemcpyAsync(const_cast<uint8_t*>(f.plabel), h_labels + (size_t)k * n, (size_t)n,
-                           cudaMemcpyHostToDevice, ctx->fe_st));
+                           cudaMemcpyHostToDevice, ctx->fe_cp));
       }
+      CK(cudaEventRecord(ctx->ev_cp[c], ctx->fe_cp));
+      CK(cudaStreamWaitEvent(ctx->fe_st, ctx->ev_cp[c], 0));
     }
     // the scratch set of chunk c - 2 is re-armed by that chunk's compaction
     if (c >= 2) CK(cudaStreamWaitEvent(ctx->fe_st, ctx->ev_fe[3 * (c - 2) + 2], 0));
