@@ -234,11 +234,13 @@ extern "C" int sloam_internal_tables(const sloam_params* p, float* px_tab, float
 // Keyframes per batch projection launch: 64 when the scans are already in
 // device memory (one launch group for a 64-keyframe batch: the grid's ramp
 // and tail are paid once; measured 30 us per 16 keyframes against 37 us in
-// chunks of 16), 8 when they stream from host memory (uploads of the next
-// chunk overlap the projection of this one and the keyframes of the last).
+// chunks of 16), 4 when they stream from host memory (uploads of the next
+// chunk overlap the projection of this one and the keyframes of the last;
+// the first keyframes start after 9 MB of upload: the host batch ran 1.3 %
+// faster than in chunks of 8, and 2 and 16 were slower).
 // Consecutive chunks alternate between two scratch sets, so a chunk's label
 // kernels overlap the next chunk's projection.
-constexpr int kFrontChunkHost = 8, kFrontChunkDevice = 64;
+constexpr int kFrontChunkHost = 4, kFrontChunkDevice = 64;
 constexpr int kFrontChunkMax = kFrontChunkDevice;
 
 // A slot's second stream and the two events of the fork and join inside
