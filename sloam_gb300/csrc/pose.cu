@@ -304,6 +304,50 @@ __device__ void aa_mats(const double* r, double* Rm, double* Rj, double* Jr) {
   }
 }
 
+// aa_mats on one warp, as floats for the residual pass: lane i < 9 writes
+// Rm_i and Rj_i, lane 9 + i writes Jr_i, each entry by the formulas of
+// aa_mats and so3_exp (all 32 lanes call it; lanes 18..31 write nothing).
+// Every lane takes the same sin, cos and quotients, so the FP64 work is one
+// warp instruction per step for all 18 entries: the narrow FP64 pipe costs
+// the same for one lane or 32, and aa_mats on one thread runs its 27
+// entries one after another with sin and cos twice.
+__device__ void warp_aa_mats_f(const double* r, float* sRm, float* sRj, float* sJr) {
+  const int lane = threadIdx.x & 31;
+  const double th2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  const double K[9] = {0, -r[2], r[1], r[2], 0, -r[0], -r[1], r[0], 0};
+  const int i = lane < 9 ? lane : (lane < 18 ? lane - 9 : 0);
+  const int a = i / 3, b = i - 3 * a;
+  const double k2 = K[3 * a] * K[b] + K[3 * a + 1] * K[3 + b] + K[3 * a + 2] * K[6 + b];
+  const double id = (i % 4 == 0) ? 1.0 : 0.0;
+  double rm, rj, jr;
+  if (th2 > DBL_EPSILON) {
+    const double th = sqrt(th2);
+    const double sn = sin(th), cs = cos(th);
+    double A, B;  // exp([r]x) = I + A K + B K^2 (so3_exp)
+    if (th2 < 1e-2) {
+      A = 1.0 - th2 / 6.0 * (1.0 - th2 / 20.0 * (1.0 - th2 / 42.0));
+      B = 0.5 - th2 / 24.0 * (1.0 - th2 / 30.0 * (1.0 - th2 / 56.0));
+    } else {
+      A = sn / th;
+      B = (1.0 - cs) / th2;
+    }
+    const double Aj = (1.0 - cs) / th2, Bj = (th - sn) / (th2 * th);
+    rm = id + A * K[i] + B * k2;
+    rj = rm;
+    jr = id - Aj * K[i] + Bj * k2;
+  } else {
+    rm = id + K[i];
+    rj = id;
+    jr = id;
+  }
+  if (lane < 9) {
+    sRm[i] = (float)rm;
+    sRj[i] = (float)rj;
+  } else if (lane < 18) {
+    sJr[i] = (float)jr;
+  }
+}
+
 // Residual table entry i: [kind, px, py, pz, m0..m7] with kind 0 = none,
 // 1 = cylinder (root - anchor, ray, 1/ray.ray, radius), 2 = plane (n, d + n.anchor, 1/|n|).
 __device__ void build_residual(const Dev& d, const KParams& kp, int i, int nc, const double* a,
@@ -786,15 +830,10 @@ __global__ void __launch_bounds__(kGN) k_gn(Dev d, KParams kp) {
       }
     } else {
       for (int itn = 0; itn < kp.gn_iters && s_ok; ++itn) {
-        if (threadIdx.x == 0) {
-          double Rm[9], Rj[9], Jr[9];
-          aa_mats(s_x + 3, Rm, Rj, Jr);
-          for (int k = 0; k < 9; ++k) {
-            sR[k] = (float)Rm[k];
-            sRj[k] = (float)Rj[k];
-            sJr[k] = (float)Jr[k];
-          }
-          for (int k = 0; k < 3; ++k) sT[k] = (float)(s_x[k] - s_anchor[k]);
+        if (threadIdx.x < 32) {
+          warp_aa_mats_f(s_x + 3, sR, sRj, sJr);
+          if (threadIdx.x >= 18 && threadIdx.x < 21)
+            sT[threadIdx.x - 18] = (float)(s_x[threadIdx.x - 18] - s_anchor[threadIdx.x - 18]);
         }
         __syncthreads();
         float acc[9];
