@@ -250,9 +250,9 @@ __device__ bool warp_chol_solve(const double* H, const double* g, double* x) {
     const double piv = __shfl_sync(0xffffffffu, v, k * (k + 1) / 2 + k);
     ok = ok && piv > 0.0;
     inv[k] = rsqrt(piv);
-    if (ri == k && rj == k) v = piv * inv[k];          // L_kk
-    else if (rj == k && ri > k) v *= inv[k];           // L_ik
-    else if (rj < 0 && ri == k) v *= inv[k];           // y_k
+    // L_kk (the pivot's own lane, v == piv), L_ik (i > k) and y_k: one
+    // predicated multiply for all three
+    if ((rj == k && ri >= k) || (rj < 0 && ri == k)) v *= inv[k];
     // trailing update: matrix (i, j), k < j <= i: -= L_ik L_jk;
     // rhs i > k: -= L_ik y_k
     int s1 = 0, s2 = 0;
